@@ -1,0 +1,1762 @@
+/*
+ * spirit_oracle.c -- CPU FP64 restatement of the reference's spin-dynamics hot path.
+ * TEST INFRASTRUCTURE ONLY (see spirit_oracle.h): the product never calls this code.
+ *
+ * Reference = Spirit v2.2.0 CPU build with OpenMP (redundant neighbour lists,
+ * Hamiltonian_Heisenberg.cpp:101-109) and FP64 scalars.  File:line citations below are
+ * relative to the reference project root.
+ */
+#include "spirit_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* core/include/utility/Constants.hpp:18-43 (SI-meV unit system) */
+#define C_MU_B 0.057883817555
+#define C_MU_0 ( 2.0133545 * 1e-28 )
+#define C_K_B 0.08617330350
+#define C_GAMMA 0.1760859644
+#define C_PI 3.141592653589793238462643383279502884197169399375105820974
+
+typedef struct
+{
+    int i, j, t[3];
+} og_pair;
+
+struct og_system
+{
+    int n_cells[3];
+    int n_cell_atoms;
+    int nos;
+    int n_cells_total;
+    double bravais[3][3];
+    double cell_atoms[OG_MAX_BASIS][3];
+    double lattice_constant;
+    int bc[3];
+    double * positions; /* nos*3 */
+    double * mu_s;      /* nos */
+
+    /* Zeeman: magnitude stored times mu_B (Hamiltonian_Heisenberg.cpp:35) */
+    double field_mag, field_normal[3];
+    /* uniaxial anisotropy */
+    int n_aniso;
+    int aniso_idx[OG_MAX_BASIS];
+    double aniso_mag[OG_MAX_BASIS], aniso_normal[OG_MAX_BASIS][3];
+    /* exchange and DMI (redundant lists) */
+    int n_ex;
+    og_pair * ex_pairs;
+    double * ex_mag;
+    int n_dmi;
+    og_pair * dmi_pairs;
+    double * dmi_mag;
+    double * dmi_normal; /* n_dmi*3 */
+    /* DDI */
+    int ddi_method;
+    int ddi_images[3];
+    double ddi_radius;
+    int ddi_pb_zero_padding;
+    int ddi_ready;
+    int pad[3];        /* padded FFT extents per lattice direction */
+    int fft_total;     /* pad[0]*pad[1]*pad[2] */
+    double * ddi_Dhat; /* [B][B][6][fft_total] complex (re,im interleaved) */
+};
+
+static int og_threads = 0;
+void og_set_threads( int n )
+{
+    og_threads = n;
+#ifdef _OPENMP
+    if( n > 0 )
+        omp_set_num_threads( n );
+#endif
+}
+
+/* ---------------------------------------------------------------- small vector helpers */
+static inline double dot3( const double * a, const double * b )
+{
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+static inline void cross3( const double * a, const double * b, double * o )
+{
+    double x = a[1] * b[2] - a[2] * b[1];
+    double y = a[2] * b[0] - a[0] * b[2];
+    double z = a[0] * b[1] - a[1] * b[0];
+    o[0]     = x;
+    o[1]     = y;
+    o[2]     = z;
+}
+static inline double norm3( const double * a )
+{
+    return sqrt( dot3( a, a ) );
+}
+/* Eigen's normalize(): leaves a zero vector untouched */
+static inline void normalize3( double * a )
+{
+    double n2 = dot3( a, a );
+    if( n2 > 0 )
+    {
+        double n = sqrt( n2 );
+        a[0] /= n;
+        a[1] /= n;
+        a[2] /= n;
+    }
+}
+
+/* ---------------------------------------------------------------- geometry
+ * positions: core/src/data/Geometry.cpp:141-160 */
+og_system * og_create(
+    const int n_cells[3], int n_cell_atoms, const double bravais[9], const double * cell_atoms,
+    double lattice_constant, const double * mu_s_basis, const int boundary_conditions[3] )
+{
+    if( n_cell_atoms < 1 || n_cell_atoms > OG_MAX_BASIS )
+        return NULL;
+    og_system * s = (og_system *)calloc( 1, sizeof( og_system ) );
+    for( int d = 0; d < 3; ++d )
+    {
+        s->n_cells[d] = n_cells[d];
+        s->bc[d]      = boundary_conditions[d];
+        for( int e = 0; e < 3; ++e )
+            s->bravais[d][e] = bravais[3 * d + e];
+    }
+    s->n_cell_atoms = n_cell_atoms;
+    for( int b = 0; b < n_cell_atoms; ++b )
+        for( int e = 0; e < 3; ++e )
+            s->cell_atoms[b][e] = cell_atoms[3 * b + e];
+    s->lattice_constant = lattice_constant;
+    s->n_cells_total    = n_cells[0] * n_cells[1] * n_cells[2];
+    s->nos              = n_cell_atoms * s->n_cells_total;
+    s->positions        = (double *)malloc( sizeof( double ) * 3 * s->nos );
+    s->mu_s             = (double *)malloc( sizeof( double ) * s->nos );
+    int N               = n_cell_atoms;
+    for( int dc = 0; dc < n_cells[2]; ++dc )
+        for( int db = 0; db < n_cells[1]; ++db )
+            for( int da = 0; da < n_cells[0]; ++da )
+                for( int ia = 0; ia < N; ++ia )
+                {
+                    int ispin = ia + dc * N * n_cells[1] * n_cells[0] + db * N * n_cells[0] + da * N;
+                    double fa = (double)da + s->cell_atoms[ia][0];
+                    double fb = (double)db + s->cell_atoms[ia][1];
+                    double fc = (double)dc + s->cell_atoms[ia][2];
+                    for( int e = 0; e < 3; ++e )
+                        s->positions[3 * ispin + e]
+                            = lattice_constant
+                              * ( fa * s->bravais[0][e] + fb * s->bravais[1][e] + fc * s->bravais[2][e] );
+                    s->mu_s[ispin] = mu_s_basis[ia];
+                }
+    s->ddi_images[0] = s->ddi_images[1] = s->ddi_images[2] = 4;
+    return s;
+}
+
+void og_free( og_system * s )
+{
+    if( !s )
+        return;
+    free( s->positions );
+    free( s->mu_s );
+    free( s->ex_pairs );
+    free( s->ex_mag );
+    free( s->dmi_pairs );
+    free( s->dmi_mag );
+    free( s->dmi_normal );
+    free( s->ddi_Dhat );
+    free( s );
+}
+
+int og_nos( const og_system * s )
+{
+    return s->nos;
+}
+
+void og_positions( const og_system * s, double * out )
+{
+    memcpy( out, s->positions, sizeof( double ) * 3 * s->nos );
+}
+
+/* ---------------------------------------------------------------- neighbours
+ * Get_Shell_Radii: core/src/engine/Neighbours.cpp:15-81.  Note the reference compares the
+ * fractional basis position cell_atoms[a] with the Cartesian translation i*ta+j*tb+k*tc;
+ * that is restated as is. */
+static void shell_radii( const og_system * s, int n_shells, double * radii )
+{
+    const double min_shell_width = 1e-3;
+    double ta[3], tb[3], tc[3];
+    for( int e = 0; e < 3; ++e )
+    {
+        ta[e] = s->lattice_constant * s->bravais[0][e];
+        tb[e] = s->lattice_constant * s->bravais[1][e];
+        tc[e] = s->lattice_constant * s->bravais[2][e];
+    }
+    int max_n = n_shells + 2;
+    int i_max = max_n < s->n_cells[0] - 1 ? max_n : s->n_cells[0] - 1;
+    int j_max = max_n < s->n_cells[1] - 1 ? max_n : s->n_cells[1] - 1;
+    int k_max = max_n < s->n_cells[2] - 1 ? max_n : s->n_cells[2] - 1;
+    if( norm3( ta ) == 0.0 )
+        i_max = 0;
+    if( norm3( tb ) == 0.0 )
+        j_max = 0;
+    if( norm3( tc ) == 0.0 )
+        k_max = 0;
+    double outermost = 0, previous = 0;
+    for( int ish = 0; ish < n_shells; ++ish )
+    {
+        previous  = outermost;
+        outermost = DBL_MAX;
+        radii[ish] = 0;
+        for( int a1 = 0; a1 < s->n_cell_atoms; ++a1 )
+        {
+            const double * p1 = s->cell_atoms[a1];
+            for( int i = i_max; i >= 0; --i )
+                for( int j = j_max; j >= -j_max; --j )
+                    for( int k = k_max; k >= -k_max; --k )
+                        for( int a2 = 0; a2 < s->n_cell_atoms; ++a2 )
+                        {
+                            if( a1 == a2 && i == 0 && j == 0 && k == 0 )
+                                continue;
+                            double d[3];
+                            for( int e = 0; e < 3; ++e )
+                            {
+                                double p2 = s->cell_atoms[a2][e] + i * ta[e] + j * tb[e] + k * tc[e];
+                                d[e]      = p1[e] - p2;
+                            }
+                            double delta = norm3( d );
+                            if( delta - previous > min_shell_width && delta < outermost )
+                            {
+                                outermost  = delta;
+                                radii[ish] = delta;
+                            }
+                        }
+        }
+    }
+}
+
+/* Get_Neighbours_in_Shells with use_redundant_neighbours=true: Neighbours.cpp:83-156 */
+static int neighbours_in_shells( const og_system * s, int n_shells, og_pair ** pairs_out, int ** shells_out )
+{
+    const double min_shell_width = 1e-3;
+    double radii[OG_MAX_SHELLS];
+    shell_radii( s, n_shells, radii );
+    double ta[3], tb[3], tc[3];
+    for( int e = 0; e < 3; ++e )
+    {
+        ta[e] = s->lattice_constant * s->bravais[0][e];
+        tb[e] = s->lattice_constant * s->bravais[1][e];
+        tc[e] = s->lattice_constant * s->bravais[2][e];
+    }
+    int max_n = n_shells + 2;
+    int i_max = max_n < s->n_cells[0] - 1 ? max_n : s->n_cells[0] - 1;
+    int j_max = max_n < s->n_cells[1] - 1 ? max_n : s->n_cells[1] - 1;
+    int k_max = max_n < s->n_cells[2] - 1 ? max_n : s->n_cells[2] - 1;
+    /* the lower bounds are taken before the zero-vector checks (Neighbours.cpp:104-116) */
+    int i_min = -i_max, j_min = -j_max, k_min = -k_max;
+    if( norm3( ta ) == 0.0 )
+        i_max = 0;
+    if( norm3( tb ) == 0.0 )
+        j_max = 0;
+    if( norm3( tc ) == 0.0 )
+        k_max = 0;
+    int cap = 64, n = 0;
+    og_pair * pairs = (og_pair *)malloc( sizeof( og_pair ) * cap );
+    int * shells    = (int *)malloc( sizeof( int ) * cap );
+    for( int a1 = 0; a1 < s->n_cell_atoms; ++a1 )
+    {
+        const double * p1 = s->cell_atoms[a1];
+        for( int ish = 0; ish < n_shells; ++ish )
+        {
+            double radius = radii[ish];
+            for( int i = i_max; i >= i_min; --i )
+                for( int j = j_max; j >= j_min; --j )
+                    for( int k = k_max; k >= k_min; --k )
+                        for( int a2 = 0; a2 < s->n_cell_atoms; ++a2 )
+                        {
+                            double d[3];
+                            for( int e = 0; e < 3; ++e )
+                            {
+                                double p2 = s->cell_atoms[a2][e] + i * ta[e] + j * tb[e] + k * tc[e];
+                                d[e]      = p1[e] - p2;
+                            }
+                            if( fabs( norm3( d ) - radius ) < min_shell_width )
+                            {
+                                if( n == cap )
+                                {
+                                    cap *= 2;
+                                    pairs  = (og_pair *)realloc( pairs, sizeof( og_pair ) * cap );
+                                    shells = (int *)realloc( shells, sizeof( int ) * cap );
+                                }
+                                pairs[n].i    = a1;
+                                pairs[n].j    = a2;
+                                pairs[n].t[0] = i;
+                                pairs[n].t[1] = j;
+                                pairs[n].t[2] = k;
+                                shells[n]     = ish;
+                                ++n;
+                            }
+                        }
+        }
+    }
+    *pairs_out  = pairs;
+    *shells_out = shells;
+    return n;
+}
+
+/* DMI_Normal_from_Pair: Neighbours.cpp:249-286 */
+static void dmi_normal( const og_system * s, const og_pair * p, int chirality, double * out )
+{
+    double ipos[3], jpos[3], r[3];
+    for( int e = 0; e < 3; ++e )
+    {
+        double ta = s->lattice_constant * s->bravais[0][e];
+        double tb = s->lattice_constant * s->bravais[1][e];
+        double tc = s->lattice_constant * s->bravais[2][e];
+        ipos[e]   = s->positions[3 * p->i + e];
+        jpos[e]   = s->positions[3 * p->j + e] + p->t[0] * ta + p->t[1] * tb + p->t[2] * tc;
+        r[e]      = jpos[e] - ipos[e];
+    }
+    const double ez[3] = { 0, 0, 1 };
+    if( chirality == 1 )
+    {
+        normalize3( r );
+        memcpy( out, r, sizeof( r ) );
+    }
+    else if( chirality == -1 )
+    {
+        r[0] = -r[0];
+        r[1] = -r[1];
+        r[2] = -r[2];
+        normalize3( r );
+        memcpy( out, r, sizeof( r ) );
+    }
+    else if( chirality == 2 )
+    {
+        normalize3( r );
+        cross3( r, ez, out );
+    }
+    else if( chirality == -2 )
+    {
+        normalize3( r );
+        cross3( ez, r, out );
+    }
+    else
+        out[0] = out[1] = out[2] = 0;
+}
+
+int og_set_exchange_shells( og_system * s, int n_shells, const double * jij )
+{
+    free( s->ex_pairs );
+    free( s->ex_mag );
+    s->ex_pairs = NULL;
+    s->ex_mag   = NULL;
+    s->n_ex     = 0;
+    if( n_shells <= 0 )
+        return 0;
+    int * shells;
+    s->n_ex   = neighbours_in_shells( s, n_shells, &s->ex_pairs, &shells );
+    s->ex_mag = (double *)malloc( sizeof( double ) * ( s->n_ex + 1 ) );
+    for( int p = 0; p < s->n_ex; ++p )
+        s->ex_mag[p] = jij[shells[p]];
+    free( shells );
+    return s->n_ex;
+}
+
+int og_set_dmi_shells( og_system * s, int n_shells, const double * dij, int chirality )
+{
+    free( s->dmi_pairs );
+    free( s->dmi_mag );
+    free( s->dmi_normal );
+    s->dmi_pairs  = NULL;
+    s->dmi_mag    = NULL;
+    s->dmi_normal = NULL;
+    s->n_dmi      = 0;
+    if( n_shells <= 0 )
+        return 0;
+    int * shells;
+    s->n_dmi      = neighbours_in_shells( s, n_shells, &s->dmi_pairs, &shells );
+    s->dmi_mag    = (double *)malloc( sizeof( double ) * ( s->n_dmi + 1 ) );
+    s->dmi_normal = (double *)malloc( sizeof( double ) * 3 * ( s->n_dmi + 1 ) );
+    for( int p = 0; p < s->n_dmi; ++p )
+    {
+        s->dmi_mag[p] = dij[shells[p]];
+        dmi_normal( s, &s->dmi_pairs[p], chirality, s->dmi_normal + 3 * p );
+    }
+    free( shells );
+    return s->n_dmi;
+}
+
+/* explicit pairs + the redundant mirror (Hamiltonian_Heisenberg.cpp:126-139, 160-173) */
+int og_set_exchange_pairs( og_system * s, int n, const int * pairs, const double * jij )
+{
+    free( s->ex_pairs );
+    free( s->ex_mag );
+    s->n_ex     = 2 * n;
+    s->ex_pairs = (og_pair *)malloc( sizeof( og_pair ) * ( 2 * n + 1 ) );
+    s->ex_mag   = (double *)malloc( sizeof( double ) * ( 2 * n + 1 ) );
+    for( int p = 0; p < n; ++p )
+    {
+        const int * q        = pairs + 5 * p;
+        og_pair a            = { q[0], q[1], { q[2], q[3], q[4] } };
+        og_pair b            = { q[1], q[0], { -q[2], -q[3], -q[4] } };
+        s->ex_pairs[p]       = a;
+        s->ex_pairs[n + p]   = b;
+        s->ex_mag[p]         = jij[p];
+        s->ex_mag[n + p]     = jij[p];
+    }
+    return s->n_ex;
+}
+
+int og_set_dmi_pairs( og_system * s, int n, const int * pairs, const double * dij, const double * normals )
+{
+    free( s->dmi_pairs );
+    free( s->dmi_mag );
+    free( s->dmi_normal );
+    s->n_dmi      = 2 * n;
+    s->dmi_pairs  = (og_pair *)malloc( sizeof( og_pair ) * ( 2 * n + 1 ) );
+    s->dmi_mag    = (double *)malloc( sizeof( double ) * ( 2 * n + 1 ) );
+    s->dmi_normal = (double *)malloc( sizeof( double ) * 3 * ( 2 * n + 1 ) );
+    for( int p = 0; p < n; ++p )
+    {
+        const int * q        = pairs + 5 * p;
+        og_pair a            = { q[0], q[1], { q[2], q[3], q[4] } };
+        og_pair b            = { q[1], q[0], { -q[2], -q[3], -q[4] } };
+        s->dmi_pairs[p]      = a;
+        s->dmi_pairs[n + p]  = b;
+        s->dmi_mag[p]        = dij[p];
+        s->dmi_mag[n + p]    = dij[p];
+        for( int e = 0; e < 3; ++e )
+        {
+            s->dmi_normal[3 * p + e]       = normals[3 * p + e];
+            s->dmi_normal[3 * ( n + p ) + e] = -normals[3 * p + e];
+        }
+    }
+    return s->n_dmi;
+}
+
+int og_n_exchange_pairs( const og_system * s )
+{
+    return s->n_ex;
+}
+int og_n_dmi_pairs( const og_system * s )
+{
+    return s->n_dmi;
+}
+void og_get_exchange_pairs( const og_system * s, int * pairs, double * mag )
+{
+    for( int p = 0; p < s->n_ex; ++p )
+    {
+        pairs[5 * p + 0] = s->ex_pairs[p].i;
+        pairs[5 * p + 1] = s->ex_pairs[p].j;
+        for( int e = 0; e < 3; ++e )
+            pairs[5 * p + 2 + e] = s->ex_pairs[p].t[e];
+        mag[p] = s->ex_mag[p];
+    }
+}
+void og_get_dmi_pairs( const og_system * s, int * pairs, double * mag, double * normals )
+{
+    for( int p = 0; p < s->n_dmi; ++p )
+    {
+        pairs[5 * p + 0] = s->dmi_pairs[p].i;
+        pairs[5 * p + 1] = s->dmi_pairs[p].j;
+        for( int e = 0; e < 3; ++e )
+        {
+            pairs[5 * p + 2 + e] = s->dmi_pairs[p].t[e];
+            normals[3 * p + e]   = s->dmi_normal[3 * p + e];
+        }
+        mag[p] = s->dmi_mag[p];
+    }
+}
+
+/* idx_from_pair: core/include/engine/Vectormath.hpp:437-528 (no defects: atom types always valid) */
+static inline int idx_from_pair( const og_system * s, int ispin, const og_pair * p )
+{
+    int N = s->n_cell_atoms;
+    if( p->i != ispin % N )
+        return -1;
+    int Na = s->n_cells[0], Nb = s->n_cells[1], Nc = s->n_cells[2];
+    if( abs( p->t[0] ) > Na || abs( p->t[1] ) > Nb || abs( p->t[2] ) > Nc )
+        return -1;
+    int nic = ispin / ( N * Na * Nb );
+    int nib = ( ispin - nic * N * Na * Nb ) / ( N * Na );
+    int nia = ( ispin - nic * N * Na * Nb - nib * N * Na ) / N;
+    int nja = nia + p->t[0], njb = nib + p->t[1], njc = nic + p->t[2];
+    if( s->bc[0] || ( 0 <= nja && nja < Na ) )
+    {
+        if( nja < 0 )
+            nja += Na;
+        if( nja >= Na )
+            nja -= Na;
+    }
+    else
+        return -1;
+    if( s->bc[1] || ( 0 <= njb && njb < Nb ) )
+    {
+        if( njb < 0 )
+            njb += Nb;
+        if( njb >= Nb )
+            njb -= Nb;
+    }
+    else
+        return -1;
+    if( s->bc[2] || ( 0 <= njc && njc < Nc ) )
+    {
+        if( njc < 0 )
+            njc += Nc;
+        if( njc >= Nc )
+            njc -= Nc;
+    }
+    else
+        return -1;
+    return p->j + nja * N + njb * N * Na + njc * N * Na * Nb;
+}
+
+int og_idx_from_pair( const og_system * s, int ispin, const int pair[5] )
+{
+    og_pair p = { pair[0], pair[1], { pair[2], pair[3], pair[4] } };
+    return idx_from_pair( s, ispin, &p );
+}
+
+void og_set_field( og_system * s, double magnitude, const double normal[3] )
+{
+    s->field_mag = magnitude * C_MU_B;
+    for( int e = 0; e < 3; ++e )
+        s->field_normal[e] = normal[e];
+}
+
+void og_set_anisotropy( og_system * s, int n, const int * indices, const double * magnitudes, const double * normals )
+{
+    s->n_aniso = n;
+    for( int k = 0; k < n; ++k )
+    {
+        s->aniso_idx[k] = indices[k];
+        s->aniso_mag[k] = magnitudes[k];
+        for( int e = 0; e < 3; ++e )
+            s->aniso_normal[k][e] = normals[3 * k + e];
+    }
+}
+
+/* ---------------------------------------------------------------- FFT (FP64, any length)
+ * Mixed-radix decimation-in-time Cooley-Tukey, recursive, with an O(p^2) butterfly for each
+ * prime factor p.  Unnormalised; sign = -1 forward, +1 inverse.  This replaces the
+ * reference's kissFFT backend (core/thirdparty/kiss_fft, itself a mixed-radix Cooley-Tukey);
+ * only the convolution result matters, which is basis-independent. */
+typedef struct
+{
+    double re, im;
+} cpx;
+
+static void fft_rec( cpx * out, const cpx * in, int n, int stride, int sign, cpx * scratch )
+{
+    if( n == 1 )
+    {
+        out[0] = in[0];
+        return;
+    }
+    int p = 2;
+    while( p * p <= n && n % p )
+        ++p;
+    if( n % p )
+        p = n;
+    int m = n / p;
+    /* sub-transforms of the p decimated sequences */
+    for( int r = 0; r < p; ++r )
+        fft_rec( scratch + r * m, in + r * stride, m, stride * p, sign, out );
+    /* butterflies: X[k + q m] = sum_r W_n^{r(k+qm)} Y_r[k] */
+    for( int k = 0; k < m; ++k )
+    {
+        for( int q = 0; q < p; ++q )
+        {
+            int kk   = k + q * m;
+            double sr = 0, si = 0;
+            for( int r = 0; r < p; ++r )
+            {
+                long long e  = ( (long long)r * kk ) % n;
+                double ang   = sign * 2.0 * C_PI * (double)e / (double)n;
+                double c     = cos( ang ), sn = sin( ang );
+                cpx y        = scratch[r * m + k];
+                sr += y.re * c - y.im * sn;
+                si += y.re * sn + y.im * c;
+            }
+            out[kk].re = sr;
+            out[kk].im = si;
+        }
+    }
+}
+
+/* power-of-two fast path: iterative radix-2 with exact twiddles */
+static void fft_pow2( cpx * a, int n, int sign )
+{
+    for( int i = 1, j = 0; i < n; ++i )
+    {
+        int bit = n >> 1;
+        for( ; j & bit; bit >>= 1 )
+            j ^= bit;
+        j ^= bit;
+        if( i < j )
+        {
+            cpx t = a[i];
+            a[i]  = a[j];
+            a[j]  = t;
+        }
+    }
+    for( int len = 2; len <= n; len <<= 1 )
+    {
+        int half = len >> 1;
+        for( int k = 0; k < half; ++k )
+        {
+            double ang = sign * 2.0 * C_PI * (double)k / (double)len;
+            double c = cos( ang ), sn = sin( ang );
+            for( int i = 0; i < n; i += len )
+            {
+                cpx u      = a[i + k];
+                cpx v      = a[i + k + half];
+                double vr  = v.re * c - v.im * sn;
+                double vi  = v.re * sn + v.im * c;
+                a[i + k].re        = u.re + vr;
+                a[i + k].im        = u.im + vi;
+                a[i + k + half].re = u.re - vr;
+                a[i + k + half].im = u.im - vi;
+            }
+        }
+    }
+}
+
+static void fft_line( cpx * line, int n, int sign, cpx * w1, cpx * w2 )
+{
+    if( n <= 1 )
+        return;
+    if( ( n & ( n - 1 ) ) == 0 )
+    {
+        fft_pow2( line, n, sign );
+        return;
+    }
+    memcpy( w1, line, sizeof( cpx ) * n );
+    fft_rec( line, w1, n, 1, sign, w2 );
+}
+
+/* 3D transform of an [n2][n1][n0] array (index x0 + n0*(x1 + n1*x2)) along every axis */
+static void fft3d( cpx * data, const int n[3], int sign )
+{
+    int total = n[0] * n[1] * n[2];
+    for( int ax = 0; ax < 3; ++ax )
+    {
+        int len = n[ax];
+        if( len <= 1 )
+            continue;
+        int stride = ax == 0 ? 1 : ( ax == 1 ? n[0] : n[0] * n[1] );
+        int lines  = total / len;
+#pragma omp parallel
+        {
+            cpx * buf = (cpx *)malloc( sizeof( cpx ) * len * 3 );
+#pragma omp for schedule( static )
+            for( int l = 0; l < lines; ++l )
+            {
+                int base;
+                if( ax == 0 )
+                    base = l * len;
+                else if( ax == 1 )
+                    base = ( l % n[0] ) + ( l / n[0] ) * n[0] * n[1];
+                else
+                    base = l;
+                for( int t = 0; t < len; ++t )
+                    buf[t] = data[base + t * stride];
+                fft_line( buf, len, sign, buf + len, buf + 2 * len );
+                for( int t = 0; t < len; ++t )
+                    data[base + t * stride] = buf[t];
+            }
+            free( buf );
+        }
+    }
+}
+
+/* ---------------------------------------------------------------- DDI
+ * Prepare_DDI (Hamiltonian_Heisenberg.cpp:1501-1595) + FFT_Dipole_Matrices (1406-1499).
+ * Padding: a direction is doubled if n>1 and (open or pb_zero_padding).  The dipole tensor
+ * D(r) = m (3 r r^T / r^5 - I / r^3), m = mu_0 mu_B^2 / (4 pi 1e-30), summed over the
+ * periodic images of periodic directions, for every basis pair (b1, b2). */
+void og_set_ddi( og_system * s, int method, const int n_periodic_images[3], double radius, int pb_zero_padding )
+{
+    s->ddi_method = method;
+    for( int d = 0; d < 3; ++d )
+        s->ddi_images[d] = n_periodic_images[d];
+    s->ddi_radius          = radius;
+    s->ddi_pb_zero_padding = pb_zero_padding;
+    s->ddi_ready           = 0;
+    free( s->ddi_Dhat );
+    s->ddi_Dhat = NULL;
+    if( method != 1 )
+        return;
+    for( int d = 0; d < 3; ++d )
+    {
+        s->pad[d] = s->n_cells[d];
+        if( s->n_cells[d] > 1 && ( s->bc[d] == 0 || pb_zero_padding ) )
+            s->pad[d] *= 2;
+    }
+    s->fft_total = s->pad[0] * s->pad[1] * s->pad[2];
+    int B        = s->n_cell_atoms;
+    int T        = s->fft_total;
+    s->ddi_Dhat  = (double *)calloc( (size_t)B * B * 6 * T * 2, sizeof( double ) );
+    const double mult = C_MU_0 * C_MU_B * C_MU_B / ( 4 * C_PI * 1e-30 );
+    int img[3];
+    for( int d = 0; d < 3; ++d )
+        img[d] = s->bc[d] == 0 ? 0 : s->ddi_images[d];
+    int Na = s->n_cells[0], Nb = s->n_cells[1], Nc = s->n_cells[2];
+    for( int b1 = 0; b1 < B; ++b1 )
+        for( int b2 = 0; b2 < B; ++b2 )
+        {
+            double * Dh = s->ddi_Dhat + (size_t)( b1 * B + b2 ) * 6 * T * 2;
+#pragma omp parallel for collapse( 2 )
+            for( int c = 0; c < s->pad[2]; ++c )
+                for( int b = 0; b < s->pad[1]; ++b )
+                    for( int a = 0; a < s->pad[0]; ++a )
+                    {
+                        int a_idx = a < Na ? a : a - s->pad[0];
+                        int b_idx = b < Nb ? b : b - s->pad[1];
+                        int c_idx = c < Nc ? c : c - s->pad[2];
+                        double Dxx = 0, Dxy = 0, Dxz = 0, Dyy = 0, Dyz = 0, Dzz = 0;
+                        for( int ap = -img[0]; ap <= img[0]; ++ap )
+                            for( int bp = -img[1]; bp <= img[1]; ++bp )
+                                for( int cp = -img[2]; cp <= img[2]; ++cp )
+                                {
+                                    double fa = a_idx + ap * Na + s->cell_atoms[b1][0] - s->cell_atoms[b2][0];
+                                    double fb = b_idx + bp * Nb + s->cell_atoms[b1][1] - s->cell_atoms[b2][1];
+                                    double fc = c_idx + cp * Nc + s->cell_atoms[b1][2] - s->cell_atoms[b2][2];
+                                    double r[3];
+                                    for( int e = 0; e < 3; ++e )
+                                        r[e] = s->lattice_constant
+                                               * ( fa * s->bravais[0][e] + fb * s->bravais[1][e]
+                                                   + fc * s->bravais[2][e] );
+                                    double d = norm3( r );
+                                    if( d > 1e-10 )
+                                    {
+                                        double d3 = d * d * d, d5 = d * d * d * d * d;
+                                        Dxx += mult * ( 3 * r[0] * r[0] / d5 - 1 / d3 );
+                                        Dxy += mult * 3 * r[0] * r[1] / d5;
+                                        Dxz += mult * 3 * r[0] * r[2] / d5;
+                                        Dyy += mult * ( 3 * r[1] * r[1] / d5 - 1 / d3 );
+                                        Dyz += mult * 3 * r[1] * r[2] / d5;
+                                        Dzz += mult * ( 3 * r[2] * r[2] / d5 - 1 / d3 );
+                                    }
+                                }
+                        size_t idx = (size_t)a + s->pad[0] * ( b + (size_t)s->pad[1] * c );
+                        double v[6] = { Dxx, Dxy, Dxz, Dyy, Dyz, Dzz };
+                        for( int comp = 0; comp < 6; ++comp )
+                            Dh[2 * ( comp * (size_t)T + idx )] = v[comp];
+                    }
+            for( int comp = 0; comp < 6; ++comp )
+                fft3d( (cpx *)( Dh + 2 * (size_t)comp * T ), s->pad, -1 );
+        }
+    s->ddi_ready = 1;
+}
+
+/* Gradient_DDI_FFT: Hamiltonian_Heisenberg.cpp:920-1014 (FFT_Spins 1373-1404): g_i -= mu_i * H_i,
+ * H = (1/T) IFFT( sum_b2 Dhat_{b1 b2} . FFT(mu s)_b2 ). */
+static void gradient_ddi_fft( og_system * s, const double * spins, double * grad )
+{
+    int B = s->n_cell_atoms, T = s->fft_total;
+    int Na = s->n_cells[0], Nb = s->n_cells[1], Nc = s->n_cells[2];
+    cpx * S = (cpx *)calloc( (size_t)B * 3 * T, sizeof( cpx ) );
+    cpx * H = (cpx *)calloc( (size_t)B * 3 * T, sizeof( cpx ) );
+    for( int c = 0; c < Nc; ++c )
+        for( int b = 0; b < Nb; ++b )
+            for( int a = 0; a < Na; ++a )
+                for( int bi = 0; bi < B; ++bi )
+                {
+                    int io     = bi + B * ( a + Na * ( b + Nb * c ) );
+                    size_t idx = (size_t)a + s->pad[0] * ( b + (size_t)s->pad[1] * c );
+                    for( int e = 0; e < 3; ++e )
+                        S[(size_t)( bi * 3 + e ) * T + idx].re = spins[3 * io + e] * s->mu_s[io];
+                }
+    for( int k = 0; k < 3 * B; ++k )
+        fft3d( S + (size_t)k * T, s->pad, -1 );
+#pragma omp parallel for
+    for( long long q = 0; q < (long long)T; ++q )
+    {
+        for( int b1 = 0; b1 < B; ++b1 )
+        {
+            double hr[3] = { 0, 0, 0 }, hi[3] = { 0, 0, 0 };
+            for( int b2 = 0; b2 < B; ++b2 )
+            {
+                const cpx * D = (const cpx *)( s->ddi_Dhat + (size_t)( b1 * B + b2 ) * 6 * T * 2 );
+                cpx d[6];
+                for( int comp = 0; comp < 6; ++comp )
+                    d[comp] = D[(size_t)comp * T + q];
+                cpx sx = S[(size_t)( b2 * 3 + 0 ) * T + q], sy = S[(size_t)( b2 * 3 + 1 ) * T + q],
+                    sz = S[(size_t)( b2 * 3 + 2 ) * T + q];
+                /* rows of the symmetric tensor: (xx xy xz) (xy yy yz) (xz yz zz), FFT.hpp:42-49 */
+                const int row[3][3] = { { 0, 1, 2 }, { 1, 3, 4 }, { 2, 4, 5 } };
+                for( int e = 0; e < 3; ++e )
+                {
+                    cpx d1 = d[row[e][0]], d2 = d[row[e][1]], d3 = d[row[e][2]];
+                    hr[e] += d1.re * sx.re + d2.re * sy.re + d3.re * sz.re - d1.im * sx.im - d2.im * sy.im
+                             - d3.im * sz.im;
+                    hi[e] += d1.re * sx.im + d2.re * sy.im + d3.re * sz.im + d1.im * sx.re + d2.im * sy.re
+                             + d3.im * sz.re;
+                }
+            }
+            for( int e = 0; e < 3; ++e )
+            {
+                H[(size_t)( b1 * 3 + e ) * T + q].re = hr[e];
+                H[(size_t)( b1 * 3 + e ) * T + q].im = hi[e];
+            }
+        }
+    }
+    for( int k = 0; k < 3 * B; ++k )
+        fft3d( H + (size_t)k * T, s->pad, +1 );
+    for( int c = 0; c < Nc; ++c )
+        for( int b = 0; b < Nb; ++b )
+            for( int a = 0; a < Na; ++a )
+                for( int bi = 0; bi < B; ++bi )
+                {
+                    int io     = bi + B * ( a + Na * ( b + Nb * c ) );
+                    size_t idx = (size_t)a + s->pad[0] * ( b + (size_t)s->pad[1] * c );
+                    for( int e = 0; e < 3; ++e )
+                        grad[3 * io + e] -= s->mu_s[io] * H[(size_t)( bi * 3 + e ) * T + idx].re / T;
+                }
+    free( S );
+    free( H );
+}
+
+/* Gradient_DDI_Direct: Hamiltonian_Heisenberg.cpp:1016-1071 */
+void og_gradient_ddi_direct( og_system * s, const double * spins, double * grad )
+{
+    const double mult = C_MU_0 * C_MU_B * C_MU_B / ( 4 * C_PI * 1e-30 );
+    int img[3];
+    for( int d = 0; d < 3; ++d )
+        img[d] = s->bc[d] == 0 ? 0 : s->ddi_images[d];
+#pragma omp parallel for schedule( dynamic, 16 )
+    for( int i1 = 0; i1 < s->nos; ++i1 )
+    {
+        for( int i2 = 0; i2 < s->nos; ++i2 )
+        {
+            const double * m2 = spins + 3 * i2;
+            double diff[3];
+            for( int e = 0; e < 3; ++e )
+                diff[e] = s->positions[3 * i2 + e] - s->positions[3 * i1 + e];
+            double Dxx = 0, Dxy = 0, Dxz = 0, Dyy = 0, Dyz = 0, Dzz = 0;
+            for( int ap = -img[0]; ap <= img[0]; ++ap )
+                for( int bp = -img[1]; bp <= img[1]; ++bp )
+                    for( int cp = -img[2]; cp <= img[2]; ++cp )
+                    {
+                        double r[3];
+                        for( int e = 0; e < 3; ++e )
+                            r[e] = diff[e] + ap * s->n_cells[0] * s->bravais[0][e] * s->lattice_constant
+                                   + bp * s->n_cells[1] * s->bravais[1][e] * s->lattice_constant
+                                   + cp * s->n_cells[2] * s->bravais[2][e] * s->lattice_constant;
+                        double d = norm3( r );
+                        if( d > 1e-10 )
+                        {
+                            double d3 = d * d * d, d5 = d * d * d * d * d;
+                            Dxx += mult * ( 3 * r[0] * r[0] / d5 - 1 / d3 );
+                            Dxy += mult * 3 * r[0] * r[1] / d5;
+                            Dxz += mult * 3 * r[0] * r[2] / d5;
+                            Dyy += mult * ( 3 * r[1] * r[1] / d5 - 1 / d3 );
+                            Dyz += mult * 3 * r[1] * r[2] / d5;
+                            Dzz += mult * ( 3 * r[2] * r[2] / d5 - 1 / d3 );
+                        }
+                    }
+            double mm = s->mu_s[i1] * s->mu_s[i2];
+            grad[3 * i1 + 0] -= ( Dxx * m2[0] + Dxy * m2[1] + Dxz * m2[2] ) * mm;
+            grad[3 * i1 + 1] -= ( Dxy * m2[0] + Dyy * m2[1] + Dyz * m2[2] ) * mm;
+            grad[3 * i1 + 2] -= ( Dxz * m2[0] + Dyz * m2[1] + Dzz * m2[2] ) * mm;
+        }
+    }
+}
+
+static void gradient_ddi( og_system * s, const double * spins, double * grad )
+{
+    if( s->ddi_method == 1 )
+        gradient_ddi_fft( s, spins, grad );
+    else if( s->ddi_method == 3 && s->ddi_radius < 0 )
+        og_gradient_ddi_direct( s, spins, grad );
+}
+
+/* ---------------------------------------------------------------- local terms
+ * Gradient_Zeeman 768-783, Gradient_Anisotropy 785-800, Gradient_Exchange 822-842,
+ * Gradient_DMI 844-864 (redundant lists: only spin i is updated per pair) */
+static void gradient_anisotropy( const og_system * s, const double * spins, double * g )
+{
+    int N = s->n_cell_atoms;
+#pragma omp parallel for
+    for( int ic = 0; ic < s->n_cells_total; ++ic )
+        for( int k = 0; k < s->n_aniso; ++k )
+        {
+            int i              = ic * N + s->aniso_idx[k];
+            const double * n   = s->aniso_normal[k];
+            double sc          = 2.0 * s->aniso_mag[k] * dot3( n, spins + 3 * i );
+            for( int e = 0; e < 3; ++e )
+                g[3 * i + e] -= sc * n[e];
+        }
+}
+
+static void gradient_exchange( const og_system * s, const double * spins, double * g )
+{
+#pragma omp parallel for
+    for( int ic = 0; ic < s->n_cells_total; ++ic )
+        for( int p = 0; p < s->n_ex; ++p )
+        {
+            int i = s->ex_pairs[p].i + ic * s->n_cell_atoms;
+            int j = idx_from_pair( s, i, &s->ex_pairs[p] );
+            if( j >= 0 )
+                for( int e = 0; e < 3; ++e )
+                    g[3 * i + e] -= s->ex_mag[p] * spins[3 * j + e];
+        }
+}
+
+static void gradient_dmi( const og_system * s, const double * spins, double * g )
+{
+#pragma omp parallel for
+    for( int ic = 0; ic < s->n_cells_total; ++ic )
+        for( int p = 0; p < s->n_dmi; ++p )
+        {
+            int i = s->dmi_pairs[p].i + ic * s->n_cell_atoms;
+            int j = idx_from_pair( s, i, &s->dmi_pairs[p] );
+            if( j >= 0 )
+            {
+                double c[3];
+                cross3( spins + 3 * j, s->dmi_normal + 3 * p, c );
+                for( int e = 0; e < 3; ++e )
+                    g[3 * i + e] -= s->dmi_mag[p] * c[e];
+            }
+        }
+}
+
+static void gradient_zeeman( const og_system * s, double * g )
+{
+#pragma omp parallel for
+    for( int i = 0; i < s->nos; ++i )
+        for( int e = 0; e < 3; ++e )
+            g[3 * i + e] -= s->mu_s[i] * s->field_mag * s->field_normal[e];
+}
+
+static int has_zeeman( const og_system * s )
+{
+    return fabs( s->field_mag ) > 1e-60; /* Update_Energy_Contributions, cpp:205 */
+}
+
+/* Gradient: cpp:670-702 */
+void og_gradient( og_system * s, const double * spins, double * g )
+{
+    memset( g, 0, sizeof( double ) * 3 * s->nos );
+    if( has_zeeman( s ) )
+        gradient_zeeman( s, g );
+    if( s->n_aniso > 0 )
+        gradient_anisotropy( s, spins, g );
+    if( s->n_ex > 0 )
+        gradient_exchange( s, spins, g );
+    if( s->n_dmi > 0 )
+        gradient_dmi( s, spins, g );
+    if( s->ddi_method != 0 )
+        gradient_ddi( s, spins, g );
+}
+
+/* Gradient_and_Energy: cpp:704-766.  E = sum 0.5 g.s over the quadratic terms, then the
+ * Zeeman gradient and energy sum -mu_i B.s_i. */
+double og_gradient_and_energy( og_system * s, const double * spins, double * g )
+{
+    memset( g, 0, sizeof( double ) * 3 * s->nos );
+    if( s->n_aniso > 0 )
+        gradient_anisotropy( s, spins, g );
+    if( s->n_ex > 0 )
+        gradient_exchange( s, spins, g );
+    if( s->n_dmi > 0 )
+        gradient_dmi( s, spins, g );
+    if( s->ddi_method != 0 )
+        gradient_ddi( s, spins, g );
+    double E = 0;
+#pragma omp parallel for reduction( + : E )
+    for( int i = 0; i < s->nos; ++i )
+        E += 0.5 * dot3( g + 3 * i, spins + 3 * i );
+    if( has_zeeman( s ) )
+    {
+        gradient_zeeman( s, g );
+        double Ez = 0;
+#pragma omp parallel for reduction( + : Ez )
+        for( int i = 0; i < s->nos; ++i )
+        {
+            double b[3] = { s->field_normal[0] * s->field_mag, s->field_normal[1] * s->field_mag,
+                            s->field_normal[2] * s->field_mag };
+            Ez += -s->mu_s[i] * dot3( b, spins + 3 * i );
+        }
+        E += Ez;
+    }
+    return E;
+}
+
+/* Energy_Contributions_per_Spin: cpp:262-305; E_Zeeman 307-322, E_Anisotropy 324-338,
+ * E_Exchange 357-377, E_DMI 379-401, E_DDI_FFT 465-511 (0.5 s.g_DDI) */
+int og_energy_contributions( og_system * s, const double * spins, double * out, char * names, int names_len )
+{
+    int nos = s->nos, n = 0;
+    char buf[256] = { 0 };
+    if( has_zeeman( s ) )
+    {
+        double * E = out + (size_t)n * nos;
+        for( int i = 0; i < nos; ++i )
+            E[i] = -s->mu_s[i] * s->field_mag * dot3( s->field_normal, spins + 3 * i );
+        strcat( buf, "Zeeman," );
+        ++n;
+    }
+    if( s->n_aniso > 0 )
+    {
+        double * E = out + (size_t)n * nos;
+        memset( E, 0, sizeof( double ) * nos );
+        for( int ic = 0; ic < s->n_cells_total; ++ic )
+            for( int k = 0; k < s->n_aniso; ++k )
+            {
+                int i    = ic * s->n_cell_atoms + s->aniso_idx[k];
+                double d = dot3( s->aniso_normal[k], spins + 3 * i );
+                E[i] -= s->aniso_mag[k] * d * d;
+            }
+        strcat( buf, "Anisotropy," );
+        ++n;
+    }
+    if( s->n_ex > 0 )
+    {
+        double * E = out + (size_t)n * nos;
+        memset( E, 0, sizeof( double ) * nos );
+#pragma omp parallel for
+        for( int ic = 0; ic < s->n_cells_total; ++ic )
+            for( int p = 0; p < s->n_ex; ++p )
+            {
+                int i = s->ex_pairs[p].i + ic * s->n_cell_atoms;
+                int j = idx_from_pair( s, i, &s->ex_pairs[p] );
+                if( j >= 0 )
+                    E[i] -= 0.5 * s->ex_mag[p] * dot3( spins + 3 * i, spins + 3 * j );
+            }
+        strcat( buf, "Exchange," );
+        ++n;
+    }
+    if( s->n_dmi > 0 )
+    {
+        double * E = out + (size_t)n * nos;
+        memset( E, 0, sizeof( double ) * nos );
+#pragma omp parallel for
+        for( int ic = 0; ic < s->n_cells_total; ++ic )
+            for( int p = 0; p < s->n_dmi; ++p )
+            {
+                int i = s->dmi_pairs[p].i + ic * s->n_cell_atoms;
+                int j = idx_from_pair( s, i, &s->dmi_pairs[p] );
+                if( j >= 0 )
+                {
+                    double c[3];
+                    cross3( spins + 3 * i, spins + 3 * j, c );
+                    E[i] -= 0.5 * s->dmi_mag[p] * dot3( s->dmi_normal + 3 * p, c );
+                }
+            }
+        strcat( buf, "DMI," );
+        ++n;
+    }
+    if( s->ddi_method != 0 )
+    {
+        double * E = out + (size_t)n * nos;
+        double * g = (double *)calloc( (size_t)3 * nos, sizeof( double ) );
+        gradient_ddi( s, spins, g );
+        for( int i = 0; i < nos; ++i )
+            E[i] = 0.5 * dot3( spins + 3 * i, g + 3 * i );
+        free( g );
+        strcat( buf, "DDI," );
+        ++n;
+    }
+    if( names && names_len > 0 )
+    {
+        size_t l = strlen( buf );
+        if( l > 0 )
+            buf[l - 1] = 0;
+        strncpy( names, buf, names_len - 1 );
+        names[names_len - 1] = 0;
+    }
+    return n;
+}
+
+double og_energy( og_system * s, const double * spins )
+{
+    int nos    = s->nos;
+    double * E = (double *)malloc( sizeof( double ) * 5 * nos );
+    int n      = og_energy_contributions( s, spins, E, NULL, 0 );
+    double sum = 0;
+    for( int t = 0; t < n; ++t )
+    {
+        double part = 0;
+        for( int i = 0; i < nos; ++i )
+            part += E[(size_t)t * nos + i];
+        sum += part;
+    }
+    free( E );
+    return sum;
+}
+
+/* ---------------------------------------------------------------- Philox4x32-10
+ * Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3" (SC'11):
+ * 10 rounds of (mulhilo by 0xD2511F53 / 0xCD9E8D57, xor with key) with Weyl key
+ * increments 0x9E3779B9 / 0xBB67AE85.  The CUDA kernels implement the same function. */
+void og_philox4x32( const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4] )
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for( int r = 0; r < 10; ++r )
+    {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)( p0 >> 32 ), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)( p1 >> 32 ), lo1 = (uint32_t)p1;
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+/* Gaussian triple for spin i at a given iteration: counter (i, iteration, stream, 0x53504E00),
+ * key (seed lo, seed hi); uniforms u = (x + 0.5) 2^-32; Box-Muller on (u0,u1) and (u2,u3). */
+static void gauss3( uint64_t seed, uint32_t stream, uint32_t iteration, uint32_t i, double * z )
+{
+    uint32_t ctr[4] = { i, iteration, stream, 0x53504E00u };
+    uint32_t key[2] = { (uint32_t)seed, (uint32_t)( seed >> 32 ) };
+    uint32_t x[4];
+    og_philox4x32( ctr, key, x );
+    double u0 = ( x[0] + 0.5 ) * ( 1.0 / 4294967296.0 );
+    double u1 = ( x[1] + 0.5 ) * ( 1.0 / 4294967296.0 );
+    double u2 = ( x[2] + 0.5 ) * ( 1.0 / 4294967296.0 );
+    double u3 = ( x[3] + 0.5 ) * ( 1.0 / 4294967296.0 );
+    double r0 = sqrt( -2.0 * log( u0 ) );
+    double r1 = sqrt( -2.0 * log( u2 ) );
+    z[0]      = r0 * cos( 2.0 * C_PI * u1 );
+    z[1]      = r0 * sin( 2.0 * C_PI * u1 );
+    z[2]      = r1 * cos( 2.0 * C_PI * u3 );
+}
+
+/* Prepare_Thermal_Field: core/src/engine/Method_LLG.cpp:65-110 (homogeneous temperature) */
+void og_thermal_noise(
+    const og_system * s, double temperature, double damping, double dt, uint64_t seed, uint32_t stream,
+    uint32_t iteration, double * xi )
+{
+    double eps = sqrt( 2 * damping * dt * C_GAMMA / C_MU_B * C_K_B ) / ( 1 + damping * damping );
+#pragma omp parallel for
+    for( int i = 0; i < s->nos; ++i )
+    {
+        double z[3];
+        gauss3( seed, stream, iteration, (uint32_t)i, z );
+        double sc = eps * sqrt( temperature / s->mu_s[i] );
+        for( int e = 0; e < 3; ++e )
+            xi[3 * i + e] = sc * z[e];
+    }
+}
+
+/* ---------------------------------------------------------------- LLG
+ * Calculate_Force_Virtual: Method_LLG.cpp:132-226.
+ *  dynamics:             fv = (dtg F + dtg a s x F) / mu_s [+ xi + a s x xi],  dtg = dt g/mu_B/(1+a^2)
+ *  direct min. and VP:   fv = dt g/mu_B (s x F) */
+static void force_virtual(
+    const og_system * s, const og_llg_params * p, int solver, const double * spins, const double * F,
+    const double * xi, double * fv )
+{
+    double a   = p->damping;
+    double dtg = p->dt * C_GAMMA / C_MU_B / ( 1 + a * a );
+    int thermal = p->temperature > 0;
+    if( p->direct_minimization || solver == 0 )
+    {
+        double d = p->dt * C_GAMMA / C_MU_B;
+#pragma omp parallel for
+        for( int i = 0; i < s->nos; ++i )
+        {
+            double c[3];
+            cross3( spins + 3 * i, F + 3 * i, c );
+            for( int e = 0; e < 3; ++e )
+                fv[3 * i + e] = d * c[e];
+        }
+        return;
+    }
+#pragma omp parallel for
+    for( int i = 0; i < s->nos; ++i )
+    {
+        const double * si = spins + 3 * i;
+        double c[3];
+        cross3( si, F + 3 * i, c );
+        for( int e = 0; e < 3; ++e )
+        {
+            double v = dtg * F[3 * i + e];
+            v += dtg * a * c[e];
+            fv[3 * i + e] = v / s->mu_s[i];
+        }
+        if( thermal )
+        {
+            double cx[3];
+            cross3( si, xi + 3 * i, cx );
+            for( int e = 0; e < 3; ++e )
+            {
+                fv[3 * i + e] += xi[3 * i + e];
+                fv[3 * i + e] += a * cx[e];
+            }
+        }
+    }
+}
+
+/* force = -gradient (Method_LLG::Calculate_Force, 113-129) */
+static double calc_force( og_system * s, const double * spins, double * F )
+{
+    double E = og_gradient_and_energy( s, spins, F );
+    for( int k = 0; k < 3 * s->nos; ++k )
+        F[k] = -F[k];
+    return E;
+}
+
+/* Vectormath::rotate (Vectormath.cpp:474-479), Rodrigues */
+static inline void rotate3( const double * v, const double * axis, double angle, double * out )
+{
+    double c = cos( angle ), sn = sin( angle );
+    double ax[3];
+    cross3( axis, v, ax );
+    double ad = dot3( axis, v );
+    double r[3];
+    for( int e = 0; e < 3; ++e )
+        r[e] = v[e] * c + ax[e] * sn + axis[e] * ad * ( 1 - c );
+    memcpy( out, r, sizeof( r ) );
+}
+
+/* sib_transform: core/src/engine/Solver_Kernels.cpp:15-48 */
+static inline void sib_transform( const double * e1, const double * f, double * o )
+{
+    double A[3] = { 0.5 * f[0], 0.5 * f[1], 0.5 * f[2] };
+    double nA   = norm3( A );
+    double detAi = 1.0 / ( 1 + pow( nA, 2.0 ) );
+    double c[3];
+    cross3( e1, A, c );
+    double a2[3] = { e1[0] - c[0], e1[1] - c[1], e1[2] - c[2] };
+    double r[3];
+    r[0] = ( a2[0] * ( A[0] * A[0] + 1 ) + a2[1] * ( A[0] * A[1] - A[2] ) + a2[2] * ( A[0] * A[2] + A[1] ) ) * detAi;
+    r[1] = ( a2[0] * ( A[1] * A[0] + A[2] ) + a2[1] * ( A[1] * A[1] + 1 ) + a2[2] * ( A[1] * A[2] - A[0] ) ) * detAi;
+    r[2] = ( a2[0] * ( A[2] * A[0] - A[1] ) + a2[1] * ( A[2] * A[1] + A[0] ) + a2[2] * ( A[2] * A[2] + 1 ) ) * detAi;
+    memcpy( o, r, sizeof( r ) );
+}
+
+/* max_i |fv_i - (fv_i . s_i) s_i|  (MaxTorque_on_Image, Method_Solver.hpp:225-230) */
+static double max_torque( int nos, const double * spins, const double * fv )
+{
+    double m2 = 0;
+#pragma omp parallel for reduction( max : m2 )
+    for( int i = 0; i < nos; ++i )
+    {
+        const double * si = spins + 3 * i;
+        double d          = dot3( fv + 3 * i, si );
+        double t[3]       = { fv[3 * i] - d * si[0], fv[3 * i + 1] - d * si[1], fv[3 * i + 2] - d * si[2] };
+        double n2         = dot3( t, t );
+        if( n2 > m2 )
+            m2 = n2;
+    }
+    return sqrt( m2 );
+}
+
+/* One iteration per solver: Solver_SIB.hpp:21-50, Solver_Depondt.hpp:28-77,
+ * Solver_Heun.hpp:29-80, Solver_RK4.hpp:40-147.  Returns the energy of the last force call. */
+static double llg_iteration(
+    og_system * s, const og_llg_params * p, int solver, double * spins, const double * xi, double * fv1,
+    double * work )
+{
+    int nos    = s->nos;
+    size_t n3  = (size_t)3 * nos;
+    double * F  = work;
+    double * fv = work + n3;
+    double * pr = work + 2 * n3;
+    double * t1 = work + 3 * n3;
+    double * k1 = work + 4 * n3;
+    double * k2 = work + 5 * n3;
+    double * k3 = work + 6 * n3;
+    double E    = calc_force( s, spins, F );
+    force_virtual( s, p, solver, spins, F, xi, fv1 );
+    if( solver == 1 ) /* SIB */
+    {
+#pragma omp parallel for
+        for( int i = 0; i < nos; ++i )
+        {
+            sib_transform( spins + 3 * i, fv1 + 3 * i, pr + 3 * i );
+            for( int e = 0; e < 3; ++e )
+            {
+                pr[3 * i + e] += spins[3 * i + e];
+                pr[3 * i + e] *= 0.5;
+            }
+        }
+        E = calc_force( s, pr, F );
+        force_virtual( s, p, solver, pr, F, xi, fv );
+#pragma omp parallel for
+        for( int i = 0; i < nos; ++i )
+            sib_transform( spins + 3 * i, fv + 3 * i, spins + 3 * i );
+    }
+    else if( solver == 2 ) /* Depondt */
+    {
+#pragma omp parallel for
+        for( int i = 0; i < nos; ++i )
+        {
+            double ax[3] = { fv1[3 * i], fv1[3 * i + 1], fv1[3 * i + 2] };
+            double ang   = norm3( ax );
+            normalize3( ax );
+            rotate3( spins + 3 * i, ax, ang, pr + 3 * i );
+        }
+        E = calc_force( s, pr, F );
+        force_virtual( s, p, solver, pr, F, xi, fv );
+#pragma omp parallel for
+        for( int i = 0; i < nos; ++i )
+        {
+            double ax[3];
+            for( int e = 0; e < 3; ++e )
+            {
+                ax[e] = 0.5 * fv1[3 * i + e];
+                ax[e] += 0.5 * fv[3 * i + e];
+            }
+            double ang = norm3( ax );
+            normalize3( ax );
+            rotate3( spins + 3 * i, ax, ang, spins + 3 * i );
+        }
+    }
+    else if( solver == 3 ) /* Heun */
+    {
+#pragma omp parallel for
+        for( int i = 0; i < nos; ++i )
+        {
+            double c[3];
+            cross3( spins + 3 * i, fv1 + 3 * i, c );
+            for( int e = 0; e < 3; ++e )
+            {
+                t1[3 * i + e] = -1 * c[e];
+                pr[3 * i + e] = spins[3 * i + e] + t1[3 * i + e];
+            }
+            normalize3( pr + 3 * i );
+        }
+        E = calc_force( s, pr, F );
+        force_virtual( s, p, solver, pr, F, xi, fv );
+#pragma omp parallel for
+        for( int i = 0; i < nos; ++i )
+        {
+            double c[3], t[3];
+            cross3( pr + 3 * i, fv + 3 * i, c );
+            for( int e = 0; e < 3; ++e )
+            {
+                t[e] = t1[3 * i + e] * 0.5;
+                t[e] += spins[3 * i + e];
+                t[e] += 0.5 * ( -1 * c[e] );
+            }
+            normalize3( t );
+            memcpy( spins + 3 * i, t, sizeof( t ) );
+        }
+    }
+    else if( solver == 4 ) /* RK4 */
+    {
+        double * cfg   = pr;
+        double * stage = t1;
+#pragma omp parallel for
+        for( int i = 0; i < nos; ++i )
+        {
+            double c[3];
+            cross3( spins + 3 * i, fv1 + 3 * i, c );
+            for( int e = 0; e < 3; ++e )
+            {
+                k1[3 * i + e]  = -1 * c[e];
+                cfg[3 * i + e] = spins[3 * i + e] + 0.5 * k1[3 * i + e];
+            }
+            normalize3( cfg + 3 * i );
+        }
+        double * ks[3] = { k2, k3, stage };
+        const double wnext[2] = { 0.5, 1.0 };
+        for( int st = 0; st < 3; ++st )
+        {
+            E = calc_force( s, cfg, F );
+            force_virtual( s, p, solver, cfg, F, xi, fv );
+            double * k = ks[st];
+#pragma omp parallel for
+            for( int i = 0; i < nos; ++i )
+            {
+                double c[3];
+                cross3( cfg + 3 * i, fv + 3 * i, c );
+                for( int e = 0; e < 3; ++e )
+                    k[3 * i + e] = -1 * c[e];
+            }
+            if( st < 2 )
+            {
+#pragma omp parallel for
+                for( int i = 0; i < nos; ++i )
+                {
+                    for( int e = 0; e < 3; ++e )
+                        cfg[3 * i + e] = spins[3 * i + e] + wnext[st] * k[3 * i + e];
+                    normalize3( cfg + 3 * i );
+                }
+            }
+        }
+#pragma omp parallel for
+        for( int i = 0; i < nos; ++i )
+        {
+            double t[3];
+            for( int e = 0; e < 3; ++e )
+            {
+                t[e] = spins[3 * i + e];
+                t[e] += 1.0 / 6.0 * k1[3 * i + e];
+                t[e] += 1.0 / 3.0 * k2[3 * i + e];
+                t[e] += 1.0 / 3.0 * k3[3 * i + e];
+                t[e] += 1.0 / 6.0 * stage[3 * i + e];
+            }
+            normalize3( t );
+            memcpy( spins + 3 * i, t, sizeof( t ) );
+        }
+    }
+    return E;
+}
+
+/* Method::Iterate (Method.cpp:57-113) + Method_LLG ctor (Method_LLG.cpp:22-63) and
+ * Hook_Post_Iteration (247-301): the constructor evaluates the initial max torque, the loop
+ * runs while iteration < n_iter and max_torque >= force_convergence. */
+int og_llg_run(
+    og_system * s, const og_llg_params * p, int solver, int n_iter, double * spins, double * energy,
+    double * max_torque_out )
+{
+    int nos    = s->nos;
+    size_t n3  = (size_t)3 * nos;
+    double * work = (double *)calloc( 8 * n3, sizeof( double ) );
+    double * xi   = (double *)calloc( n3, sizeof( double ) );
+    double * fv1  = (double *)calloc( n3, sizeof( double ) );
+    /* constructor: Prepare_Thermal_Field + force + virtual force + post hook on the initial state
+     * (the constructor draws noise too; with Philox the draw is indexed, so it uses iteration
+     * index 0xFFFFFFFF and never collides with the loop's draws) */
+    if( p->temperature > 0 )
+        og_thermal_noise( s, p->temperature, p->damping, p->dt, p->seed, p->stream, 0xFFFFFFFFu, xi );
+    double E = calc_force( s, spins, work );
+    force_virtual( s, p, solver, spins, work, xi, fv1 );
+    double mt = max_torque( nos, spins, fv1 );
+    int it    = 0;
+    for( it = 0; it < n_iter && !( mt < p->force_convergence ); ++it )
+    {
+        if( p->temperature > 0 )
+            og_thermal_noise( s, p->temperature, p->damping, p->dt, p->seed, p->stream, (uint32_t)it, xi );
+        E  = llg_iteration( s, p, solver, spins, xi, fv1, work );
+        mt = max_torque( nos, spins, fv1 );
+    }
+    if( energy )
+        *energy = E;
+    if( max_torque_out )
+        *max_torque_out = mt;
+    free( work );
+    free( xi );
+    free( fv1 );
+    return it;
+}
+
+/* ---------------------------------------------------------------- GNEB
+ * Manifoldmath.cpp: project_tangential 59-64, dist_geodesic 66-72 (angle: Vectormath.cpp:434-441),
+ * Geodesic_Tangent 78-113, Tangents 115-215, project_orthogonal 31-38, invert_parallel 40-47,
+ * normalize 224-229.  Method_GNEB.cpp:88-357 (Calculate_Force, no spring-force ratio, no path
+ * shortening, fixed endpoints), Solver_VP.hpp:28-114, Hook_Post_Iteration 411-456. */
+static double vdot( int n3, const double * a, const double * b )
+{
+    double r = 0;
+#pragma omp parallel for reduction( + : r )
+    for( int k = 0; k < n3; ++k )
+        r += a[k] * b[k];
+    return r;
+}
+
+static double dist_geodesic( int nos, const double * a, const double * b )
+{
+    double d = 0;
+#pragma omp parallel for reduction( + : d )
+    for( int i = 0; i < nos; ++i )
+    {
+        double r = dot3( a + 3 * i, b + 3 * i );
+        r        = fmax( -1.0, fmin( 1.0, r ) );
+        double ang = acos( r );
+        d += pow( ang, 2 );
+    }
+    return sqrt( d );
+}
+
+static void project_tangential( int nos, double * v, const double * s )
+{
+#pragma omp parallel for
+    for( int i = 0; i < nos; ++i )
+    {
+        double d = dot3( v + 3 * i, s + 3 * i );
+        for( int e = 0; e < 3; ++e )
+            v[3 * i + e] -= d * s[3 * i + e];
+    }
+}
+
+static void normalize_3n( int n3, double * v )
+{
+    double sc = 1.0 / sqrt( vdot( n3, v, v ) );
+    for( int k = 0; k < n3; ++k )
+        v[k] *= sc;
+}
+
+static void geodesic_tangent( int nos, double * t, const double * im_minus, const double * im_plus, const double * mid )
+{
+    const double ex[3] = { 1, 0, 0 }, ey[3] = { 0, 1, 0 };
+    const double epsilon = 1e-15;
+#pragma omp parallel for
+    for( int i = 0; i < nos; ++i )
+    {
+        double axis[3];
+        cross3( im_plus + 3 * i, im_minus + 3 * i, axis );
+        if( fabs( dot3( im_minus + 3 * i, im_plus + 3 * i ) + 1 ) < epsilon )
+        {
+            if( fabs( dot3( mid + 3 * i, ex ) - 1 ) > epsilon )
+                memcpy( axis, ex, sizeof( axis ) );
+            else
+                memcpy( axis, ey, sizeof( axis ) );
+        }
+        cross3( mid + 3 * i, axis, t + 3 * i );
+    }
+    normalize_3n( 3 * nos, t );
+}
+
+static void tangents( int nos, int noi, const double * chain, const double * energies, double * tang )
+{
+    size_t n3 = (size_t)3 * nos;
+    for( int img = 0; img < noi; ++img )
+    {
+        const double * im = chain + img * n3;
+        double * t        = tang + img * n3;
+        if( img == 0 )
+            geodesic_tangent( nos, t, im, chain + n3, im );
+        else if( img == noi - 1 )
+            geodesic_tangent( nos, t, chain + ( img - 1 ) * n3, im, im );
+        else
+        {
+            const double * ip = chain + ( img + 1 ) * n3;
+            const double * imn = chain + ( img - 1 ) * n3;
+            double Em = energies[img], Ep = energies[img + 1], En = energies[img - 1];
+            double cp = 0, cm = 0; /* coefficients of t_plus and t_minus */
+            if( ( Ep < Em && Em > En ) || ( Ep > Em && Em < En ) )
+            {
+                double Emax = fmax( fabs( Ep - Em ), fabs( En - Em ) );
+                double Emin = fmin( fabs( Ep - Em ), fabs( En - Em ) );
+                if( Ep > En )
+                {
+                    cp = Emax;
+                    cm = Emin;
+                }
+                else
+                {
+                    cp = Emin;
+                    cm = Emax;
+                }
+            }
+            else if( Ep > Em && Em > En )
+                cp = 1;
+            else if( Ep < Em && Em < En )
+                cm = 1;
+            else
+            {
+                cp = 1;
+                cm = 1;
+            }
+            for( size_t k = 0; k < n3; ++k )
+            {
+                double tp = ip[k] - im[k];
+                double tm = im[k] - imn[k];
+                if( cp != 0 && cm != 0 )
+                {
+                    double v = cp * tp;
+                    v += cm * tm;
+                    t[k] = v;
+                }
+                else if( cp != 0 )
+                    t[k] = cp * tp;
+                else
+                    t[k] = cm * tm;
+            }
+            project_tangential( nos, t, im );
+            normalize_3n( (int)n3, t );
+        }
+    }
+}
+
+int og_gneb_run(
+    og_system * s, const og_gneb_params * p, int noi, int n_iter, double * chain, const int * image_type,
+    double * energies, double * Rx, double * max_torque_out )
+{
+    int nos   = s->nos;
+    size_t n3 = (size_t)3 * nos;
+    double * F      = (double *)calloc( noi * n3, sizeof( double ) ); /* forces */
+    double * Fp     = (double *)calloc( noi * n3, sizeof( double ) ); /* forces_previous */
+    double * V      = (double *)calloc( noi * n3, sizeof( double ) );
+    double * Fg     = (double *)calloc( noi * n3, sizeof( double ) ); /* F_gradient */
+    double * Ft     = (double *)calloc( noi * n3, sizeof( double ) ); /* F_total */
+    double * T      = (double *)calloc( noi * n3, sizeof( double ) );
+    const double m  = 1.0;
+    double mt       = p->force_convergence + 1.0;
+    int it;
+    for( it = 0; it < n_iter && !( mt < p->force_convergence ); ++it )
+    {
+        memcpy( Fp, F, sizeof( double ) * noi * n3 );
+        /* Calculate_Force */
+        int aborted = 0;
+        for( int img = 0; img < noi; ++img )
+        {
+            double * g = Fg + img * n3;
+            energies[img] = og_gradient_and_energy( s, chain + img * n3, g );
+            for( size_t k = 0; k < n3; ++k )
+                g[k] *= -1;
+            if( img == 0 )
+                Rx[0] = 0;
+            else
+            {
+                Rx[img] = Rx[img - 1] + dist_geodesic( nos, chain + img * n3, chain + ( img - 1 ) * n3 );
+                if( Rx[img] - Rx[img - 1] < 1e-10 )
+                    aborted = 1;
+            }
+        }
+        if( aborted )
+            break;
+        tangents( nos, noi, chain, energies, T );
+        for( int img = 1; img < noi - 1; ++img )
+        {
+            double * g  = Fg + img * n3;
+            double * t  = T + img * n3;
+            double * ft = Ft + img * n3;
+            project_tangential( nos, g, chain + img * n3 );
+            if( image_type[img] == 1 )
+            {
+                double x = vdot( (int)n3, g, t );
+                for( size_t k = 0; k < n3; ++k )
+                    g[k] -= 2 * x * t[k];
+                memcpy( ft, g, sizeof( double ) * n3 );
+            }
+            else if( image_type[img] == 2 )
+                memcpy( ft, g, sizeof( double ) * n3 );
+            else if( image_type[img] == 0 )
+            {
+                double x = vdot( (int)n3, g, t );
+                for( size_t k = 0; k < n3; ++k )
+                    g[k] -= x * t[k];
+                double d = p->spring_constant * ( Rx[img + 1] - 2 * Rx[img] + Rx[img - 1] );
+                for( size_t k = 0; k < n3; ++k )
+                {
+                    double v = g[k];
+                    v += d * t[k];
+                    ft[k] = v;
+                }
+            }
+            else
+                memset( ft, 0, sizeof( double ) * n3 );
+            memcpy( F + img * n3, ft, sizeof( double ) * n3 );
+        }
+        /* Solver_VP::Iteration */
+        double proj = 0, fn2 = 0;
+        for( int img = 0; img < noi; ++img )
+        {
+            double * f  = F + img * n3;
+            double * fp = Fp + img * n3;
+            double * v  = V + img * n3;
+            for( size_t k = 0; k < n3; ++k )
+                v[k] += 0.5 / m * ( fp[k] + f[k] );
+            proj += vdot( (int)n3, v, f );
+            fn2 += vdot( (int)n3, f, f );
+        }
+        for( int img = 0; img < noi; ++img )
+        {
+            double * f  = F + img * n3;
+            double * v  = V + img * n3;
+            double * sp = chain + img * n3;
+            double ratio = proj / fn2;
+            if( proj <= 0 )
+                memset( v, 0, sizeof( double ) * n3 );
+            else
+                for( size_t k = 0; k < n3; ++k )
+                    v[k] = f[k] * ratio;
+            for( int i = 0; i < nos; ++i )
+            {
+                double c[3];
+                for( int e = 0; e < 3; ++e )
+                    c[e] = sp[3 * i + e] + p->dt * v[3 * i + e] + 0.5 / m * p->dt * f[3 * i + e];
+                normalize3( c );
+                memcpy( sp + 3 * i, c, sizeof( c ) );
+            }
+        }
+        /* Hook_Post_Iteration: max over images of max_i |P_perp F_total|; it also projects the
+         * stored forces onto the new tangent planes in place (Method_GNEB.cpp:428), which the VP
+         * solver then reuses as forces_previous */
+        mt = 0;
+        for( int img = 0; img < noi; ++img )
+        {
+            double * ft = Ft + img * n3;
+            project_tangential( nos, ft, chain + img * n3 );
+            project_tangential( nos, F + img * n3, chain + img * n3 );
+            double m2 = 0;
+            for( int i = 0; i < nos; ++i )
+            {
+                double n2 = dot3( ft + 3 * i, ft + 3 * i );
+                if( n2 > m2 )
+                    m2 = n2;
+            }
+            if( sqrt( m2 ) > mt )
+                mt = sqrt( m2 );
+        }
+    }
+    if( max_torque_out )
+        *max_torque_out = mt;
+    free( F );
+    free( Fp );
+    free( V );
+    free( Fg );
+    free( Ft );
+    free( T );
+    return it;
+}
+
+void og_gneb_image_types_auto( int noi, const double * E, int * type )
+{
+    for( int img = 1; img < noi - 1; ++img )
+    {
+        if( E[img - 1] < E[img] && E[img] > E[img + 1] )
+            type[img] = 1;
+        else if( E[img - 1] > E[img] && E[img] < E[img + 1] )
+            type[img] = 2;
+        else if( type[img] != 3 )
+            type[img] = 0;
+    }
+}
+
+/* Homogeneous_Rotation: core/src/utility/Configuration_Chain.cpp:28-75 (the antiparallel axis
+ * test there is always false, so the axis is e_y for antiparallel spins; restated as is) */
+void og_transition_homogeneous( int nos, int noi, double * chain, int idx_1, int idx_2 )
+{
+    size_t n3          = (size_t)3 * nos;
+    const double * s1  = chain + idx_1 * n3;
+    const double * s2  = chain + idx_2 * n3;
+    const double ex[3] = { 1, 0, 0 }, ey[3] = { 0, 1, 0 };
+    (void)noi;
+    for( int i = 0; i < nos; ++i )
+    {
+        double r = dot3( s1 + 3 * i, s2 + 3 * i );
+        r        = fmax( -1.0, fmin( 1.0, r ) );
+        double rot_angle = acos( r );
+        double axis[3];
+        cross3( s1 + 3 * i, s2 + 3 * i, axis );
+        normalize3( axis );
+        if( fabs( rot_angle - C_PI ) < 1e-4 )
+        {
+            if( fabs( dot3( s1 + 3 * i, ex ) ) - 1 > 1e-4 )
+                memcpy( axis, ex, sizeof( axis ) );
+            else
+                memcpy( axis, ey, sizeof( axis ) );
+        }
+        for( int img = idx_1 + 1; img < idx_2; ++img )
+        {
+            double * o = chain + img * n3 + 3 * i;
+            if( rot_angle > 1e-8 )
+            {
+                double angle = rot_angle * (double)( img - idx_1 ) / (double)( idx_2 - idx_1 );
+                rotate3( s1 + 3 * i, axis, angle, o );
+            }
+            else
+                memcpy( o, s1 + 3 * i, sizeof( double ) * 3 );
+        }
+    }
+}

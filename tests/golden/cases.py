@@ -1,0 +1,109 @@
+"""Golden cases: small systems whose reference outputs are committed as fixtures.
+
+Each case is a spec dictionary (spirit_gb300.configs) plus the operations run on it.  The
+fixtures were produced by make_golden.py from the reference's own code (Spirit v2.2.0 CPU
+build, FP64, OpenMP, kissFFT) and are read by the parity tests.  The cases cover the
+lattices and terms of the benchmark configurations at sizes that finish in seconds.
+"""
+
+SQ_C1 = dict(  # 64x64 plain-LLG configuration, shrunk: SC 2D, periodic, Neel DMI
+    bravais="sc", n_cells=[8, 8, 1], lattice_constant=1.0, mu_s=[2.0], bc=[1, 1, 0],
+    field=(1.0, (0, 0, 1)), anisotropy=(0.1, (0, 0, 1)), jij=[1.0], dij=[0.3], dm_chirality=2,
+    llg=dict(dt=1e-3, damping=0.3, temperature=0.0),
+)
+
+SC3D_DDI = dict(  # 128x128x16 dipolar configuration, shrunk: bulk DMI, open z, DDI FFT z-padded
+    bravais="sc", n_cells=[8, 8, 4], lattice_constant=4.0, mu_s=[2.0], bc=[1, 1, 0],
+    field=(0.5, (0, 0, 1)), anisotropy=(0.05, (0, 0, 1)), jij=[1.0], dij=[0.2], dm_chirality=1,
+    ddi=dict(method="fft", n_periodic_images=[4, 4, 0], radius=0.0, pb_zero_padding=0),
+    llg=dict(dt=5e-4, damping=0.1, temperature=0.0),
+)
+
+HEX2D = dict(  # triangular GNEB configuration, shrunk
+    bravais="hex2d60", n_cells=[12, 12, 1], lattice_constant=1.0, mu_s=[2.0], bc=[1, 1, 0],
+    field=(1.5, (0, 0, 1)), anisotropy=(0.08, (0, 0, 1)), jij=[1.0], dij=[0.35], dm_chirality=2,
+    llg=dict(dt=1e-3, damping=0.3, temperature=0.0),
+)
+
+OPEN2D_DDI = dict(  # adjoint configuration, shrunk: open square lattice, padded 2D DDI
+    bravais="sc", n_cells=[8, 8, 1], lattice_constant=1.0, mu_s=[2.0], bc=[0, 0, 0],
+    field=(0.8, (0, 0, 1)), anisotropy=(0.1, (0, 0, 1)), jij=[1.0], dij=[0.3], dm_chirality=2,
+    ddi=dict(method="fft", n_periodic_images=[4, 4, 4], radius=0.0, pb_zero_padding=1),
+    llg=dict(dt=1e-3, damping=0.3, temperature=0.0),
+)
+
+# reference test input core/test/input/physics_ddi.cfg: irregular 2-atom basis, DDI only
+DDI_IRREGULAR = dict(
+    bravais_vectors=[[3, 0, -1], [0, 1, 0], [0.3, -2, 1]], n_cells=[5, 5, 5],
+    basis=[[0, 0, 0], [0.5, 0.2, 0.7]], lattice_constant=2.77, mu_s=[2.17, 2.17], bc=[1, 0, 0],
+    field=(0.0, (0, 0, 1)), anisotropy=(0.0, (0, 0, 1)), pairs=[],
+    ddi=dict(method="fft", n_periodic_images=[4, 4, 4], radius=10.0, pb_zero_padding=1),
+)
+
+# periodic DDI with explicit zero padding on all periodic axes and several images
+PERIODIC_DDI = dict(
+    bravais="sc", n_cells=[6, 5, 3], lattice_constant=2.5, mu_s=[1.5], bc=[1, 1, 1],
+    field=(0.3, (0, 1, 1)), anisotropy=(0.2, (1, 0, 1)), jij=[1.0, -0.2], dij=[0.3, 0.1], dm_chirality=-1,
+    ddi=dict(method="fft", n_periodic_images=[2, 1, 3], radius=0.0, pb_zero_padding=0),
+)
+
+# reference test input core/test/input/fd_pairs.cfg: explicit pairs, open 2x2x1
+FD_PAIRS = dict(
+    bravais="sc", n_cells=[2, 2, 1], lattice_constant=1.0, mu_s=[2.0], bc=[0, 0, 0],
+    field=(25.0, (0, 0, 1)), anisotropy=(0.0, (0, 0, 1)),
+    pairs=[(0, 0, 1, 0, 0, 10.0, 6.0, 0.0, 0.0), (0, 0, 0, 1, 0, 10.0, 0.0, 6.0, 0.0),
+           (0, 0, 0, 0, 1, 10.0, 0.0, 0.0, 6.0)],
+)
+
+# reference test input core/test/input/solvers.cfg (16x16 SC, J=10, Bloch D=6, B=25 T)
+SOLVERS = dict(
+    bravais="sc", n_cells=[16, 16, 1], lattice_constant=1.0, mu_s=[2.0], bc=[1, 1, 0],
+    field=(25.0, (0, 0, 1)), anisotropy=(0.0, (0, 0, 1)), jij=[10.0], dij=[6.0], dm_chirality=1,
+    llg=dict(dt=1e-3, damping=0.3, temperature=0.0, force_convergence=1e-8),
+    gneb=dict(spring_constant=1.0, force_convergence=1e-6),
+)
+
+# neighbour-shell geometries (pair lists must be bit-exact)
+PAIR_GEOMETRIES = {
+    "sc3d_3shells": dict(bravais="sc", n_cells=[5, 5, 5], bc=[1, 1, 1], jij=[1.0, 0.5, 0.25], dij=[0.1, 0.2, 0.3],
+                         dm_chirality=1),
+    "sc2d_open": dict(bravais="sc", n_cells=[4, 3, 1], bc=[0, 0, 0], jij=[1.0, 0.5], dij=[0.3], dm_chirality=2),
+    "hex2d60_3shells": dict(bravais="hex2d60", n_cells=[6, 6, 1], bc=[1, 1, 0], jij=[1.0, 0.2, 0.1],
+                            dij=[0.35, 0.1], dm_chirality=2),
+    "hex2d120": dict(bravais="hex2d120", n_cells=[6, 6, 1], bc=[1, 1, 0], jij=[1.0], dij=[0.35],
+                     dm_chirality=-2),
+    "bcc_2shells": dict(bravais="bcc", n_cells=[4, 4, 4], bc=[1, 1, 1], jij=[1.0, 0.5], dij=[0.2],
+                        dm_chirality=1),
+    "fcc_2shells": dict(bravais="fcc", n_cells=[4, 4, 4], bc=[1, 1, 1], jij=[1.0, 0.5], dij=[0.2],
+                        dm_chirality=-1),
+    "irregular_2basis": dict(bravais_vectors=[[3, 0, -1], [0, 1, 0], [0.3, -2, 1]], n_cells=[5, 5, 5],
+                             basis=[[0, 0, 0], [0.5, 0.2, 0.7]], lattice_constant=2.77, mu_s=[2.17, 2.17],
+                             bc=[1, 0, 0], jij=[1.0, 0.5], dij=[0.3], dm_chirality=1),
+    "chain1d": dict(bravais="sc", n_cells=[7, 1, 1], bc=[1, 0, 0], jij=[1.0, 0.3], dij=[0.2], dm_chirality=1),
+    "lattice_const_hex": dict(bravais="hex2d", n_cells=[5, 4, 2], lattice_constant=2.5, bc=[1, 1, 0],
+                              jij=[1.0, 0.5], dij=[0.2], dm_chirality=2),
+}
+
+GRAD_CASES = {
+    "sq_c1": SQ_C1,
+    "sc3d_ddi": SC3D_DDI,
+    "hex2d": HEX2D,
+    "open2d_ddi": OPEN2D_DDI,
+    "ddi_irregular": DDI_IRREGULAR,
+    "periodic_ddi": PERIODIC_DDI,
+    "fd_pairs": FD_PAIRS,
+}
+
+# (case, solver name, solver id, iterations)
+LLG_CASES = [
+    ("sq_c1", "Depondt", 2, 200),
+    ("sq_c1", "Heun", 3, 200),
+    ("sq_c1", "SIB", 1, 200),
+    ("sq_c1", "RK4", 4, 200),
+    ("sc3d_ddi", "Heun", 3, 50),
+    ("open2d_ddi", "RK4", 4, 50),
+    ("hex2d", "SIB", 1, 100),
+]
+
+SPIN_SEED = {"sq_c1": 11, "sc3d_ddi": 12, "hex2d": 13, "open2d_ddi": 14, "ddi_irregular": 15,
+             "periodic_ddi": 16, "fd_pairs": 17}

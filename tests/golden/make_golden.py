@@ -1,0 +1,152 @@
+"""Generate the golden fixtures in tests/golden/ from the reference's own code.
+
+Runs oracle/_ref/golden_harness (the reference, Spirit v2.2.0, CPU/OpenMP FP64 with kissFFT,
+compiled from its sources by oracle/ref/Makefile) on the cases of cases.py, with input spins
+generated here from fixed seeds and injected through System_Get_Spin_Directions, and packs
+its outputs into small .npz files.  Needs the reference sources (only in the build
+container); the fixtures it writes are committed and the tests read only those.
+
+    make -C oracle/ref -j8 && python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+from cases import GRAD_CASES, LLG_CASES, PAIR_GEOMETRIES, SOLVERS, SPIN_SEED  # noqa: E402
+from oracle.oracle import OracleSystem, random_spins, transition_homogeneous  # noqa: E402
+from spirit_gb300.configs import config_text, write_config  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "golden_harness")
+
+
+def run(args, cwd):
+    r = subprocess.run([HARNESS] + args, cwd=cwd, capture_output=True, text=True,
+                       env=dict(os.environ, OMP_NUM_THREADS="4"))
+    if r.returncode != 0:
+        raise RuntimeError("harness failed: %s\n%s" % (args, r.stderr[-2000:]))
+
+
+def load_bin(path, shape=None):
+    a = np.fromfile(path, dtype=np.float64)
+    return a.reshape(shape) if shape is not None else a
+
+
+def load_kv(path):
+    out = {}
+    for line in open(path):
+        k, v = line.split()[:2]
+        out[k] = float(v)
+    return out
+
+
+def nos_of(spec):
+    n = spec["n_cells"]
+    return n[0] * n[1] * n[2] * len(spec.get("basis", [[0, 0, 0]]))
+
+
+def main():
+    tmp = tempfile.mkdtemp(prefix="golden_")
+    out = {}
+    # --- neighbour / DMI pair lists
+    for name, spec in PAIR_GEOMETRIES.items():
+        cfg = write_config(spec, os.path.join(tmp, name + ".cfg"))
+        run(["pairs", cfg, os.path.join(tmp, name)], tmp)
+        ex = np.loadtxt(os.path.join(tmp, name + "_exchange.txt"), ndmin=2)
+        dm = np.loadtxt(os.path.join(tmp, name + "_dmi.txt"), ndmin=2)
+        np.savez_compressed(
+            os.path.join(HERE, "pairs_%s.npz" % name), config=config_text(spec),
+            exchange_pairs=ex[:, :5].astype(np.int32), exchange_magnitudes=ex[:, 5],
+            dmi_pairs=dm[:, :5].astype(np.int32), dmi_magnitudes=dm[:, 5], dmi_normals=dm[:, 6:9],
+            positions=load_bin(os.path.join(tmp, name + "_positions.bin"), (-1, 3)),
+        )
+        out[name] = (len(ex), len(dm))
+    # --- gradients and energies
+    for name, spec in GRAD_CASES.items():
+        cfg = write_config(spec, os.path.join(tmp, name + ".cfg"))
+        nos = nos_of(spec)
+        spins = random_spins(nos, SPIN_SEED[name])
+        sp = os.path.join(tmp, name + "_spins.bin")
+        spins.tofile(sp)
+        run(["grad", cfg, sp, os.path.join(tmp, name)], tmp)
+        E = load_kv(os.path.join(tmp, name + "_energy.txt"))
+        terms = {k: v for k, v in E.items() if k not in ("grad_and_energy", "total")}
+        per_spin = {"energy_" + k: load_bin(os.path.join(tmp, "%s_energy_%s.bin" % (name, k))) for k in terms}
+        extra = {}
+        if spec.get("ddi"):
+            run(["direct", cfg, sp, os.path.join(tmp, name + "_direct")], tmp)
+            extra["gradient_direct"] = load_bin(os.path.join(tmp, name + "_direct_gradient.bin"), (-1, 3))
+            Ed = load_kv(os.path.join(tmp, name + "_direct_energy.txt"))
+            extra["energy_direct"] = Ed["total"]
+        np.savez_compressed(
+            os.path.join(HERE, "grad_%s.npz" % name), config=config_text(spec), spins=spins,
+            gradient=load_bin(os.path.join(tmp, name + "_gradient.bin"), (-1, 3)),
+            gradient_ge=load_bin(os.path.join(tmp, name + "_grad_and_energy_gradient.bin"), (-1, 3)),
+            energy_ge=E["grad_and_energy"], energy_total=E["total"],
+            term_names=np.array(list(terms.keys())), term_energies=np.array(list(terms.values())),
+            **per_spin, **extra,
+        )
+        out[name] = E["total"]
+    # --- LLG trajectories (T = 0)
+    for case, sname, sid, n_iter in LLG_CASES:
+        spec = GRAD_CASES[case]
+        cfg = write_config(spec, os.path.join(tmp, case + ".cfg"))
+        nos = nos_of(spec)
+        spins = random_spins(nos, SPIN_SEED[case] + 100)
+        sp = os.path.join(tmp, case + "_llg_spins.bin")
+        spins.tofile(sp)
+        tag = os.path.join(tmp, "llg_%s_%s" % (case, sname))
+        run(["llg", cfg, sp, tag, str(sid), str(n_iter)], tmp)
+        res = load_kv(tag + "_result.txt")
+        np.savez_compressed(
+            os.path.join(HERE, "llg_%s_%s.npz" % (case, sname)), config=config_text(spec), spins_in=spins,
+            spins_out=load_bin(tag + "_spins.bin", (-1, 3)), solver=sid, n_iter=n_iter,
+            energy=res["energy_image"], max_torque=res["max_torque"], iterations=int(res["iterations"]),
+        )
+        out["llg_%s_%s" % (case, sname)] = res
+    # --- GNEB (VP) on the reference solver-test system: skyrmion collapse, 9 images
+    spec = SOLVERS
+    cfg = write_config(spec, os.path.join(tmp, "solvers.cfg"))
+    nos = nos_of(spec)
+    noi = 9
+    o = OracleSystem(spec)
+    pos = o.positions()
+    centre = pos.mean(axis=0)
+    r = np.linalg.norm(pos[:, :2] - centre[:2], axis=1)
+    theta = np.pi * np.clip(1 - r / 5.0, 0, 1)  # linear-profile skyrmion of radius 5
+    phi = np.arctan2(pos[:, 1] - centre[1], pos[:, 0] - centre[0]) + np.pi / 2  # Bloch helicity
+    sk = np.stack([np.sin(theta) * np.cos(phi), np.sin(theta) * np.sin(phi), np.cos(theta)], axis=1)
+    chain = np.zeros((noi, nos, 3))
+    chain[0] = sk
+    chain[-1] = np.array([0, 0, 1.0])
+    chain = transition_homogeneous(chain, 0, noi - 1)
+    cp = os.path.join(tmp, "chain.bin")
+    chain.tofile(cp)
+    # VP with a chain-global velocity projection switches branches on rounding-level differences,
+    # so step-by-step parity is pinned over a short run; the converged run pins the saddle.
+    for tag_name, n1, n2 in (("gneb_vp", 20, 0), ("gneb_vp_ci", 20, 20), ("gneb_converged", 20000, 200000)):
+        tag = os.path.join(tmp, tag_name)
+        run(["gneb", cfg, cp, tag, str(noi), "0", str(n1), str(n2)], tmp)
+        rows = [l.split() for l in open(tag + "_result.txt")]
+        img = [r_ for r_ in rows if r_[0] == "image"]
+        np.savez_compressed(
+            os.path.join(HERE, "%s.npz" % tag_name), config=config_text(spec), chain_in=chain,
+            chain_out=load_bin(tag + "_chain.bin", (noi, nos, 3)),
+            energies=np.array([float(r_[3]) for r_ in img]), Rx=np.array([float(r_[5]) for r_ in img]),
+            image_type=np.array([int(r_[7]) for r_ in img]), n_iter=n1, n_iter_ci=n2,
+            max_torque=float([r_ for r_ in rows if r_[0] == "max_torque"][0][1]),
+        )
+        out[tag_name] = [float(r_[3]) for r_ in img]
+    for k, v in out.items():
+        print(k, v)
+
+
+if __name__ == "__main__":
+    main()
