@@ -1,0 +1,99 @@
+// Shared host/device definitions of the GB300 spin-dynamics engine.
+//
+// Device data layout (HBM): a "batch" holds any number of independent spin systems
+// (ensemble members, parameter sweeps, GNEB images).  Spins are stored structure-of-arrays,
+// one component array per direction (x[], y[], z[]), each system occupying the range
+// [spin_offset, spin_offset + nos) of every component array; spin_offset is a multiple of
+// 32 so every system starts on a 128-byte boundary.  Inside a system the spin index is the
+// reference's ispin = ib + nb * (a + Na * (b + Nb * c)) (core/include/engine/Vectormath.hpp:61-74).
+#pragma once
+#include <cstdint>
+
+namespace sg
+{
+
+constexpr int MAX_BASIS        = 8;
+constexpr int MAX_PAIRS        = 96; // merged exchange+DMI pairs over all basis atoms of one system
+constexpr int SPIN_ALIGN       = 32;
+constexpr int MAX_FFT_LEN      = 1024;
+
+// LLG solver ids (core/include/Spirit/Simulation.h): VP=0, SIB=1, Depondt=2, Heun=3, RK4=4
+enum Solver : int
+{
+    SOLVER_VP      = 0,
+    SOLVER_SIB     = 1,
+    SOLVER_DEPONDT = 2,
+    SOLVER_HEUN    = 3,
+    SOLVER_RK4     = 4,
+};
+
+// One interaction pair of basis atom i with atom j in the cell translated by (da, db, dc).
+// Exchange (J) and DMI (D * normal) pairs with the same (i, j, t) are merged:
+//   g_i -= J s_j + s_j x Dvec        (Hamiltonian_Heisenberg.cpp:822-864)
+struct PairEntry
+{
+    int i, j, da, db, dc;
+    double J;
+    double D[3];
+};
+
+// Per-system constants.  Read by every kernel; double so the FP64 path loses nothing.
+struct SysDesc
+{
+    int n_cells[3];
+    int nb;
+    int nos;
+    int bc[3];
+    long long spin_offset; // into the batch's component arrays
+    int pair_begin[MAX_BASIS + 1]; // pairs of basis atom ib: [pair_begin[ib], pair_begin[ib+1]) in pairs[]
+    int n_pairs;
+    int max_t[3]; // largest |translation| along each axis (stencil halo)
+    PairEntry pairs[MAX_PAIRS];
+    double mu_s[MAX_BASIS];
+    double zeeman[3];           // mu_B * B * normal: Zeeman gradient is -mu_s * zeeman
+    int has_zeeman;
+    int n_aniso;                // uniaxial anisotropy entries (one per basis atom at most)
+    int aniso_idx[MAX_BASIS];
+    double aniso_K[MAX_BASIS];
+    double aniso_n[MAX_BASIS][3];
+    // LLG
+    double dt, damping, temperature;
+    int direct_minimization;
+    double force_convergence;
+    unsigned long long seed;
+    unsigned int stream;
+    int n_iterations;
+    // DDI
+    int ddi;                    // 0 none, 1 FFT
+    int fft_slot;               // index into the batch's FFT plan table
+};
+
+// Mutable per-system run state on the device.  Written only by the last block of the last
+// kernel of a step (or of the probe kernel), read by every block of the following kernels.
+struct SysRun
+{
+    int iteration;      // completed iterations
+    int active;         // 1 while the method keeps iterating this system
+    float max_torque;   // last max |P_perp fv| (Hook_Post_Iteration)
+    unsigned int torque_bits; // running max of |t|^2 as float bits (non-negative floats order like uints)
+    unsigned int blocks_done; // last-block detection counter
+    double energy;      // energy of the last force evaluation (Spin_System::E)
+    double energy_acc;  // running sum of the current evaluation
+    double reserved;
+};
+
+// FFT plan of one system's dipolar convolution.  Padded extents M[d] = N[d] or 2 N[d]
+// (Hamiltonian_Heisenberg.cpp:1510-1518); the real-to-complex axis is a (half length Ma/2+1).
+struct FFTDesc
+{
+    int N[3];      // original cells per axis
+    int M[3];      // padded FFT extents
+    int Mh;        // M[0] / 2 + 1
+    int nb;        // basis atoms
+    long long spec_offset;   // complex element offset of this system's spectrum work arrays
+    long long dhat_offset;   // complex element offset of its dipole spectrum
+    long long tw_offset[3];  // twiddle table offsets (one table of M[d] entries per axis)
+    int radix[3][12];        // radix sequence per axis (0-terminated)
+};
+
+} // namespace sg

@@ -1,0 +1,69 @@
+// Dipolar FFT plan for a batch of systems (see fft.cuh / ddi.cu).
+#pragma once
+#include "common.hpp"
+
+#include <cuda_runtime.h>
+
+#include <array>
+#include <vector>
+
+namespace sg
+{
+
+struct DDISystem
+{
+    int sys; // index of the system in the batch
+    std::array<int, 3> n_cells;
+    std::array<int, 3> padded;
+    std::array<int, 3> bc;
+    std::array<int, 3> images;
+    int nb;
+    double lattice_constant;
+    std::array<std::array<double, 3>, 3> bravais;
+    std::vector<std::array<double, 3>> cell_atoms;
+};
+
+class DDIPlan
+{
+public:
+    ~DDIPlan();
+    void build( const std::vector<DDISystem> & systems, bool fp64, const SysDesc * d_sd, cudaStream_t stream );
+    // h = D * (mu s) for every DDI system of the batch whose SysRun is active (runs may be null)
+    void run( const SysDesc * d_sd, const SysRun * runs, const void * sx, const void * sy, const void * sz,
+              void * hx, void * hy, void * hz, cudaStream_t stream ) const;
+    void release();
+    int n_sys = 0;
+    bool fp64 = false;
+
+    // device tables (public for the pass launchers)
+    FFTDesc * d_fd = nullptr;
+    void * d_tw    = nullptr;
+    void * d_W1    = nullptr;
+    void * d_W2    = nullptr;
+    void * d_Dhat  = nullptr;
+    int4 * d_blocks[5] = { nullptr, nullptr, nullptr, nullptr, nullptr };
+    int n_blocks[5]    = { 0, 0, 0, 0, 0 };
+    size_t max_smem_a = 0, max_smem_b = 0, max_smem_c = 0;
+    long long spec_elems = 0;
+    std::vector<FFTDesc> fd_host;
+    std::vector<int> sys_index;
+
+private:
+    void build_block_tables( const std::vector<DDISystem> & systems );
+    void compute_dhat( const std::vector<DDISystem> & systems, const SysDesc * d_sd, cudaStream_t stream );
+    template<typename R>
+    void run_t( const SysDesc * d_sd, const SysRun * runs, const R * sx, const R * sy, const R * sz, R * hx, R * hy,
+                R * hz, cudaStream_t stream ) const;
+};
+
+// Padded FFT extent per axis (Prepare_DDI, Hamiltonian_Heisenberg.cpp:1510-1518): doubled when the
+// axis has more than one cell and is open or explicitly zero-padded.
+inline std::array<int, 3> ddi_padding( const std::array<int, 3> & n, const std::array<int, 3> & bc, bool pb_zero_padding )
+{
+    std::array<int, 3> m;
+    for( int d = 0; d < 3; ++d )
+        m[d] = ( n[d] > 1 && ( bc[d] == 0 || pb_zero_padding ) ) ? 2 * n[d] : n[d];
+    return m;
+}
+
+} // namespace sg

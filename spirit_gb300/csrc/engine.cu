@@ -1,0 +1,865 @@
+// Fused field + LLG stage kernels for a batch of spin systems (sm_103a).
+//
+// One launch per integrator stage evaluates, for every spin of every active system of the
+// batch: the Heisenberg gradient at the stage configuration (anisotropy, merged exchange +
+// DMI pair stencil, dipolar field from the FFT pipeline, Zeeman), the LLG virtual force with
+// in-kernel Philox thermal noise, and the solver's update -- reading each spin once per stage.
+// The last stage also reduces the FP64 energy of the evaluated configuration and the maximum
+// torque |P_perp(s_new) fv_1| per system; the last block of each system finalises the
+// iteration counter and the convergence flag on the device, so a whole step sequence can be
+// captured in a CUDA graph and replayed without host round trips.
+//
+// Reference algorithms (file:line in Spirit v2.2.0):
+//   gradient terms        core/src/engine/Hamiltonian_Heisenberg.cpp:704-864
+//   virtual force         core/src/engine/Method_LLG.cpp:132-226
+//   thermal field         core/src/engine/Method_LLG.cpp:65-110 (Philox stream instead of mt19937)
+//   SIB                   core/include/engine/Solver_SIB.hpp:21-50, core/src/engine/Solver_Kernels.cpp:15-48
+//   Depondt               core/include/engine/Solver_Depondt.hpp:28-77, Vectormath.cpp:474-485
+//   Heun                  core/include/engine/Solver_Heun.hpp:29-80
+//   RK4                   core/include/engine/Solver_RK4.hpp:40-147
+//   max torque            core/include/engine/Method_Solver.hpp:225-230, Method_LLG.cpp:247-301
+#include "engine.hpp"
+#include "kernels.cuh"
+#include "util.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace sg
+{
+
+// ------------------------------------------------------------------ stage kernel
+template<typename R>
+struct StageArgs
+{
+    const SysDesc * sd;
+    SysRun * runs;
+    const int2 * blkmap;  // (system, first local spin)
+    const int * blkcount; // blocks per system
+    SoA3<R> s;            // state
+    SoA3<R> cfg;          // stage configuration (neighbour reads)
+    SoA3<R> out;          // predictor output
+    SoA3<R> aux1;         // fv of stage 1
+    SoA3<R> aux2;         // RK4 running sum
+    SoA3<R> h;            // dipolar field of cfg (x == nullptr: none)
+};
+
+enum
+{
+    ST_PROBE = 0
+};
+
+// SOLVER / STAGE are compile-time; STAGE 0 is the constructor probe (initial torque + energy).
+template<typename R, int SOLVER, int STAGE>
+__global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
+{
+    __shared__ PairR<R> pairs[MAX_PAIRS];
+    __shared__ double red_d[32];
+    __shared__ float red_f[32];
+    __shared__ int is_last;
+    const int2 bm = A.blkmap[blockIdx.x];
+    const int s   = bm.x;
+    SysRun * run  = A.runs + s;
+    if( !run->active )
+        return;
+    const SysDesc & d = A.sd[s];
+    for( int p = threadIdx.x; p < d.n_pairs; p += blockDim.x )
+    {
+        const PairEntry & q = d.pairs[p];
+        pairs[p]            = { q.j, q.da, q.db, q.dc, (R)q.J, (R)q.D[0], (R)q.D[1], (R)q.D[2] };
+    }
+    __syncthreads();
+    constexpr bool FINAL = ( SOLVER == SOLVER_RK4 ) ? ( STAGE == 4 ) : ( STAGE == 2 );
+    constexpr bool PROBE = STAGE == ST_PROBE;
+    const int iteration  = run->iteration;
+    const int i          = bm.y + threadIdx.x; // local spin index
+    const bool valid     = i < d.nos;
+    double e             = 0;
+    float t2             = 0;
+    if( valid )
+    {
+        const long long gi = d.spin_offset + i;
+        const int nb       = d.nb;
+        const int cell     = i / nb;
+        const int ib       = i - cell * nb;
+        const int a        = cell % d.n_cells[0];
+        const int rest     = cell / d.n_cells[0];
+        const int b        = rest % d.n_cells[1];
+        const int c        = rest / d.n_cells[1];
+        const R mu         = (R)d.mu_s[ib];
+        const V3<R> ci     = A.cfg.ld( gi );
+        V3<R> g            = gradient_at<R>( d, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu, e );
+        const bool thermal = d.temperature > 0 && !d.direct_minimization;
+        V3<R> xi           = { 0, 0, 0 };
+        if( thermal )
+        {
+            const double eps = sqrt( 2 * d.damping * d.dt * C_GAMMA / C_MU_B * C_K_B ) / ( 1 + d.damping * d.damping );
+            R sc             = (R)( eps * sqrt( d.temperature / d.mu_s[ib] ) );
+            V3<R> z          = gauss3<R>( d.seed, d.stream, PROBE ? 0xFFFFFFFFu : (unsigned int)iteration, (unsigned int)i );
+            xi               = { sc * z.x, sc * z.y, sc * z.z };
+        }
+        V3<R> fv = virtual_force<R>( d, ci, g, mu, xi, thermal, d.direct_minimization != 0 );
+        if( PROBE )
+        {
+            t2 = (float)torque2( fv, ci );
+        }
+        else if( SOLVER == SOLVER_SIB )
+        {
+            const V3<R> si = ( STAGE == 1 ) ? ci : A.s.ld( gi );
+            if( STAGE == 1 )
+            {
+                V3<R> p = sib( si, fv );
+                p.x += si.x;
+                p.y += si.y;
+                p.z += si.z;
+                p.x *= R( 0.5 );
+                p.y *= R( 0.5 );
+                p.z *= R( 0.5 );
+                A.out.st( gi, p );
+                A.aux1.st( gi, fv );
+            }
+            else
+            {
+                V3<R> sn = sib( si, fv );
+                A.s.st( gi, sn );
+                t2 = (float)torque2( A.aux1.ld( gi ), sn );
+            }
+        }
+        else if( SOLVER == SOLVER_HEUN )
+        {
+            if( STAGE == 1 )
+            {
+                V3<R> cr = cross( ci, fv );
+                V3<R> p  = { ci.x + R( -1 ) * cr.x, ci.y + R( -1 ) * cr.y, ci.z + R( -1 ) * cr.z };
+                A.out.st( gi, normalized( p ) );
+                A.aux1.st( gi, fv );
+            }
+            else
+            {
+                const V3<R> si  = A.s.ld( gi );
+                const V3<R> fv1 = A.aux1.ld( gi );
+                V3<R> c1        = cross( si, fv1 );
+                V3<R> t1        = { R( -1 ) * c1.x, R( -1 ) * c1.y, R( -1 ) * c1.z };
+                V3<R> c2        = cross( ci, fv );
+                V3<R> t         = { t1.x * R( 0.5 ), t1.y * R( 0.5 ), t1.z * R( 0.5 ) };
+                t.x += si.x;
+                t.y += si.y;
+                t.z += si.z;
+                t.x += R( 0.5 ) * ( R( -1 ) * c2.x );
+                t.y += R( 0.5 ) * ( R( -1 ) * c2.y );
+                t.z += R( 0.5 ) * ( R( -1 ) * c2.z );
+                V3<R> sn = normalized( t );
+                A.s.st( gi, sn );
+                t2 = (float)torque2( fv1, sn );
+            }
+        }
+        else if( SOLVER == SOLVER_DEPONDT )
+        {
+            if( STAGE == 1 )
+            {
+                R ang    = sqrt( dot( fv, fv ) );
+                V3<R> ax = normalized( fv );
+                A.out.st( gi, rotate( ci, ax, ang ) );
+                A.aux1.st( gi, fv );
+            }
+            else
+            {
+                const V3<R> si  = A.s.ld( gi );
+                const V3<R> fv1 = A.aux1.ld( gi );
+                V3<R> ax        = { R( 0.5 ) * fv1.x, R( 0.5 ) * fv1.y, R( 0.5 ) * fv1.z };
+                ax.x += R( 0.5 ) * fv.x;
+                ax.y += R( 0.5 ) * fv.y;
+                ax.z += R( 0.5 ) * fv.z;
+                R ang    = sqrt( dot( ax, ax ) );
+                V3<R> sn = rotate( si, normalized( ax ), ang );
+                A.s.st( gi, sn );
+                t2 = (float)torque2( fv1, sn );
+            }
+        }
+        else if( SOLVER == SOLVER_RK4 )
+        {
+            // k_m = -(cfg_m x fv_m); cfg_{m+1} = normalize(s + w k_m); running sum acc = s + k1/6 + k2/3 + ...
+            V3<R> cr = cross( ci, fv );
+            V3<R> k  = { R( -1 ) * cr.x, R( -1 ) * cr.y, R( -1 ) * cr.z };
+            const V3<R> si = ( STAGE == 1 ) ? ci : A.s.ld( gi );
+            if( STAGE == 1 )
+            {
+                A.aux1.st( gi, fv );
+                V3<R> acc = si;
+                R w6      = R( 1.0 / 6.0 );
+                acc.x += w6 * k.x;
+                acc.y += w6 * k.y;
+                acc.z += w6 * k.z;
+                A.aux2.st( gi, acc );
+                V3<R> p = { si.x + R( 0.5 ) * k.x, si.y + R( 0.5 ) * k.y, si.z + R( 0.5 ) * k.z };
+                A.out.st( gi, normalized( p ) );
+            }
+            else if( STAGE == 2 || STAGE == 3 )
+            {
+                V3<R> acc = A.aux2.ld( gi );
+                R w3      = R( 1.0 / 3.0 );
+                acc.x += w3 * k.x;
+                acc.y += w3 * k.y;
+                acc.z += w3 * k.z;
+                A.aux2.st( gi, acc );
+                R wn    = STAGE == 2 ? R( 0.5 ) : R( 1 );
+                V3<R> p = { si.x + wn * k.x, si.y + wn * k.y, si.z + wn * k.z };
+                A.out.st( gi, normalized( p ) );
+            }
+            else
+            {
+                V3<R> acc = A.aux2.ld( gi );
+                R w6      = R( 1.0 / 6.0 );
+                acc.x += w6 * k.x;
+                acc.y += w6 * k.y;
+                acc.z += w6 * k.z;
+                V3<R> sn = normalized( acc );
+                A.s.st( gi, sn );
+                t2 = (float)torque2( A.aux1.ld( gi ), sn );
+            }
+        }
+    }
+    if( !( FINAL || PROBE ) )
+        return;
+    // energy of the evaluated configuration and max torque of the step, per system
+    double es = block_sum( e, red_d );
+    float tm  = block_max( t2, red_f );
+    if( threadIdx.x == 0 )
+    {
+        atomicAdd( &run->energy_acc, es );
+        atomicMax( &run->torque_bits, __float_as_uint( tm ) );
+        __threadfence();
+        unsigned int prev = atomicAdd( &run->blocks_done, 1u );
+        is_last           = ( prev == (unsigned int)A.blkcount[s] - 1 );
+    }
+    __syncthreads();
+    if( is_last && threadIdx.x == 0 )
+    {
+        __threadfence();
+        volatile SysRun * vr = run;
+        float mt             = sqrtf( __uint_as_float( vr->torque_bits ) );
+        vr->max_torque       = mt;
+        vr->energy           = vr->energy_acc;
+        vr->energy_acc       = 0;
+        vr->torque_bits      = 0;
+        vr->blocks_done      = 0;
+        int it               = vr->iteration + ( PROBE ? 0 : 1 );
+        vr->iteration        = it;
+        vr->active           = ( it < d.n_iterations ) && !( mt < (float)d.force_convergence );
+    }
+}
+
+// ------------------------------------------------------------------ evaluation kernel
+// gradient (AoS double out), per-term energy sums (5 doubles per system) and optional per-spin
+// per-term energies.  Used by the API getters and the parity tests.
+template<typename R>
+__global__ void __launch_bounds__( 256 ) eval_kernel( const SysDesc * sd, const int2 * blkmap, SoA3<R> spins,
+                                                      SoA3<R> h, int only_sys, double * grad, double * term_sums,
+                                                      double * per_spin )
+{
+    __shared__ PairR<R> pairs[MAX_PAIRS];
+    __shared__ double red[32];
+    const int2 bm = blkmap[blockIdx.x];
+    const int s   = bm.x;
+    if( s != only_sys )
+        return;
+    const SysDesc & d = sd[s];
+    for( int p = threadIdx.x; p < d.n_pairs; p += blockDim.x )
+    {
+        const PairEntry & q = d.pairs[p];
+        pairs[p]            = { q.j, q.da, q.db, q.dc, (R)q.J, (R)q.D[0], (R)q.D[1], (R)q.D[2] };
+    }
+    __syncthreads();
+    const int i      = bm.y + threadIdx.x;
+    double et[N_TERMS] = { 0, 0, 0, 0, 0 };
+    if( i < d.nos )
+    {
+        const long long gi = d.spin_offset + i;
+        const int nb = d.nb, cell = i / nb, ib = i - cell * nb;
+        const int a = cell % d.n_cells[0], rest = cell / d.n_cells[0];
+        const int b = rest % d.n_cells[1], c = rest / d.n_cells[1];
+        const R mu      = (R)d.mu_s[ib];
+        const V3<R> si  = spins.ld( gi );
+        double e        = 0;
+        V3<R> g         = gradient_at<R>( d, pairs, spins, h, gi, ib, a, b, c, si, mu, e );
+        grad[3 * (size_t)i + 0] = g.x;
+        grad[3 * (size_t)i + 1] = g.y;
+        grad[3 * (size_t)i + 2] = g.z;
+        // per-term energies (E_Zeeman, E_Anisotropy, E_Exchange, E_DMI, E_DDI; cpp:307-511)
+        if( d.has_zeeman )
+            et[TERM_ZEEMAN] = -(double)mu * ( d.zeeman[0] * si.x + d.zeeman[1] * si.y + d.zeeman[2] * si.z );
+        for( int k = 0; k < d.n_aniso; ++k )
+            if( d.aniso_idx[k] == ib )
+            {
+                double dd = d.aniso_n[k][0] * si.x + d.aniso_n[k][1] * si.y + d.aniso_n[k][2] * si.z;
+                et[TERM_ANISOTROPY] -= d.aniso_K[k] * dd * dd;
+            }
+        for( int p = d.pair_begin[ib]; p < d.pair_begin[ib + 1]; ++p )
+        {
+            const PairR<R> P = pairs[p];
+            long long j      = pair_index( d, a, b, c, P.j, P.da, P.db, P.dc );
+            if( j >= 0 )
+            {
+                V3<R> sj = spins.ld( j );
+                et[TERM_EXCHANGE] -= 0.5 * (double)P.J * ( (double)si.x * sj.x + (double)si.y * sj.y + (double)si.z * sj.z );
+                V3<R> cr = cross( si, sj );
+                et[TERM_DMI] -= 0.5 * ( (double)P.Dx * cr.x + (double)P.Dy * cr.y + (double)P.Dz * cr.z );
+            }
+        }
+        if( h.x )
+        {
+            V3<R> hh      = h.ld( gi );
+            et[TERM_DDI]  = -0.5 * (double)mu * ( (double)hh.x * si.x + (double)hh.y * si.y + (double)hh.z * si.z );
+        }
+        if( per_spin )
+            for( int t = 0; t < N_TERMS; ++t )
+                per_spin[(size_t)t * d.nos + i] = et[t];
+    }
+    for( int t = 0; t < N_TERMS; ++t )
+    {
+        double v = block_sum( et[t], red );
+        if( threadIdx.x == 0 )
+            atomicAdd( &term_sums[t], v );
+    }
+}
+
+// ------------------------------------------------------------------ transfers
+template<typename R>
+__global__ void aos_to_soa( const double * aos, SoA3<R> dst, long long off, int n )
+{
+    for( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+        dst.st( off + i, V3<R>{ (R)aos[3 * (size_t)i], (R)aos[3 * (size_t)i + 1], (R)aos[3 * (size_t)i + 2] } );
+}
+template<typename R>
+__global__ void soa_to_aos( SoA3<R> src, long long off, int n, double * aos )
+{
+    for( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+    {
+        V3<R> v                  = src.ld( off + i );
+        aos[3 * (size_t)i]       = v.x;
+        aos[3 * (size_t)i + 1]   = v.y;
+        aos[3 * (size_t)i + 2]   = v.z;
+    }
+}
+
+// ================================================================== host
+static void fill_desc( SysDesc & d, const SystemInput & in )
+{
+    const Geometry & g        = *in.geom;
+    const HamiltonianParams & h = *in.ham;
+    for( int e = 0; e < 3; ++e )
+    {
+        d.n_cells[e] = g.n_cells[e];
+        d.bc[e]      = h.bc[e] ? 1 : 0;
+    }
+    d.nb  = g.nb();
+    d.nos = g.nos();
+    if( d.nb > MAX_BASIS )
+        throw std::runtime_error( "too many basis atoms for the device engine" );
+    for( int b = 0; b < d.nb; ++b )
+        d.mu_s[b] = g.mu_s_basis[b];
+    // Zeeman: stored times mu_B (Hamiltonian_Heisenberg.cpp:35); active if |B mu_B| > 1e-60 (cpp:205)
+    double Bm    = h.B * C_MU_B;
+    d.has_zeeman = std::abs( Bm ) > 1e-60;
+    for( int e = 0; e < 3; ++e )
+        d.zeeman[e] = h.B_normal[e] * Bm;
+    d.n_aniso = (int)h.aniso_idx.size();
+    if( d.n_aniso > MAX_BASIS )
+        throw std::runtime_error( "too many anisotropy entries" );
+    for( int k = 0; k < d.n_aniso; ++k )
+    {
+        d.aniso_idx[k] = h.aniso_idx[k];
+        d.aniso_K[k]   = h.aniso_K[k];
+        for( int e = 0; e < 3; ++e )
+            d.aniso_n[k][e] = h.aniso_n[k][e];
+    }
+    // merge exchange and DMI pairs per basis atom, keeping the reference's pair order
+    std::vector<std::vector<PairEntry>> per( d.nb );
+    auto add = [&]( const Pair & p, double J, const Vec3 * Dv ) {
+        if( p.i < 0 || p.i >= d.nb || p.j < 0 || p.j >= d.nb )
+            return;
+        auto & L = per[p.i];
+        for( auto & q : L )
+            if( q.j == p.j && q.da == p.t[0] && q.db == p.t[1] && q.dc == p.t[2] )
+            {
+                q.J += J;
+                if( Dv )
+                    for( int e = 0; e < 3; ++e )
+                        q.D[e] += ( *Dv )[e];
+                return;
+            }
+        PairEntry q{};
+        q.i  = p.i;
+        q.j  = p.j;
+        q.da = p.t[0];
+        q.db = p.t[1];
+        q.dc = p.t[2];
+        q.J  = J;
+        if( Dv )
+            for( int e = 0; e < 3; ++e )
+                q.D[e] = ( *Dv )[e];
+        L.push_back( q );
+    };
+    for( size_t k = 0; k < h.ex_pairs.size(); ++k )
+        add( h.ex_pairs[k], h.ex_J[k], nullptr );
+    for( size_t k = 0; k < h.dmi_pairs.size(); ++k )
+    {
+        Vec3 Dv{ h.dmi_D[k] * h.dmi_n[k][0], h.dmi_D[k] * h.dmi_n[k][1], h.dmi_D[k] * h.dmi_n[k][2] };
+        add( h.dmi_pairs[k], 0.0, &Dv );
+    }
+    int n = 0;
+    d.max_t[0] = d.max_t[1] = d.max_t[2] = 0;
+    for( int b = 0; b < d.nb; ++b )
+    {
+        d.pair_begin[b] = n;
+        for( auto & q : per[b] )
+        {
+            if( n >= MAX_PAIRS )
+                throw std::runtime_error( "too many interaction pairs for the device engine" );
+            d.pairs[n++] = q;
+            d.max_t[0]   = std::max( d.max_t[0], std::abs( q.da ) );
+            d.max_t[1]   = std::max( d.max_t[1], std::abs( q.db ) );
+            d.max_t[2]   = std::max( d.max_t[2], std::abs( q.dc ) );
+        }
+    }
+    d.pair_begin[d.nb] = n;
+    d.n_pairs          = n;
+    d.dt                  = in.dt;
+    d.damping             = in.damping;
+    d.temperature         = in.temperature;
+    d.direct_minimization = in.direct_minimization ? 1 : 0;
+    d.force_convergence   = in.force_convergence;
+    d.seed                = in.seed;
+    d.stream              = in.stream;
+    d.n_iterations        = 0;
+    d.ddi                 = ( h.ddi_method == 1 ) ? 1 : 0;
+}
+
+Engine::Engine( const std::vector<SystemInput> & systems, bool fp64 ) : fp64_( fp64 )
+{
+    elem_ = fp64 ? sizeof( double ) : sizeof( float );
+    CUDA_CHECK( cudaStreamCreateWithFlags( &stream_, cudaStreamNonBlocking ) );
+    build_systems( systems );
+}
+
+Engine::~Engine()
+{
+    if( graph_ )
+        cudaGraphExecDestroy( graph_ );
+    for( int c = 0; c < 3; ++c )
+    {
+        dfree( spins_[c] );
+        dfree( predA_[c] );
+        dfree( predB_[c] );
+        dfree( aux1_[c] );
+        dfree( aux2_[c] );
+        dfree( field_[c] );
+    }
+    dfree( d_desc_ );
+    dfree( d_runs_ );
+    dfree( d_stage_ );
+    dfree( d_red_ );
+    dfree( d_grad_ );
+    dfree( d_blkmap_ );
+    dfree( d_blkcount_ );
+    if( stream_ )
+        cudaStreamDestroy( stream_ );
+}
+
+void Engine::build_systems( const std::vector<SystemInput> & systems )
+{
+    desc_.assign( systems.size(), SysDesc{} );
+    geoms_.clear();
+    long long off = 0;
+    int max_nos   = 0;
+    std::vector<int2> blkmap;
+    std::vector<int> blkcount;
+    std::vector<DDISystem> ddis;
+    for( size_t s = 0; s < systems.size(); ++s )
+    {
+        fill_desc( desc_[s], systems[s] );
+        desc_[s].spin_offset = off;
+        off += ( desc_[s].nos + SPIN_ALIGN - 1 ) / SPIN_ALIGN * SPIN_ALIGN;
+        max_nos = std::max( max_nos, desc_[s].nos );
+        geoms_.push_back( systems[s].geom );
+        int nbk = ( desc_[s].nos + threads_ - 1 ) / threads_;
+        for( int k = 0; k < nbk; ++k )
+            blkmap.push_back( make_int2( (int)s, k * threads_ ) );
+        blkcount.push_back( nbk );
+        if( desc_[s].ddi )
+        {
+            const Geometry & g = *systems[s].geom;
+            const auto & h     = *systems[s].ham;
+            DDISystem D;
+            D.sys              = (int)s;
+            D.n_cells          = g.n_cells;
+            D.bc               = { desc_[s].bc[0], desc_[s].bc[1], desc_[s].bc[2] };
+            D.padded           = ddi_padding( g.n_cells, D.bc, h.ddi_pb_zero_padding );
+            D.images           = h.ddi_images;
+            D.nb               = g.nb();
+            D.lattice_constant = g.lattice_constant;
+            D.bravais          = g.bravais;
+            D.cell_atoms       = g.cell_atoms;
+            ddis.push_back( D );
+            desc_[s].fft_slot = (int)ddis.size() - 1;
+        }
+    }
+    total_    = std::max<long long>( off, SPIN_ALIGN );
+    n_blocks_ = (int)blkmap.size();
+    for( int c = 0; c < 3; ++c )
+    {
+        spins_[c] = dalloc_bytes( total_ * elem_ );
+        predA_[c] = dalloc_bytes( total_ * elem_ );
+        predB_[c] = dalloc_bytes( total_ * elem_ );
+        aux1_[c]  = dalloc_bytes( total_ * elem_ );
+        aux2_[c]  = dalloc_bytes( total_ * elem_ );
+    }
+    d_desc_     = dalloc<SysDesc>( desc_.size() );
+    d_runs_     = dalloc<SysRun>( desc_.size() );
+    d_stage_    = dalloc<double>( 3 * (size_t)total_ );
+    d_grad_     = dalloc<double>( 3 * (size_t)std::max( max_nos, 1 ) );
+    d_red_      = dalloc<double>( N_TERMS * 2 );
+    d_blkmap_   = dalloc<int2>( std::max<size_t>( blkmap.size(), 1 ) );
+    d_blkcount_ = dalloc<int>( std::max<size_t>( blkcount.size(), 1 ) );
+    h2d( d_desc_, desc_.data(), desc_.size() );
+    h2d( d_blkmap_, blkmap.data(), blkmap.size() );
+    h2d( d_blkcount_, blkcount.data(), blkcount.size() );
+    any_ddi_ = !ddis.empty();
+    if( any_ddi_ )
+    {
+        for( int c = 0; c < 3; ++c )
+            field_[c] = dalloc_bytes( total_ * elem_ );
+        ddi_.build( ddis, fp64_, d_desc_, stream_ );
+    }
+}
+
+void Engine::set_params( int s, const SystemInput & in )
+{
+    SysDesc & d = desc_[s];
+    d.dt                  = in.dt;
+    d.damping             = in.damping;
+    d.temperature         = in.temperature;
+    d.direct_minimization = in.direct_minimization ? 1 : 0;
+    d.force_convergence   = in.force_convergence;
+    d.seed                = in.seed;
+    d.stream              = in.stream;
+    CUDA_CHECK( cudaMemcpyAsync( d_desc_ + s, &d, sizeof( SysDesc ), cudaMemcpyHostToDevice, stream_ ) );
+    CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+}
+
+template<typename R>
+static SoA3<R> soa( void * const * p )
+{
+    return { (R *)p[0], (R *)p[1], (R *)p[2] };
+}
+
+void Engine::set_spins( int s, const double * aos )
+{
+    const SysDesc & d = desc_[s];
+    CUDA_CHECK( cudaMemcpyAsync( d_stage_, aos, sizeof( double ) * 3 * d.nos, cudaMemcpyHostToDevice, stream_ ) );
+    int grid = std::min( 1024, ( d.nos + 255 ) / 256 );
+    if( fp64_ )
+        aos_to_soa<double><<<grid, 256, 0, stream_>>>( d_stage_, soa<double>( spins_ ), d.spin_offset, d.nos );
+    else
+        aos_to_soa<float><<<grid, 256, 0, stream_>>>( d_stage_, soa<float>( spins_ ), d.spin_offset, d.nos );
+    CUDA_CHECK( cudaGetLastError() );
+    CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+}
+
+void Engine::get_spins( int s, double * aos )
+{
+    const SysDesc & d = desc_[s];
+    int grid          = std::min( 1024, ( d.nos + 255 ) / 256 );
+    if( fp64_ )
+        soa_to_aos<double><<<grid, 256, 0, stream_>>>( soa<double>( spins_ ), d.spin_offset, d.nos, d_stage_ );
+    else
+        soa_to_aos<float><<<grid, 256, 0, stream_>>>( soa<float>( spins_ ), d.spin_offset, d.nos, d_stage_ );
+    CUDA_CHECK( cudaGetLastError() );
+    CUDA_CHECK( cudaMemcpyAsync( aos, d_stage_, sizeof( double ) * 3 * d.nos, cudaMemcpyDeviceToHost, stream_ ) );
+    CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+}
+
+void Engine::set_all_spins( const double * aos )
+{
+    // one host->device copy of the concatenated systems, then per-system conversion kernels
+    size_t n = 0;
+    for( auto & d : desc_ )
+        n += 3 * (size_t)d.nos;
+    CUDA_CHECK( cudaMemcpyAsync( d_stage_, aos, sizeof( double ) * n, cudaMemcpyHostToDevice, stream_ ) );
+    size_t o = 0;
+    for( auto & d : desc_ )
+    {
+        int grid = std::min( 1024, ( d.nos + 255 ) / 256 );
+        if( fp64_ )
+            aos_to_soa<double><<<grid, 256, 0, stream_>>>( d_stage_ + o, soa<double>( spins_ ), d.spin_offset, d.nos );
+        else
+            aos_to_soa<float><<<grid, 256, 0, stream_>>>( d_stage_ + o, soa<float>( spins_ ), d.spin_offset, d.nos );
+        o += 3 * (size_t)d.nos;
+    }
+    CUDA_CHECK( cudaGetLastError() );
+}
+
+void Engine::get_all_spins( double * aos )
+{
+    size_t o = 0;
+    for( auto & d : desc_ )
+    {
+        int grid = std::min( 1024, ( d.nos + 255 ) / 256 );
+        if( fp64_ )
+            soa_to_aos<double><<<grid, 256, 0, stream_>>>( soa<double>( spins_ ), d.spin_offset, d.nos, d_stage_ + o );
+        else
+            soa_to_aos<float><<<grid, 256, 0, stream_>>>( soa<float>( spins_ ), d.spin_offset, d.nos, d_stage_ + o );
+        o += 3 * (size_t)d.nos;
+    }
+    CUDA_CHECK( cudaGetLastError() );
+    CUDA_CHECK( cudaMemcpyAsync( aos, d_stage_, sizeof( double ) * o, cudaMemcpyDeviceToHost, stream_ ) );
+}
+
+template<typename R>
+void Engine::gradient_t( int s, double * grad_aos, double * energy, double * terms, double * per_spin_host )
+{
+    const SysDesc & d = desc_[s];
+    SoA3<R> h{ nullptr, nullptr, nullptr };
+    if( d.ddi )
+    {
+        ddi_.run( d_desc_, nullptr, spins_[0], spins_[1], spins_[2], field_[0], field_[1], field_[2], stream_ );
+        h = soa<R>( field_ );
+    }
+    CUDA_CHECK( cudaMemsetAsync( d_red_, 0, sizeof( double ) * N_TERMS, stream_ ) );
+    double * d_ps = nullptr;
+    if( per_spin_host )
+        d_ps = dalloc<double>( (size_t)N_TERMS * d.nos );
+    eval_kernel<R><<<n_blocks_, threads_, 0, stream_>>>( d_desc_, d_blkmap_, soa<R>( spins_ ), h, s, d_grad_, d_red_,
+                                                         d_ps );
+    CUDA_CHECK( cudaGetLastError() );
+    double sums[N_TERMS];
+    CUDA_CHECK( cudaMemcpyAsync( sums, d_red_, sizeof( sums ), cudaMemcpyDeviceToHost, stream_ ) );
+    if( grad_aos )
+        CUDA_CHECK( cudaMemcpyAsync( grad_aos, d_grad_, sizeof( double ) * 3 * d.nos, cudaMemcpyDeviceToHost, stream_ ) );
+    if( per_spin_host )
+        CUDA_CHECK( cudaMemcpyAsync( per_spin_host, d_ps, sizeof( double ) * N_TERMS * d.nos, cudaMemcpyDeviceToHost,
+                                     stream_ ) );
+    CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+    if( d_ps )
+        dfree( d_ps );
+    double E = 0;
+    for( int t = 0; t < N_TERMS; ++t )
+        E += sums[t];
+    if( energy )
+        *energy = E;
+    if( terms )
+        for( int t = 0; t < N_TERMS; ++t )
+            terms[t] = sums[t];
+}
+
+void Engine::gradient( int s, double * grad_aos, double * energy, double * terms )
+{
+    if( fp64_ )
+        gradient_t<double>( s, grad_aos, energy, terms, nullptr );
+    else
+        gradient_t<float>( s, grad_aos, energy, terms, nullptr );
+}
+
+void Engine::energy_per_spin( int s, double * per_term )
+{
+    if( fp64_ )
+        gradient_t<double>( s, nullptr, nullptr, nullptr, per_term );
+    else
+        gradient_t<float>( s, nullptr, nullptr, nullptr, per_term );
+}
+
+void Engine::ddi_field( int s, double * h_aos )
+{
+    const SysDesc & d = desc_[s];
+    if( !d.ddi )
+    {
+        std::fill( h_aos, h_aos + 3 * (size_t)d.nos, 0.0 );
+        return;
+    }
+    ddi_.run( d_desc_, nullptr, spins_[0], spins_[1], spins_[2], field_[0], field_[1], field_[2], stream_ );
+    int grid = std::min( 1024, ( d.nos + 255 ) / 256 );
+    if( fp64_ )
+        soa_to_aos<double><<<grid, 256, 0, stream_>>>( soa<double>( field_ ), d.spin_offset, d.nos, d_stage_ );
+    else
+        soa_to_aos<float><<<grid, 256, 0, stream_>>>( soa<float>( field_ ), d.spin_offset, d.nos, d_stage_ );
+    CUDA_CHECK( cudaGetLastError() );
+    CUDA_CHECK( cudaMemcpyAsync( h_aos, d_stage_, sizeof( double ) * 3 * d.nos, cudaMemcpyDeviceToHost, stream_ ) );
+    CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+}
+
+template<typename R, int SOLVER, int STAGE>
+static void launch_stage( int nblk, cudaStream_t st, const StageArgs<R> & a )
+{
+    llg_stage<R, SOLVER, STAGE><<<nblk, 256, 0, st>>>( a );
+}
+
+template<typename R>
+void Engine::launch_probe_t()
+{
+    StageArgs<R> a{};
+    a.sd       = d_desc_;
+    a.runs     = d_runs_;
+    a.blkmap   = d_blkmap_;
+    a.blkcount = d_blkcount_;
+    a.s        = soa<R>( spins_ );
+    a.cfg      = a.s;
+    a.h        = { nullptr, nullptr, nullptr };
+    if( any_ddi_ )
+    {
+        ddi_.run( d_desc_, d_runs_, spins_[0], spins_[1], spins_[2], field_[0], field_[1], field_[2], stream_ );
+        a.h = soa<R>( field_ );
+    }
+    // the probe uses the solver's force definition (direct minimisation / dynamics) only
+    llg_stage<R, SOLVER_HEUN, ST_PROBE><<<n_blocks_, 256, 0, stream_>>>( a );
+    CUDA_CHECK( cudaGetLastError() );
+}
+
+template<typename R>
+void Engine::launch_step_t()
+{
+    StageArgs<R> a{};
+    a.sd       = d_desc_;
+    a.runs     = d_runs_;
+    a.blkmap   = d_blkmap_;
+    a.blkcount = d_blkcount_;
+    a.s        = soa<R>( spins_ );
+    a.aux1     = soa<R>( aux1_ );
+    a.aux2     = soa<R>( aux2_ );
+    SoA3<R> pA = soa<R>( predA_ ), pB = soa<R>( predB_ );
+    SoA3<R> hf = any_ddi_ ? soa<R>( field_ ) : SoA3<R>{ nullptr, nullptr, nullptr };
+    auto field = [&]( const SoA3<R> & cfg ) {
+        if( any_ddi_ )
+            ddi_.run( d_desc_, d_runs_, cfg.x, cfg.y, cfg.z, field_[0], field_[1], field_[2], stream_ );
+    };
+    a.h = hf;
+    const int nb = n_blocks_;
+    switch( solver_ )
+    {
+    case SOLVER_SIB:
+    case SOLVER_HEUN:
+    case SOLVER_DEPONDT:
+    {
+        a.cfg = a.s;
+        a.out = pA;
+        field( a.cfg );
+        if( solver_ == SOLVER_SIB )
+            launch_stage<R, SOLVER_SIB, 1>( nb, stream_, a );
+        else if( solver_ == SOLVER_HEUN )
+            launch_stage<R, SOLVER_HEUN, 1>( nb, stream_, a );
+        else
+            launch_stage<R, SOLVER_DEPONDT, 1>( nb, stream_, a );
+        a.cfg = pA;
+        field( a.cfg );
+        if( solver_ == SOLVER_SIB )
+            launch_stage<R, SOLVER_SIB, 2>( nb, stream_, a );
+        else if( solver_ == SOLVER_HEUN )
+            launch_stage<R, SOLVER_HEUN, 2>( nb, stream_, a );
+        else
+            launch_stage<R, SOLVER_DEPONDT, 2>( nb, stream_, a );
+        break;
+    }
+    case SOLVER_RK4:
+    {
+        a.cfg = a.s;
+        a.out = pA;
+        field( a.cfg );
+        launch_stage<R, SOLVER_RK4, 1>( nb, stream_, a );
+        a.cfg = pA;
+        a.out = pB;
+        field( a.cfg );
+        launch_stage<R, SOLVER_RK4, 2>( nb, stream_, a );
+        a.cfg = pB;
+        a.out = pA;
+        field( a.cfg );
+        launch_stage<R, SOLVER_RK4, 3>( nb, stream_, a );
+        a.cfg = pA;
+        field( a.cfg );
+        launch_stage<R, SOLVER_RK4, 4>( nb, stream_, a );
+        break;
+    }
+    default:
+        throw std::runtime_error( "solver not supported by the LLG engine" );
+    }
+    CUDA_CHECK( cudaGetLastError() );
+}
+
+void Engine::launch_step_kernels()
+{
+    if( fp64_ )
+        launch_step_t<double>();
+    else
+        launch_step_t<float>();
+}
+
+int Engine::kernels_per_step() const
+{
+    int stages = solver_ == SOLVER_RK4 ? 4 : 2;
+    return stages * ( 1 + ( any_ddi_ ? 5 : 0 ) );
+}
+
+void Engine::llg_start( int solver, const std::vector<int> & n_iterations )
+{
+    if( solver != SOLVER_SIB && solver != SOLVER_HEUN && solver != SOLVER_DEPONDT && solver != SOLVER_RK4 )
+        throw std::runtime_error( "solver not supported by the LLG engine" );
+    solver_ = solver;
+    for( size_t s = 0; s < desc_.size(); ++s )
+        desc_[s].n_iterations = n_iterations.size() == 1 ? n_iterations[0] : n_iterations[s];
+    CUDA_CHECK( cudaMemcpyAsync( d_desc_, desc_.data(), sizeof( SysDesc ) * desc_.size(), cudaMemcpyHostToDevice,
+                                 stream_ ) );
+    std::vector<SysRun> r( desc_.size() );
+    for( auto & x : r )
+    {
+        std::memset( &x, 0, sizeof( x ) );
+        x.active = 1; // the probe runs on every system
+    }
+    CUDA_CHECK( cudaMemcpyAsync( d_runs_, r.data(), sizeof( SysRun ) * r.size(), cudaMemcpyHostToDevice, stream_ ) );
+    if( fp64_ )
+        launch_probe_t<double>();
+    else
+        launch_probe_t<float>();
+    CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+}
+
+void Engine::llg_launch( int n_steps )
+{
+    // steps are replayed from a CUDA graph of G steps; surplus steps are no-ops on the device
+    const int G = 8;
+    if( !graph_ || graph_solver_ != solver_ )
+    {
+        if( graph_ )
+            cudaGraphExecDestroy( graph_ );
+        cudaGraph_t g;
+        CUDA_CHECK( cudaStreamBeginCapture( stream_, cudaStreamCaptureModeThreadLocal ) );
+        for( int k = 0; k < G; ++k )
+            launch_step_kernels();
+        CUDA_CHECK( cudaStreamEndCapture( stream_, &g ) );
+        CUDA_CHECK( cudaGraphInstantiate( &graph_, g, 0 ) );
+        cudaGraphDestroy( g );
+        graph_solver_ = solver_;
+        graph_steps_  = G;
+    }
+    int full = n_steps / G, rem = n_steps % G;
+    for( int k = 0; k < full; ++k )
+        CUDA_CHECK( cudaGraphLaunch( graph_, stream_ ) );
+    for( int k = 0; k < rem; ++k )
+        launch_step_kernels();
+}
+
+void Engine::sync()
+{
+    CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+}
+
+std::vector<Engine::Status> Engine::status()
+{
+    std::vector<SysRun> r( desc_.size() );
+    CUDA_CHECK( cudaMemcpyAsync( r.data(), d_runs_, sizeof( SysRun ) * r.size(), cudaMemcpyDeviceToHost, stream_ ) );
+    CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+    std::vector<Status> out( r.size() );
+    for( size_t s = 0; s < r.size(); ++s )
+        out[s] = { r[s].iteration, r[s].active, r[s].max_torque, r[s].energy };
+    return out;
+}
+
+} // namespace sg

@@ -1,0 +1,185 @@
+// Device engine: one batch of independent spin systems resident in HBM, advanced together.
+#pragma once
+#include "common.hpp"
+#include "ddi.hpp"
+#include "geometry.hpp"
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <vector>
+
+namespace sg
+{
+
+struct SystemInput
+{
+    const Geometry * geom         = nullptr;
+    const HamiltonianParams * ham = nullptr;
+    double dt                     = 1e-3;
+    double damping                = 0.3;
+    double temperature            = 0;
+    double force_convergence      = 1e-10;
+    bool direct_minimization      = false;
+    unsigned long long seed       = 2006;
+    unsigned int stream           = 0;
+};
+
+// Energy terms in the reference's order (Energy_Contributions_per_Spin, cpp:262-305)
+enum Term
+{
+    TERM_ZEEMAN = 0,
+    TERM_ANISOTROPY,
+    TERM_EXCHANGE,
+    TERM_DMI,
+    TERM_DDI,
+    N_TERMS
+};
+
+class Engine
+{
+public:
+    Engine( const std::vector<SystemInput> & systems, bool fp64 );
+    ~Engine();
+    Engine( const Engine & )             = delete;
+    Engine & operator=( const Engine & ) = delete;
+
+    int n_sys() const
+    {
+        return (int)desc_.size();
+    }
+    int nos( int s ) const
+    {
+        return desc_[s].nos;
+    }
+    bool fp64() const
+    {
+        return fp64_;
+    }
+    long long total_spins() const
+    {
+        return total_;
+    }
+
+    // host AoS [nos][3] double <-> device SoA in the engine precision
+    void set_spins( int s, const double * aos );
+    void get_spins( int s, double * aos );
+    // batched transfers of every system (one copy each way, converted on the device)
+    void set_all_spins( const double * aos_concat );
+    void get_all_spins( double * aos_concat );
+
+    // Gradient, FP64 total energy and per-term energies of the current device spins of system s.
+    void gradient( int s, double * grad_aos, double * energy, double * terms );
+    // per-spin energy contributions [N_TERMS][nos] of system s
+    void energy_per_spin( int s, double * per_term );
+
+    // LLG: start a run (constructor probe: initial torque), then advance in steps.
+    void llg_start( int solver, const std::vector<int> & n_iterations );
+    // Launches n_steps steps (no host synchronisation).  Systems stop by themselves on
+    // convergence or when their iteration budget is used up.
+    void llg_launch( int n_steps );
+    void sync();
+    struct Status
+    {
+        int iteration;
+        int active;
+        float max_torque;
+        double energy;
+    };
+    std::vector<Status> status();
+    void set_params( int s, const SystemInput & in );
+    // time one step of the current method on the stream with CUDA events (ms)
+    cudaStream_t stream() const
+    {
+        return stream_;
+    }
+    int kernels_per_step() const;
+    // DDI field h of the current spins (tests)
+    void ddi_field( int s, double * h_aos );
+
+    // raw device pointers (component arrays) for the adjoint / GNEB layers
+    void * spin_ptr( int comp ) const
+    {
+        return spins_[comp];
+    }
+    const SysDesc * d_desc() const
+    {
+        return d_desc_;
+    }
+    SysRun * d_runs() const
+    {
+        return d_runs_;
+    }
+    const int2 * d_blkmap() const
+    {
+        return d_blkmap_;
+    }
+    const int * d_blkcount() const
+    {
+        return d_blkcount_;
+    }
+    int n_blocks() const
+    {
+        return n_blocks_;
+    }
+    bool has_ddi() const
+    {
+        return any_ddi_;
+    }
+    void * field_ptr( int comp ) const
+    {
+        return field_[comp];
+    }
+    const SysDesc & desc( int s ) const
+    {
+        return desc_[s];
+    }
+    // dipolar field of the configuration cfg (3 component arrays) into field_ptr();
+    // systems whose SysRun is inactive are skipped when runs != nullptr
+    void run_ddi( void * const * cfg, const SysRun * runs )
+    {
+        if( any_ddi_ )
+            ddi_.run( d_desc_, runs, cfg[0], cfg[1], cfg[2], field_[0], field_[1], field_[2], stream_ );
+    }
+
+private:
+    void build_systems( const std::vector<SystemInput> & systems );
+    void launch_step_kernels();
+    template<typename R>
+    void launch_step_t();
+    template<typename R>
+    void launch_probe_t();
+    template<typename R>
+    void gradient_t( int s, double * grad_aos, double * energy, double * terms, double * per_spin );
+
+    bool fp64_;
+    size_t elem_;
+    cudaStream_t stream_ = nullptr;
+    std::vector<SysDesc> desc_;
+    std::vector<const Geometry *> geoms_;
+    SysDesc * d_desc_ = nullptr;
+    SysRun * d_runs_  = nullptr;
+    long long total_  = 0; // padded total spins
+    // SoA buffers (engine precision): state, predictor A/B, aux fv1, aux acc, DDI field
+    void * spins_[3] = { nullptr, nullptr, nullptr };
+    void * predA_[3] = { nullptr, nullptr, nullptr };
+    void * predB_[3] = { nullptr, nullptr, nullptr };
+    void * aux1_[3]  = { nullptr, nullptr, nullptr };
+    void * aux2_[3]  = { nullptr, nullptr, nullptr };
+    void * field_[3] = { nullptr, nullptr, nullptr };
+    double * d_stage_ = nullptr; // AoS double staging for transfers
+    double * d_red_   = nullptr; // reduction scratch (per-term sums)
+    double * d_grad_  = nullptr; // AoS double gradient output
+    int2 * d_blkmap_  = nullptr;
+    int * d_blkcount_ = nullptr;
+    int n_blocks_     = 0;
+    int threads_      = 256;
+    bool any_ddi_     = false;
+    DDIPlan ddi_;
+    int solver_       = SOLVER_HEUN;
+    cudaGraphExec_t graph_ = nullptr;
+    int graph_steps_       = 0;
+    int graph_solver_      = -1;
+};
+
+} // namespace sg

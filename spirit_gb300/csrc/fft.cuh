@@ -1,0 +1,149 @@
+// Hand-written batched mixed-radix Stockham FFT for the dipole-dipole convolution.
+//
+// The reference computes the dipolar gradient as a zero-padded 3D convolution through
+// kissFFT / cuFFT (core/src/engine/Hamiltonian_Heisenberg.cpp:920-1014, FFT.cu:23-80):
+//     g_i -= mu_i * (1/T) IFFT( sum_b2 Dhat_{b1 b2}(k) . FFT(mu s)_{b2}(k) )
+// Here the 3D transform is split into 1D passes along a (real-to-complex, half length),
+// b and c, each done by a CTA on a group of lines held in shared memory:
+//     A : R2C along a of every nonzero (b, c) row of mu*s        (zero padding is implicit)
+//     B : C2C along b of every (ka, c) column, rows b >= Nb are implicit zeros
+//     C : C2C along c, 6-component symmetric tensor product with Dhat, inverse along c;
+//         only c < Nc of the result is kept (the padded half is never written)
+//     B': inverse along b, only b < Nb kept
+//     A': C2R along a, only a < Na kept, scaled by 1/T, written as the field h = D * (mu s)
+// so the padded volume is never materialised.  Twiddles come from a table of exp(-2 pi i t / L)
+// computed in FP64 on the host.
+#pragma once
+#include "common.hpp"
+
+#include <cuda_runtime.h>
+
+namespace sg
+{
+
+template<typename R>
+struct cplx
+{
+    R x, y;
+};
+
+template<typename R>
+__device__ __forceinline__ cplx<R> cmul( cplx<R> a, cplx<R> b )
+{
+    return { a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x };
+}
+template<typename R>
+__device__ __forceinline__ cplx<R> cconj( cplx<R> a )
+{
+    return { a.x, -a.y };
+}
+
+// Stockham stage loop over nl lines of length L in shared memory (a -> b -> a ...).
+// rad: 0-terminated radix list; tw: L twiddles exp(-2 pi i t/L) (in shared memory).
+// Returns the buffer that holds the result.  Must be called by all threads of the block.
+template<typename R>
+__device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int nl, const int * rad, const cplx<R> * tw,
+                               bool inverse )
+{
+    int Ns = 1;
+    for( int s = 0; s < 12 && rad[s] > 0; ++s )
+    {
+        const int Rr   = rad[s];
+        const int LR   = L / Rr;
+        const int span = L / ( Ns * Rr );
+        if( Rr <= 8 )
+        {
+            for( int idx = threadIdx.x; idx < nl * LR; idx += blockDim.x )
+            {
+                int line           = idx / LR;
+                int j              = idx - line * LR;
+                const cplx<R> * src = a + line * L;
+                cplx<R> * dst       = b + line * L;
+                int k              = j % Ns;
+                cplx<R> v[8];
+#pragma unroll
+                for( int r = 0; r < 8; ++r )
+                {
+                    if( r < Rr )
+                    {
+                        cplx<R> w = tw[r * k * span];
+                        if( inverse )
+                            w = cconj( w );
+                        v[r] = r == 0 ? src[j] : cmul( src[j + r * LR], w );
+                    }
+                }
+                int d0 = ( j / Ns ) * Ns * Rr + k;
+                if( Rr == 2 )
+                {
+                    dst[d0]      = { v[0].x + v[1].x, v[0].y + v[1].y };
+                    dst[d0 + Ns] = { v[0].x - v[1].x, v[0].y - v[1].y };
+                }
+                else if( Rr == 4 )
+                {
+                    // W4 = -i (forward) / +i (inverse)
+                    cplx<R> s02 = { v[0].x + v[2].x, v[0].y + v[2].y };
+                    cplx<R> d02 = { v[0].x - v[2].x, v[0].y - v[2].y };
+                    cplx<R> s13 = { v[1].x + v[3].x, v[1].y + v[3].y };
+                    cplx<R> d13 = { v[1].x - v[3].x, v[1].y - v[3].y };
+                    // forward: out1 = d02 - i d13, out3 = d02 + i d13
+                    cplx<R> id13 = inverse ? cplx<R>{ -d13.y, d13.x } : cplx<R>{ d13.y, -d13.x };
+                    dst[d0]          = { s02.x + s13.x, s02.y + s13.y };
+                    dst[d0 + Ns]     = { d02.x + id13.x, d02.y + id13.y };
+                    dst[d0 + 2 * Ns] = { s02.x - s13.x, s02.y - s13.y };
+                    dst[d0 + 3 * Ns] = { d02.x - id13.x, d02.y - id13.y };
+                }
+                else
+                {
+                    for( int m = 0; m < Rr; ++m )
+                    {
+                        cplx<R> acc = v[0];
+                        for( int r = 1; r < Rr; ++r )
+                        {
+                            cplx<R> w = tw[( ( r * m ) % Rr ) * LR];
+                            if( inverse )
+                                w = cconj( w );
+                            cplx<R> t = cmul( v[r], w );
+                            acc.x += t.x;
+                            acc.y += t.y;
+                        }
+                        dst[d0 + m * Ns] = acc;
+                    }
+                }
+            }
+        }
+        else
+        {
+            // large prime radix: one output per thread, O(R) work each
+            for( int o = threadIdx.x; o < nl * L; o += blockDim.x )
+            {
+                int line           = o / L;
+                int q              = o - line * L;
+                const cplx<R> * src = a + line * L;
+                int k              = q % Ns;
+                int m              = ( q / Ns ) % Rr;
+                int jhi            = q / ( Ns * Rr );
+                int j              = jhi * Ns + k;
+                cplx<R> acc        = { 0, 0 };
+                for( int r = 0; r < Rr; ++r )
+                {
+                    int t     = ( r * k * span + ( ( r * m ) % Rr ) * LR ) % L;
+                    cplx<R> w = tw[t];
+                    if( inverse )
+                        w = cconj( w );
+                    cplx<R> p = cmul( src[j + r * LR], w );
+                    acc.x += p.x;
+                    acc.y += p.y;
+                }
+                b[line * L + q] = acc;
+            }
+        }
+        __syncthreads();
+        cplx<R> * t = a;
+        a           = b;
+        b           = t;
+        Ns *= Rr;
+    }
+    return a;
+}
+
+} // namespace sg

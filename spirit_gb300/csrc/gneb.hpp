@@ -1,0 +1,22 @@
+// GNEB (chain of images, VP solver) and the VP / batched LLG drivers behind the C API.
+#pragma once
+#include "state.hpp"
+
+#include <vector>
+
+namespace sg
+{
+
+void gneb_start( State * st, Chain & chain, bool singleshot );
+void gneb_n_shot( State * st, Chain & chain, int n );
+void gneb_update_rx( Chain & chain );
+const std::vector<double> & gneb_torques( Chain & chain );
+
+// LLG with the VP solver on one image (direct minimisation; Solver_VP.hpp:28-114 with Method_LLG)
+void llg_vp_run( State * st, Image & img, bool singleshot );
+void llg_vp_shot( State * st, Image & img, int n );
+
+// batched LLG over the active images of several States (one device batch)
+void llg_run_batched( State ** states, int n_states, int solver, int n_iterations, void * info, size_t info_size );
+
+} // namespace sg

@@ -1,0 +1,308 @@
+// Device helpers shared by the LLG stage kernels (engine.cu) and the GNEB kernels (gneb.cu).
+#pragma once
+#include "common.hpp"
+
+#include <cuda_runtime.h>
+
+namespace sg
+{
+
+constexpr double C_MU_B  = 0.057883817555;
+constexpr double C_K_B   = 0.08617330350;
+constexpr double C_GAMMA = 0.1760859644;
+
+template<typename R>
+struct V3
+{
+    R x, y, z;
+};
+template<typename R>
+__device__ __forceinline__ V3<R> cross( V3<R> a, V3<R> b )
+{
+    return { a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x };
+}
+template<typename R>
+__device__ __forceinline__ R dot( V3<R> a, V3<R> b )
+{
+    return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+// Eigen normalize(): zero vectors stay zero
+template<typename R>
+__device__ __forceinline__ V3<R> normalized( V3<R> v )
+{
+    R n2 = dot( v, v );
+    if( n2 > R( 0 ) )
+    {
+        R n = sqrt( n2 );
+        return { v.x / n, v.y / n, v.z / n };
+    }
+    return v;
+}
+
+template<typename R>
+struct PairR
+{
+    int j, da, db, dc;
+    R J, Dx, Dy, Dz;
+};
+
+template<typename R>
+struct SoA3
+{
+    R * x;
+    R * y;
+    R * z;
+    __device__ __forceinline__ V3<R> ld( long long i ) const
+    {
+        return { x[i], y[i], z[i] };
+    }
+    __device__ __forceinline__ void st( long long i, V3<R> v ) const
+    {
+        x[i] = v.x;
+        y[i] = v.y;
+        z[i] = v.z;
+    }
+};
+
+// ------------------------------------------------------------------ Philox4x32-10
+// Salmon et al., SC'11.  Counter (spin, iteration, stream, 0x53504E00), key = seed.
+__device__ __forceinline__ uint4 philox4x32( uint4 c, uint2 k )
+{
+#pragma unroll
+    for( int r = 0; r < 10; ++r )
+    {
+        unsigned int hi0 = __umulhi( 0xD2511F53u, c.x ), lo0 = 0xD2511F53u * c.x;
+        unsigned int hi1 = __umulhi( 0xCD9E8D57u, c.z ), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4( hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0 );
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// three standard normals for spin i: Box-Muller on 23-bit uniforms u = (x>>9 + 1/2) 2^-23
+template<typename R>
+__device__ __forceinline__ V3<R> gauss3( unsigned long long seed, unsigned int stream, unsigned int iteration,
+                                         unsigned int i )
+{
+    uint4 x = philox4x32( make_uint4( i, iteration, stream, 0x53504E00u ),
+                          make_uint2( (unsigned int)seed, (unsigned int)( seed >> 32 ) ) );
+    const R sc = R( 1.0 / 8388608.0 );
+    R u0 = ( R( x.x >> 9 ) + R( 0.5 ) ) * sc;
+    R u1 = ( R( x.y >> 9 ) + R( 0.5 ) ) * sc;
+    R u2 = ( R( x.z >> 9 ) + R( 0.5 ) ) * sc;
+    R u3 = ( R( x.w >> 9 ) + R( 0.5 ) ) * sc;
+    R r0 = sqrt( R( -2 ) * log( u0 ) );
+    R r1 = sqrt( R( -2 ) * log( u2 ) );
+    R s1, c1, s3, c3;
+    sincospi( R( 2 ) * u1, &s1, &c1 );
+    sincospi( R( 2 ) * u3, &s3, &c3 );
+    return { r0 * c1, r0 * s1, r1 * c3 };
+}
+
+// ------------------------------------------------------------------ neighbour index
+// idx_from_pair (core/include/engine/Vectormath.hpp:437-528) for a spin at cell (a, b, c)
+__device__ __forceinline__ long long pair_index( const SysDesc & d, int a, int b, int c, int j, int da, int db, int dc )
+{
+    const int Na = d.n_cells[0], Nb = d.n_cells[1], Nc = d.n_cells[2];
+    if( abs( da ) > Na || abs( db ) > Nb || abs( dc ) > Nc )
+        return -1;
+    int ja = a + da, jb = b + db, jc = c + dc;
+    if( d.bc[0] || ( ja >= 0 && ja < Na ) )
+    {
+        if( ja < 0 )
+            ja += Na;
+        if( ja >= Na )
+            ja -= Na;
+    }
+    else
+        return -1;
+    if( d.bc[1] || ( jb >= 0 && jb < Nb ) )
+    {
+        if( jb < 0 )
+            jb += Nb;
+        if( jb >= Nb )
+            jb -= Nb;
+    }
+    else
+        return -1;
+    if( d.bc[2] || ( jc >= 0 && jc < Nc ) )
+    {
+        if( jc < 0 )
+            jc += Nc;
+        if( jc >= Nc )
+            jc -= Nc;
+    }
+    else
+        return -1;
+    return d.spin_offset + j + (long long)d.nb * ( ja + Na * ( jb + (long long)Nb * jc ) );
+}
+
+// ------------------------------------------------------------------ block reductions
+__device__ __forceinline__ double block_sum( double v, double * sh )
+{
+    for( int o = 16; o > 0; o >>= 1 )
+        v += __shfl_down_sync( 0xffffffffu, v, o );
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if( l == 0 )
+        sh[w] = v;
+    __syncthreads();
+    double r = 0;
+    if( threadIdx.x < 32 )
+    {
+        r = threadIdx.x < ( blockDim.x >> 5 ) ? sh[threadIdx.x] : 0.0;
+        for( int o = 16; o > 0; o >>= 1 )
+            r += __shfl_down_sync( 0xffffffffu, r, o );
+    }
+    return r; // valid in thread 0
+}
+
+__device__ __forceinline__ float block_max( float v, float * sh )
+{
+    for( int o = 16; o > 0; o >>= 1 )
+        v = fmaxf( v, __shfl_down_sync( 0xffffffffu, v, o ) );
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if( l == 0 )
+        sh[w] = v;
+    __syncthreads();
+    float r = 0;
+    if( threadIdx.x < 32 )
+    {
+        r = threadIdx.x < ( blockDim.x >> 5 ) ? sh[threadIdx.x] : 0.f;
+        for( int o = 16; o > 0; o >>= 1 )
+            r = fmaxf( r, __shfl_down_sync( 0xffffffffu, r, o ) );
+    }
+    return r;
+}
+
+// Gradient of the Heisenberg Hamiltonian at spin i of configuration cfg, and the quadratic
+// (0.5 g.s) plus Zeeman energy of that spin.
+template<typename R>
+__device__ __forceinline__ V3<R> gradient_at( const SysDesc & d, const PairR<R> * pairs, const SoA3<R> & cfg,
+                                              const SoA3<R> & h, long long gi, int ib, int a, int b, int c, V3<R> si,
+                                              R mu, double & e )
+{
+    V3<R> g = { 0, 0, 0 };
+    for( int k = 0; k < d.n_aniso; ++k )
+        if( d.aniso_idx[k] == ib )
+        {
+            V3<R> n = { (R)d.aniso_n[k][0], (R)d.aniso_n[k][1], (R)d.aniso_n[k][2] };
+            R sc    = R( 2 ) * (R)d.aniso_K[k] * dot( n, si );
+            g.x -= sc * n.x;
+            g.y -= sc * n.y;
+            g.z -= sc * n.z;
+        }
+    const int p0 = d.pair_begin[ib], p1 = d.pair_begin[ib + 1];
+    for( int p = p0; p < p1; ++p )
+    {
+        const PairR<R> P = pairs[p];
+        long long j      = pair_index( d, a, b, c, P.j, P.da, P.db, P.dc );
+        if( j >= 0 )
+        {
+            V3<R> sj = cfg.ld( j );
+            g.x -= P.J * sj.x;
+            g.y -= P.J * sj.y;
+            g.z -= P.J * sj.z;
+            V3<R> cr = cross( sj, V3<R>{ P.Dx, P.Dy, P.Dz } );
+            g.x -= cr.x;
+            g.y -= cr.y;
+            g.z -= cr.z;
+        }
+    }
+    if( h.x )
+    {
+        V3<R> hh = h.ld( gi );
+        g.x -= mu * hh.x;
+        g.y -= mu * hh.y;
+        g.z -= mu * hh.z;
+    }
+    e = 0.5 * ( (double)g.x * si.x + (double)g.y * si.y + (double)g.z * si.z );
+    if( d.has_zeeman )
+    {
+        V3<R> B = { (R)d.zeeman[0], (R)d.zeeman[1], (R)d.zeeman[2] };
+        g.x -= mu * B.x;
+        g.y -= mu * B.y;
+        g.z -= mu * B.z;
+        e += -(double)mu * ( (double)B.x * si.x + (double)B.y * si.y + (double)B.z * si.z );
+    }
+    return g;
+}
+
+// Calculate_Force_Virtual for spin configuration cfg, force F = -g
+template<typename R>
+__device__ __forceinline__ V3<R> virtual_force( const SysDesc & d, V3<R> c, V3<R> g, R mu, V3<R> xi, bool thermal,
+                                                bool direct )
+{
+    V3<R> F = { -g.x, -g.y, -g.z };
+    if( direct )
+    {
+        R k      = (R)( d.dt * C_GAMMA / C_MU_B );
+        V3<R> cr = cross( c, F );
+        return { k * cr.x, k * cr.y, k * cr.z };
+    }
+    const double a = d.damping;
+    R dtg          = (R)( d.dt * C_GAMMA / C_MU_B / ( 1 + a * a ) );
+    R dtga         = (R)( ( d.dt * C_GAMMA / C_MU_B / ( 1 + a * a ) ) * a );
+    V3<R> cr       = cross( c, F );
+    V3<R> fv       = { dtg * F.x, dtg * F.y, dtg * F.z };
+    fv.x += dtga * cr.x;
+    fv.y += dtga * cr.y;
+    fv.z += dtga * cr.z;
+    fv.x /= mu;
+    fv.y /= mu;
+    fv.z /= mu;
+    if( thermal )
+    {
+        V3<R> cx = cross( c, xi );
+        fv.x += xi.x;
+        fv.y += xi.y;
+        fv.z += xi.z;
+        R ra = (R)a;
+        fv.x += ra * cx.x;
+        fv.y += ra * cx.y;
+        fv.z += ra * cx.z;
+    }
+    return fv;
+}
+
+// sib_transform (Solver_Kernels.cpp:15-48)
+template<typename R>
+__device__ __forceinline__ V3<R> sib( V3<R> e1, V3<R> f )
+{
+    V3<R> A  = { R( 0.5 ) * f.x, R( 0.5 ) * f.y, R( 0.5 ) * f.z };
+    R nA     = sqrt( dot( A, A ) );
+    R detAi  = R( 1 ) / ( R( 1 ) + nA * nA );
+    V3<R> cr = cross( e1, A );
+    V3<R> a2 = { e1.x - cr.x, e1.y - cr.y, e1.z - cr.z };
+    V3<R> o;
+    o.x = ( a2.x * ( A.x * A.x + R( 1 ) ) + a2.y * ( A.x * A.y - A.z ) + a2.z * ( A.x * A.z + A.y ) ) * detAi;
+    o.y = ( a2.x * ( A.y * A.x + A.z ) + a2.y * ( A.y * A.y + R( 1 ) ) + a2.z * ( A.y * A.z - A.x ) ) * detAi;
+    o.z = ( a2.x * ( A.z * A.x - A.y ) + a2.y * ( A.z * A.y + A.x ) + a2.z * ( A.z * A.z + R( 1 ) ) ) * detAi;
+    return o;
+}
+
+// Rodrigues rotation (Vectormath::rotate, Vectormath.cpp:474-479)
+template<typename R>
+__device__ __forceinline__ V3<R> rotate( V3<R> v, V3<R> axis, R angle )
+{
+    R sn, cs;
+    sincos( angle, &sn, &cs );
+    V3<R> ax = cross( axis, v );
+    R ad     = dot( axis, v );
+    R omc    = R( 1 ) - cs;
+    return { v.x * cs + ax.x * sn + axis.x * ad * omc, v.y * cs + ax.y * sn + axis.y * ad * omc,
+             v.z * cs + ax.z * sn + axis.z * ad * omc };
+}
+
+template<typename R>
+__device__ __forceinline__ R torque2( V3<R> fv, V3<R> s )
+{
+    R d      = dot( fv, s );
+    V3<R> t  = { fv.x - d * s.x, fv.y - d * s.y, fv.z - d * s.z };
+    return dot( t, t );
+}
+
+
+} // namespace sg

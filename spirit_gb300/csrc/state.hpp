@@ -1,0 +1,133 @@
+// Host data model behind the C API: a State holds one chain of images (spin systems); each
+// image owns its geometry, Heisenberg parameters, LLG parameters and the host mirror of its
+// spins in the API scalar type (double, AoS [nos][3], the buffer System_Get_Spin_Directions
+// hands out).  Mirrors core/include/data/State.hpp, Spin_System.hpp, Spin_System_Chain.hpp.
+#pragma once
+#include "engine.hpp"
+#include "geometry.hpp"
+
+#include <atomic>
+#include <chrono>
+#include <memory>
+#include <mutex>
+#include <random>
+#include <string>
+#include <vector>
+
+namespace sg
+{
+
+struct LLGParams
+{
+    double dt                 = 1e-3;
+    double damping            = 0.3;
+    double beta               = 0;
+    double temperature        = 0;
+    double force_convergence  = 1e-10;
+    bool direct_minimization  = false;
+    long n_iterations         = 1000000;
+    long n_iterations_log     = 1000;
+    long max_walltime_sec     = 0;
+    int rng_seed              = 2006;
+    std::string output_folder = "output";
+    std::string output_tag    = "<time>";
+};
+
+struct GNEBParams
+{
+    double spring_constant          = 1;
+    double spring_force_ratio       = 0;
+    double path_shortening_constant = 0;
+    double force_convergence        = 1e-10;
+    int n_E_interpolations          = 10;
+    long n_iterations               = 1000000;
+    long n_iterations_log           = 1000;
+    long max_walltime_sec           = 0;
+    bool moving_endpoints           = false;
+    bool translating_endpoints      = false;
+    double eq_delta_Rx_left = 1, eq_delta_Rx_right = 1;
+    std::string output_folder = "output";
+    std::string output_tag    = "<time>";
+};
+
+// per-run bookkeeping of a method (Method.hpp members the API reports)
+struct MethodInfo
+{
+    std::string method = "None", solver = "None";
+    int solver_id       = -1;
+    int iteration       = 0;
+    double time_ps      = 0;
+    float max_torque    = 0;
+    double ips          = 0;
+    long long wall_ms   = 0;
+    int n_iterations    = 0;
+    std::chrono::steady_clock::time_point t_start;
+};
+
+struct Image
+{
+    std::shared_ptr<Geometry> geom;
+    HamiltonianParams ham;
+    LLGParams llg;
+    std::vector<double> spins;     // API mirror, AoS
+    std::vector<double> eff_field; // AoS
+    std::vector<double> positions; // AoS
+    double E = 0;
+    int gneb_type = 0; // GNEB_IMAGE_NORMAL
+    std::atomic<bool> iteration_allowed{ false };
+    bool singleshot_allowed = false;
+    MethodInfo info;
+    std::mt19937 prng{ 2006 };
+    std::recursive_mutex mtx;
+    // device engines (cached; rebuilt when `version` changes)
+    long version = 0;
+    std::unique_ptr<Engine> eval64;
+    long eval64_version = -1;
+    std::unique_ptr<Engine> run;
+    long run_version  = -1;
+    bool run_fp64     = false;
+    std::shared_ptr<void> vp_run; // single-shot LLG run with the VP solver
+
+    int nos() const
+    {
+        return geom->nos();
+    }
+    void touch()
+    {
+        ++version;
+    }
+};
+
+struct Chain
+{
+    std::vector<std::shared_ptr<Image>> images;
+    GNEBParams gneb;
+    std::vector<double> Rx, Rx_interpolated, E_interpolated;
+    std::atomic<bool> iteration_allowed{ false };
+    bool singleshot_allowed = false;
+    MethodInfo info;
+    std::recursive_mutex mtx;
+    std::shared_ptr<void> gneb_run; // GNEB engine of a running/singleshot chain method
+    std::vector<double> torques;    // per-image max torque of the last GNEB iteration
+};
+
+struct State
+{
+    std::shared_ptr<Chain> chain;
+    int idx_active_image = 0;
+    std::shared_ptr<Image> clipboard;
+    std::string config_file;
+    bool quiet = false;
+    int precision = 32; // device arithmetic of the LLG/GNEB step loop: 32 (FP32 bulk) or 64
+    std::string datetime;
+    std::vector<std::string> log;
+    int log_console_level = 2;
+};
+
+std::shared_ptr<Image> make_image_from_config( const std::string & cfg, State & st );
+std::shared_ptr<Image> clone_image( const Image & src );
+void refresh_positions( Image & img );
+Engine & eval_engine( Image & img );
+void log_msg( State * st, int level, const std::string & msg );
+
+} // namespace sg

@@ -1,0 +1,68 @@
+// CUDA error handling and device-memory helpers.  Device errors become C++ exceptions on the
+// host; the C API catches them per call (the reference logs and, for CUDA errors, exits the
+// process: core/src/utility/Exception.cpp:70-110 -- here the API reports and returns instead).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <stdexcept>
+#include <string>
+
+namespace sg
+{
+
+struct CudaError : std::runtime_error
+{
+    using std::runtime_error::runtime_error;
+};
+
+inline void cuda_check( cudaError_t e, const char * what, const char * file, int line )
+{
+    if( e != cudaSuccess )
+        throw CudaError( std::string( "CUDA error in " ) + what + " (" + file + ":" + std::to_string( line )
+                         + "): " + cudaGetErrorString( e ) );
+}
+
+#define CUDA_CHECK( x ) ::sg::cuda_check( ( x ), #x, __FILE__, __LINE__ )
+
+inline void * dalloc_bytes( size_t bytes )
+{
+    void * p = nullptr;
+    if( bytes == 0 )
+        bytes = 16;
+    CUDA_CHECK( cudaMalloc( &p, bytes ) );
+    CUDA_CHECK( cudaMemset( p, 0, bytes ) );
+    return p;
+}
+
+template<typename T>
+inline T * dalloc( size_t n )
+{
+    return static_cast<T *>( dalloc_bytes( n * sizeof( T ) ) );
+}
+
+template<typename T>
+inline void dfree( T *& p )
+{
+    if( p )
+        cudaFree( (void *)p );
+    p = nullptr;
+}
+
+template<typename T>
+inline void h2d( T * d, const T * h, size_t n )
+{
+    CUDA_CHECK( cudaMemcpy( d, h, n * sizeof( T ), cudaMemcpyHostToDevice ) );
+}
+
+inline void h2d_bytes( void * d, const void * h, size_t n )
+{
+    CUDA_CHECK( cudaMemcpy( d, h, n, cudaMemcpyHostToDevice ) );
+}
+
+template<typename T>
+inline void d2h( T * h, const T * d, size_t n )
+{
+    CUDA_CHECK( cudaMemcpy( h, d, n * sizeof( T ), cudaMemcpyDeviceToHost ) );
+}
+
+} // namespace sg
