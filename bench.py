@@ -1,0 +1,302 @@
+#!/usr/bin/env python
+"""Benchmark: spin-updates/s of LLG with dipolar interaction on one GB300.
+
+Workload (one "step" = one stochastic Heun iteration of the whole system, both predictor and
+corrector stages, each with the full dipolar FFT convolution):
+    simple cubic 128 x 128 x 16, lattice constant 4 Angstrom, mu_s = 2 mu_B, J = 1 meV (nearest
+    neighbours), bulk (Bloch) DMI D = 0.2 meV, uniaxial K = 0.05 meV along z, B_z = 0.5 T,
+    periodic in a and b, open in c; dipole-dipole by zero-padded FFT (padding along c only:
+    the "2N" padded volume 128 x 128 x 32, 4 periodic images in a and b);
+    T = 10 K (Philox thermal noise), alpha = 0.1, dt = 5e-4 ps, FP32 bulk arithmetic.
+Inputs are seeded random unit spins; the device timing flushes L2 (writes a 512 MiB buffer)
+before every timed step, because the working set (~35 MB) would otherwise stay in the 129 MB L2.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Under torchrun every rank runs an independent replica (the path has no exchange between
+systems: "replicas only"); rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "spin-updates/s LLG+dipolar, batched vs plain on 1 GB300 at max|Δm|<=1e-5; vs CPU"
+N_CELLS = [128, 128, 16]
+SPEC = dict(
+    bravais="sc", n_cells=N_CELLS, lattice_constant=4.0, mu_s=[2.0], bc=[1, 1, 0],
+    field=(0.5, (0, 0, 1)), anisotropy=(0.05, (0, 0, 1)), jij=[1.0], dij=[0.2], dm_chirality=1,
+    ddi=dict(method="fft", n_periodic_images=[4, 4, 0], radius=0.0, pb_zero_padding=0),
+    llg=dict(dt=5e-4, damping=0.1, temperature=10.0, seed=2, force_convergence=1e-10),
+)
+NOS = N_CELLS[0] * N_CELLS[1] * N_CELLS[2]
+CONFIG = {
+    "workload": "SC 128x128x16 LLG stochastic Heun T=10K + DDI FFT (2N z-padding), FP32 bulk",
+    "n_spins": NOS, "solver": "Heun", "dt_ps": 5e-4, "alpha": 0.1, "temperature_K": 10.0,
+    "ddi_padded_extent": [128, 128, 32], "l2": "flushed before every timed step (512 MiB write)",
+}
+KERNELS = ["stage", "fft_pass_a", "fft_pass_b", "fft_pass_c_tensor", "fft_pass_b_inv", "fft_pass_a_inv_c2r"]
+
+
+def algorithmic_bytes(kernel, stage):
+    """Algorithmic HBM bytes of one launch at the workload size, FP32 (SoA spins 12 B/spin,
+    complex 8 B).  Stage 1 of Heun reads s and h, writes predictor and fv1 (48 B/spin); stage 2
+    reads predictor, s, fv1, h and writes s (60 B/spin).  FFT passes read and write their
+    half-spectrum arrays once; pass C also reads the 6-component dipole spectrum."""
+    Mh, Mb, Mc, Nb, Nc = 65, 128, 32, 128, 16
+    W1 = 3 * Nc * Nb * Mh * 8
+    W2 = 3 * Nc * Mb * Mh * 8
+    D = 6 * Mc * Mb * Mh * 8
+    S = 12 * NOS
+    return {
+        "stage": (48 if stage == 1 else 60) * NOS,
+        "fft_pass_a": S + W1,
+        "fft_pass_b": W1 + W2,
+        "fft_pass_c_tensor": 2 * W2 + D,
+        "fft_pass_b_inv": W2 + W1,
+        "fft_pass_a_inv_c2r": W1 + S,
+    }[kernel]
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 6:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax = max(smax, float(p[1]))
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if p[2 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_baseline(seconds=12.0):
+    """The oracle (CPU FP64 restatement of the reference path, OpenMP over all host cores) on a
+    bounded sample of the same workload: as many Heun steps as fit in ~`seconds`."""
+    from oracle.oracle import OracleSystem, random_spins
+
+    o = OracleSystem(SPEC)
+    s0 = random_spins(NOS, 1)
+    t0 = time.perf_counter()
+    o.llg(s0, "Heun", 1, dt=5e-4, damping=0.1, temperature=10.0, seed=2)
+    t1 = time.perf_counter() - t0
+    n = max(1, min(40, int(seconds / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    o.llg(s0, "Heun", n, dt=5e-4, damping=0.1, temperature=10.0, seed=2)
+    dt = time.perf_counter() - t0
+    return {"value": NOS * n / dt, "unit": "spin-updates/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "%d stochastic Heun steps of the full 128x128x16 DDI system (FP64, OpenMP)" % n}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    steps = []
+    for k in range(args.warmup + args.steps):
+        r = cpu_baseline(seconds=4.0)
+        if k >= args.warmup:
+            steps.append(r)
+    v = statistics.median([s["value"] for s in steps])
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "spin-updates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * NOS / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random spins)",
+        "config": CONFIG,
+        "cpu_baseline": {"value": v, "unit": "spin-updates/s", "cores": steps[0]["cores"], "kind": "port",
+                         "sample": steps[0]["sample"] + " per step"},
+        "e2e": {"value": v, "unit": "spin-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gb300(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from spirit_gb300 import build as _b
+
+    if not os.path.exists(os.path.join(ROOT, "spirit_gb300", "libspirit_gb300.so")):
+        _b.build()
+    import ctypes
+
+    from oracle.oracle import random_spins
+    from spirit_gb300 import simulation, state, system
+    from spirit_gb300.configs import write_config
+    from spirit_gb300.spiritlib import fn
+
+    profile = fn("Simulation_Profile_Steps", [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong,
+                                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
+                                              ctypes.c_int, ctypes.c_int])
+    launch = fn("Simulation_Launch_Steps", [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int])
+    kps = fn("Simulation_Get_Kernels_Per_Step", [ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int)
+    cfg = write_config(SPEC, os.path.join(tempfile.mkdtemp(), "bench.cfg"))
+    p = state.setup(cfg, True)
+    system.get_spin_directions(p)[:] = random_spins(NOS, 1 + rank)
+    simulation.set_precision(p, 32)
+    stream = torch.cuda.Stream()
+    simulation.set_stream(p, stream.cuda_stream)
+    flush = torch.empty(512 * 2**20, dtype=torch.uint8, device="cuda")
+    # --- device-timed steps (inputs resident in HBM)
+    simulation.start(p, simulation.METHOD_LLG, simulation.SOLVER_HEUN, 10**9, -1, True)
+    launch(p, args.warmup, -1, -1)
+    stream.synchronize()
+    e0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    e1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)
+                e0[k].record(stream)
+            launch(p, 1, -1, -1)
+            e1[k].record(stream)
+        stream.synchronize()
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in zip(e0, e1))
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    n_kernels = kps(p, -1, -1)
+    value = NOS * args.steps * world / (ms / 1000.0)
+    # --- per-kernel durations (CUDA events between launches, L2 flushed before every step)
+    kms = (ctypes.c_double * 16)()
+    kcount = (ctypes.c_int * 16)()
+    profile(p, args.steps, ctypes.c_void_p(flush.data_ptr()), flush.numel(), kms, kcount, -1, -1)
+    stream.synchronize()
+    per = {KERNELS[i]: (kms[i], kcount[i]) for i in range(len(KERNELS)) if kcount[i] > 0}
+    total = sum(v[0] for v in per.values())
+    dom = max(per, key=lambda k: per[k][0])
+    avg_ms = per[dom][0] / per[dom][1]
+    if dom == "stage":
+        # both Heun stages share the kernel name; average their algorithmic bytes
+        alg = 0.5 * (algorithmic_bytes("stage", 1) + algorithmic_bytes("stage", 2))
+    else:
+        alg = algorithmic_bytes(dom, 1)
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (avg_ms * 1e-3) / 1e9
+    # --- end to end through the public API: every step uploads the host spin buffer (H2D),
+    # runs one Heun step and brings the spins back (D2H) -- Simulation_SingleShot semantics
+    simulation.stop(p)
+    simulation.set_stream(p, None)
+    simulation.start(p, simulation.METHOD_LLG, simulation.SOLVER_HEUN, 10**9, -1, True)
+    for _ in range(args.warmup):
+        simulation.single_shot(p)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        simulation.single_shot(p)
+    e2e_s = time.perf_counter() - t0
+    simulation.stop(p)
+    state.delete(p)
+    if rank != 0:
+        return
+    cpu = cpu_baseline() if world == 1 else None
+    line = {
+        "metric": METRIC, "value": value, "unit": "spin-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded random spins)", "config": CONFIG,
+        "e2e": {"value": NOS * args.steps / e2e_s, "unit": "spin-updates/s",
+                "h2d_bytes_per_step": NOS * 3 * 8, "d2h_bytes_per_step": NOS * 3 * 8},
+        "gpu_launches": n_kernels * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_ms},
+        "kernel_share": {k: round(v[0] / total, 4) for k, v in per.items()},
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

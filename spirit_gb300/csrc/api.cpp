@@ -102,6 +102,7 @@ Engine & run_engine( State * st, Image & img )
         img.run_version = img.version;
         img.run_fp64    = fp64;
     }
+    img.run->set_stream( (cudaStream_t)st->stream );
     return *img.run;
 }
 
@@ -1792,7 +1793,9 @@ void Simulation_N_Shot( State * state, int N, int idx_image, int idx_chain ) noe
             return;
         }
         Engine & E = *img.run;
-        auto s     = E.status()[0];
+        // the host spin buffer is the state: callers may have written into it since the last call
+        E.set_spins( 0, img.spins.data() );
+        auto s = E.status()[0];
         if( s.active )
         {
             E.llg_launch( N );
@@ -2039,6 +2042,94 @@ void Simulation_GNEB_Start( State * state, int solver_type, int n_iterations, in
 }
 
 // ---- extensions
+// Run the device work of this State on the caller's CUDA stream (nullptr: the engine's own).
+void Simulation_Set_Stream( State * state, void * stream ) noexcept
+{
+    try
+    {
+        state->stream = stream;
+        for( auto & img : state->chain->images )
+            if( img->run )
+                img->run->set_stream( (cudaStream_t)stream );
+    }
+    catch( ... )
+    {
+        handle( state, "Simulation_Set_Stream" );
+    }
+}
+
+// Launch n steps of a started single-shot LLG run without host transfers or synchronisation
+// (for pipelined callers and device-side timing); Simulation_SingleShot/N_Shot or
+// System_Update_Spins_From_Device bring the spins back.
+void Simulation_Launch_Steps( State * state, int n, int idx_image, int idx_chain ) noexcept
+{
+    try
+    {
+        auto I = from_indices( state, idx_image, idx_chain );
+        if( !( I.img->iteration_allowed && I.img->singleshot_allowed ) || !I.img->run )
+        {
+            log_msg( state, 2, "Simulation_Launch_Steps needs a started single-shot LLG simulation" );
+            return;
+        }
+        I.img->run->llg_launch( n );
+    }
+    catch( ... )
+    {
+        handle( state, "Simulation_Launch_Steps" );
+    }
+}
+
+// Wait for the device work of the image and copy its spins into the host buffer.
+void System_Update_Spins_From_Device( State * state, int idx_image, int idx_chain ) noexcept
+{
+    try
+    {
+        auto I = from_indices( state, idx_image, idx_chain );
+        if( I.img->run )
+        {
+            I.img->run->sync();
+            finish_llg( *I.img, *I.img->run );
+        }
+    }
+    catch( ... )
+    {
+        handle( state, "System_Update_Spins_From_Device" );
+    }
+}
+
+// Per-kernel device time of n steps of the started single-shot LLG run (CUDA events between the
+// launches on the engine stream); ms[] and count[] have KERNEL_ID slots (stage, FFT passes A, B,
+// C, B', A').  flush_buf/flush_bytes: device buffer overwritten before every step (L2 flush).
+void Simulation_Profile_Steps( State * state, int n, void * flush_buf, long long flush_bytes, double * ms,
+                               int * count, int idx_image, int idx_chain ) noexcept
+{
+    try
+    {
+        auto I = from_indices( state, idx_image, idx_chain );
+        if( !I.img->run )
+            return;
+        I.img->run->profile_steps( n, flush_buf, (size_t)flush_bytes, ms, count );
+    }
+    catch( ... )
+    {
+        handle( state, "Simulation_Profile_Steps" );
+    }
+}
+
+// Device kernels launched per step of the image's current LLG method.
+int Simulation_Get_Kernels_Per_Step( State * state, int idx_image, int idx_chain ) noexcept
+{
+    try
+    {
+        auto I = from_indices( state, idx_image, idx_chain );
+        return I.img->run ? I.img->run->kernels_per_step() : 0;
+    }
+    catch( ... )
+    {
+        return 0;
+    }
+}
+
 void Simulation_Set_Precision( State * state, int bits ) noexcept
 {
     if( bits == 32 || bits == 64 )

@@ -17,6 +17,19 @@ constexpr int MAX_PAIRS        = 96; // merged exchange+DMI pairs over all basis
 constexpr int SPIN_ALIGN       = 32;
 constexpr int MAX_FFT_LEN      = 1024;
 
+// kernel ids of the per-launch profiling trace
+enum KernelId : int
+{
+    KERNEL_STAGE = 0,
+    KERNEL_PASS_A,
+    KERNEL_PASS_B,
+    KERNEL_PASS_C,
+    KERNEL_PASS_B_INV,
+    KERNEL_PASS_A_INV,
+    KERNEL_END,
+    N_KERNEL_IDS
+};
+
 // LLG solver ids (core/include/Spirit/Simulation.h): VP=0, SIB=1, Depondt=2, Heun=3, RK4=4
 enum Solver : int
 {

@@ -699,15 +699,29 @@ void DDIPlan::run_t( const SysDesc * d_sd, const SysRun * runs, const R * sx, co
     a.mode        = 0;
     size_t elem   = sizeof( cplx<R> );
     (void)elem;
+    auto mark = [&]( int id ) {
+        if( trace )
+        {
+            cudaEvent_t e;
+            CUDA_CHECK( cudaEventCreate( &e ) );
+            CUDA_CHECK( cudaEventRecord( e, stream ) );
+            trace->push_back( { id, e } );
+        }
+    };
     a.blocks = (const int4 *)d_blocks[0];
+    mark( KERNEL_PASS_A );
     pass_a<R><<<n_blocks[0], 256, max_smem_a, stream>>>( a );
     a.blocks = (const int4 *)d_blocks[1];
+    mark( KERNEL_PASS_B );
     pass_b<R><<<n_blocks[1], 256, max_smem_b, stream>>>( a, 0 );
     a.blocks = (const int4 *)d_blocks[2];
+    mark( KERNEL_PASS_C );
     pass_c<R><<<n_blocks[2], 256, max_smem_c, stream>>>( a );
     a.blocks = (const int4 *)d_blocks[1];
+    mark( KERNEL_PASS_B_INV );
     pass_b<R><<<n_blocks[1], 256, max_smem_b, stream>>>( a, 1 );
     a.blocks = (const int4 *)d_blocks[0];
+    mark( KERNEL_PASS_A_INV );
     pass_a_inv<R><<<n_blocks[0], 256, max_smem_a, stream>>>( a );
     CUDA_CHECK( cudaGetLastError() );
 }

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <array>
+#include <utility>
 #include <vector>
 
 namespace sg
@@ -32,6 +33,8 @@ public:
     void run( const SysDesc * d_sd, const SysRun * runs, const void * sx, const void * sy, const void * sz,
               void * hx, void * hy, void * hz, cudaStream_t stream ) const;
     void release();
+    // optional per-launch event trace (kernel id, event recorded before the launch)
+    std::vector<std::pair<int, cudaEvent_t>> * trace = nullptr;
     int n_sys = 0;
     bool fp64 = false;
 

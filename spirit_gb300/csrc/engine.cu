@@ -439,7 +439,8 @@ static void fill_desc( SysDesc & d, const SystemInput & in )
 Engine::Engine( const std::vector<SystemInput> & systems, bool fp64 ) : fp64_( fp64 )
 {
     elem_ = fp64 ? sizeof( double ) : sizeof( float );
-    CUDA_CHECK( cudaStreamCreateWithFlags( &stream_, cudaStreamNonBlocking ) );
+    CUDA_CHECK( cudaStreamCreateWithFlags( &own_stream_, cudaStreamNonBlocking ) );
+    stream_ = own_stream_;
     build_systems( systems );
 }
 
@@ -447,6 +448,8 @@ Engine::~Engine()
 {
     if( graph_ )
         cudaGraphExecDestroy( graph_ );
+    if( graph1_ )
+        cudaGraphExecDestroy( graph1_ );
     for( int c = 0; c < 3; ++c )
     {
         dfree( spins_[c] );
@@ -463,8 +466,14 @@ Engine::~Engine()
     dfree( d_grad_ );
     dfree( d_blkmap_ );
     dfree( d_blkcount_ );
-    if( stream_ )
-        cudaStreamDestroy( stream_ );
+    if( own_stream_ )
+        cudaStreamDestroy( own_stream_ );
+}
+
+void Engine::set_stream( cudaStream_t s )
+{
+    CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+    stream_ = s ? s : own_stream_;
 }
 
 void Engine::build_systems( const std::vector<SystemInput> & systems )
@@ -688,9 +697,21 @@ void Engine::ddi_field( int s, double * h_aos )
     CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
 }
 
-template<typename R, int SOLVER, int STAGE>
-static void launch_stage( int nblk, cudaStream_t st, const StageArgs<R> & a )
+static void trace_mark( std::vector<std::pair<int, cudaEvent_t>> * trace, int id, cudaStream_t st )
 {
+    if( !trace )
+        return;
+    cudaEvent_t e;
+    CUDA_CHECK( cudaEventCreate( &e ) );
+    CUDA_CHECK( cudaEventRecord( e, st ) );
+    trace->push_back( { id, e } );
+}
+
+template<typename R, int SOLVER, int STAGE>
+static void launch_stage( int nblk, cudaStream_t st, const StageArgs<R> & a,
+                          std::vector<std::pair<int, cudaEvent_t>> * trace = nullptr )
+{
+    trace_mark( trace, KERNEL_STAGE, st );
     llg_stage<R, SOLVER, STAGE><<<nblk, 256, 0, st>>>( a );
 }
 
@@ -744,19 +765,19 @@ void Engine::launch_step_t()
         a.out = pA;
         field( a.cfg );
         if( solver_ == SOLVER_SIB )
-            launch_stage<R, SOLVER_SIB, 1>( nb, stream_, a );
+            launch_stage<R, SOLVER_SIB, 1>( nb, stream_, a, trace_ );
         else if( solver_ == SOLVER_HEUN )
-            launch_stage<R, SOLVER_HEUN, 1>( nb, stream_, a );
+            launch_stage<R, SOLVER_HEUN, 1>( nb, stream_, a, trace_ );
         else
-            launch_stage<R, SOLVER_DEPONDT, 1>( nb, stream_, a );
+            launch_stage<R, SOLVER_DEPONDT, 1>( nb, stream_, a, trace_ );
         a.cfg = pA;
         field( a.cfg );
         if( solver_ == SOLVER_SIB )
-            launch_stage<R, SOLVER_SIB, 2>( nb, stream_, a );
+            launch_stage<R, SOLVER_SIB, 2>( nb, stream_, a, trace_ );
         else if( solver_ == SOLVER_HEUN )
-            launch_stage<R, SOLVER_HEUN, 2>( nb, stream_, a );
+            launch_stage<R, SOLVER_HEUN, 2>( nb, stream_, a, trace_ );
         else
-            launch_stage<R, SOLVER_DEPONDT, 2>( nb, stream_, a );
+            launch_stage<R, SOLVER_DEPONDT, 2>( nb, stream_, a, trace_ );
         break;
     }
     case SOLVER_RK4:
@@ -764,18 +785,18 @@ void Engine::launch_step_t()
         a.cfg = a.s;
         a.out = pA;
         field( a.cfg );
-        launch_stage<R, SOLVER_RK4, 1>( nb, stream_, a );
+        launch_stage<R, SOLVER_RK4, 1>( nb, stream_, a, trace_ );
         a.cfg = pA;
         a.out = pB;
         field( a.cfg );
-        launch_stage<R, SOLVER_RK4, 2>( nb, stream_, a );
+        launch_stage<R, SOLVER_RK4, 2>( nb, stream_, a, trace_ );
         a.cfg = pB;
         a.out = pA;
         field( a.cfg );
-        launch_stage<R, SOLVER_RK4, 3>( nb, stream_, a );
+        launch_stage<R, SOLVER_RK4, 3>( nb, stream_, a, trace_ );
         a.cfg = pA;
         field( a.cfg );
-        launch_stage<R, SOLVER_RK4, 4>( nb, stream_, a );
+        launch_stage<R, SOLVER_RK4, 4>( nb, stream_, a, trace_ );
         break;
     }
     default:
@@ -790,6 +811,33 @@ void Engine::launch_step_kernels()
         launch_step_t<double>();
     else
         launch_step_t<float>();
+}
+
+void Engine::profile_steps( int n, void * flush_buf, size_t flush_bytes, double * ms, int * count )
+{
+    std::vector<std::pair<int, cudaEvent_t>> tr;
+    for( int k = 0; k < n; ++k )
+    {
+        if( flush_buf && flush_bytes )
+            CUDA_CHECK( cudaMemsetAsync( flush_buf, k & 0xff, flush_bytes, stream_ ) );
+        tr.clear();
+        trace_    = &tr;
+        ddi_.trace = &tr;
+        launch_step_kernels();
+        trace_mark( &tr, KERNEL_END, stream_ );
+        trace_     = nullptr;
+        ddi_.trace = nullptr;
+        CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+        for( size_t e = 0; e + 1 < tr.size(); ++e )
+        {
+            float t = 0;
+            CUDA_CHECK( cudaEventElapsedTime( &t, tr[e].second, tr[e + 1].second ) );
+            ms[tr[e].first] += t;
+            count[tr[e].first] += 1;
+        }
+        for( auto & x : tr )
+            cudaEventDestroy( x.second );
+    }
 }
 
 int Engine::kernels_per_step() const
@@ -823,19 +871,25 @@ void Engine::llg_start( int solver, const std::vector<int> & n_iterations )
 
 void Engine::llg_launch( int n_steps )
 {
-    // steps are replayed from a CUDA graph of G steps; surplus steps are no-ops on the device
+    // steps are replayed from CUDA graphs of G steps and of one step; steps beyond a system's
+    // budget or after its convergence are no-ops on the device
     const int G = 8;
     if( !graph_ || graph_solver_ != solver_ )
     {
         if( graph_ )
             cudaGraphExecDestroy( graph_ );
-        cudaGraph_t g;
-        CUDA_CHECK( cudaStreamBeginCapture( stream_, cudaStreamCaptureModeThreadLocal ) );
-        for( int k = 0; k < G; ++k )
-            launch_step_kernels();
-        CUDA_CHECK( cudaStreamEndCapture( stream_, &g ) );
-        CUDA_CHECK( cudaGraphInstantiate( &graph_, g, 0 ) );
-        cudaGraphDestroy( g );
+        if( graph1_ )
+            cudaGraphExecDestroy( graph1_ );
+        for( int which = 0; which < 2; ++which )
+        {
+            cudaGraph_t g;
+            CUDA_CHECK( cudaStreamBeginCapture( stream_, cudaStreamCaptureModeThreadLocal ) );
+            for( int k = 0; k < ( which == 0 ? G : 1 ); ++k )
+                launch_step_kernels();
+            CUDA_CHECK( cudaStreamEndCapture( stream_, &g ) );
+            CUDA_CHECK( cudaGraphInstantiate( which == 0 ? &graph_ : &graph1_, g, 0 ) );
+            cudaGraphDestroy( g );
+        }
         graph_solver_ = solver_;
         graph_steps_  = G;
     }
@@ -843,7 +897,7 @@ void Engine::llg_launch( int n_steps )
     for( int k = 0; k < full; ++k )
         CUDA_CHECK( cudaGraphLaunch( graph_, stream_ ) );
     for( int k = 0; k < rem; ++k )
-        launch_step_kernels();
+        CUDA_CHECK( cudaGraphLaunch( graph1_, stream_ ) );
 }
 
 void Engine::sync()

@@ -93,7 +93,14 @@ public:
     {
         return stream_;
     }
+    // run on a caller's stream (e.g. a framework stream whose events time the kernels);
+    // nullptr returns to the engine's own stream
+    void set_stream( cudaStream_t s );
     int kernels_per_step() const;
+    // n steps launched kernel by kernel with CUDA events between launches on the engine stream;
+    // before every step `flush_bytes` of `flush_buf` are overwritten (L2 flush; may be null).
+    // Adds per-kernel-id total ms and launch counts (arrays of N_KERNEL_IDS).
+    void profile_steps( int n, void * flush_buf, size_t flush_bytes, double * ms, int * count );
     // DDI field h of the current spins (tests)
     void ddi_field( int s, double * h_aos );
 
@@ -155,6 +162,7 @@ private:
     bool fp64_;
     size_t elem_;
     cudaStream_t stream_ = nullptr;
+    cudaStream_t own_stream_ = nullptr;
     std::vector<SysDesc> desc_;
     std::vector<const Geometry *> geoms_;
     SysDesc * d_desc_ = nullptr;
@@ -178,6 +186,8 @@ private:
     DDIPlan ddi_;
     int solver_       = SOLVER_HEUN;
     cudaGraphExec_t graph_ = nullptr;
+    cudaGraphExec_t graph1_ = nullptr; // single step
+    std::vector<std::pair<int, cudaEvent_t>> * trace_ = nullptr;
     int graph_steps_       = 0;
     int graph_solver_      = -1;
 };

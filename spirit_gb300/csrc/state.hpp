@@ -119,6 +119,7 @@ struct State
     std::string config_file;
     bool quiet = false;
     int precision = 32; // device arithmetic of the LLG/GNEB step loop: 32 (FP32 bulk) or 64
+    void * stream = nullptr; // caller-provided cudaStream_t for the device work (optional)
     std::string datetime;
     std::vector<std::string> log;
     int log_console_level = 2;

@@ -140,3 +140,12 @@ def set_precision(p_state, bits):
 
 def get_precision(p_state):
     return int(_Get_Precision(_vp(p_state)))
+
+
+_Set_Stream = fn("Simulation_Set_Stream", [_vp, _vp])
+
+
+def set_stream(p_state, stream):
+    """Run this State's device work on a caller CUDA stream (a cudaStream_t as int), or on the
+    engine's own stream with None (extension)."""
+    _Set_Stream(_vp(p_state), _vp(stream) if stream else None)
