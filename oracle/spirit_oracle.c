@@ -1118,17 +1118,19 @@ void og_philox4x32( const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4
 }
 
 /* Gaussian triple for spin i at a given iteration: counter (i, iteration, stream, 0x53504E00),
- * key (seed lo, seed hi); uniforms u = (x + 0.5) 2^-32; Box-Muller on (u0,u1) and (u2,u3). */
+ * key (seed lo, seed hi); 23-bit uniforms u = ((x >> 9) + 1/2) 2^-23 (exact in FP32 and FP64);
+ * Box-Muller on (u0,u1) and (u2,u3).  The CUDA kernels use the same mapping. */
 static void gauss3( uint64_t seed, uint32_t stream, uint32_t iteration, uint32_t i, double * z )
 {
     uint32_t ctr[4] = { i, iteration, stream, 0x53504E00u };
     uint32_t key[2] = { (uint32_t)seed, (uint32_t)( seed >> 32 ) };
     uint32_t x[4];
     og_philox4x32( ctr, key, x );
-    double u0 = ( x[0] + 0.5 ) * ( 1.0 / 4294967296.0 );
-    double u1 = ( x[1] + 0.5 ) * ( 1.0 / 4294967296.0 );
-    double u2 = ( x[2] + 0.5 ) * ( 1.0 / 4294967296.0 );
-    double u3 = ( x[3] + 0.5 ) * ( 1.0 / 4294967296.0 );
+    const double sc = 1.0 / 8388608.0;
+    double u0 = ( (double)( x[0] >> 9 ) + 0.5 ) * sc;
+    double u1 = ( (double)( x[1] >> 9 ) + 0.5 ) * sc;
+    double u2 = ( (double)( x[2] >> 9 ) + 0.5 ) * sc;
+    double u3 = ( (double)( x[3] >> 9 ) + 0.5 ) * sc;
     double r0 = sqrt( -2.0 * log( u0 ) );
     double r1 = sqrt( -2.0 * log( u2 ) );
     z[0]      = r0 * cos( 2.0 * C_PI * u1 );

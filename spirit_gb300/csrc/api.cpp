@@ -2099,16 +2099,17 @@ void System_Update_Spins_From_Device( State * state, int idx_image, int idx_chai
 
 // Per-kernel device time of n steps of the started single-shot LLG run (CUDA events between the
 // launches on the engine stream); ms[] and count[] have KERNEL_ID slots (stage, FFT passes A, B,
-// C, B', A').  flush_buf/flush_bytes: device buffer overwritten before every step (L2 flush).
-void Simulation_Profile_Steps( State * state, int n, void * flush_buf, long long flush_bytes, double * ms,
-                               int * count, int idx_image, int idx_chain ) noexcept
+// C, B', A').  Before every step flush_buf is overwritten and read_buf read (L2 flush that leaves
+// clean lines); both may be null.
+void Simulation_Profile_Steps( State * state, int n, void * flush_buf, long long flush_bytes, void * read_buf,
+                               long long read_bytes, double * ms, int * count, int idx_image, int idx_chain ) noexcept
 {
     try
     {
         auto I = from_indices( state, idx_image, idx_chain );
         if( !I.img->run )
             return;
-        I.img->run->profile_steps( n, flush_buf, (size_t)flush_bytes, ms, count );
+        I.img->run->profile_steps( n, flush_buf, (size_t)flush_bytes, read_buf, (size_t)read_bytes, ms, count );
     }
     catch( ... )
     {

@@ -7,6 +7,8 @@
 // 32 so every system starts on a 128-byte boundary.  Inside a system the spin index is the
 // reference's ispin = ib + nb * (a + Na * (b + Nb * c)) (core/include/engine/Vectormath.hpp:61-74).
 #pragma once
+#include <cuda_runtime.h>
+
 #include <cstdint>
 
 namespace sg
@@ -50,6 +52,30 @@ struct PairEntry
     double D[3];
 };
 
+struct FFTDesc;
+
+// Per-system constants of the stage arithmetic, precomputed on the host in FP64 and kept in
+// the precision of the kernel that reads them (no FP64 division or square root on the device).
+template<typename R>
+struct SysConst
+{
+    R dtg;                      // dt gamma / mu_B / (1 + alpha^2)          (Method_LLG.cpp:152)
+    R dtga;                     // dtg * alpha
+    R alpha;
+    R kdm;                      // dt gamma / mu_B: direct minimisation / VP (Method_LLG.cpp:165)
+    R dt;
+    R noise[MAX_BASIS];         // epsilon sqrt(T / mu_s)                   (Method_LLG.cpp:72-107)
+    R mu[MAX_BASIS];
+    R zeeman[3];                // mu_B B n
+    R aniso_K[MAX_BASIS];
+    R aniso_n[MAX_BASIS][3];
+    int aniso_idx[MAX_BASIS];
+    int n_aniso;
+    int has_zeeman;
+    int thermal;
+    int direct;
+};
+
 // Per-system constants.  Read by every kernel; double so the FP64 path loses nothing.
 struct SysDesc
 {
@@ -79,7 +105,26 @@ struct SysDesc
     // DDI
     int ddi;                    // 0 none, 1 FFT
     int fft_slot;               // index into the batch's FFT plan table
+    SysConst<float> cf;
+    SysConst<double> cd;
 };
+
+template<typename R>
+__host__ __device__ inline const SysConst<R> & sys_const( const SysDesc & d );
+template<typename R>
+__host__ __device__ inline R fft_mu( const FFTDesc & f, int ib );
+template<typename R>
+__host__ __device__ inline R fft_invT( const FFTDesc & f );
+template<>
+__host__ __device__ inline const SysConst<float> & sys_const<float>( const SysDesc & d )
+{
+    return d.cf;
+}
+template<>
+__host__ __device__ inline const SysConst<double> & sys_const<double>( const SysDesc & d )
+{
+    return d.cd;
+}
 
 // Mutable per-system run state on the device.  Written only by the last block of the last
 // kernel of a step (or of the probe kernel), read by every block of the following kernels.
@@ -107,6 +152,31 @@ struct FFTDesc
     long long dhat_offset;   // complex element offset of its dipole spectrum
     long long tw_offset[3];  // twiddle table offsets (one table of M[d] entries per axis)
     int radix[3][12];        // radix sequence per axis (0-terminated)
+    float mu_f[MAX_BASIS];   // mu_s per basis atom
+    double mu_d[MAX_BASIS];
+    float invT_f;            // 1 / (Ma Mb Mc)
+    double invT_d;
 };
+
+template<>
+__host__ __device__ inline float fft_mu<float>( const FFTDesc & f, int ib )
+{
+    return f.mu_f[ib];
+}
+template<>
+__host__ __device__ inline double fft_mu<double>( const FFTDesc & f, int ib )
+{
+    return f.mu_d[ib];
+}
+template<>
+__host__ __device__ inline float fft_invT<float>( const FFTDesc & f )
+{
+    return f.invT_f;
+}
+template<>
+__host__ __device__ inline double fft_invT<double>( const FFTDesc & f )
+{
+    return f.invT_d;
+}
 
 } // namespace sg

@@ -87,7 +87,7 @@ __global__ void pass_a( PassArgs<R> p )
                 const SysDesc & d = p.sd[s];
                 long long ispin   = d.spin_offset + ib + nb * ( t + d.n_cells[0] * ( bb + d.n_cells[1] * c ) );
                 const R * src     = comp == 0 ? p.sx : ( comp == 1 ? p.sy : p.sz );
-                v                 = (R)d.mu_s[ib] * src[ispin];
+                v                 = fft_mu<R>( f, ib ) * src[ispin];
             }
             else
                 v = p.dense[(size_t)l * Ma + t];
@@ -295,7 +295,7 @@ __global__ void pass_a_inv( PassArgs<R> p )
     }
     __syncthreads();
     cplx<R> * r   = block_fft( a, b, Ma, nl, f.radix[0], tw, true );
-    const R invT = (R)( 1.0 / ( (double)Ma * f.M[1] * f.M[2] ) );
+    const R invT = fft_invT<R>( f );
     for( int e = threadIdx.x; e < nl * Na; e += blockDim.x )
     {
         int li = e / Na, t = e - li * Na;
@@ -388,6 +388,13 @@ void DDIPlan::build( const std::vector<DDISystem> & systems, bool fp64, const Sy
         }
         f.Mh = f.M[0] / 2 + 1;
         f.nb = S.nb;
+        for( int b = 0; b < S.nb && b < MAX_BASIS; ++b )
+        {
+            f.mu_d[b] = S.mu_s[b];
+            f.mu_f[b] = (float)S.mu_s[b];
+        }
+        f.invT_d = 1.0 / ( (double)f.M[0] * f.M[1] * f.M[2] );
+        f.invT_f = (float)f.invT_d;
         for( int d = 0; d < 3; ++d )
         {
             f.tw_offset[d] = (long long)tw_host.size() / 2;
@@ -449,7 +456,7 @@ static int group_for( int line_len, int lines_per_group, size_t elem, size_t bud
 void DDIPlan::build_block_tables( const std::vector<DDISystem> & systems )
 {
     size_t elem   = fp64 ? sizeof( cplx<double> ) : sizeof( cplx<float> );
-    size_t budget = 56 * 1024;
+    size_t budget = 16 * 1024;
     std::vector<int4> ta, tb, tc;
     max_smem_a = max_smem_b = max_smem_c = 0;
     for( size_t k = 0; k < systems.size(); ++k )

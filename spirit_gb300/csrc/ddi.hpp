@@ -22,6 +22,7 @@ struct DDISystem
     double lattice_constant;
     std::array<std::array<double, 3>, 3> bravais;
     std::vector<std::array<double, 3>> cell_atoms;
+    std::vector<double> mu_s; // per basis atom
 };
 
 class DDIPlan

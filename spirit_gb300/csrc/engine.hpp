@@ -98,9 +98,11 @@ public:
     void set_stream( cudaStream_t s );
     int kernels_per_step() const;
     // n steps launched kernel by kernel with CUDA events between launches on the engine stream;
-    // before every step `flush_bytes` of `flush_buf` are overwritten (L2 flush; may be null).
+    // before every step `flush_buf` is overwritten and `read_buf` read back (an L2 flush that
+    // leaves clean lines; both may be null).
     // Adds per-kernel-id total ms and launch counts (arrays of N_KERNEL_IDS).
-    void profile_steps( int n, void * flush_buf, size_t flush_bytes, double * ms, int * count );
+    void profile_steps( int n, void * flush_buf, size_t flush_bytes, void * read_buf, size_t read_bytes, double * ms,
+                        int * count );
     // DDI field h of the current spins (tests)
     void ddi_field( int s, double * h_aos );
 

@@ -38,6 +38,70 @@ __device__ __forceinline__ cplx<R> cconj( cplx<R> a )
     return { a.x, -a.y };
 }
 
+// Power-of-two lines: radix-4 stages (and one radix-2 stage if log2 L is odd) with shift/mask
+// index arithmetic.
+template<typename R>
+__device__ cplx<R> * block_fft_pow2( cplx<R> * a, cplx<R> * b, int L, int nl, const cplx<R> * tw, bool inverse )
+{
+    const int lgL = __ffs( L ) - 1;
+    int lgNs      = 0;
+    while( lgNs < lgL )
+    {
+        const int lgR  = ( lgL - lgNs >= 2 ) ? 2 : 1;
+        const int lgLR = lgL - lgR;
+        const int LR   = 1 << lgLR;
+        const int Ns   = 1 << lgNs;
+        const int lgSp = lgL - lgNs - lgR;
+        for( int idx = threadIdx.x; idx < ( nl << lgLR ); idx += blockDim.x )
+        {
+            const int line     = idx >> lgLR;
+            const int j        = idx & ( LR - 1 );
+            const cplx<R> * src = a + ( line << lgL );
+            cplx<R> * dst       = b + ( line << lgL );
+            const int k        = j & ( Ns - 1 );
+            const int d0       = ( ( j >> lgNs ) << ( lgNs + lgR ) ) + k;
+            if( lgR == 1 )
+            {
+                cplx<R> v0 = src[j];
+                cplx<R> w  = tw[k << lgSp];
+                if( inverse )
+                    w = cconj( w );
+                cplx<R> v1   = cmul( src[j + LR], w );
+                dst[d0]      = { v0.x + v1.x, v0.y + v1.y };
+                dst[d0 + Ns] = { v0.x - v1.x, v0.y - v1.y };
+            }
+            else
+            {
+                cplx<R> v[4];
+                v[0] = src[j];
+#pragma unroll
+                for( int r = 1; r < 4; ++r )
+                {
+                    cplx<R> w = tw[( r * k ) << lgSp];
+                    if( inverse )
+                        w = cconj( w );
+                    v[r] = cmul( src[j + r * LR], w );
+                }
+                cplx<R> s02  = { v[0].x + v[2].x, v[0].y + v[2].y };
+                cplx<R> d02  = { v[0].x - v[2].x, v[0].y - v[2].y };
+                cplx<R> s13  = { v[1].x + v[3].x, v[1].y + v[3].y };
+                cplx<R> d13  = { v[1].x - v[3].x, v[1].y - v[3].y };
+                cplx<R> id13 = inverse ? cplx<R>{ -d13.y, d13.x } : cplx<R>{ d13.y, -d13.x };
+                dst[d0]          = { s02.x + s13.x, s02.y + s13.y };
+                dst[d0 + Ns]     = { d02.x + id13.x, d02.y + id13.y };
+                dst[d0 + 2 * Ns] = { s02.x - s13.x, s02.y - s13.y };
+                dst[d0 + 3 * Ns] = { d02.x - id13.x, d02.y - id13.y };
+            }
+        }
+        __syncthreads();
+        cplx<R> * t = a;
+        a           = b;
+        b           = t;
+        lgNs += lgR;
+    }
+    return a;
+}
+
 // Stockham stage loop over nl lines of length L in shared memory (a -> b -> a ...).
 // rad: 0-terminated radix list; tw: L twiddles exp(-2 pi i t/L) (in shared memory).
 // Returns the buffer that holds the result.  Must be called by all threads of the block.
@@ -45,6 +109,8 @@ template<typename R>
 __device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int nl, const int * rad, const cplx<R> * tw,
                                bool inverse )
 {
+    if( ( L & ( L - 1 ) ) == 0 )
+        return block_fft_pow2( a, b, L, nl, tw, inverse );
     int Ns = 1;
     for( int s = 0; s < 12 && rad[s] > 0; ++s )
     {

@@ -41,6 +41,7 @@ struct GnebCtl
     int iteration, active, n_iterations, mode; // mode 0: GNEB, 1: LLG with VP (single image)
     int noi, nos, aborted, pad;
     double force_convergence, m, proj, fn2;
+    double hm; // 0.5 / m
     float max_torque;
     unsigned int blocks_done;
     unsigned int torque_bits;
@@ -60,13 +61,15 @@ struct GArgs
 };
 
 template<typename R>
-__device__ __forceinline__ void load_pairs( PairR<R> * pairs, const SysDesc & d )
+__device__ __forceinline__ void load_pairs( PairR<R> * pairs, SysConst<R> & C, Geo & G, const SysDesc & d )
 {
     for( int p = threadIdx.x; p < d.n_pairs; p += blockDim.x )
     {
         const PairEntry & q = d.pairs[p];
         pairs[p]            = { q.j, q.da, q.db, q.dc, (R)q.J, (R)q.D[0], (R)q.D[1], (R)q.D[2] };
     }
+    load_const( C, d );
+    load_geo( G, d );
     __syncthreads();
 }
 
@@ -75,24 +78,27 @@ template<typename R>
 __global__ void __launch_bounds__( 256 ) gneb_eval( GArgs<R> A, int probe )
 {
     __shared__ PairR<R> pairs[MAX_PAIRS];
+    __shared__ SysConst<R> C;
+    __shared__ Geo GS;
     __shared__ double red[32];
     if( !A.ctl->active )
         return;
     const int2 bm     = A.blkmap[blockIdx.x];
     const int im      = bm.x;
     const SysDesc & d = A.sd[im];
-    load_pairs( pairs, d );
+    load_pairs( pairs, C, GS, d );
     const int i = bm.y + threadIdx.x;
-    double e = 0, a2 = 0;
+    R e         = 0;
+    double a2   = 0;
     if( i < d.nos )
     {
         const long long gi = d.spin_offset + i;
         const int nb = d.nb, cell = i / nb, ib = i - cell * nb;
         const int a = cell % d.n_cells[0], rest = cell / d.n_cells[0];
         const int b = rest % d.n_cells[1], c = rest / d.n_cells[1];
-        const R mu     = (R)d.mu_s[ib];
+        const R mu     = C.mu[ib];
         const V3<R> si = A.s.ld( gi );
-        V3<R> g        = gradient_at<R>( d, pairs, A.s, A.h, gi, ib, a, b, c, si, mu, e );
+        V3<R> g        = gradient_at<R>( GS, C, pairs, A.s, A.h, gi, ib, a, b, c, si, mu, e );
         V3<R> f        = { -g.x, -g.y, -g.z };
         A.G.st( gi, f );
         if( A.ctl->mode == 0 && im > 0 )
@@ -106,7 +112,7 @@ __global__ void __launch_bounds__( 256 ) gneb_eval( GArgs<R> A, int probe )
         if( A.ctl->mode == 1 )
         {
             // LLG-VP: virtual force of the direct minimisation fv = dt gamma/mu_B (s x F), kept in T
-            R k      = (R)( d.dt * C_GAMMA / C_MU_B );
+            R k      = C.kdm;
             V3<R> cr = cross( si, f );
             V3<R> fv = { k * cr.x, k * cr.y, k * cr.z };
             A.T.st( gi, fv );
@@ -120,7 +126,7 @@ __global__ void __launch_bounds__( 256 ) gneb_eval( GArgs<R> A, int probe )
             }
         }
     }
-    double es = block_sum( e, red );
+    double es = block_sum( (double)e, red );
     double ds = block_sum( a2, red );
     if( threadIdx.x == 0 )
     {
@@ -269,11 +275,10 @@ __global__ void __launch_bounds__( 256 ) gneb_force( GArgs<R> A )
         else if( im > 0 && im < noi - 1 )
         {
             const GnebImage & I = A.img[im];
-            double inv          = 1.0 / sqrt( I.tt );
+            const R inv         = R( 1 ) / sqrt( (R)I.tt );
             V3<R> t             = A.T.ld( gi );
-            R s                 = (R)inv;
-            t                   = { t.x * s, t.y * s, t.z * s };
-            R ftn               = (R)( I.ft * inv );
+            t                   = { t.x * inv, t.y * inv, t.z * inv };
+            R ftn               = (R)I.ft * inv;
             V3<R> f             = A.G.ld( gi );
             if( I.type == 1 ) // climbing: invert the parallel component, no spring
                 fnew = { f.x - R( 2 ) * ftn * t.x, f.y - R( 2 ) * ftn * t.y, f.z - R( 2 ) * ftn * t.z };
@@ -290,7 +295,7 @@ __global__ void __launch_bounds__( 256 ) gneb_force( GArgs<R> A )
         }
         const V3<R> fp = A.F.ld( gi );
         V3<R> v        = A.V.ld( gi );
-        const R hm     = (R)( 0.5 / A.ctl->m );
+        const R hm     = (R)A.ctl->hm;
         v.x += hm * ( fp.x + fnew.x );
         v.y += hm * ( fp.y + fnew.y );
         v.z += hm * ( fp.z + fnew.z );
@@ -332,12 +337,12 @@ __global__ void __launch_bounds__( 256 ) gneb_update( GArgs<R> A )
             v = { 0, 0, 0 };
         else
         {
-            R ratio = (R)( ctl->proj / ctl->fn2 );
+            R ratio = (R)ctl->proj / (R)ctl->fn2;
             v       = { f.x * ratio, f.y * ratio, f.z * ratio };
         }
         A.V.st( gi, v );
-        const R dt   = (R)d.dt;
-        const R hmdt = (R)( 0.5 / ctl->m ) * dt;
+        const R dt   = sys_const<R>( d ).dt;
+        const R hmdt = (R)ctl->hm * dt;
         V3<R> s      = A.s.ld( gi );
         V3<R> c      = { s.x + dt * v.x + hmdt * f.x, s.y + dt * v.y + hmdt * f.y, s.z + dt * v.z + hmdt * f.z };
         V3<R> sn     = normalized( c );
@@ -500,6 +505,7 @@ public:
         c.nos               = eng->nos( 0 );
         c.force_convergence = conv;
         c.m                 = 1.0;
+        c.hm                = 0.5 / c.m;
         c.active            = 1;
         h2d( d_ctl, &c, 1 );
         size_t el = eng->fp64() ? sizeof( double ) : sizeof( float );
@@ -710,6 +716,9 @@ void gneb_n_shot( State * st, Chain & chain, int n )
     auto R = std::static_pointer_cast<GnebRun>( chain.gneb_run );
     if( !R )
         return;
+    // the host spin buffers are the state: callers may have written into them since the last call
+    for( int k = 0; k < R->noi; ++k )
+        R->eng->set_spins( k, chain.images[k]->spins.data() );
     if( R->ctl().active )
     {
         R->launch( n );
@@ -784,6 +793,7 @@ void llg_vp_shot( State * st, Image & img, int n )
     auto R = std::static_pointer_cast<GnebRun>( img.vp_run );
     if( !R )
         return;
+    R->eng->set_spins( 0, img.spins.data() );
     if( R->ctl().active )
     {
         R->launch( n );

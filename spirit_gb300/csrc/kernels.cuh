@@ -100,15 +100,43 @@ __device__ __forceinline__ V3<R> gauss3( unsigned long long seed, unsigned int s
     return { r0 * c1, r0 * s1, r1 * c3 };
 }
 
+// Geometry scalars of one system, staged in shared memory by every kernel that walks pairs.
+struct Geo
+{
+    int n[3];
+    int bc[3];
+    int nb;
+    int nos;
+    long long off;
+    int pair_begin[MAX_BASIS + 1];
+};
+
+__device__ __forceinline__ void load_geo( Geo & G, const SysDesc & d )
+{
+    if( threadIdx.x == 0 )
+    {
+        for( int e = 0; e < 3; ++e )
+        {
+            G.n[e]  = d.n_cells[e];
+            G.bc[e] = d.bc[e];
+        }
+        G.nb  = d.nb;
+        G.nos = d.nos;
+        G.off = d.spin_offset;
+        for( int b = 0; b <= d.nb; ++b )
+            G.pair_begin[b] = d.pair_begin[b];
+    }
+}
+
 // ------------------------------------------------------------------ neighbour index
 // idx_from_pair (core/include/engine/Vectormath.hpp:437-528) for a spin at cell (a, b, c)
-__device__ __forceinline__ long long pair_index( const SysDesc & d, int a, int b, int c, int j, int da, int db, int dc )
+__device__ __forceinline__ long long pair_index( const Geo & G, int a, int b, int c, int j, int da, int db, int dc )
 {
-    const int Na = d.n_cells[0], Nb = d.n_cells[1], Nc = d.n_cells[2];
+    const int Na = G.n[0], Nb = G.n[1], Nc = G.n[2];
     if( abs( da ) > Na || abs( db ) > Nb || abs( dc ) > Nc )
         return -1;
     int ja = a + da, jb = b + db, jc = c + dc;
-    if( d.bc[0] || ( ja >= 0 && ja < Na ) )
+    if( G.bc[0] || ( ja >= 0 && ja < Na ) )
     {
         if( ja < 0 )
             ja += Na;
@@ -117,7 +145,7 @@ __device__ __forceinline__ long long pair_index( const SysDesc & d, int a, int b
     }
     else
         return -1;
-    if( d.bc[1] || ( jb >= 0 && jb < Nb ) )
+    if( G.bc[1] || ( jb >= 0 && jb < Nb ) )
     {
         if( jb < 0 )
             jb += Nb;
@@ -126,7 +154,7 @@ __device__ __forceinline__ long long pair_index( const SysDesc & d, int a, int b
     }
     else
         return -1;
-    if( d.bc[2] || ( jc >= 0 && jc < Nc ) )
+    if( G.bc[2] || ( jc >= 0 && jc < Nc ) )
     {
         if( jc < 0 )
             jc += Nc;
@@ -135,7 +163,7 @@ __device__ __forceinline__ long long pair_index( const SysDesc & d, int a, int b
     }
     else
         return -1;
-    return d.spin_offset + j + (long long)d.nb * ( ja + Na * ( jb + (long long)Nb * jc ) );
+    return G.off + j + (long long)G.nb * ( ja + Na * ( jb + (long long)Nb * jc ) );
 }
 
 // ------------------------------------------------------------------ block reductions
@@ -177,24 +205,37 @@ __device__ __forceinline__ float block_max( float v, float * sh )
     return r;
 }
 
-// Gradient of the Heisenberg Hamiltonian at spin i of configuration cfg, and the quadratic
-// (0.5 g.s) plus Zeeman energy of that spin.
+// Copy the per-system constants into shared memory (all threads; followed by __syncthreads by
+// the caller).
 template<typename R>
-__device__ __forceinline__ V3<R> gradient_at( const SysDesc & d, const PairR<R> * pairs, const SoA3<R> & cfg,
-                                              const SoA3<R> & h, long long gi, int ib, int a, int b, int c, V3<R> si,
-                                              R mu, double & e )
+__device__ __forceinline__ void load_const( SysConst<R> & dst, const SysDesc & d )
+{
+    const unsigned int * src = reinterpret_cast<const unsigned int *>( &sys_const<R>( d ) );
+    unsigned int * o         = reinterpret_cast<unsigned int *>( &dst );
+    for( int w = threadIdx.x; w < (int)( sizeof( SysConst<R> ) / 4 ); w += blockDim.x )
+        o[w] = src[w];
+}
+
+// Gradient of the Heisenberg Hamiltonian at spin i of configuration cfg (Gradient_and_Energy,
+// Hamiltonian_Heisenberg.cpp:704-766: anisotropy, exchange + DMI pairs, dipolar field, then
+// Zeeman), and the energy of that spin: 0.5 g_quadratic . s + Zeeman, in the working precision.
+template<typename R>
+__device__ __forceinline__ V3<R> gradient_at( const Geo & d, const SysConst<R> & C, const PairR<R> * pairs,
+                                              const SoA3<R> & cfg, const SoA3<R> & h, long long gi, int ib, int a,
+                                              int b, int c, V3<R> si, R mu, R & e )
 {
     V3<R> g = { 0, 0, 0 };
-    for( int k = 0; k < d.n_aniso; ++k )
-        if( d.aniso_idx[k] == ib )
+    for( int k = 0; k < C.n_aniso; ++k )
+        if( C.aniso_idx[k] == ib )
         {
-            V3<R> n = { (R)d.aniso_n[k][0], (R)d.aniso_n[k][1], (R)d.aniso_n[k][2] };
-            R sc    = R( 2 ) * (R)d.aniso_K[k] * dot( n, si );
+            V3<R> n = { C.aniso_n[k][0], C.aniso_n[k][1], C.aniso_n[k][2] };
+            R sc    = R( 2 ) * C.aniso_K[k] * dot( n, si );
             g.x -= sc * n.x;
             g.y -= sc * n.y;
             g.z -= sc * n.z;
         }
     const int p0 = d.pair_begin[ib], p1 = d.pair_begin[ib + 1];
+#pragma unroll 6
     for( int p = p0; p < p1; ++p )
     {
         const PairR<R> P = pairs[p];
@@ -218,51 +259,45 @@ __device__ __forceinline__ V3<R> gradient_at( const SysDesc & d, const PairR<R> 
         g.y -= mu * hh.y;
         g.z -= mu * hh.z;
     }
-    e = 0.5 * ( (double)g.x * si.x + (double)g.y * si.y + (double)g.z * si.z );
-    if( d.has_zeeman )
+    e = R( 0.5 ) * ( g.x * si.x + g.y * si.y + g.z * si.z );
+    if( C.has_zeeman )
     {
-        V3<R> B = { (R)d.zeeman[0], (R)d.zeeman[1], (R)d.zeeman[2] };
+        V3<R> B = { C.zeeman[0], C.zeeman[1], C.zeeman[2] };
         g.x -= mu * B.x;
         g.y -= mu * B.y;
         g.z -= mu * B.z;
-        e += -(double)mu * ( (double)B.x * si.x + (double)B.y * si.y + (double)B.z * si.z );
+        e += -mu * ( B.x * si.x + B.y * si.y + B.z * si.z );
     }
     return g;
 }
 
-// Calculate_Force_Virtual for spin configuration cfg, force F = -g
+// Calculate_Force_Virtual for spin configuration c, force F = -g
 template<typename R>
-__device__ __forceinline__ V3<R> virtual_force( const SysDesc & d, V3<R> c, V3<R> g, R mu, V3<R> xi, bool thermal,
-                                                bool direct )
+__device__ __forceinline__ V3<R> virtual_force( const SysConst<R> & C, V3<R> c, V3<R> g, R mu, V3<R> xi )
 {
     V3<R> F = { -g.x, -g.y, -g.z };
-    if( direct )
+    if( C.direct )
     {
-        R k      = (R)( d.dt * C_GAMMA / C_MU_B );
         V3<R> cr = cross( c, F );
-        return { k * cr.x, k * cr.y, k * cr.z };
+        return { C.kdm * cr.x, C.kdm * cr.y, C.kdm * cr.z };
     }
-    const double a = d.damping;
-    R dtg          = (R)( d.dt * C_GAMMA / C_MU_B / ( 1 + a * a ) );
-    R dtga         = (R)( ( d.dt * C_GAMMA / C_MU_B / ( 1 + a * a ) ) * a );
-    V3<R> cr       = cross( c, F );
-    V3<R> fv       = { dtg * F.x, dtg * F.y, dtg * F.z };
-    fv.x += dtga * cr.x;
-    fv.y += dtga * cr.y;
-    fv.z += dtga * cr.z;
+    V3<R> cr = cross( c, F );
+    V3<R> fv = { C.dtg * F.x, C.dtg * F.y, C.dtg * F.z };
+    fv.x += C.dtga * cr.x;
+    fv.y += C.dtga * cr.y;
+    fv.z += C.dtga * cr.z;
     fv.x /= mu;
     fv.y /= mu;
     fv.z /= mu;
-    if( thermal )
+    if( C.thermal )
     {
         V3<R> cx = cross( c, xi );
         fv.x += xi.x;
         fv.y += xi.y;
         fv.z += xi.z;
-        R ra = (R)a;
-        fv.x += ra * cx.x;
-        fv.y += ra * cx.y;
-        fv.z += ra * cx.z;
+        fv.x += C.alpha * cx.x;
+        fv.y += C.alpha * cx.y;
+        fv.z += C.alpha * cx.z;
     }
     return fv;
 }
