@@ -54,6 +54,31 @@ struct PairEntry
 
 struct FFTDesc;
 
+// Exact unsigned division by a runtime constant d: q = floor(n * M / 2^64) with
+// M = ceil(2^64 / d) is exact for every 32-bit n (d = 1 is the identity, M = 0).
+struct FastDiv
+{
+    unsigned int d;
+    unsigned int pad;
+    unsigned long long m;
+};
+
+inline FastDiv make_fastdiv( unsigned int d )
+{
+    FastDiv f;
+    f.d   = d;
+    f.pad = 0;
+    f.m   = d > 1 ? ( ~0ULL ) / d + 1 : 0;
+    return f;
+}
+
+#ifdef __CUDACC__
+__device__ __forceinline__ unsigned int fdiv( unsigned int n, const FastDiv & f )
+{
+    return f.d == 1 ? n : (unsigned int)__umul64hi( (unsigned long long)n, f.m );
+}
+#endif
+
 // Per-system constants of the stage arithmetic, precomputed on the host in FP64 and kept in
 // the precision of the kernel that reads them (no FP64 division or square root on the device).
 template<typename R>
@@ -66,6 +91,7 @@ struct SysConst
     R dt;
     R noise[MAX_BASIS];         // epsilon sqrt(T / mu_s)                   (Method_LLG.cpp:72-107)
     R mu[MAX_BASIS];
+    R inv_mu[MAX_BASIS];
     R zeeman[3];                // mu_B B n
     R aniso_K[MAX_BASIS];
     R aniso_n[MAX_BASIS][3];
@@ -87,6 +113,7 @@ struct SysDesc
     int pair_begin[MAX_BASIS + 1]; // pairs of basis atom ib: [pair_begin[ib], pair_begin[ib+1]) in pairs[]
     int n_pairs;
     int max_t[3]; // largest |translation| along each axis (stencil halo)
+    FastDiv div_nb, div_na, div_nbb; // division by nb, Na, Nb
     PairEntry pairs[MAX_PAIRS];
     double mu_s[MAX_BASIS];
     double zeeman[3];           // mu_B * B * normal: Zeeman gradient is -mu_s * zeeman
@@ -156,6 +183,7 @@ struct FFTDesc
     double mu_d[MAX_BASIS];
     float invT_f;            // 1 / (Ma Mb Mc)
     double invT_d;
+    FastDiv div_Ma, div_Mh, div_Mb, div_Mc;
 };
 
 template<>

@@ -52,6 +52,9 @@ __device__ __forceinline__ bool sys_inactive( const PassArgs<R> & p, int s )
     return p.runs && !p.runs[s].active;
 }
 
+// Block tables:
+//   pass A / A' : (system, row = cb*Cin + c, first b, number of lines)
+//   pass B / C  : (system, group index, G = lines per group (a power of two), 0)
 // ------------------------------------------------------------------ pass A: R2C along a
 template<typename R>
 __global__ void pass_a( PassArgs<R> p )
@@ -66,46 +69,50 @@ __global__ void pass_a( PassArgs<R> p )
     const int Cin = p.mode ? f.M[2] : f.N[2];
     const int Bin = p.mode ? f.M[1] : f.N[1];
     const int Ain = p.mode ? f.M[0] : f.N[0];
+    const int row = blk.y, b0 = blk.z, nl = blk.w;
+    const int ls  = line_stride( Ma );
     cplx<R> * tw  = reinterpret_cast<cplx<R> *>( smem_raw );
     cplx<R> * a   = tw + Ma;
-    const int nl  = blk.z;
-    cplx<R> * b   = a + nl * Ma;
+    cplx<R> * b   = a + nl * ls;
     load_tw( tw, p.tw + f.tw_offset[0], Ma );
-    const int line0 = blk.y;
-    // load lines: line l = (cb*Cin + c)*Bin + bb
-    for( int e = threadIdx.x; e < nl * Ma; e += blockDim.x )
+    const int cb = row / Cin, c = row - cb * Cin;
+    const int ib = cb / 3, comp = cb - 3 * ib;
+    if( p.mode == 0 )
     {
-        int li = e / Ma, t = e - li * Ma;
-        int l  = line0 + li;
-        R v    = 0;
-        if( t < Ain )
+        const SysDesc & d  = p.sd[s];
+        const R mu         = fft_mu<R>( f, ib );
+        const R * src      = comp == 0 ? p.sx : ( comp == 1 ? p.sy : p.sz );
+        const long long base = d.spin_offset + ib + (long long)nb * d.n_cells[0] * ( (long long)b0 + (long long)d.n_cells[1] * c );
+        const int rowlen   = nb * d.n_cells[0];
+        for( int e = threadIdx.x; e < nl * Ma; e += blockDim.x )
         {
-            if( p.mode == 0 )
-            {
-                int bb = l % Bin, c = ( l / Bin ) % Cin, cb = l / ( Bin * Cin );
-                int ib = cb / 3, comp = cb - 3 * ib;
-                const SysDesc & d = p.sd[s];
-                long long ispin   = d.spin_offset + ib + nb * ( t + d.n_cells[0] * ( bb + d.n_cells[1] * c ) );
-                const R * src     = comp == 0 ? p.sx : ( comp == 1 ? p.sy : p.sz );
-                v                 = fft_mu<R>( f, ib ) * src[ispin];
-            }
-            else
-                v = p.dense[(size_t)l * Ma + t];
+            int li = (int)fdiv( (unsigned)e, f.div_Ma ), t = e - li * Ma;
+            R v    = 0;
+            if( t < Ain )
+                v = mu * src[base + (long long)li * rowlen + (long long)nb * t];
+            a[li * ls + t] = { v, (R)0 };
         }
-        a[e] = { v, (R)0 };
+    }
+    else
+    {
+        for( int e = threadIdx.x; e < nl * Ma; e += blockDim.x )
+        {
+            int li = (int)fdiv( (unsigned)e, f.div_Ma ), t = e - li * Ma;
+            a[li * ls + t] = { p.dense[( (size_t)row * Bin + b0 + li ) * Ma + t], (R)0 };
+        }
     }
     __syncthreads();
-    cplx<R> * r = block_fft( a, b, Ma, nl, f.radix[0], tw, false );
-    cplx<R> * W1 = p.W1 + f.spec_offset;
+    cplx<R> * r  = block_fft( a, b, Ma, ls, nl, f.radix[0], tw, false );
+    cplx<R> * W1 = p.W1 + f.spec_offset + ( (size_t)row * Bin + b0 ) * Mh;
     for( int e = threadIdx.x; e < nl * Mh; e += blockDim.x )
     {
-        int li = e / Mh, k = e - li * Mh;
-        W1[(size_t)( line0 + li ) * Mh + k] = r[li * Ma + k];
+        int li = (int)fdiv( (unsigned)e, f.div_Mh ), k = e - li * Mh;
+        W1[e]  = r[li * ls + k];
     }
 }
 
 // ------------------------------------------------------------------ pass B: C2C along b
-// block: fixed (cb, c), a group of consecutive ka.  forward: W1 -> W2, inverse: W2 -> W1.
+// block: fixed row = (cb, c), a group of G consecutive ka.  forward: W1 -> W2, inverse: W2 -> W1.
 template<typename R>
 __global__ void pass_b( PassArgs<R> p, int inverse )
 {
@@ -116,24 +123,26 @@ __global__ void pass_b( PassArgs<R> p, int inverse )
         return;
     const FFTDesc & f = p.fd[s];
     const int Mb = f.M[1], Mh = f.Mh;
-    const int Cin = p.mode ? f.M[2] : f.N[2];
     const int Bin = p.mode ? f.M[1] : f.N[1];
     const int G   = blk.z;
-    const int ngk = ( Mh + G - 1 ) / G;
-    const int grp = blk.y; // (cb*Cin + c)*ngk + kg
-    const int kg  = grp % ngk;
-    const int row = grp / ngk; // cb*Cin + c
-    const int ka0 = kg * G;
+    const int lgG = __ffs( G ) - 1;
+    const int ngk = ( Mh + G - 1 ) >> lgG;
+    const int row = blk.y / ngk;
+    const int kg  = blk.y - row * ngk;
+    const int ka0 = kg << lgG;
     const int nl  = min( G, Mh - ka0 );
+    const int ls  = line_stride( Mb );
     cplx<R> * tw  = reinterpret_cast<cplx<R> *>( smem_raw );
     cplx<R> * a   = tw + Mb;
-    cplx<R> * b   = a + G * Mb;
+    cplx<R> * b   = a + G * ls;
     load_tw( tw, p.tw + f.tw_offset[1], Mb );
     cplx<R> * W1 = p.W1 + f.spec_offset;
     cplx<R> * W2 = p.W2 + f.spec_offset;
-    for( int e = threadIdx.x; e < nl * Mb; e += blockDim.x )
+    for( int e = threadIdx.x; e < ( Mb << lgG ); e += blockDim.x )
     {
-        int t = e / nl, li = e - t * nl; // consecutive threads -> consecutive ka (coalesced)
+        int t = e >> lgG, li = e & ( G - 1 ); // consecutive threads -> consecutive ka (coalesced)
+        if( li >= nl )
+            continue;
         cplx<R> v = { 0, 0 };
         if( !inverse )
         {
@@ -142,31 +151,25 @@ __global__ void pass_b( PassArgs<R> p, int inverse )
         }
         else
             v = W2[( (size_t)row * Mb + t ) * Mh + ka0 + li];
-        a[li * Mb + t] = v;
+        a[li * ls + t] = v;
     }
     __syncthreads();
-    cplx<R> * r = block_fft( a, b, Mb, nl, f.radix[1], tw, inverse != 0 );
-    if( !inverse )
+    cplx<R> * r = block_fft( a, b, Mb, ls, nl, f.radix[1], tw, inverse != 0 );
+    const int Bout = inverse ? f.N[1] : Mb;
+    for( int e = threadIdx.x; e < ( Bout << lgG ); e += blockDim.x )
     {
-        for( int e = threadIdx.x; e < nl * Mb; e += blockDim.x )
-        {
-            int t = e / nl, li = e - t * nl;
-            W2[( (size_t)row * Mb + t ) * Mh + ka0 + li] = r[li * Mb + t];
-        }
-    }
-    else
-    {
-        const int Bout = f.N[1];
-        for( int e = threadIdx.x; e < nl * Bout; e += blockDim.x )
-        {
-            int t = e / nl, li = e - t * nl;
-            W1[( (size_t)row * Bout + t ) * Mh + ka0 + li] = r[li * Mb + t];
-        }
+        int t = e >> lgG, li = e & ( G - 1 );
+        if( li >= nl )
+            continue;
+        if( !inverse )
+            W2[( (size_t)row * Mb + t ) * Mh + ka0 + li] = r[li * ls + t];
+        else
+            W1[( (size_t)row * Bout + t ) * Mh + ka0 + li] = r[li * ls + t];
     }
 }
 
 // ------------------------------------------------------------------ pass C: along c + tensor product
-// block: fixed kb, a group of consecutive ka, all 3*nb components.
+// block: fixed kb, a group of G consecutive ka, all 3*nb components (line li = cb*G + g).
 template<typename R>
 __global__ void pass_c( PassArgs<R> p )
 {
@@ -180,51 +183,60 @@ __global__ void pass_c( PassArgs<R> p )
     const int ncb = 3 * nb;
     const int Cin = p.mode ? f.M[2] : f.N[2];
     const int G   = blk.z;
-    const int ngk = ( Mh + G - 1 ) / G;
-    const int kg  = blk.y % ngk;
+    const int lgG = __ffs( G ) - 1;
+    const int ngk = ( Mh + G - 1 ) >> lgG;
     const int kb  = blk.y / ngk;
-    const int ka0 = kg * G;
+    const int kg  = blk.y - kb * ngk;
+    const int ka0 = kg << lgG;
     const int ng  = min( G, Mh - ka0 );
-    const int nl  = ncb * ng; // line li = cb*ng + g
+    const int ls  = line_stride( Mc );
+    const int nl  = ncb << lgG; // lines g >= ng are computed but never stored
     cplx<R> * tw  = reinterpret_cast<cplx<R> *>( smem_raw );
     cplx<R> * a   = tw + Mc;
-    cplx<R> * b   = a + ncb * G * Mc;
+    cplx<R> * b   = a + nl * ls;
     load_tw( tw, p.tw + f.tw_offset[2], Mc );
     cplx<R> * W2 = p.W2 + f.spec_offset;
-    for( int e = threadIdx.x; e < nl * Mc; e += blockDim.x )
+    const int total = nl * Mc;
+    for( int e = threadIdx.x; e < total; e += blockDim.x )
     {
         // e -> (cb, c, g) with g fastest for coalescing
-        int g  = e % ng;
-        int c  = ( e / ng ) % Mc;
-        int cb = e / ( ng * Mc );
+        int g    = e & ( G - 1 );
+        int rest = e >> lgG;
+        int cb   = (int)fdiv( (unsigned)rest, f.div_Mc );
+        int c    = rest - cb * Mc;
         cplx<R> v = { 0, 0 };
-        if( c < Cin )
+        if( c < Cin && g < ng )
             v = W2[( ( (size_t)cb * Cin + c ) * Mb + kb ) * Mh + ka0 + g];
-        a[( cb * ng + g ) * Mc + c] = v;
+        a[( cb * G + g ) * ls + c] = v;
     }
     __syncthreads();
-    cplx<R> * r = Mc > 1 ? block_fft( a, b, Mc, nl, f.radix[2], tw, false ) : a;
+    cplx<R> * r = Mc > 1 ? block_fft( a, b, Mc, ls, nl, f.radix[2], tw, false ) : a;
     if( p.mode == 1 )
     {
         // dense forward transform: write every kc
-        for( int e = threadIdx.x; e < nl * Mc; e += blockDim.x )
+        for( int e = threadIdx.x; e < total; e += blockDim.x )
         {
-            int g  = e % ng;
-            int c  = ( e / ng ) % Mc;
-            int cb = e / ( ng * Mc );
-            W2[( ( (size_t)cb * Mc + c ) * Mb + kb ) * Mh + ka0 + g] = r[( cb * ng + g ) * Mc + c];
+            int g    = e & ( G - 1 );
+            int rest = e >> lgG;
+            int cb   = (int)fdiv( (unsigned)rest, f.div_Mc );
+            int c    = rest - cb * Mc;
+            if( g < ng )
+                W2[( ( (size_t)cb * Mc + c ) * Mb + kb ) * Mh + ka0 + g] = r[( cb * G + g ) * ls + c];
         }
         return;
     }
     // tensor product H_b1 = sum_b2 D_b1b2 . S_b2 (FFT.hpp:42-49 mult3D rows: xx xy xz | xy yy yz | xz yz zz)
-    cplx<R> * h = ( r == a ) ? b : a;
+    cplx<R> * h        = ( r == a ) ? b : a;
     const cplx<R> * Dh = p.Dhat + f.dhat_offset;
     const int npair    = nb * nb;
-    for( int e = threadIdx.x; e < nb * ng * Mc; e += blockDim.x )
+    for( int e = threadIdx.x; e < ( nb * Mc ) << lgG; e += blockDim.x )
     {
-        int kc = e % Mc;
-        int g  = ( e / Mc ) % ng;
-        int b1 = e / ( Mc * ng );
+        int g    = e & ( G - 1 );
+        int rest = e >> lgG;
+        int b1   = (int)fdiv( (unsigned)rest, f.div_Mc );
+        int kc   = rest - b1 * Mc;
+        if( g >= ng )
+            continue;
         cplx<R> acc[3] = { { 0, 0 }, { 0, 0 }, { 0, 0 } };
         for( int b2 = 0; b2 < nb; ++b2 )
         {
@@ -233,9 +245,9 @@ __global__ void pass_c( PassArgs<R> p )
 #pragma unroll
             for( int q = 0; q < 6; ++q )
                 d[q] = D[q * Mc];
-            cplx<R> sx = r[( ( b2 * 3 + 0 ) * ng + g ) * Mc + kc];
-            cplx<R> sy = r[( ( b2 * 3 + 1 ) * ng + g ) * Mc + kc];
-            cplx<R> sz = r[( ( b2 * 3 + 2 ) * ng + g ) * Mc + kc];
+            cplx<R> sx = r[( ( b2 * 3 + 0 ) * G + g ) * ls + kc];
+            cplx<R> sy = r[( ( b2 * 3 + 1 ) * G + g ) * ls + kc];
+            cplx<R> sz = r[( ( b2 * 3 + 2 ) * G + g ) * ls + kc];
             const int row[3][3] = { { 0, 1, 2 }, { 1, 3, 4 }, { 2, 4, 5 } };
 #pragma unroll
             for( int c3 = 0; c3 < 3; ++c3 )
@@ -247,18 +259,20 @@ __global__ void pass_c( PassArgs<R> p )
         }
 #pragma unroll
         for( int c3 = 0; c3 < 3; ++c3 )
-            h[( ( b1 * 3 + c3 ) * ng + g ) * Mc + kc] = acc[c3];
+            h[( ( b1 * 3 + c3 ) * G + g ) * ls + kc] = acc[c3];
     }
     __syncthreads();
     cplx<R> * other = ( h == a ) ? b : a;
-    cplx<R> * o     = Mc > 1 ? block_fft( h, other, Mc, nl, f.radix[2], tw, true ) : h;
+    cplx<R> * o     = Mc > 1 ? block_fft( h, other, Mc, ls, nl, f.radix[2], tw, true ) : h;
     const int Cout  = f.N[2];
-    for( int e = threadIdx.x; e < ncb * ng * Cout; e += blockDim.x )
+    for( int e = threadIdx.x; e < total; e += blockDim.x )
     {
-        int g  = e % ng;
-        int c  = ( e / ng ) % Cout;
-        int cb = e / ( ng * Cout );
-        W2[( ( (size_t)cb * Cin + c ) * Mb + kb ) * Mh + ka0 + g] = o[( cb * ng + g ) * Mc + c];
+        int g    = e & ( G - 1 );
+        int rest = e >> lgG;
+        int cb   = (int)fdiv( (unsigned)rest, f.div_Mc );
+        int c    = rest - cb * Mc;
+        if( c < Cout && g < ng )
+            W2[( ( (size_t)cb * Cin + c ) * Mb + kb ) * Mh + ka0 + g] = o[( cb * G + g ) * ls + c];
     }
 }
 
@@ -275,36 +289,36 @@ __global__ void pass_a_inv( PassArgs<R> p )
     const SysDesc & d = p.sd[s];
     const int Ma = f.M[0], Mh = f.Mh, nb = f.nb;
     const int Nc = f.N[2], Nb = f.N[1], Na = f.N[0];
-    cplx<R> * tw = reinterpret_cast<cplx<R> *>( smem_raw );
-    cplx<R> * a  = tw + Ma;
-    const int nl = blk.z;
-    cplx<R> * b  = a + nl * Ma;
+    const int row = blk.y, b0 = blk.z, nl = blk.w;
+    const int ls  = line_stride( Ma );
+    cplx<R> * tw  = reinterpret_cast<cplx<R> *>( smem_raw );
+    cplx<R> * a   = tw + Ma;
+    cplx<R> * b   = a + nl * ls;
     load_tw( tw, p.tw + f.tw_offset[0], Ma );
-    const int line0 = blk.y;
-    const cplx<R> * W1 = p.W1 + f.spec_offset;
+    const cplx<R> * W1 = p.W1 + f.spec_offset + ( (size_t)row * Nb + b0 ) * Mh;
     for( int e = threadIdx.x; e < nl * Ma; e += blockDim.x )
     {
-        int li = e / Ma, k = e - li * Ma;
-        int l  = line0 + li;
+        int li = (int)fdiv( (unsigned)e, f.div_Ma ), k = e - li * Ma;
         cplx<R> v;
         if( k < Mh )
-            v = W1[(size_t)l * Mh + k];
+            v = W1[li * Mh + k];
         else
-            v = cconj( W1[(size_t)l * Mh + ( Ma - k )] );
-        a[e] = v;
+            v = cconj( W1[li * Mh + ( Ma - k )] );
+        a[li * ls + k] = v;
     }
     __syncthreads();
-    cplx<R> * r   = block_fft( a, b, Ma, nl, f.radix[0], tw, true );
+    cplx<R> * r  = block_fft( a, b, Ma, ls, nl, f.radix[0], tw, true );
     const R invT = fft_invT<R>( f );
-    for( int e = threadIdx.x; e < nl * Na; e += blockDim.x )
+    const int cb = row / Nc, c = row - cb * Nc;
+    const int ib = cb / 3, comp = cb - 3 * ib;
+    R * dst      = comp == 0 ? p.hx : ( comp == 1 ? p.hy : p.hz );
+    const long long base = d.spin_offset + ib + (long long)nb * Na * ( (long long)b0 + (long long)Nb * c );
+    const int rowlen     = nb * Na;
+    for( int e = threadIdx.x; e < nl * Ma; e += blockDim.x )
     {
-        int li = e / Na, t = e - li * Na;
-        int l  = line0 + li;
-        int bb = l % Nb, c = ( l / Nb ) % Nc, cb = l / ( Nb * Nc );
-        int ib = cb / 3, comp = cb - 3 * ib;
-        long long ispin = d.spin_offset + ib + nb * ( t + d.n_cells[0] * ( bb + d.n_cells[1] * c ) );
-        R * dst         = comp == 0 ? p.hx : ( comp == 1 ? p.hy : p.hz );
-        dst[ispin]      = r[li * Ma + t].x * invT;
+        int li = (int)fdiv( (unsigned)e, f.div_Ma ), t = e - li * Ma;
+        if( t < Na )
+            dst[base + (long long)li * rowlen + (long long)nb * t] = r[li * ls + t].x * invT;
     }
 }
 
@@ -395,6 +409,10 @@ void DDIPlan::build( const std::vector<DDISystem> & systems, bool fp64, const Sy
         }
         f.invT_d = 1.0 / ( (double)f.M[0] * f.M[1] * f.M[2] );
         f.invT_f = (float)f.invT_d;
+        f.div_Ma = make_fastdiv( f.M[0] );
+        f.div_Mh = make_fastdiv( f.Mh );
+        f.div_Mb = make_fastdiv( f.M[1] );
+        f.div_Mc = make_fastdiv( f.M[2] );
         for( int d = 0; d < 3; ++d )
         {
             f.tw_offset[d] = (long long)tw_host.size() / 2;
@@ -446,11 +464,21 @@ void DDIPlan::build( const std::vector<DDISystem> & systems, bool fp64, const Sy
     compute_dhat( systems, d_sd, stream );
 }
 
-// Lines per block: keep the two ping-pong buffers of a block within `budget` bytes.
+// Lines per block: keep the two ping-pong buffers of a block within `budget` bytes; the result is
+// a power of two (block tables of passes B and C rely on it).
 static int group_for( int line_len, int lines_per_group, size_t elem, size_t budget, int cap )
 {
-    int g = (int)( budget / ( 2 * elem * (size_t)line_len * lines_per_group ) );
-    return g < 1 ? 1 : ( g > cap ? cap : g );
+    int ls = line_stride( line_len );
+    int g  = (int)( budget / ( 2 * elem * (size_t)ls * lines_per_group ) );
+    int p  = 1;
+    while( p * 2 <= g && p * 2 <= cap )
+        p *= 2;
+    return p;
+}
+
+static size_t smem_a( size_t elem, int Ma, int nl )
+{
+    return elem * ( Ma + 2 * (size_t)nl * line_stride( Ma ) );
 }
 
 void DDIPlan::build_block_tables( const std::vector<DDISystem> & systems )
@@ -463,21 +491,21 @@ void DDIPlan::build_block_tables( const std::vector<DDISystem> & systems )
     {
         const FFTDesc & f = fd_host[k];
         int s             = systems[k].sys;
-        int nlines        = 3 * f.nb * f.N[2] * f.N[1];
-        int nl            = group_for( f.M[0], 1, elem, budget, 64 );
-        for( int l = 0; l < nlines; l += nl )
-            ta.push_back( make_int4( s, l, std::min( nl, nlines - l ), 0 ) );
-        max_smem_a = std::max( max_smem_a, elem * ( f.M[0] + 2 * (size_t)nl * f.M[0] ) );
+        int nl            = group_for( f.M[0], 1, elem, budget, 32 );
+        for( int row = 0; row < 3 * f.nb * f.N[2]; ++row )
+            for( int b0 = 0; b0 < f.N[1]; b0 += nl )
+                ta.push_back( make_int4( s, row, b0, std::min( nl, f.N[1] - b0 ) ) );
+        max_smem_a = std::max( max_smem_a, smem_a( elem, f.M[0], nl ) );
         int gb  = group_for( f.M[1], 1, elem, budget, 32 );
         int ngb = ( f.Mh + gb - 1 ) / gb;
         for( int g = 0; g < 3 * f.nb * f.N[2] * ngb; ++g )
             tb.push_back( make_int4( s, g, gb, 0 ) );
-        max_smem_b = std::max( max_smem_b, elem * ( f.M[1] + 2 * (size_t)gb * f.M[1] ) );
+        max_smem_b = std::max( max_smem_b, elem * ( f.M[1] + 2 * (size_t)gb * line_stride( f.M[1] ) ) );
         int gc  = group_for( f.M[2], 3 * f.nb, elem, budget, 32 );
         int ngc = ( f.Mh + gc - 1 ) / gc;
         for( int g = 0; g < f.M[1] * ngc; ++g )
             tc.push_back( make_int4( s, g, gc, 0 ) );
-        max_smem_c = std::max( max_smem_c, elem * ( f.M[2] + 2 * (size_t)3 * f.nb * gc * f.M[2] ) );
+        max_smem_c = std::max( max_smem_c, elem * ( f.M[2] + 2 * (size_t)3 * f.nb * gc * line_stride( f.M[2] ) ) );
     }
     n_blocks[0] = (int)ta.size();
     n_blocks[1] = (int)tb.size();
@@ -623,15 +651,15 @@ void DDIPlan::compute_dhat( const std::vector<DDISystem> & systems, const SysDes
         pa.W2 = dW2;
         // pass A (dense): lines = nrows * Mc * Mb, each of length Ma
         {
-            int nl = group_for( Ma, 1, sizeof( cplx<double> ), 56 * 1024, 64 );
+            int nl = group_for( Ma, 1, sizeof( cplx<double> ), 56 * 1024, 32 );
             std::vector<int4> t;
-            int nlines = nrows * Mc * Mb;
-            for( int l = 0; l < nlines; l += nl )
-                t.push_back( make_int4( 0, l, std::min( nl, nlines - l ), 0 ) );
+            for( int row = 0; row < nrows * Mc; ++row )
+                for( int b0 = 0; b0 < Mb; b0 += nl )
+                    t.push_back( make_int4( 0, row, b0, std::min( nl, Mb - b0 ) ) );
             int4 * dt = dalloc<int4>( t.size() );
             h2d( dt, t.data(), t.size() );
             pa.blocks = dt;
-            size_t sm = sizeof( cplx<double> ) * ( Ma + 2 * (size_t)nl * Ma );
+            size_t sm = smem_a( sizeof( cplx<double> ), Ma, nl );
             pass_a<double><<<(unsigned)t.size(), 256, sm, stream>>>( pa );
             CUDA_CHECK( cudaGetLastError() );
             CUDA_CHECK( cudaStreamSynchronize( stream ) );
@@ -647,7 +675,7 @@ void DDIPlan::compute_dhat( const std::vector<DDISystem> & systems, const SysDes
             int4 * dt = dalloc<int4>( t.size() );
             h2d( dt, t.data(), t.size() );
             pa.blocks = dt;
-            size_t sm = sizeof( cplx<double> ) * ( Mb + 2 * (size_t)gb * Mb );
+            size_t sm = sizeof( cplx<double> ) * ( Mb + 2 * (size_t)gb * line_stride( Mb ) );
             pass_b<double><<<(unsigned)t.size(), 256, sm, stream>>>( pa, 0 );
             CUDA_CHECK( cudaGetLastError() );
             CUDA_CHECK( cudaStreamSynchronize( stream ) );
@@ -666,7 +694,7 @@ void DDIPlan::compute_dhat( const std::vector<DDISystem> & systems, const SysDes
             int4 * dt = dalloc<int4>( t.size() );
             h2d( dt, t.data(), t.size() );
             pa.blocks = dt;
-            size_t sm = sizeof( cplx<double> ) * ( Mc + 2 * (size_t)nrows * gc * Mc );
+            size_t sm = sizeof( cplx<double> ) * ( Mc + 2 * (size_t)nrows * gc * line_stride( Mc ) );
             pass_c<double><<<(unsigned)t.size(), 256, sm, stream>>>( pa );
             CUDA_CHECK( cudaGetLastError() );
             CUDA_CHECK( cudaStreamSynchronize( stream ) );

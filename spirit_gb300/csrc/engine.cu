@@ -83,14 +83,13 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
     float t2             = 0;
     if( valid )
     {
-        const long long gi = d.spin_offset + i;
-        const int nb       = d.nb;
-        const int cell     = i / nb;
-        const int ib       = i - cell * nb;
-        const int a        = cell % d.n_cells[0];
-        const int rest     = cell / d.n_cells[0];
-        const int b        = rest % d.n_cells[1];
-        const int c        = rest / d.n_cells[1];
+        const long long gi = GS.off + i;
+        const int cell     = (int)fdiv( (unsigned)i, GS.div_nb );
+        const int ib       = i - cell * GS.nb;
+        const int rest     = (int)fdiv( (unsigned)cell, GS.div_na );
+        const int a        = cell - rest * GS.n[0];
+        const int c        = (int)fdiv( (unsigned)rest, GS.div_nbb );
+        const int b        = rest - c * GS.n[1];
         const R mu         = C.mu[ib];
         const V3<R> ci     = A.cfg.ld( gi );
         V3<R> g            = gradient_at<R>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu, e );
@@ -101,7 +100,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
             V3<R> z    = gauss3<R>( d.seed, d.stream, PROBE ? 0xFFFFFFFFu : (unsigned int)iteration, (unsigned int)i );
             xi         = { sc * z.x, sc * z.y, sc * z.z };
         }
-        V3<R> fv = virtual_force<R>( C, ci, g, mu, xi );
+        V3<R> fv = virtual_force<R>( C, ci, g, C.inv_mu[ib], xi );
         if( PROBE )
         {
             t2 = (float)torque2( fv, ci );
@@ -287,10 +286,13 @@ __global__ void __launch_bounds__( 256 ) eval_kernel( const SysDesc * sd, const 
     double et[N_TERMS] = { 0, 0, 0, 0, 0 };
     if( i < d.nos )
     {
-        const long long gi = d.spin_offset + i;
-        const int nb = d.nb, cell = i / nb, ib = i - cell * nb;
-        const int a = cell % d.n_cells[0], rest = cell / d.n_cells[0];
-        const int b = rest % d.n_cells[1], c = rest / d.n_cells[1];
+        const long long gi = GS.off + i;
+        const int cell     = (int)fdiv( (unsigned)i, GS.div_nb );
+        const int ib       = i - cell * GS.nb;
+        const int rest     = (int)fdiv( (unsigned)cell, GS.div_na );
+        const int a        = cell - rest * GS.n[0];
+        const int c        = (int)fdiv( (unsigned)rest, GS.div_nbb );
+        const int b        = rest - c * GS.n[1];
         const R mu      = C.mu[ib];
         const V3<R> si  = spins.ld( gi );
         R e             = 0;
@@ -369,8 +371,9 @@ static void fill_const( SysConst<R> & c, const SysDesc & d )
     const double eps = std::sqrt( 2 * a * d.dt * C_GAMMA / C_MU_B * C_K_B ) / ( 1 + a * a );
     for( int b = 0; b < d.nb; ++b )
     {
-        c.noise[b] = (R)( eps * std::sqrt( d.temperature / d.mu_s[b] ) );
-        c.mu[b]    = (R)d.mu_s[b];
+        c.noise[b]  = (R)( eps * std::sqrt( d.temperature / d.mu_s[b] ) );
+        c.mu[b]     = (R)d.mu_s[b];
+        c.inv_mu[b] = (R)( 1.0 / d.mu_s[b] );
     }
     for( int e = 0; e < 3; ++e )
         c.zeeman[e] = (R)d.zeeman[e];
@@ -402,8 +405,11 @@ static void fill_desc( SysDesc & d, const SystemInput & in )
         d.n_cells[e] = g.n_cells[e];
         d.bc[e]      = h.bc[e] ? 1 : 0;
     }
-    d.nb  = g.nb();
-    d.nos = g.nos();
+    d.nb      = g.nb();
+    d.nos     = g.nos();
+    d.div_nb  = make_fastdiv( d.nb );
+    d.div_na  = make_fastdiv( d.n_cells[0] );
+    d.div_nbb = make_fastdiv( d.n_cells[1] );
     if( d.nb > MAX_BASIS )
         throw std::runtime_error( "too many basis atoms for the device engine" );
     for( int b = 0; b < d.nb; ++b )

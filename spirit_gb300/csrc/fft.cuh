@@ -41,7 +41,8 @@ __device__ __forceinline__ cplx<R> cconj( cplx<R> a )
 // Power-of-two lines: radix-4 stages (and one radix-2 stage if log2 L is odd) with shift/mask
 // index arithmetic.
 template<typename R>
-__device__ cplx<R> * block_fft_pow2( cplx<R> * a, cplx<R> * b, int L, int nl, const cplx<R> * tw, bool inverse )
+__device__ cplx<R> * block_fft_pow2( cplx<R> * a, cplx<R> * b, int L, int ls, int nl, const cplx<R> * tw,
+                                    bool inverse )
 {
     const int lgL = __ffs( L ) - 1;
     int lgNs      = 0;
@@ -56,8 +57,8 @@ __device__ cplx<R> * block_fft_pow2( cplx<R> * a, cplx<R> * b, int L, int nl, co
         {
             const int line     = idx >> lgLR;
             const int j        = idx & ( LR - 1 );
-            const cplx<R> * src = a + ( line << lgL );
-            cplx<R> * dst       = b + ( line << lgL );
+            const cplx<R> * src = a + line * ls;
+            cplx<R> * dst       = b + line * ls;
             const int k        = j & ( Ns - 1 );
             const int d0       = ( ( j >> lgNs ) << ( lgNs + lgR ) ) + k;
             if( lgR == 1 )
@@ -102,15 +103,16 @@ __device__ cplx<R> * block_fft_pow2( cplx<R> * a, cplx<R> * b, int L, int nl, co
     return a;
 }
 
-// Stockham stage loop over nl lines of length L in shared memory (a -> b -> a ...).
+// Stockham stage loop over nl lines of length L in shared memory (a -> b -> a ...); line k
+// starts at k * ls (ls = L, or L + 1 for power-of-two lengths to spread shared-memory banks).
 // rad: 0-terminated radix list; tw: L twiddles exp(-2 pi i t/L) (in shared memory).
 // Returns the buffer that holds the result.  Must be called by all threads of the block.
 template<typename R>
-__device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int nl, const int * rad, const cplx<R> * tw,
-                               bool inverse )
+__device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int ls, int nl, const int * rad,
+                               const cplx<R> * tw, bool inverse )
 {
     if( ( L & ( L - 1 ) ) == 0 )
-        return block_fft_pow2( a, b, L, nl, tw, inverse );
+        return block_fft_pow2( a, b, L, ls, nl, tw, inverse );
     int Ns = 1;
     for( int s = 0; s < 12 && rad[s] > 0; ++s )
     {
@@ -210,6 +212,12 @@ __device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int nl, const i
         Ns *= Rr;
     }
     return a;
+}
+
+// shared-memory line stride for lines of length L
+__host__ __device__ inline int line_stride( int L )
+{
+    return ( ( L & ( L - 1 ) ) == 0 && L >= 8 && L <= 64 ) ? L + 1 : L;
 }
 
 } // namespace sg

@@ -92,10 +92,13 @@ __global__ void __launch_bounds__( 256 ) gneb_eval( GArgs<R> A, int probe )
     double a2   = 0;
     if( i < d.nos )
     {
-        const long long gi = d.spin_offset + i;
-        const int nb = d.nb, cell = i / nb, ib = i - cell * nb;
-        const int a = cell % d.n_cells[0], rest = cell / d.n_cells[0];
-        const int b = rest % d.n_cells[1], c = rest / d.n_cells[1];
+        const long long gi = GS.off + i;
+        const int cell     = (int)fdiv( (unsigned)i, GS.div_nb );
+        const int ib       = i - cell * GS.nb;
+        const int rest     = (int)fdiv( (unsigned)cell, GS.div_na );
+        const int a        = cell - rest * GS.n[0];
+        const int c        = (int)fdiv( (unsigned)rest, GS.div_nbb );
+        const int b        = rest - c * GS.n[1];
         const R mu     = C.mu[ib];
         const V3<R> si = A.s.ld( gi );
         V3<R> g        = gradient_at<R>( GS, C, pairs, A.s, A.h, gi, ib, a, b, c, si, mu, e );

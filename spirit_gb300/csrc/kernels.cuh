@@ -33,8 +33,8 @@ __device__ __forceinline__ V3<R> normalized( V3<R> v )
     R n2 = dot( v, v );
     if( n2 > R( 0 ) )
     {
-        R n = sqrt( n2 );
-        return { v.x / n, v.y / n, v.z / n };
+        R inv = R( 1 ) / sqrt( n2 );
+        return { v.x * inv, v.y * inv, v.z * inv };
     }
     return v;
 }
@@ -108,6 +108,7 @@ struct Geo
     int nb;
     int nos;
     long long off;
+    FastDiv div_nb, div_na, div_nbb;
     int pair_begin[MAX_BASIS + 1];
 };
 
@@ -120,9 +121,12 @@ __device__ __forceinline__ void load_geo( Geo & G, const SysDesc & d )
             G.n[e]  = d.n_cells[e];
             G.bc[e] = d.bc[e];
         }
-        G.nb  = d.nb;
-        G.nos = d.nos;
-        G.off = d.spin_offset;
+        G.nb      = d.nb;
+        G.nos     = d.nos;
+        G.off     = d.spin_offset;
+        G.div_nb  = d.div_nb;
+        G.div_na  = d.div_na;
+        G.div_nbb = d.div_nbb;
         for( int b = 0; b <= d.nb; ++b )
             G.pair_begin[b] = d.pair_begin[b];
     }
@@ -273,7 +277,7 @@ __device__ __forceinline__ V3<R> gradient_at( const Geo & d, const SysConst<R> &
 
 // Calculate_Force_Virtual for spin configuration c, force F = -g
 template<typename R>
-__device__ __forceinline__ V3<R> virtual_force( const SysConst<R> & C, V3<R> c, V3<R> g, R mu, V3<R> xi )
+__device__ __forceinline__ V3<R> virtual_force( const SysConst<R> & C, V3<R> c, V3<R> g, R inv_mu, V3<R> xi )
 {
     V3<R> F = { -g.x, -g.y, -g.z };
     if( C.direct )
@@ -286,9 +290,9 @@ __device__ __forceinline__ V3<R> virtual_force( const SysConst<R> & C, V3<R> c, 
     fv.x += C.dtga * cr.x;
     fv.y += C.dtga * cr.y;
     fv.z += C.dtga * cr.z;
-    fv.x /= mu;
-    fv.y /= mu;
-    fv.z /= mu;
+    fv.x *= inv_mu;
+    fv.y *= inv_mu;
+    fv.z *= inv_mu;
     if( C.thermal )
     {
         V3<R> cx = cross( c, xi );
