@@ -37,6 +37,8 @@ struct PassArgs
     // dense real input for the dipole precompute (pass A mode 1)
     const R * dense;
     int mode; // 0: spin convolution, 1: dense forward transform
+    int g;    // lines (pass B) / columns (pass C) per block
+    FastDiv div_g;
 };
 
 template<typename R>
@@ -54,8 +56,13 @@ __device__ __forceinline__ bool sys_inactive( const PassArgs<R> & p, int s )
 
 // Block tables:
 //   pass A / A' : (system, row = cb*Cin + c, first b, number of lines)
-//   pass B / C  : (system, group index, G = lines per group (a power of two), 0)
+//   pass B / B' : (system, first line, number of lines) over the flattened lines (row, ka)
+//   pass C      : (system, first column, number of columns) over the flattened columns kb*Mh + ka
+// Passes B and C hold p.g lines (columns) per block; the block tables and p.g come from the
+// autotuner of DDIPlan.
 // ------------------------------------------------------------------ pass A: R2C along a
+// Two real lines x, y go through one complex transform of z = x + i y:
+//   X[k] = (Z[k] + conj Z[-k]) / 2,   Y[k] = (Z[k] - conj Z[-k]) / 2i
 template<typename R>
 __global__ void pass_a( PassArgs<R> p )
 {
@@ -70,49 +77,62 @@ __global__ void pass_a( PassArgs<R> p )
     const int Bin = p.mode ? f.M[1] : f.N[1];
     const int Ain = p.mode ? f.M[0] : f.N[0];
     const int row = blk.y, b0 = blk.z, nl = blk.w;
+    const int nq  = ( nl + 1 ) >> 1;
     const int ls  = line_stride( Ma );
     cplx<R> * tw  = reinterpret_cast<cplx<R> *>( smem_raw );
     cplx<R> * a   = tw + Ma;
-    cplx<R> * b   = a + nl * ls;
+    cplx<R> * b   = a + nq * ls;
     load_tw( tw, p.tw + f.tw_offset[0], Ma );
-    const int cb = row / Cin, c = row - cb * Cin;
-    const int ib = cb / 3, comp = cb - 3 * ib;
     if( p.mode == 0 )
     {
-        const SysDesc & d  = p.sd[s];
-        const R mu         = fft_mu<R>( f, ib );
-        const R * src      = comp == 0 ? p.sx : ( comp == 1 ? p.sy : p.sz );
-        const long long base = d.spin_offset + ib + (long long)nb * d.n_cells[0] * ( (long long)b0 + (long long)d.n_cells[1] * c );
-        const int rowlen   = nb * d.n_cells[0];
-        for( int e = threadIdx.x; e < nl * Ma; e += blockDim.x )
+        const int cb = row / Cin, c = row - cb * Cin;
+        const int ib = cb / 3, comp = cb - 3 * ib;
+        const SysDesc & d    = p.sd[s];
+        const R mu           = fft_mu<R>( f, ib );
+        const R * src        = comp == 0 ? p.sx : ( comp == 1 ? p.sy : p.sz );
+        const int rowlen     = nb * d.n_cells[0];
+        const long long base = d.spin_offset + ib + (long long)rowlen * ( (long long)b0 + (long long)d.n_cells[1] * c );
+        for( int e = threadIdx.x; e < nq * Ma; e += blockDim.x )
         {
-            int li = (int)fdiv( (unsigned)e, f.div_Ma ), t = e - li * Ma;
-            R v    = 0;
+            const int q = (int)fdiv( (unsigned)e, f.div_Ma ), t = e - q * Ma;
+            R x = 0, y = 0;
             if( t < Ain )
-                v = mu * src[base + (long long)li * rowlen + (long long)nb * t];
-            a[li * ls + t] = { v, (R)0 };
+            {
+                const long long o = base + (long long)( 2 * q ) * rowlen + (long long)nb * t;
+                x                 = mu * src[o];
+                if( 2 * q + 1 < nl )
+                    y = mu * src[o + rowlen];
+            }
+            a[q * ls + t] = { x, y };
         }
     }
     else
     {
-        for( int e = threadIdx.x; e < nl * Ma; e += blockDim.x )
+        const R * src = p.dense + ( (size_t)row * Bin + b0 ) * Ma;
+        for( int e = threadIdx.x; e < nq * Ma; e += blockDim.x )
         {
-            int li = (int)fdiv( (unsigned)e, f.div_Ma ), t = e - li * Ma;
-            a[li * ls + t] = { p.dense[( (size_t)row * Bin + b0 + li ) * Ma + t], (R)0 };
+            const int q = (int)fdiv( (unsigned)e, f.div_Ma ), t = e - q * Ma;
+            const R x   = src[(size_t)( 2 * q ) * Ma + t];
+            const R y   = 2 * q + 1 < nl ? src[(size_t)( 2 * q + 1 ) * Ma + t] : R( 0 );
+            a[q * ls + t] = { x, y };
         }
     }
     __syncthreads();
-    cplx<R> * r  = block_fft( a, b, Ma, ls, nl, f.radix[0], tw, false );
-    cplx<R> * W1 = p.W1 + f.spec_offset + ( (size_t)row * Bin + b0 ) * Mh;
+    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.radix[0], tw, false );
+    cplx<R> * W1      = p.W1 + f.spec_offset + ( (size_t)row * Bin + b0 ) * Mh;
     for( int e = threadIdx.x; e < nl * Mh; e += blockDim.x )
     {
-        int li = (int)fdiv( (unsigned)e, f.div_Mh ), k = e - li * Mh;
-        W1[e]  = r[li * ls + k];
+        const int li      = (int)fdiv( (unsigned)e, f.div_Mh ), k = e - li * Mh;
+        const cplx<R> * z = r + ( li >> 1 ) * ls;
+        const cplx<R> zk = z[k], zm = z[k == 0 ? 0 : Ma - k];
+        W1[e]            = ( li & 1 ) ? cplx<R>{ R( 0.5 ) * ( zk.y + zm.y ), R( -0.5 ) * ( zk.x - zm.x ) }
+                                      : cplx<R>{ R( 0.5 ) * ( zk.x + zm.x ), R( 0.5 ) * ( zk.y - zm.y ) };
     }
 }
 
 // ------------------------------------------------------------------ pass B: C2C along b
-// block: fixed row = (cb, c), a group of G consecutive ka.  forward: W1 -> W2, inverse: W2 -> W1.
+// block: p.g consecutive lines (row, ka) of the flattened line index row*Mh + ka.
+// forward: W1 -> W2 (rows b >= Bin are zero), inverse: W2 -> W1 (only b < Nb kept).
 template<typename R>
 __global__ void pass_b( PassArgs<R> p, int inverse )
 {
@@ -123,53 +143,51 @@ __global__ void pass_b( PassArgs<R> p, int inverse )
         return;
     const FFTDesc & f = p.fd[s];
     const int Mb = f.M[1], Mh = f.Mh;
-    const int Bin = p.mode ? f.M[1] : f.N[1];
-    const int G   = blk.z;
-    const int lgG = __ffs( G ) - 1;
-    const int ngk = ( Mh + G - 1 ) >> lgG;
-    const int row = blk.y / ngk;
-    const int kg  = blk.y - row * ngk;
-    const int ka0 = kg << lgG;
-    const int nl  = min( G, Mh - ka0 );
-    const int ls  = line_stride( Mb );
-    cplx<R> * tw  = reinterpret_cast<cplx<R> *>( smem_raw );
-    cplx<R> * a   = tw + Mb;
-    cplx<R> * b   = a + G * ls;
+    const int Bin   = p.mode ? f.M[1] : f.N[1];
+    const int G     = p.g;
+    const int line0 = blk.y, nl = blk.z;
+    const int ls    = line_stride( Mb );
+    cplx<R> * tw    = reinterpret_cast<cplx<R> *>( smem_raw );
+    cplx<R> * a     = tw + Mb;
+    cplx<R> * b     = a + G * ls;
     load_tw( tw, p.tw + f.tw_offset[1], Mb );
-    cplx<R> * W1 = p.W1 + f.spec_offset;
-    cplx<R> * W2 = p.W2 + f.spec_offset;
-    for( int e = threadIdx.x; e < ( Mb << lgG ); e += blockDim.x )
+    const cplx<R> * W1 = p.W1 + f.spec_offset;
+    const cplx<R> * W2 = p.W2 + f.spec_offset;
+    for( int e = threadIdx.x; e < Mb * G; e += blockDim.x )
     {
-        int t = e >> lgG, li = e & ( G - 1 ); // consecutive threads -> consecutive ka (coalesced)
+        const int t = (int)fdiv( (unsigned)e, p.div_g ), li = e - t * G; // consecutive threads -> consecutive ka
         if( li >= nl )
             continue;
-        cplx<R> v = { 0, 0 };
+        const int line = line0 + li;
+        const int row  = (int)fdiv( (unsigned)line, f.div_Mh ), ka = line - row * Mh;
+        cplx<R> v      = { 0, 0 };
         if( !inverse )
         {
             if( t < Bin )
-                v = W1[( (size_t)row * Bin + t ) * Mh + ka0 + li];
+                v = W1[( (size_t)row * Bin + t ) * Mh + ka];
         }
         else
-            v = W2[( (size_t)row * Mb + t ) * Mh + ka0 + li];
+            v = W2[( (size_t)row * Mb + t ) * Mh + ka];
         a[li * ls + t] = v;
     }
     __syncthreads();
-    cplx<R> * r = block_fft( a, b, Mb, ls, nl, f.radix[1], tw, inverse != 0 );
-    const int Bout = inverse ? f.N[1] : Mb;
-    for( int e = threadIdx.x; e < ( Bout << lgG ); e += blockDim.x )
+    const cplx<R> * r = block_fft( a, b, Mb, ls, nl, f.radix[1], tw, inverse != 0 );
+    const int Bout    = inverse ? f.N[1] : Mb;
+    cplx<R> * dst     = inverse ? p.W1 + f.spec_offset : p.W2 + f.spec_offset;
+    for( int e = threadIdx.x; e < Bout * G; e += blockDim.x )
     {
-        int t = e >> lgG, li = e & ( G - 1 );
+        const int t = (int)fdiv( (unsigned)e, p.div_g ), li = e - t * G;
         if( li >= nl )
             continue;
-        if( !inverse )
-            W2[( (size_t)row * Mb + t ) * Mh + ka0 + li] = r[li * ls + t];
-        else
-            W1[( (size_t)row * Bout + t ) * Mh + ka0 + li] = r[li * ls + t];
+        const int line = line0 + li;
+        const int row  = (int)fdiv( (unsigned)line, f.div_Mh ), ka = line - row * Mh;
+        dst[( (size_t)row * Bout + t ) * Mh + ka] = r[li * ls + t];
     }
 }
 
 // ------------------------------------------------------------------ pass C: along c + tensor product
-// block: fixed kb, a group of G consecutive ka, all 3*nb components (line li = cb*G + g).
+// block: p.g consecutive columns col = kb*Mh + ka (contiguous in W2 and in Dhat), all 3*nb
+// components (smem line cb*G + g).
 template<typename R>
 __global__ void pass_c( PassArgs<R> p )
 {
@@ -180,33 +198,27 @@ __global__ void pass_c( PassArgs<R> p )
         return;
     const FFTDesc & f = p.fd[s];
     const int Mb = f.M[1], Mc = f.M[2], Mh = f.Mh, nb = f.nb;
-    const int ncb = 3 * nb;
-    const int Cin = p.mode ? f.M[2] : f.N[2];
-    const int G   = blk.z;
-    const int lgG = __ffs( G ) - 1;
-    const int ngk = ( Mh + G - 1 ) >> lgG;
-    const int kb  = blk.y / ngk;
-    const int kg  = blk.y - kb * ngk;
-    const int ka0 = kg << lgG;
-    const int ng  = min( G, Mh - ka0 );
-    const int ls  = line_stride( Mc );
-    const int nl  = ncb << lgG; // lines g >= ng are computed but never stored
-    cplx<R> * tw  = reinterpret_cast<cplx<R> *>( smem_raw );
-    cplx<R> * a   = tw + Mc;
-    cplx<R> * b   = a + nl * ls;
+    const int ncb       = 3 * nb;
+    const int Cin       = p.mode ? f.M[2] : f.N[2];
+    const int G         = p.g;
+    const int col0      = blk.y, ng = blk.z;
+    const size_t plane  = (size_t)Mb * Mh;
+    const int ls        = line_stride( Mc );
+    const int nl        = ncb * G; // lines g >= ng (last block) are zeros, computed but never stored
+    cplx<R> * tw        = reinterpret_cast<cplx<R> *>( smem_raw );
+    cplx<R> * a         = tw + Mc;
+    cplx<R> * b         = a + nl * ls;
     load_tw( tw, p.tw + f.tw_offset[2], Mc );
-    cplx<R> * W2 = p.W2 + f.spec_offset;
+    cplx<R> * W2    = p.W2 + f.spec_offset + col0;
     const int total = nl * Mc;
     for( int e = threadIdx.x; e < total; e += blockDim.x )
     {
         // e -> (cb, c, g) with g fastest for coalescing
-        int g    = e & ( G - 1 );
-        int rest = e >> lgG;
-        int cb   = (int)fdiv( (unsigned)rest, f.div_Mc );
-        int c    = rest - cb * Mc;
-        cplx<R> v = { 0, 0 };
+        const int rest = (int)fdiv( (unsigned)e, p.div_g ), g = e - rest * G;
+        const int cb   = (int)fdiv( (unsigned)rest, f.div_Mc ), c = rest - cb * Mc;
+        cplx<R> v      = { 0, 0 };
         if( c < Cin && g < ng )
-            v = W2[( ( (size_t)cb * Cin + c ) * Mb + kb ) * Mh + ka0 + g];
+            v = W2[( (size_t)cb * Cin + c ) * plane + g];
         a[( cb * G + g ) * ls + c] = v;
     }
     __syncthreads();
@@ -216,43 +228,39 @@ __global__ void pass_c( PassArgs<R> p )
         // dense forward transform: write every kc
         for( int e = threadIdx.x; e < total; e += blockDim.x )
         {
-            int g    = e & ( G - 1 );
-            int rest = e >> lgG;
-            int cb   = (int)fdiv( (unsigned)rest, f.div_Mc );
-            int c    = rest - cb * Mc;
+            const int rest = (int)fdiv( (unsigned)e, p.div_g ), g = e - rest * G;
+            const int cb   = (int)fdiv( (unsigned)rest, f.div_Mc ), c = rest - cb * Mc;
             if( g < ng )
-                W2[( ( (size_t)cb * Mc + c ) * Mb + kb ) * Mh + ka0 + g] = r[( cb * G + g ) * ls + c];
+                W2[( (size_t)cb * Mc + c ) * plane + g] = r[( cb * G + g ) * ls + c];
         }
         return;
     }
     // tensor product H_b1 = sum_b2 D_b1b2 . S_b2 (FFT.hpp:42-49 mult3D rows: xx xy xz | xy yy yz | xz yz zz)
     cplx<R> * h        = ( r == a ) ? b : a;
-    const cplx<R> * Dh = p.Dhat + f.dhat_offset;
     const int npair    = nb * nb;
-    for( int e = threadIdx.x; e < ( nb * Mc ) << lgG; e += blockDim.x )
+    const cplx<R> * Dh = p.Dhat + f.dhat_offset + (size_t)col0 * npair * 6 * Mc;
+    for( int e = threadIdx.x; e < nb * Mc * G; e += blockDim.x )
     {
-        int g    = e & ( G - 1 );
-        int rest = e >> lgG;
-        int b1   = (int)fdiv( (unsigned)rest, f.div_Mc );
-        int kc   = rest - b1 * Mc;
+        const int rest = (int)fdiv( (unsigned)e, p.div_g ), g = e - rest * G;
+        const int b1   = (int)fdiv( (unsigned)rest, f.div_Mc ), kc = rest - b1 * Mc;
         if( g >= ng )
             continue;
         cplx<R> acc[3] = { { 0, 0 }, { 0, 0 }, { 0, 0 } };
         for( int b2 = 0; b2 < nb; ++b2 )
         {
-            const cplx<R> * D = Dh + ( ( (size_t)kb * Mh + ka0 + g ) * npair + b1 * nb + b2 ) * 6 * Mc + kc;
+            const cplx<R> * D = Dh + ( (size_t)g * npair + b1 * nb + b2 ) * 6 * Mc + kc;
             cplx<R> d[6];
 #pragma unroll
             for( int q = 0; q < 6; ++q )
                 d[q] = D[q * Mc];
-            cplx<R> sx = r[( ( b2 * 3 + 0 ) * G + g ) * ls + kc];
-            cplx<R> sy = r[( ( b2 * 3 + 1 ) * G + g ) * ls + kc];
-            cplx<R> sz = r[( ( b2 * 3 + 2 ) * G + g ) * ls + kc];
-            const int row[3][3] = { { 0, 1, 2 }, { 1, 3, 4 }, { 2, 4, 5 } };
+            const cplx<R> sx = r[( ( b2 * 3 + 0 ) * G + g ) * ls + kc];
+            const cplx<R> sy = r[( ( b2 * 3 + 1 ) * G + g ) * ls + kc];
+            const cplx<R> sz = r[( ( b2 * 3 + 2 ) * G + g ) * ls + kc];
+            const int rw[3][3] = { { 0, 1, 2 }, { 1, 3, 4 }, { 2, 4, 5 } };
 #pragma unroll
             for( int c3 = 0; c3 < 3; ++c3 )
             {
-                cplx<R> d1 = d[row[c3][0]], d2 = d[row[c3][1]], d3 = d[row[c3][2]];
+                const cplx<R> d1 = d[rw[c3][0]], d2 = d[rw[c3][1]], d3 = d[rw[c3][2]];
                 acc[c3].x += d1.x * sx.x + d2.x * sy.x + d3.x * sz.x - d1.y * sx.y - d2.y * sy.y - d3.y * sz.y;
                 acc[c3].y += d1.x * sx.y + d2.x * sy.y + d3.x * sz.y + d1.y * sx.x + d2.y * sy.x + d3.y * sz.x;
             }
@@ -263,20 +271,21 @@ __global__ void pass_c( PassArgs<R> p )
     }
     __syncthreads();
     cplx<R> * other = ( h == a ) ? b : a;
-    cplx<R> * o     = Mc > 1 ? block_fft( h, other, Mc, ls, nl, f.radix[2], tw, true ) : h;
-    const int Cout  = f.N[2];
+    const cplx<R> * o = Mc > 1 ? block_fft( h, other, Mc, ls, nl, f.radix[2], tw, true ) : h;
+    const int Cout    = f.N[2];
     for( int e = threadIdx.x; e < total; e += blockDim.x )
     {
-        int g    = e & ( G - 1 );
-        int rest = e >> lgG;
-        int cb   = (int)fdiv( (unsigned)rest, f.div_Mc );
-        int c    = rest - cb * Mc;
+        const int rest = (int)fdiv( (unsigned)e, p.div_g ), g = e - rest * G;
+        const int cb   = (int)fdiv( (unsigned)rest, f.div_Mc ), c = rest - cb * Mc;
         if( c < Cout && g < ng )
-            W2[( ( (size_t)cb * Cin + c ) * Mb + kb ) * Mh + ka0 + g] = o[( cb * G + g ) * ls + c];
+            W2[( (size_t)cb * Cin + c ) * plane + g] = o[( cb * G + g ) * ls + c];
     }
 }
 
 // ------------------------------------------------------------------ pass A': C2R along a -> field
+// Two Hermitian half spectra X, Y go through one complex inverse transform of Z = X + i Y; the
+// real part is x, the imaginary part y.  The imaginary parts of X and Y at k = 0 and k = Ma/2
+// are dropped, as a real inverse transform does.
 template<typename R>
 __global__ void pass_a_inv( PassArgs<R> p )
 {
@@ -290,35 +299,48 @@ __global__ void pass_a_inv( PassArgs<R> p )
     const int Ma = f.M[0], Mh = f.Mh, nb = f.nb;
     const int Nc = f.N[2], Nb = f.N[1], Na = f.N[0];
     const int row = blk.y, b0 = blk.z, nl = blk.w;
+    const int nq  = ( nl + 1 ) >> 1;
     const int ls  = line_stride( Ma );
     cplx<R> * tw  = reinterpret_cast<cplx<R> *>( smem_raw );
     cplx<R> * a   = tw + Ma;
-    cplx<R> * b   = a + nl * ls;
+    cplx<R> * b   = a + nq * ls;
     load_tw( tw, p.tw + f.tw_offset[0], Ma );
     const cplx<R> * W1 = p.W1 + f.spec_offset + ( (size_t)row * Nb + b0 ) * Mh;
-    for( int e = threadIdx.x; e < nl * Ma; e += blockDim.x )
+    for( int e = threadIdx.x; e < nq * Ma; e += blockDim.x )
     {
-        int li = (int)fdiv( (unsigned)e, f.div_Ma ), k = e - li * Ma;
-        cplx<R> v;
-        if( k < Mh )
-            v = W1[li * Mh + k];
-        else
-            v = cconj( W1[li * Mh + ( Ma - k )] );
-        a[li * ls + k] = v;
+        const int q = (int)fdiv( (unsigned)e, f.div_Ma ), k = e - q * Ma;
+        const bool hi = k >= Mh;
+        const int kk  = hi ? Ma - k : k;
+        cplx<R> x     = W1[( 2 * q ) * Mh + kk];
+        cplx<R> y     = 2 * q + 1 < nl ? W1[( 2 * q + 1 ) * Mh + kk] : cplx<R>{ 0, 0 };
+        if( hi )
+        {
+            x.y = -x.y;
+            y.y = -y.y;
+        }
+        if( k == 0 || 2 * k == Ma )
+        {
+            x.y = 0;
+            y.y = 0;
+        }
+        a[q * ls + k] = { x.x - y.y, x.y + y.x };
     }
     __syncthreads();
-    cplx<R> * r  = block_fft( a, b, Ma, ls, nl, f.radix[0], tw, true );
+    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.radix[0], tw, true );
     const R invT = fft_invT<R>( f );
     const int cb = row / Nc, c = row - cb * Nc;
     const int ib = cb / 3, comp = cb - 3 * ib;
     R * dst      = comp == 0 ? p.hx : ( comp == 1 ? p.hy : p.hz );
-    const long long base = d.spin_offset + ib + (long long)nb * Na * ( (long long)b0 + (long long)Nb * c );
     const int rowlen     = nb * Na;
+    const long long base = d.spin_offset + ib + (long long)rowlen * ( (long long)b0 + (long long)Nb * c );
     for( int e = threadIdx.x; e < nl * Ma; e += blockDim.x )
     {
-        int li = (int)fdiv( (unsigned)e, f.div_Ma ), t = e - li * Ma;
+        const int li = (int)fdiv( (unsigned)e, f.div_Ma ), t = e - li * Ma;
         if( t < Na )
-            dst[base + (long long)li * rowlen + (long long)nb * t] = r[li * ls + t].x * invT;
+        {
+            const cplx<R> v = r[( li >> 1 ) * ls + t];
+            dst[base + (long long)li * rowlen + (long long)nb * t] = ( ( li & 1 ) ? v.y : v.x ) * invT;
+        }
     }
 }
 
@@ -464,61 +486,81 @@ void DDIPlan::build( const std::vector<DDISystem> & systems, bool fp64, const Sy
     compute_dhat( systems, d_sd, stream );
 }
 
-// Lines per block: keep the two ping-pong buffers of a block within `budget` bytes; the result is
-// a power of two (block tables of passes B and C rely on it).
-static int group_for( int line_len, int lines_per_group, size_t elem, size_t budget, int cap )
-{
-    int ls = line_stride( line_len );
-    int g  = (int)( budget / ( 2 * elem * (size_t)ls * lines_per_group ) );
-    int p  = 1;
-    while( p * 2 <= g && p * 2 <= cap )
-        p *= 2;
-    return p;
-}
-
+// Shared memory of one block of each pass (twiddles + two ping-pong line buffers)
 static size_t smem_a( size_t elem, int Ma, int nl )
 {
-    return elem * ( Ma + 2 * (size_t)nl * line_stride( Ma ) );
+    return elem * ( Ma + 2 * (size_t)( ( nl + 1 ) / 2 ) * line_stride( Ma ) );
+}
+static size_t smem_b( size_t elem, int Mb, int g )
+{
+    return elem * ( Mb + 2 * (size_t)g * line_stride( Mb ) );
+}
+static size_t smem_c( size_t elem, int Mc, int ncb, int g )
+{
+    return elem * ( Mc + 2 * (size_t)ncb * g * line_stride( Mc ) );
 }
 
-void DDIPlan::build_block_tables( const std::vector<DDISystem> & systems )
+static constexpr size_t SMEM_MAX = 200 * 1024;
+
+static void upload_table( int4 *& dst, int & n, const std::vector<int4> & t )
 {
-    size_t elem   = fp64 ? sizeof( cplx<double> ) : sizeof( cplx<float> );
-    size_t budget = 16 * 1024;
+    dfree( dst );
+    dst = dalloc<int4>( std::max<size_t>( t.size(), 1 ) );
+    if( !t.empty() )
+        h2d( dst, t.data(), t.size() );
+    n = (int)t.size();
+}
+
+// Block tables for nl_a real lines per block in passes A / A', g_b lines per block in passes
+// B / B' and g_c columns per block in pass C.
+void DDIPlan::set_tiles( int nl_a, int g_b, int g_c )
+{
+    size_t elem = fp64 ? sizeof( cplx<double> ) : sizeof( cplx<float> );
     std::vector<int4> ta, tb, tc;
     max_smem_a = max_smem_b = max_smem_c = 0;
-    for( size_t k = 0; k < systems.size(); ++k )
+    for( size_t k = 0; k < fd_host.size(); ++k )
     {
         const FFTDesc & f = fd_host[k];
-        int s             = systems[k].sys;
-        int nl            = group_for( f.M[0], 1, elem, budget, 32 );
-        for( int row = 0; row < 3 * f.nb * f.N[2]; ++row )
-            for( int b0 = 0; b0 < f.N[1]; b0 += nl )
-                ta.push_back( make_int4( s, row, b0, std::min( nl, f.N[1] - b0 ) ) );
-        max_smem_a = std::max( max_smem_a, smem_a( elem, f.M[0], nl ) );
-        int gb  = group_for( f.M[1], 1, elem, budget, 32 );
-        int ngb = ( f.Mh + gb - 1 ) / gb;
-        for( int g = 0; g < 3 * f.nb * f.N[2] * ngb; ++g )
-            tb.push_back( make_int4( s, g, gb, 0 ) );
-        max_smem_b = std::max( max_smem_b, elem * ( f.M[1] + 2 * (size_t)gb * line_stride( f.M[1] ) ) );
-        int gc  = group_for( f.M[2], 3 * f.nb, elem, budget, 32 );
-        int ngc = ( f.Mh + gc - 1 ) / gc;
-        for( int g = 0; g < f.M[1] * ngc; ++g )
-            tc.push_back( make_int4( s, g, gc, 0 ) );
-        max_smem_c = std::max( max_smem_c, elem * ( f.M[2] + 2 * (size_t)3 * f.nb * gc * line_stride( f.M[2] ) ) );
+        const int s       = sys_index[k];
+        const int rows    = 3 * f.nb * f.N[2];
+        for( int row = 0; row < rows; ++row )
+            for( int b0 = 0; b0 < f.N[1]; b0 += nl_a )
+                ta.push_back( make_int4( s, row, b0, std::min( nl_a, f.N[1] - b0 ) ) );
+        const int lines = rows * f.Mh;
+        for( int l0 = 0; l0 < lines; l0 += g_b )
+            tb.push_back( make_int4( s, l0, std::min( g_b, lines - l0 ), 0 ) );
+        const int cols = f.M[1] * f.Mh;
+        for( int c0 = 0; c0 < cols; c0 += g_c )
+            tc.push_back( make_int4( s, c0, std::min( g_c, cols - c0 ), 0 ) );
+        max_smem_a = std::max( max_smem_a, smem_a( elem, f.M[0], nl_a ) );
+        max_smem_b = std::max( max_smem_b, smem_b( elem, f.M[1], g_b ) );
+        max_smem_c = std::max( max_smem_c, smem_c( elem, f.M[2], 3 * f.nb, g_c ) );
     }
-    n_blocks[0] = (int)ta.size();
-    n_blocks[1] = (int)tb.size();
-    n_blocks[2] = (int)tc.size();
-    d_blocks[0] = dalloc<int4>( std::max<size_t>( ta.size(), 1 ) );
-    d_blocks[1] = dalloc<int4>( std::max<size_t>( tb.size(), 1 ) );
-    d_blocks[2] = dalloc<int4>( std::max<size_t>( tc.size(), 1 ) );
-    if( !ta.empty() )
-        h2d( (int4 *)d_blocks[0], ta.data(), ta.size() );
-    if( !tb.empty() )
-        h2d( (int4 *)d_blocks[1], tb.data(), tb.size() );
-    if( !tc.empty() )
-        h2d( (int4 *)d_blocks[2], tc.data(), tc.size() );
+    if( max_smem_a > SMEM_MAX || max_smem_b > SMEM_MAX || max_smem_c > SMEM_MAX )
+        throw std::runtime_error( "DDI FFT lines do not fit into shared memory (padded extent or basis too large)" );
+    upload_table( d_blocks[0], n_blocks[0], ta );
+    upload_table( d_blocks[1], n_blocks[1], tb );
+    upload_table( d_blocks[2], n_blocks[2], tc );
+    tile[0] = nl_a;
+    tile[1] = g_b;
+    tile[2] = g_c;
+}
+
+void DDIPlan::build_block_tables( const std::vector<DDISystem> & )
+{
+    // defaults until tune() measures better ones; shrink the groups until they fit (nl even)
+    size_t elem = fp64 ? sizeof( cplx<double> ) : sizeof( cplx<float> );
+    int nl = 8, gb = 8, gc = 8;
+    for( auto & f : fd_host )
+    {
+        while( nl > 2 && smem_a( elem, f.M[0], nl ) > 64 * 1024 )
+            nl /= 2;
+        while( gb > 1 && smem_b( elem, f.M[1], gb ) > 64 * 1024 )
+            gb /= 2;
+        while( gc > 1 && smem_c( elem, f.M[2], 3 * f.nb, gc ) > 64 * 1024 )
+            gc /= 2;
+    }
+    set_tiles( nl, gb, gc );
 }
 
 template<typename R>
@@ -651,7 +693,9 @@ void DDIPlan::compute_dhat( const std::vector<DDISystem> & systems, const SysDes
         pa.W2 = dW2;
         // pass A (dense): lines = nrows * Mc * Mb, each of length Ma
         {
-            int nl = group_for( Ma, 1, sizeof( cplx<double> ), 56 * 1024, 32 );
+            int nl = 16;
+            while( nl > 1 && smem_a( sizeof( cplx<double> ), Ma, nl ) > 64 * 1024 )
+                nl /= 2;
             std::vector<int4> t;
             for( int row = 0; row < nrows * Mc; ++row )
                 for( int b0 = 0; b0 < Mb; b0 += nl )
@@ -665,36 +709,44 @@ void DDIPlan::compute_dhat( const std::vector<DDISystem> & systems, const SysDes
             CUDA_CHECK( cudaStreamSynchronize( stream ) );
             dfree( dt );
         }
-        // pass B forward: rows = nrows * Mc  (3*nb*Cin with nb=1 would be 3*Mc: use a row table)
+        // pass B forward over the nrows * Mc rows (flattened lines row*Mh + ka)
         {
-            int gb  = group_for( Mb, 1, sizeof( cplx<double> ), 56 * 1024, 32 );
-            int ngk = ( Mh + gb - 1 ) / gb;
+            int gb = 16;
+            while( gb > 1 && smem_b( sizeof( cplx<double> ), Mb, gb ) > 64 * 1024 )
+                gb /= 2;
+            const int lines = nrows * Mc * Mh;
             std::vector<int4> t;
-            for( int g = 0; g < nrows * Mc * ngk; ++g )
-                t.push_back( make_int4( 0, g, gb, 0 ) );
+            for( int l0 = 0; l0 < lines; l0 += gb )
+                t.push_back( make_int4( 0, l0, std::min( gb, lines - l0 ), 0 ) );
             int4 * dt = dalloc<int4>( t.size() );
             h2d( dt, t.data(), t.size() );
             pa.blocks = dt;
-            size_t sm = sizeof( cplx<double> ) * ( Mb + 2 * (size_t)gb * line_stride( Mb ) );
-            pass_b<double><<<(unsigned)t.size(), 256, sm, stream>>>( pa, 0 );
+            pa.g      = gb;
+            pa.div_g  = make_fastdiv( gb );
+            pass_b<double><<<(unsigned)t.size(), 256, smem_b( sizeof( cplx<double> ), Mb, gb ), stream>>>( pa, 0 );
             CUDA_CHECK( cudaGetLastError() );
             CUDA_CHECK( cudaStreamSynchronize( stream ) );
             dfree( dt );
         }
-        // pass C forward along c: every (kb, ka-group); the 3*nb lines per group are the nrows rows
+        // pass C forward along c: every column; the 3*nb lines per column are the nrows rows
         {
-            // nrows = 6*npair is a multiple of 3: the 3*nb lines of a group are the nrows rows
-            fl.nb = nrows / 3;
+            fl.nb = nrows / 3; // nrows = 6*npair is a multiple of 3
             h2d( d_fdd, &fl, 1 );
-            int gc  = group_for( Mc, nrows, sizeof( cplx<double> ), 120 * 1024, 32 );
-            int ngk = ( Mh + gc - 1 ) / gc;
+            int gc = 16;
+            while( gc > 1 && smem_c( sizeof( cplx<double> ), Mc, nrows, gc ) > 120 * 1024 )
+                gc /= 2;
+            const size_t sm = smem_c( sizeof( cplx<double> ), Mc, nrows, gc );
+            if( sm > SMEM_MAX )
+                throw std::runtime_error( "DDI dipole tensor lines do not fit into shared memory" );
+            const int cols = Mb * Mh;
             std::vector<int4> t;
-            for( int g = 0; g < Mb * ngk; ++g )
-                t.push_back( make_int4( 0, g, gc, 0 ) );
+            for( int c0 = 0; c0 < cols; c0 += gc )
+                t.push_back( make_int4( 0, c0, std::min( gc, cols - c0 ), 0 ) );
             int4 * dt = dalloc<int4>( t.size() );
             h2d( dt, t.data(), t.size() );
             pa.blocks = dt;
-            size_t sm = sizeof( cplx<double> ) * ( Mc + 2 * (size_t)nrows * gc * line_stride( Mc ) );
+            pa.g      = gc;
+            pa.div_g  = make_fastdiv( gc );
             pass_c<double><<<(unsigned)t.size(), 256, sm, stream>>>( pa );
             CUDA_CHECK( cudaGetLastError() );
             CUDA_CHECK( cudaStreamSynchronize( stream ) );
@@ -715,6 +767,172 @@ void DDIPlan::compute_dhat( const std::vector<DDISystem> & systems, const SysDes
         dfree( d_fdd );
         dfree( d_twd );
     }
+}
+
+// pass k of the convolution: 0 A, 1 B, 2 C, 3 B', 4 A'
+template<typename R>
+void DDIPlan::launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const
+{
+    switch( k )
+    {
+    case 0:
+        a.blocks = d_blocks[0];
+        pass_a<R><<<n_blocks[0], threads[0], max_smem_a, stream>>>( a );
+        break;
+    case 1:
+    case 3:
+        a.blocks = d_blocks[1];
+        a.g      = tile[1];
+        a.div_g  = make_fastdiv( tile[1] );
+        pass_b<R><<<n_blocks[1], threads[1], max_smem_b, stream>>>( a, k == 3 );
+        break;
+    case 2:
+        a.blocks = d_blocks[2];
+        a.g      = tile[2];
+        a.div_g  = make_fastdiv( tile[2] );
+        pass_c<R><<<n_blocks[2], threads[2], max_smem_c, stream>>>( a );
+        break;
+    default:
+        a.blocks = d_blocks[0];
+        pass_a_inv<R><<<n_blocks[0], threads[0], max_smem_a, stream>>>( a );
+        break;
+    }
+}
+
+// Autotuner: for each pass, time the candidate lines (columns) per block on the plan's own
+// systems with CUDA events and keep the fastest.  Passes A/A' and B/B' share a table and are
+// timed together.  Runs outside any stream capture; overwrites the field arrays and the work
+// spectra only.
+template<typename R>
+void DDIPlan::tune_t( const SysDesc * d_sd, const R * sx, const R * sy, const R * sz, R * hx, R * hy, R * hz,
+                      cudaStream_t stream )
+{
+    if( n_sys == 0 )
+        return;
+    set_smem_limits<R>();
+    PassArgs<R> a = make_args<R>( *this, d_sd, nullptr );
+    a.sx          = sx;
+    a.sy          = sy;
+    a.sz          = sz;
+    a.hx          = hx;
+    a.hy          = hy;
+    a.hz          = hz;
+    a.mode        = 0;
+    const size_t elem = sizeof( cplx<R> );
+    int maxN1 = 1, maxM0 = 1, maxM1 = 1, maxM2 = 1, maxnb = 1;
+    long long lines_b = 0, cols_c = 0;
+    for( auto & f : fd_host )
+    {
+        maxN1 = std::max( maxN1, f.N[1] );
+        maxM0 = std::max( maxM0, f.M[0] );
+        maxM1 = std::max( maxM1, f.M[1] );
+        maxM2 = std::max( maxM2, f.M[2] );
+        maxnb = std::max( maxnb, f.nb );
+        lines_b += 3LL * f.nb * f.N[2] * f.Mh;
+        cols_c += (long long)f.M[1] * f.Mh;
+    }
+    cudaEvent_t e0, e1;
+    CUDA_CHECK( cudaEventCreate( &e0 ) );
+    CUDA_CHECK( cudaEventCreate( &e1 ) );
+    auto timed = [&]( std::initializer_list<int> passes ) {
+        for( int k : passes )
+            launch_pass<R>( k, a, stream );
+        CUDA_CHECK( cudaEventRecord( e0, stream ) );
+        const int reps = 4;
+        for( int r = 0; r < reps; ++r )
+            for( int k : passes )
+                launch_pass<R>( k, a, stream );
+        CUDA_CHECK( cudaEventRecord( e1, stream ) );
+        CUDA_CHECK( cudaEventSynchronize( e1 ) );
+        CUDA_CHECK( cudaGetLastError() );
+        float ms = 0;
+        CUDA_CHECK( cudaEventElapsedTime( &ms, e0, e1 ) );
+        return ms;
+    };
+    // warm-up of the whole chain (first launches pay module loading)
+    timed( { 0, 1, 2, 3, 4 } );
+    int best[3] = { tile[0], tile[1], tile[2] };
+    int bthr[3] = { threads[0], threads[1], threads[2] };
+    const int thread_opts[3] = { 64, 128, 256 };
+    {
+        float bt = 1e30f;
+        for( int nl : { 2, 4, 6, 8, 12, 16, 24, 32, 48, 64 } )
+        {
+            // even counts only: lines are then always paired (even b, odd b) whatever the tile,
+            // so the results do not depend on the tuner's choice
+            if( ( nl > maxN1 && nl > 2 ) || smem_a( elem, maxM0, nl ) > 96 * 1024 )
+                continue;
+            set_tiles( nl, best[1], best[2] );
+            for( int th : thread_opts )
+            {
+                threads[0] = th;
+                float t    = timed( { 0, 4 } );
+                if( t < bt )
+                {
+                    bt      = t;
+                    best[0] = nl;
+                    bthr[0] = th;
+                }
+            }
+        }
+        threads[0] = bthr[0];
+    }
+    {
+        float bt = 1e30f;
+        for( int g : { 1, 2, 3, 4, 5, 6, 8, 10, 12, 16, 24, 32 } )
+        {
+            if( g > lines_b || smem_b( elem, maxM1, g ) > 96 * 1024 )
+                continue;
+            set_tiles( best[0], g, best[2] );
+            for( int th : thread_opts )
+            {
+                threads[1] = th;
+                float t    = timed( { 1, 3 } );
+                if( t < bt )
+                {
+                    bt      = t;
+                    best[1] = g;
+                    bthr[1] = th;
+                }
+            }
+        }
+        threads[1] = bthr[1];
+    }
+    {
+        float bt = 1e30f;
+        for( int g : { 1, 2, 3, 4, 5, 6, 8, 10, 12, 16 } )
+        {
+            if( g > cols_c || smem_c( elem, maxM2, 3 * maxnb, g ) > 96 * 1024 )
+                continue;
+            set_tiles( best[0], best[1], g );
+            for( int th : thread_opts )
+            {
+                threads[2] = th;
+                float t    = timed( { 2 } );
+                if( t < bt )
+                {
+                    bt      = t;
+                    best[2] = g;
+                    bthr[2] = th;
+                }
+            }
+        }
+        threads[2] = bthr[2];
+    }
+    set_tiles( best[0], best[1], best[2] );
+    CUDA_CHECK( cudaEventDestroy( e0 ) );
+    CUDA_CHECK( cudaEventDestroy( e1 ) );
+}
+
+void DDIPlan::tune( const SysDesc * d_sd, const void * sx, const void * sy, const void * sz, void * hx, void * hy,
+                    void * hz, cudaStream_t stream )
+{
+    if( fp64 )
+        tune_t<double>( d_sd, (const double *)sx, (const double *)sy, (const double *)sz, (double *)hx, (double *)hy,
+                        (double *)hz, stream );
+    else
+        tune_t<float>( d_sd, (const float *)sx, (const float *)sy, (const float *)sz, (float *)hx, (float *)hy,
+                       (float *)hz, stream );
 }
 
 template<typename R>
@@ -743,21 +961,12 @@ void DDIPlan::run_t( const SysDesc * d_sd, const SysRun * runs, const R * sx, co
             trace->push_back( { id, e } );
         }
     };
-    a.blocks = (const int4 *)d_blocks[0];
-    mark( KERNEL_PASS_A );
-    pass_a<R><<<n_blocks[0], 256, max_smem_a, stream>>>( a );
-    a.blocks = (const int4 *)d_blocks[1];
-    mark( KERNEL_PASS_B );
-    pass_b<R><<<n_blocks[1], 256, max_smem_b, stream>>>( a, 0 );
-    a.blocks = (const int4 *)d_blocks[2];
-    mark( KERNEL_PASS_C );
-    pass_c<R><<<n_blocks[2], 256, max_smem_c, stream>>>( a );
-    a.blocks = (const int4 *)d_blocks[1];
-    mark( KERNEL_PASS_B_INV );
-    pass_b<R><<<n_blocks[1], 256, max_smem_b, stream>>>( a, 1 );
-    a.blocks = (const int4 *)d_blocks[0];
-    mark( KERNEL_PASS_A_INV );
-    pass_a_inv<R><<<n_blocks[0], 256, max_smem_a, stream>>>( a );
+    for( int k = 0; k < 5; ++k )
+    {
+        static const int ids[5] = { KERNEL_PASS_A, KERNEL_PASS_B, KERNEL_PASS_C, KERNEL_PASS_B_INV, KERNEL_PASS_A_INV };
+        mark( ids[k] );
+        launch_pass<R>( k, a, stream );
+    }
     CUDA_CHECK( cudaGetLastError() );
 }
 

@@ -11,6 +11,9 @@
 namespace sg
 {
 
+template<typename R>
+struct PassArgs;
+
 struct DDISystem
 {
     int sys; // index of the system in the batch
@@ -34,6 +37,10 @@ public:
     void run( const SysDesc * d_sd, const SysRun * runs, const void * sx, const void * sy, const void * sz,
               void * hx, void * hy, void * hz, cudaStream_t stream ) const;
     void release();
+    // measure and keep the fastest lines (columns) per block of every pass (outside stream capture)
+    void tune( const SysDesc * d_sd, const void * sx, const void * sy, const void * sz, void * hx, void * hy,
+               void * hz, cudaStream_t stream );
+    void set_tiles( int nl_a, int g_b, int g_c );
     // optional per-launch event trace (kernel id, event recorded before the launch)
     std::vector<std::pair<int, cudaEvent_t>> * trace = nullptr;
     int n_sys = 0;
@@ -47,6 +54,8 @@ public:
     void * d_Dhat  = nullptr;
     int4 * d_blocks[5] = { nullptr, nullptr, nullptr, nullptr, nullptr };
     int n_blocks[5]    = { 0, 0, 0, 0, 0 };
+    int tile[3]        = { 8, 8, 8 }; // lines per block of A/A', lines per block of B/B', columns per block of C
+    int threads[3]     = { 256, 256, 256 }; // threads per block of A/A', B/B', C
     size_t max_smem_a = 0, max_smem_b = 0, max_smem_c = 0;
     long long spec_elems = 0;
     std::vector<FFTDesc> fd_host;
@@ -55,6 +64,11 @@ public:
 private:
     void build_block_tables( const std::vector<DDISystem> & systems );
     void compute_dhat( const std::vector<DDISystem> & systems, const SysDesc * d_sd, cudaStream_t stream );
+    template<typename R>
+    void tune_t( const SysDesc * d_sd, const R * sx, const R * sy, const R * sz, R * hx, R * hy, R * hz,
+                 cudaStream_t stream );
+    template<typename R>
+    void launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const;
     template<typename R>
     void run_t( const SysDesc * d_sd, const SysRun * runs, const R * sx, const R * sy, const R * sz, R * hx, R * hy,
                 R * hz, cudaStream_t stream ) const;

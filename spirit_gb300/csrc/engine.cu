@@ -66,11 +66,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
     if( !run->active )
         return;
     const SysDesc & d = A.sd[s];
-    for( int p = threadIdx.x; p < d.n_pairs; p += blockDim.x )
-    {
-        const PairEntry & q = d.pairs[p];
-        pairs[p]            = { q.j, q.da, q.db, q.dc, (R)q.J, (R)q.D[0], (R)q.D[1], (R)q.D[2] };
-    }
+    load_pairs_smem( pairs, d );
     load_const( C, d );
     load_geo( GS, d );
     __syncthreads();
@@ -81,18 +77,15 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
     const bool valid     = i < d.nos;
     R e                  = 0;
     float t2             = 0;
+    int ib, a, b, c;
+    cell_of( GS, valid ? i : 0, ib, a, b, c );
+    const int smode = warp_stencil_mode( GS, a, b, c, valid );
     if( valid )
     {
         const long long gi = GS.off + i;
-        const int cell     = (int)fdiv( (unsigned)i, GS.div_nb );
-        const int ib       = i - cell * GS.nb;
-        const int rest     = (int)fdiv( (unsigned)cell, GS.div_na );
-        const int a        = cell - rest * GS.n[0];
-        const int c        = (int)fdiv( (unsigned)rest, GS.div_nbb );
-        const int b        = rest - c * GS.n[1];
         const R mu         = C.mu[ib];
         const V3<R> ci     = A.cfg.ld( gi );
-        V3<R> g            = gradient_at<R>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu, e );
+        V3<R> g            = gradient_at<R>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu, e, smode );
         V3<R> xi           = { 0, 0, 0 };
         if( C.thermal )
         {
@@ -229,8 +222,9 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
     }
     if( !( FINAL || PROBE ) )
         return;
-    // energy of the evaluated configuration and max torque of the step, per system
-    double es = block_sum( (double)e, red_d );
+    // energy of the evaluated configuration and max torque of the step, per system: warp sums in
+    // the working precision, FP64 only across the warps of the block
+    double es = block_sum_w( e, red_d );
     float tm  = block_max( t2, red_f );
     if( threadIdx.x == 0 )
     {
@@ -274,11 +268,7 @@ __global__ void __launch_bounds__( 256 ) eval_kernel( const SysDesc * sd, const 
     if( s != only_sys )
         return;
     const SysDesc & d = sd[s];
-    for( int p = threadIdx.x; p < d.n_pairs; p += blockDim.x )
-    {
-        const PairEntry & q = d.pairs[p];
-        pairs[p]            = { q.j, q.da, q.db, q.dc, (R)q.J, (R)q.D[0], (R)q.D[1], (R)q.D[2] };
-    }
+    load_pairs_smem( pairs, d );
     load_const( C, d );
     load_geo( GS, d );
     __syncthreads();
@@ -597,6 +587,7 @@ void Engine::build_systems( const std::vector<SystemInput> & systems )
         for( int c = 0; c < 3; ++c )
             field_[c] = dalloc_bytes( total_ * elem_ );
         ddi_.build( ddis, fp64_, d_desc_, stream_ );
+        ddi_.tune( d_desc_, spins_[0], spins_[1], spins_[2], field_[0], field_[1], field_[2], stream_ );
     }
 }
 

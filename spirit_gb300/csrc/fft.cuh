@@ -103,6 +103,74 @@ __device__ cplx<R> * block_fft_pow2( cplx<R> * a, cplx<R> * b, int L, int ls, in
     return a;
 }
 
+// Compile-time length version of block_fft_pow2 (the common extents 16..1024): constant
+// strides and shifts, fully unrolled radix-4 butterflies.
+template<typename R, int L>
+__device__ __forceinline__ cplx<R> * block_fft_const( cplx<R> * a, cplx<R> * b, int ls, int nl, const cplx<R> * tw,
+                                                     bool inverse )
+{
+    constexpr int lgL = ( L <= 1 ) ? 0 : ( L <= 2 ) ? 1 : ( L <= 4 ) ? 2 : ( L <= 8 ) ? 3 : ( L <= 16 ) ? 4
+                        : ( L <= 32 ) ? 5 : ( L <= 64 ) ? 6 : ( L <= 128 ) ? 7 : ( L <= 256 ) ? 8 : ( L <= 512 ) ? 9 : 10;
+#pragma unroll
+    for( int lgNs = 0; lgNs < lgL; lgNs += 2 )
+    {
+        const int lgR  = ( lgL - lgNs >= 2 ) ? 2 : 1;
+        const int lgLR = lgL - lgR;
+        const int LR   = 1 << lgLR;
+        const int Ns   = 1 << lgNs;
+        const int lgSp = lgL - lgNs - lgR;
+        for( int idx = threadIdx.x; idx < ( nl << lgLR ); idx += blockDim.x )
+        {
+            const int line     = idx >> lgLR;
+            const int j        = idx & ( LR - 1 );
+            const cplx<R> * src = a + line * ls;
+            cplx<R> * dst       = b + line * ls;
+            const int k        = j & ( Ns - 1 );
+            const int d0       = ( ( j >> lgNs ) << ( lgNs + lgR ) ) + k;
+            if( lgR == 1 )
+            {
+                cplx<R> v0 = src[j];
+                cplx<R> w  = tw[k << lgSp];
+                if( inverse )
+                    w = cconj( w );
+                cplx<R> v1   = cmul( src[j + LR], w );
+                dst[d0]      = { v0.x + v1.x, v0.y + v1.y };
+                dst[d0 + Ns] = { v0.x - v1.x, v0.y - v1.y };
+            }
+            else
+            {
+                cplx<R> v0 = src[j];
+                cplx<R> w1 = tw[k << lgSp], w2 = tw[( 2 * k ) << lgSp], w3 = tw[( 3 * k ) << lgSp];
+                if( inverse )
+                {
+                    w1 = cconj( w1 );
+                    w2 = cconj( w2 );
+                    w3 = cconj( w3 );
+                }
+                cplx<R> v1   = cmul( src[j + LR], w1 );
+                cplx<R> v2   = cmul( src[j + 2 * LR], w2 );
+                cplx<R> v3   = cmul( src[j + 3 * LR], w3 );
+                cplx<R> s02  = { v0.x + v2.x, v0.y + v2.y };
+                cplx<R> d02  = { v0.x - v2.x, v0.y - v2.y };
+                cplx<R> s13  = { v1.x + v3.x, v1.y + v3.y };
+                cplx<R> d13  = { v1.x - v3.x, v1.y - v3.y };
+                cplx<R> id13 = inverse ? cplx<R>{ -d13.y, d13.x } : cplx<R>{ d13.y, -d13.x };
+                dst[d0]          = { s02.x + s13.x, s02.y + s13.y };
+                dst[d0 + Ns]     = { d02.x + id13.x, d02.y + id13.y };
+                dst[d0 + 2 * Ns] = { s02.x - s13.x, s02.y - s13.y };
+                dst[d0 + 3 * Ns] = { d02.x - id13.x, d02.y - id13.y };
+            }
+        }
+        __syncthreads();
+        cplx<R> * t = a;
+        a           = b;
+        b           = t;
+        if( lgR == 1 )
+            break; // the radix-2 stage is the last one
+    }
+    return a;
+}
+
 // Stockham stage loop over nl lines of length L in shared memory (a -> b -> a ...); line k
 // starts at k * ls (ls = L, or L + 1 for power-of-two lengths to spread shared-memory banks).
 // rad: 0-terminated radix list; tw: L twiddles exp(-2 pi i t/L) (in shared memory).
@@ -111,6 +179,25 @@ template<typename R>
 __device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int ls, int nl, const int * rad,
                                const cplx<R> * tw, bool inverse )
 {
+    switch( L )
+    {
+    case 1:
+        return a;
+    case 16:
+        return block_fft_const<R, 16>( a, b, ls, nl, tw, inverse );
+    case 32:
+        return block_fft_const<R, 32>( a, b, ls, nl, tw, inverse );
+    case 64:
+        return block_fft_const<R, 64>( a, b, ls, nl, tw, inverse );
+    case 128:
+        return block_fft_const<R, 128>( a, b, ls, nl, tw, inverse );
+    case 256:
+        return block_fft_const<R, 256>( a, b, ls, nl, tw, inverse );
+    case 512:
+        return block_fft_const<R, 512>( a, b, ls, nl, tw, inverse );
+    default:
+        break;
+    }
     if( ( L & ( L - 1 ) ) == 0 )
         return block_fft_pow2( a, b, L, ls, nl, tw, inverse );
     int Ns = 1;

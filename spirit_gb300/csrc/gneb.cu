@@ -63,11 +63,7 @@ struct GArgs
 template<typename R>
 __device__ __forceinline__ void load_pairs( PairR<R> * pairs, SysConst<R> & C, Geo & G, const SysDesc & d )
 {
-    for( int p = threadIdx.x; p < d.n_pairs; p += blockDim.x )
-    {
-        const PairEntry & q = d.pairs[p];
-        pairs[p]            = { q.j, q.da, q.db, q.dc, (R)q.J, (R)q.D[0], (R)q.D[1], (R)q.D[2] };
-    }
+    load_pairs_smem( pairs, d );
     load_const( C, d );
     load_geo( G, d );
     __syncthreads();
@@ -90,18 +86,15 @@ __global__ void __launch_bounds__( 256 ) gneb_eval( GArgs<R> A, int probe )
     const int i = bm.y + threadIdx.x;
     R e         = 0;
     double a2   = 0;
+    int ib, a, b, c;
+    cell_of( GS, i < d.nos ? i : 0, ib, a, b, c );
+    const int smode = warp_stencil_mode( GS, a, b, c, i < d.nos );
     if( i < d.nos )
     {
         const long long gi = GS.off + i;
-        const int cell     = (int)fdiv( (unsigned)i, GS.div_nb );
-        const int ib       = i - cell * GS.nb;
-        const int rest     = (int)fdiv( (unsigned)cell, GS.div_na );
-        const int a        = cell - rest * GS.n[0];
-        const int c        = (int)fdiv( (unsigned)rest, GS.div_nbb );
-        const int b        = rest - c * GS.n[1];
         const R mu     = C.mu[ib];
         const V3<R> si = A.s.ld( gi );
-        V3<R> g        = gradient_at<R>( GS, C, pairs, A.s, A.h, gi, ib, a, b, c, si, mu, e );
+        V3<R> g        = gradient_at<R>( GS, C, pairs, A.s, A.h, gi, ib, a, b, c, si, mu, e, smode );
         V3<R> f        = { -g.x, -g.y, -g.z };
         A.G.st( gi, f );
         if( A.ctl->mode == 0 && im > 0 )

@@ -39,10 +39,12 @@ __device__ __forceinline__ V3<R> normalized( V3<R> v )
     return v;
 }
 
+// Pair of the stencil in the kernels' working precision.  lin is the linear index offset of
+// the neighbour, valid for cells whose whole stencil lies inside the system (no wrap, no cut).
 template<typename R>
 struct PairR
 {
-    int j, da, db, dc;
+    int j, da, db, dc, lin;
     R J, Dx, Dy, Dz;
 };
 
@@ -110,6 +112,18 @@ struct Geo
     long long off;
     FastDiv div_nb, div_na, div_nbb;
     int pair_begin[MAX_BASIS + 1];
+    int lo[3], hi[3]; // interior cells: lo[e] <= cell[e] < hi[e] on every axis
+    int row_len;      // nb * Na: index distance of one wrap along a
+    int a_single;     // every |da| < Na: one wrap along a reaches any neighbour
+};
+
+// Neighbour addressing of a warp: general (idx_from_pair), interior along b and c with the a-axis
+// wrap done per lane, or fully interior (neighbour = spin index + lin).
+enum StencilMode : int
+{
+    STENCIL_GENERAL = 0,
+    STENCIL_ROW     = 1,
+    STENCIL_INTERIOR = 2
 };
 
 __device__ __forceinline__ void load_geo( Geo & G, const SysDesc & d )
@@ -129,7 +143,50 @@ __device__ __forceinline__ void load_geo( Geo & G, const SysDesc & d )
         G.div_nbb = d.div_nbb;
         for( int b = 0; b <= d.nb; ++b )
             G.pair_begin[b] = d.pair_begin[b];
+        for( int e = 0; e < 3; ++e )
+        {
+            G.lo[e] = d.max_t[e];
+            G.hi[e] = d.n_cells[e] - d.max_t[e];
+        }
+        G.row_len  = d.nb * d.n_cells[0];
+        G.a_single = d.max_t[0] < d.n_cells[0];
     }
+}
+
+// Stage the system's merged pairs in shared memory in the working precision (all threads).
+template<typename R>
+__device__ __forceinline__ void load_pairs_smem( PairR<R> * pairs, const SysDesc & d )
+{
+    const int nb = d.nb, Na = d.n_cells[0], Nb = d.n_cells[1];
+    for( int p = threadIdx.x; p < d.n_pairs; p += blockDim.x )
+    {
+        const PairEntry & q = d.pairs[p];
+        const int lin       = q.j - q.i + nb * ( q.da + Na * ( q.db + Nb * q.dc ) );
+        pairs[p]            = { q.j, q.da, q.db, q.dc, lin, (R)q.J, (R)q.D[0], (R)q.D[1], (R)q.D[2] };
+    }
+}
+
+// Cell coordinates (a, b, c) and basis index ib of local spin index i
+__device__ __forceinline__ void cell_of( const Geo & G, int i, int & ib, int & a, int & b, int & c )
+{
+    const int cell = (int)fdiv( (unsigned)i, G.div_nb );
+    ib             = i - cell * G.nb;
+    const int rest = (int)fdiv( (unsigned)cell, G.div_na );
+    a              = cell - rest * G.n[0];
+    c              = (int)fdiv( (unsigned)rest, G.div_nbb );
+    b              = rest - c * G.n[1];
+}
+
+// Warp-uniform stencil mode: STENCIL_INTERIOR when every valid lane sits on an interior cell
+// (neighbour of pair p = spin gi + lin_p), STENCIL_ROW when every valid lane is interior along b
+// and c and one wrap along a suffices.  Called by all 32 lanes.
+__device__ __forceinline__ int warp_stencil_mode( const Geo & G, int a, int b, int c, bool valid )
+{
+    const bool in_bc = !valid || ( b >= G.lo[1] && b < G.hi[1] && c >= G.lo[2] && c < G.hi[2] );
+    const bool in_a  = !valid || ( a >= G.lo[0] && a < G.hi[0] );
+    if( !__all_sync( 0xffffffffu, in_bc ) || !G.a_single )
+        return STENCIL_GENERAL;
+    return __all_sync( 0xffffffffu, in_a ) ? STENCIL_INTERIOR : STENCIL_ROW;
 }
 
 // ------------------------------------------------------------------ neighbour index
@@ -190,6 +247,28 @@ __device__ __forceinline__ double block_sum( double v, double * sh )
     return r; // valid in thread 0
 }
 
+// Block sum of per-thread values of the working precision: a shuffle tree in R inside each
+// warp, then the warp partials summed in FP64 by warp 0 (result valid in thread 0).
+template<typename R>
+__device__ __forceinline__ double block_sum_w( R v, double * sh )
+{
+    for( int o = 16; o > 0; o >>= 1 )
+        v += __shfl_down_sync( 0xffffffffu, v, o );
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if( l == 0 )
+        sh[w] = (double)v;
+    __syncthreads();
+    double r = 0;
+    if( threadIdx.x < 32 )
+    {
+        r = threadIdx.x < ( blockDim.x >> 5 ) ? sh[threadIdx.x] : 0.0;
+        for( int o = 16; o > 0; o >>= 1 )
+            r += __shfl_down_sync( 0xffffffffu, r, o );
+    }
+    return r;
+}
+
 __device__ __forceinline__ float block_max( float v, float * sh )
 {
     for( int o = 16; o > 0; o >>= 1 )
@@ -226,7 +305,7 @@ __device__ __forceinline__ void load_const( SysConst<R> & dst, const SysDesc & d
 template<typename R>
 __device__ __forceinline__ V3<R> gradient_at( const Geo & d, const SysConst<R> & C, const PairR<R> * pairs,
                                               const SoA3<R> & cfg, const SoA3<R> & h, long long gi, int ib, int a,
-                                              int b, int c, V3<R> si, R mu, R & e )
+                                              int b, int c, V3<R> si, R mu, R & e, int mode = STENCIL_GENERAL )
 {
     V3<R> g = { 0, 0, 0 };
     for( int k = 0; k < C.n_aniso; ++k )
@@ -243,7 +322,20 @@ __device__ __forceinline__ V3<R> gradient_at( const Geo & d, const SysConst<R> &
     for( int p = p0; p < p1; ++p )
     {
         const PairR<R> P = pairs[p];
-        long long j      = pair_index( d, a, b, c, P.j, P.da, P.db, P.dc );
+        long long j;
+        if( mode == STENCIL_INTERIOR )
+            j = gi + P.lin;
+        else if( mode == STENCIL_ROW )
+        {
+            const int ja = a + P.da;
+            j            = gi + P.lin;
+            if( ja < 0 )
+                j = d.bc[0] ? j + d.row_len : -1;
+            else if( ja >= d.n[0] )
+                j = d.bc[0] ? j - d.row_len : -1;
+        }
+        else
+            j = pair_index( d, a, b, c, P.j, P.da, P.db, P.dc );
         if( j >= 0 )
         {
             V3<R> sj = cfg.ld( j );
