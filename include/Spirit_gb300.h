@@ -90,6 +90,18 @@ double Hamiltonian_Get_Energy_Contributions( State * state, double * terms, doub
                                             int idx_chain );
 /* EXTENSION: dipolar field h = D * (mu s) of the image's spins, AoS [nos][3] (FP64 device FFT). */
 void Hamiltonian_Get_DDI_Field( State * state, double * field, int idx_image, int idx_chain );
+/* EXTENSION, no counterpart in the reference: allocation-free FP64 gradient and energy of the
+ * stencil terms (exchange, DMI, anisotropy, Zeeman; no dipolar term) of the image's geometry and
+ * Hamiltonian, for spins already on the device (SoA sx/sy/sz[nos]).  Writes gx/gy/gz[nos] and
+ * energy[0] (all caller-owned device memory) asynchronously on `stream` (a cudaStream_t, NULL =
+ * legacy default stream).  Makes no device allocation: its scratch is a static device array.
+ * At most 4,194,304 spins.  Calls that overlap in time share that scratch and race.  The first
+ * call on a device looks the scratch up and should precede any stream capture.  Returns 0 on
+ * success, 1 bad arguments, 2 too many spins, 3 dipolar interaction enabled, 4 CUDA error,
+ * 5 host error. */
+int Hamiltonian_Get_Gradient_NoAlloc( State * state, const double * sx, const double * sy, const double * sz,
+                                      double * gx, double * gy, double * gz, double * energy, void * stream,
+                                      int idx_image, int idx_chain );
 
 /* ================================================================ Geometry (core/include/Spirit/Geometry.h) */
 void Geometry_Set_Bravais_Lattice_Type( State * state, int lattice_type );               /* :51 */

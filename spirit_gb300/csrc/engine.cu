@@ -482,6 +482,12 @@ static void fill_desc( SysDesc & d, const SystemInput & in )
     fill_consts( d );
 }
 
+void fill_system_desc( SysDesc & d, const SystemInput & in )
+{
+    d = SysDesc{};
+    fill_desc( d, in );
+}
+
 Engine::Engine( const std::vector<SystemInput> & systems, bool fp64 ) : fp64_( fp64 )
 {
     elem_ = fp64 ? sizeof( double ) : sizeof( float );

@@ -25,6 +25,9 @@ struct SystemInput
     unsigned int stream           = 0;
 };
 
+// Host-side system descriptor of one system (spin_offset 0), as the engine builds it
+void fill_system_desc( SysDesc & d, const SystemInput & in );
+
 // Energy terms in the reference's order (Energy_Contributions_per_Spin, cpp:262-305)
 enum Term
 {

@@ -139,3 +139,17 @@ def get_ddi_field(p_state, idx_image=-1, idx_chain=-1):
     h = np.zeros((nos, 3))
     _Get_DDI_Field(_vp(p_state), h.ctypes.data_as(_PD), _i(idx_image), _i(idx_chain))
     return h
+
+
+_Get_Gradient_NoAlloc = fn("Hamiltonian_Get_Gradient_NoAlloc",
+                           [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i], _i)
+
+
+def get_gradient_noalloc(p_state, sx, sy, sz, gx, gy, gz, energy, stream=None, idx_image=-1, idx_chain=-1):
+    """Allocation-free FP64 gradient + energy of the stencil terms (no dipolar term) for spins
+    already on the device.  All arguments after p_state are device addresses (ints) of FP64
+    arrays: sx/sy/sz and gx/gy/gz of length nos, energy of length 1; stream is a cudaStream_t
+    address (None: legacy default stream).  Asynchronous on that stream; allocates no device
+    memory.  Returns the status code (0 = success)."""
+    return int(_Get_Gradient_NoAlloc(_vp(p_state), sx, sy, sz, gx, gy, gz, energy, stream,
+                                     _i(idx_image), _i(idx_chain)))

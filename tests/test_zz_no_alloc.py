@@ -1,0 +1,70 @@
+"""Allocation-free gradient entry point Hamiltonian_Get_Gradient_NoAlloc against the engine's
+Hamiltonian_Get_Gradient on the same spins (both FP64 on the device).
+
+The caller owns every device buffer (allocated here with torch); the entry point itself uses a
+static device scratch array.  Each case calls it twice in a row on the same buffers: nothing may
+carry over between calls.  The file name puts it last in collection; it also passes alone.
+
+Tolerance: gradients 1e-12 relative to max |g| (same per-spin arithmetic, only the energy
+summation order differs), energies 1e-12 relative.
+"""
+import numpy as np
+import pytest
+
+from cases import FD_PAIRS, HEX2D, SQ_C1
+from helpers import make_state, spins_of
+
+pytestmark = pytest.mark.gpu
+
+SC3D_OPEN_C = dict(  # stencil with wraps along a, cuts along b and c, two exchange shells
+    bravais="sc", n_cells=[64, 48, 6], lattice_constant=1.0, mu_s=[2.0], bc=[1, 0, 0],
+    field=(0.7, (0.3, 0, 1)), anisotropy=(0.2, (0, 0.6, 0.8)), jij=[1.0, 0.25], dij=[0.3], dm_chirality=1,
+    llg=dict(dt=1e-3, damping=0.3, temperature=0.0),
+)
+
+CASES = {"sq_c1": SQ_C1, "hex2d": HEX2D, "fd_pairs": FD_PAIRS, "sc3d_open_c": SC3D_OPEN_C}
+
+
+def _nos(spec):
+    n = spec["n_cells"]
+    return n[0] * n[1] * n[2] * len(spec["mu_s"])
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_noalloc_matches_gradient(name):
+    torch = pytest.importorskip("torch")
+    from oracle.oracle import random_spins
+    from spirit_gb300 import hamiltonian
+
+    spec = CASES[name]
+    nos = _nos(spec)
+    spins = random_spins(nos, 20240 + nos)
+    with make_state(spec, spins) as p:
+        g_ref, e_ref = hamiltonian.get_gradient(p)
+        s = torch.tensor(np.ascontiguousarray(spins_of(p).T), dtype=torch.float64, device="cuda")
+        g = torch.full_like(s, float("nan"))
+        e = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+        stream = torch.cuda.current_stream().cuda_stream
+        for call in range(2):
+            rc = hamiltonian.get_gradient_noalloc(p, s[0].data_ptr(), s[1].data_ptr(), s[2].data_ptr(),
+                                                  g[0].data_ptr(), g[1].data_ptr(), g[2].data_ptr(),
+                                                  e.data_ptr(), stream)
+            torch.cuda.synchronize()
+            assert rc == 0
+            got = g.T.cpu().numpy()
+            scale = np.abs(g_ref).max()
+            np.testing.assert_allclose(got, g_ref, rtol=0, atol=1e-12 * scale, err_msg="call %d" % call)
+            assert abs(float(e.item()) - e_ref) <= 1e-12 * abs(e_ref), (call, float(e.item()), e_ref)
+
+
+def test_noalloc_rejects_dipolar():
+    torch = pytest.importorskip("torch")
+    from cases import SC3D_DDI
+    from spirit_gb300 import hamiltonian
+
+    nos = _nos(SC3D_DDI)
+    with make_state(SC3D_DDI) as p:
+        b = torch.zeros((7, nos), dtype=torch.float64, device="cuda")
+        rc = hamiltonian.get_gradient_noalloc(p, *[b[k].data_ptr() for k in range(7)])
+        torch.cuda.synchronize()
+    assert rc == 3
