@@ -235,6 +235,12 @@ bool Simulation_Running_Anywhere_On_Chain( State * state, int idx_chain );      
  * or NULL.  The reference iterates exactly one image per method (core/src/engine/Method_LLG.cpp:25-26). */
 void Simulation_LLG_Start_Batched( State ** states, int n_states, int solver_type, int n_iterations,
                                    Simulation_Run_Info * info );
+/* EXTENSION: enqueue n_steps of an open-ended batched LLG run of the States' active images on
+ * states[0]'s stream (Simulation_Set_Stream), no transfers or synchronisation; the first call
+ * uploads the spins and starts the batch.  Simulation_LLG_Batched_Finish copies the spins back
+ * into the host buffers and ends the run. */
+void Simulation_LLG_Batched_Launch_Steps( State ** states, int n_states, int solver_type, int n_steps );
+void Simulation_LLG_Batched_Finish( State ** states, int n_states );
 /* EXTENSION: device arithmetic of the step loop: 32 (FP32 bulk, default) or 64 */
 void Simulation_Set_Precision( State * state, int bits );
 int Simulation_Get_Precision( State * state );

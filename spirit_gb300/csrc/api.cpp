@@ -2164,6 +2164,35 @@ void Simulation_LLG_Start_Batched( State ** states, int n_states, int solver_typ
     }
 }
 
+// Enqueue n_steps of an open-ended batched LLG run of the States' active images on states[0]'s
+// stream, without transfers or synchronisation (the first call uploads the spins and starts the
+// batch).  Simulation_LLG_Batched_Finish brings the spins back and ends the run.
+void Simulation_LLG_Batched_Launch_Steps( State ** states, int n_states, int solver_type, int n_steps ) noexcept
+{
+    State * first = n_states > 0 ? states[0] : nullptr;
+    try
+    {
+        llg_batched_launch( states, n_states, solver_type, n_steps );
+    }
+    catch( ... )
+    {
+        handle( first, "Simulation_LLG_Batched_Launch_Steps" );
+    }
+}
+
+void Simulation_LLG_Batched_Finish( State ** states, int n_states ) noexcept
+{
+    State * first = n_states > 0 ? states[0] : nullptr;
+    try
+    {
+        llg_batched_finish( states, n_states );
+    }
+    catch( ... )
+    {
+        handle( first, "Simulation_LLG_Batched_Finish" );
+    }
+}
+
 // ============================================================== System (core/include/Spirit/System.h)
 int System_Get_Index( State * state ) noexcept
 {

@@ -826,17 +826,16 @@ static BatchCache & batch_cache()
     return c;
 }
 
-void llg_run_batched( State ** states, int n_states, int solver, int n_iterations, void * info, size_t info_size )
+// Upload the active images of the States into the cached batch engine (rebuilt when the set of
+// images or their versions changed) and start the LLG method of every system.
+static Engine & batched_prepare( State ** states, int n_states, int solver, int n_iterations,
+                                 std::vector<Image *> & ims )
 {
-    (void)info;
-    (void)info_size;
-    if( n_states <= 0 )
-        return;
-    std::vector<Image *> ims;
+    ims.clear();
     std::vector<std::pair<const Image *, long>> key;
     for( int k = 0; k < n_states; ++k )
     {
-        State * s = states[k];
+        State * s  = states[k];
         Image * im = s->chain->images[s->idx_active_image].get();
         if( im->iteration_allowed )
             throw std::runtime_error( "a simulation is already running on one of the batched images" );
@@ -852,8 +851,8 @@ void llg_run_batched( State ** states, int n_states, int solver, int n_iteration
         for( int k = 0; k < n_states; ++k )
         {
             SystemInput s;
-            s.geom                = ims[k]->geom.get();
-            s.ham                 = &ims[k]->ham;
+            s.geom = ims[k]->geom.get();
+            s.ham  = &ims[k]->ham;
             in.push_back( s );
         }
         C.eng  = std::make_unique<Engine>( in, fp64 );
@@ -861,6 +860,7 @@ void llg_run_batched( State ** states, int n_states, int solver, int n_iteration
         C.fp64 = fp64;
     }
     Engine & E = *C.eng;
+    E.set_stream( (cudaStream_t)states[0]->stream );
     size_t total = 0;
     for( auto * im : ims )
         total += im->spins.size();
@@ -868,6 +868,7 @@ void llg_run_batched( State ** states, int n_states, int solver, int n_iteration
     {
         if( C.pinned )
             cudaFreeHost( C.pinned );
+        C.pinned = nullptr;
         CUDA_CHECK( cudaMallocHost( (void **)&C.pinned, total * sizeof( double ) ) );
         C.pinned_n = total;
     }
@@ -899,26 +900,19 @@ void llg_run_batched( State ** states, int n_states, int solver, int n_iteration
     for( int k = 0; k < n_states; ++k )
         nit[k] = n_iterations > 0 ? n_iterations : (int)ims[k]->llg.n_iterations;
     E.llg_start( solver, nit );
-    // run until every system stopped (convergence / budget) or Simulation_Stop on the first state
-    int chunk = 8;
-    while( true )
-    {
-        auto stv  = E.status();
-        bool any  = false;
-        for( auto & s : stv )
-            any = any || s.active;
-        if( !any || !ims[0]->iteration_allowed.load() || stop_file() )
-            break;
-        E.llg_launch( chunk );
-        E.sync();
-        chunk = std::min( 512, chunk * 2 );
-    }
+    return E;
+}
+
+// Bring the batch's spins and run state back into the images and end their runs.
+static void batched_finish( Engine & E, const std::vector<Image *> & ims )
+{
+    BatchCache & C = batch_cache();
     E.get_all_spins( C.pinned );
     E.sync();
     auto stv = E.status();
-    o        = 0;
+    size_t o = 0;
     auto now = std::chrono::steady_clock::now();
-    for( int k = 0; k < n_states; ++k )
+    for( size_t k = 0; k < ims.size(); ++k )
     {
         std::memcpy( ims[k]->spins.data(), C.pinned + o, ims[k]->spins.size() * sizeof( double ) );
         o += ims[k]->spins.size();
@@ -930,6 +924,76 @@ void llg_run_batched( State ** states, int n_states, int solver, int n_iteration
         ims[k]->info.ips     = ims[k]->info.wall_ms > 0 ? 1000.0 * stv[k].iteration / ims[k]->info.wall_ms : 0;
         ims[k]->iteration_allowed = false;
     }
+}
+
+void llg_run_batched( State ** states, int n_states, int solver, int n_iterations, void * info, size_t info_size )
+{
+    (void)info;
+    (void)info_size;
+    if( n_states <= 0 )
+        return;
+    std::vector<Image *> ims;
+    Engine & E = batched_prepare( states, n_states, solver, n_iterations, ims );
+    // run until every system stopped (convergence / budget) or Simulation_Stop on the first state
+    int chunk = 8;
+    while( true )
+    {
+        auto stv = E.status();
+        bool any = false;
+        for( auto & s : stv )
+            any = any || s.active;
+        if( !any || !ims[0]->iteration_allowed.load() || stop_file() )
+            break;
+        E.llg_launch( chunk );
+        E.sync();
+        chunk = std::min( 512, chunk * 2 );
+    }
+    batched_finish( E, ims );
+}
+
+// Open-ended batched run driven by the caller: the first call (or a call for another set of
+// States) uploads and starts the batch; every call enqueues n_steps on the batch's stream
+// (states[0]'s stream) without synchronising.  llg_batched_finish ends the run.
+struct BatchedRun
+{
+    std::vector<State *> states;
+    std::vector<Image *> ims;
+    int solver   = -1;
+    Engine * eng = nullptr;
+};
+
+static BatchedRun & batched_run()
+{
+    static BatchedRun r;
+    return r;
+}
+
+void llg_batched_launch( State ** states, int n_states, int solver, int n_steps )
+{
+    if( n_states <= 0 )
+        return;
+    BatchedRun & R = batched_run();
+    std::vector<State *> st( states, states + n_states );
+    if( !R.eng || R.states != st || R.solver != solver )
+    {
+        if( R.eng )
+            batched_finish( *R.eng, R.ims );
+        R.eng    = nullptr;
+        R.states = st;
+        R.solver = solver;
+        R.eng    = &batched_prepare( states, n_states, solver, std::numeric_limits<int>::max() / 2, R.ims );
+    }
+    R.eng->llg_launch( n_steps );
+}
+
+void llg_batched_finish( State ** states, int n_states )
+{
+    BatchedRun & R = batched_run();
+    std::vector<State *> st( states, states + n_states );
+    if( !R.eng || R.states != st )
+        throw std::runtime_error( "no open batched run for these States" );
+    batched_finish( *R.eng, R.ims );
+    R = BatchedRun{};
 }
 
 } // namespace sg

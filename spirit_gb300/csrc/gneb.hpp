@@ -18,5 +18,8 @@ void llg_vp_shot( State * st, Image & img, int n );
 
 // batched LLG over the active images of several States (one device batch)
 void llg_run_batched( State ** states, int n_states, int solver, int n_iterations, void * info, size_t info_size );
+// caller-driven batched run: enqueue n_steps (first call uploads and starts), then finish
+void llg_batched_launch( State ** states, int n_states, int solver, int n_steps );
+void llg_batched_finish( State ** states, int n_states );
 
 } // namespace sg

@@ -77,6 +77,23 @@ def start_batched(p_states, solver_type, n_iterations=-1):
     return list(infos)
 
 
+_LLG_Batched_Launch_Steps = fn("Simulation_LLG_Batched_Launch_Steps", [ctypes.POINTER(_vp), _i, _i, _i])
+_LLG_Batched_Finish = fn("Simulation_LLG_Batched_Finish", [ctypes.POINTER(_vp), _i])
+
+
+def batched_launch_steps(p_states, solver_type, n_steps):
+    """Enqueue n_steps of an open-ended batched LLG run on the first state's stream, without
+    transfers or synchronisation; the first call uploads the spins and starts (extension)."""
+    arr = (_vp * len(p_states))(*p_states)
+    _LLG_Batched_Launch_Steps(arr, _i(len(p_states)), _i(solver_type), _i(n_steps))
+
+
+def batched_finish(p_states):
+    """End the open batched run: spins back into the host buffers (extension)."""
+    arr = (_vp * len(p_states))(*p_states)
+    _LLG_Batched_Finish(arr, _i(len(p_states)))
+
+
 def single_shot(p_state, idx_image=-1, idx_chain=-1):
     _SingleShot(_vp(p_state), _i(idx_image), _i(idx_chain))
 

@@ -144,3 +144,35 @@ def test_batched_uneven_vs_oracle():
     for k, (s, x) in enumerate(zip(specs, inits)):
         ref, _ = OracleSystem(s).llg(x, "SIB", 25, dt=1e-3, damping=0.2, temperature=10.0 * k, seed=5, stream=k)
         assert np.abs(out[k] - ref).max() < 1e-9, k
+
+
+def test_batched_launch_steps_equals_start_batched():
+    """The caller-driven batched run (Launch_Steps in pieces, then Finish) gives the same spins,
+    bit for bit, as one Simulation_LLG_Start_Batched of the same number of steps (T > 0: the
+    Philox counters advance with the device iteration, not with the host calls)."""
+    from oracle.oracle import random_spins
+    from spirit_gb300 import simulation
+
+    specs = []
+    for k, L in enumerate([10, 23, 17]):
+        s = dict(GRAD_CASES["sq_c1"])
+        s["n_cells"] = [L, 30 - L, 1]
+        s["llg"] = dict(dt=1e-3, damping=0.2, temperature=15.0 * (k + 1), seed=9)
+        specs.append(s)
+    inits = [random_spins(s["n_cells"][0] * s["n_cells"][1], 90 + k) for k, s in enumerate(specs)]
+    out = []
+    for mode in range(2):
+        ctxs = [make_state(s, x, precision=32, name="l%d_%d" % (mode, k)) for k, (s, x) in enumerate(zip(specs, inits))]
+        ps = [c.__enter__() for c in ctxs]
+        if mode == 0:
+            simulation.start_batched(ps, simulation.SOLVER_SIB, 37)
+        else:
+            for n in (5, 16, 9, 7):
+                simulation.batched_launch_steps(ps, simulation.SOLVER_SIB, n)
+            simulation.batched_finish(ps)
+            assert simulation.get_iteration(ps[0]) == 37
+        out.append([spins_of(p) for p in ps])
+        for c in ctxs:
+            c.__exit__(None, None, None)
+    for a, b in zip(out[0], out[1]):
+        np.testing.assert_array_equal(a, b)
