@@ -206,7 +206,7 @@ def c4_specs(n=256, seed=4):
     return specs
 
 
-def run_batched_vs_plain(steps, warmup):
+def run_batched_vs_plain(steps, warmup, plain=True, check=True):
     """256 uneven systems: spin-updates/s of the batched path (all systems in one launch per SIB
     stage, CUDA graphs) against the plain path (every system its own engine and launches, on the
     same stream), both FP32 and device-timed with CUDA events; the ensemble's arrays (~290 MB)
@@ -236,22 +236,24 @@ def run_batched_vs_plain(steps, warmup):
         simulation.set_stream(p, stream.cuda_stream)
     ev = lambda: torch.cuda.Event(enable_timing=True)
     # plain: one engine and one launch sequence per system
-    for p in states:
+    plain_ms = float("nan")
+    for p in (states if plain else []):
         simulation.start(p, simulation.METHOD_LLG, simulation.SOLVER_SIB, 10**9, -1, True)
-    for _ in range(warmup):
+    if plain:
+        for _ in range(warmup):
+            for p in states:
+                launch(p, 1, -1, -1)
+        stream.synchronize()
+        a, b = ev(), ev()
+        a.record(stream)
+        for _ in range(steps):
+            for p in states:
+                launch(p, 1, -1, -1)
+        b.record(stream)
+        stream.synchronize()
+        plain_ms = a.elapsed_time(b)
         for p in states:
-            launch(p, 1, -1, -1)
-    stream.synchronize()
-    a, b = ev(), ev()
-    a.record(stream)
-    for _ in range(steps):
-        for p in states:
-            launch(p, 1, -1, -1)
-    b.record(stream)
-    stream.synchronize()
-    plain_ms = a.elapsed_time(b)
-    for p in states:
-        simulation.stop(p)
+            simulation.stop(p)
     # batched: all systems in one engine
     simulation.batched_launch_steps(states, simulation.SOLVER_SIB, warmup)
     stream.synchronize()
@@ -263,13 +265,14 @@ def run_batched_vs_plain(steps, warmup):
     batched_ms = a.elapsed_time(b)
     simulation.batched_finish(states)
     # accuracy after 1000 steps: 8 smallest systems, batched FP32 vs the FP64 oracle
-    small = sorted(range(len(specs)), key=lambda k: nos[k])[:8]
+    small = sorted(range(len(specs)), key=lambda k: nos[k])[:8 if check else 0]
     sub = [states[k] for k in small]
     s0 = [random_spins(nos[k], 5000 + k) for k in small]
     for p, s in zip(sub, s0):
         system.get_spin_directions(p)[:] = s
-    simulation.start_batched(sub, simulation.SOLVER_SIB, 1000)
-    dm = 0.0
+    if sub:
+        simulation.start_batched(sub, simulation.SOLVER_SIB, 1000)
+    dm = 0.0 if sub else None
     for j, k in enumerate(small):
         sp = specs[k]
         o = OracleSystem(sp)
@@ -417,7 +420,15 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-batched", dest="batched", action="store_false",
                     help="skip the 256-system batched-vs-plain measurement")
+    ap.add_argument("--only-batched", action="store_true",
+                    help="run and print only the 256-system batched-vs-plain measurement (profiling)")
     args = ap.parse_args()
+    if args.only_batched:
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps(run_batched_vs_plain(args.steps, args.warmup, plain=False, check=False)))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -43,6 +43,8 @@ struct StageArgs
     SoA3<R> aux1;         // fv of stage 1
     SoA3<R> aux2;         // RK4 running sum
     SoA3<R> h;            // dipolar field of cfg (x == nullptr: none)
+    SoA3<R> xi;           // thermal field of the iteration: written by stage 1, read by later stages
+    int tune;             // 1: timing run of the tuner (ignores and keeps the run state)
 };
 
 enum
@@ -50,8 +52,13 @@ enum
     ST_PROBE = 0
 };
 
+// spins per thread of the FP32 stage kernels (index = Engine::spt_idx_); FP64 uses 1
+static const int SPT_OPTIONS[3] = { 1, 2, 4 };
+
 // SOLVER / STAGE are compile-time; STAGE 0 is the constructor probe (initial torque + energy).
-template<typename R, int SOLVER, int STAGE>
+// A block of 256 threads covers SPT * 256 consecutive spins of one system (thread t: spins
+// t, t + 256, ...), so the per-block set-up and reductions are shared by SPT spins per thread.
+template<typename R, int SOLVER, int STAGE, int SPT>
 __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
 {
     __shared__ PairR<R> pairs[MAX_PAIRS];
@@ -63,7 +70,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
     const int2 bm = A.blkmap[blockIdx.x];
     const int s   = bm.x;
     SysRun * run  = A.runs + s;
-    if( !run->active )
+    if( !A.tune && !run->active )
         return;
     const SysDesc & d = A.sd[s];
     load_pairs_smem( pairs, d );
@@ -73,10 +80,13 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
     constexpr bool FINAL = ( SOLVER == SOLVER_RK4 ) ? ( STAGE == 4 ) : ( STAGE == 2 );
     constexpr bool PROBE = STAGE == ST_PROBE;
     const int iteration  = run->iteration;
-    const int i          = bm.y + threadIdx.x; // local spin index
-    const bool valid     = i < d.nos;
     R e                  = 0;
     float t2             = 0;
+#pragma unroll
+    for( int k = 0; k < SPT; ++k )
+    {
+    const int i      = bm.y + threadIdx.x + k * 256; // local spin index
+    const bool valid = i < d.nos;
     int ib, a, b, c;
     cell_of( GS, valid ? i : 0, ib, a, b, c );
     const int smode = warp_stencil_mode( GS, a, b, c, valid );
@@ -85,18 +95,29 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
         const long long gi = GS.off + i;
         const R mu         = C.mu[ib];
         const V3<R> ci     = A.cfg.ld( gi );
-        V3<R> g            = gradient_at<R>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu, e, smode );
+        R ek               = 0;
+        V3<R> g            = gradient_at<R>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu, ek, smode );
+        e += ek;
         V3<R> xi           = { 0, 0, 0 };
         if( C.thermal )
         {
-            const R sc = C.noise[ib];
-            V3<R> z    = gauss3<R>( d.seed, d.stream, PROBE ? 0xFFFFFFFFu : (unsigned int)iteration, (unsigned int)i );
-            xi         = { sc * z.x, sc * z.y, sc * z.z };
+            // drawn once per iteration (Prepare_Thermal_Field, Method_LLG.cpp:65-110) by the first
+            // stage and kept for the later stages of the same iteration
+            if( PROBE || STAGE == 1 )
+            {
+                const R sc = C.noise[ib];
+                V3<R> z = gauss3<R>( d.seed, d.stream, PROBE ? 0xFFFFFFFFu : (unsigned int)iteration, (unsigned int)i );
+                xi      = { sc * z.x, sc * z.y, sc * z.z };
+                if( STAGE == 1 )
+                    A.xi.st( gi, xi );
+            }
+            else
+                xi = A.xi.ld( gi );
         }
         V3<R> fv = virtual_force<R>( C, ci, g, C.inv_mu[ib], xi );
         if( PROBE )
         {
-            t2 = (float)torque2( fv, ci );
+            t2 = fmaxf( t2, (float)torque2( fv, ci ) );
         }
         else if( SOLVER == SOLVER_SIB )
         {
@@ -120,7 +141,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
                 if( sizeof( R ) == 4 )
                     sn = normalized( sn );
                 A.s.st( gi, sn );
-                t2 = (float)torque2( A.aux1.ld( gi ), sn );
+                t2 = fmaxf( t2, (float)torque2( A.aux1.ld( gi ), sn ) );
             }
         }
         else if( SOLVER == SOLVER_HEUN )
@@ -148,7 +169,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
                 t.z += R( 0.5 ) * ( R( -1 ) * c2.z );
                 V3<R> sn = normalized( t );
                 A.s.st( gi, sn );
-                t2 = (float)torque2( fv1, sn );
+                t2 = fmaxf( t2, (float)torque2( fv1, sn ) );
             }
         }
         else if( SOLVER == SOLVER_DEPONDT )
@@ -174,7 +195,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
                 if( sizeof( R ) == 4 )
                     sn = normalized( sn );
                 A.s.st( gi, sn );
-                t2 = (float)torque2( fv1, sn );
+                t2 = fmaxf( t2, (float)torque2( fv1, sn ) );
             }
         }
         else if( SOLVER == SOLVER_RK4 )
@@ -216,9 +237,10 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
                 acc.z += w6 * k.z;
                 V3<R> sn = normalized( acc );
                 A.s.st( gi, sn );
-                t2 = (float)torque2( A.aux1.ld( gi ), sn );
+                t2 = fmaxf( t2, (float)torque2( A.aux1.ld( gi ), sn ) );
             }
         }
+    }
     }
     if( !( FINAL || PROBE ) )
         return;
@@ -245,9 +267,12 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
         vr->energy_acc       = 0;
         vr->torque_bits      = 0;
         vr->blocks_done      = 0;
-        int it               = vr->iteration + ( PROBE ? 0 : 1 );
-        vr->iteration        = it;
-        vr->active           = ( it < d.n_iterations ) && !( mt < (float)d.force_convergence );
+        if( !A.tune )
+        {
+            int it        = vr->iteration + ( PROBE ? 0 : 1 );
+            vr->iteration = it;
+            vr->active    = ( it < d.n_iterations ) && !( mt < (float)d.force_convergence );
+        }
     }
 }
 
@@ -509,6 +534,7 @@ Engine::~Engine()
         dfree( predB_[c] );
         dfree( aux1_[c] );
         dfree( aux2_[c] );
+        dfree( noise_[c] );
         dfree( field_[c] );
     }
     dfree( d_desc_ );
@@ -518,6 +544,11 @@ Engine::~Engine()
     dfree( d_grad_ );
     dfree( d_blkmap_ );
     dfree( d_blkcount_ );
+    for( int k = 0; k < 3; ++k )
+    {
+        dfree( d_sblkmap_[k] );
+        dfree( d_sblkcount_[k] );
+    }
     if( own_stream_ )
         cudaStreamDestroy( own_stream_ );
 }
@@ -576,6 +607,7 @@ void Engine::build_systems( const std::vector<SystemInput> & systems )
         predB_[c] = dalloc_bytes( total_ * elem_ );
         aux1_[c]  = dalloc_bytes( total_ * elem_ );
         aux2_[c]  = dalloc_bytes( total_ * elem_ );
+        noise_[c] = dalloc_bytes( total_ * elem_ );
     }
     d_desc_     = dalloc<SysDesc>( desc_.size() );
     d_runs_     = dalloc<SysRun>( desc_.size() );
@@ -587,6 +619,26 @@ void Engine::build_systems( const std::vector<SystemInput> & systems )
     h2d( d_desc_, desc_.data(), desc_.size() );
     h2d( d_blkmap_, blkmap.data(), blkmap.size() );
     h2d( d_blkcount_, blkcount.data(), blkcount.size() );
+    for( int k = 0; k < 3; ++k )
+    {
+        const int span = 256 * SPT_OPTIONS[k];
+        std::vector<int2> m;
+        std::vector<int> cnt;
+        for( size_t sy = 0; sy < desc_.size(); ++sy )
+        {
+            int nbk = ( desc_[sy].nos + span - 1 ) / span;
+            for( int q = 0; q < nbk; ++q )
+                m.push_back( make_int2( (int)sy, q * span ) );
+            cnt.push_back( nbk );
+        }
+        n_sblocks_[k]   = (int)m.size();
+        d_sblkmap_[k]   = dalloc<int2>( std::max<size_t>( m.size(), 1 ) );
+        d_sblkcount_[k] = dalloc<int>( std::max<size_t>( cnt.size(), 1 ) );
+        if( !m.empty() )
+            h2d( d_sblkmap_[k], m.data(), m.size() );
+        if( !cnt.empty() )
+            h2d( d_sblkcount_[k], cnt.data(), cnt.size() );
+    }
     any_ddi_ = !ddis.empty();
     if( any_ddi_ )
     {
@@ -763,11 +815,19 @@ static void trace_mark( std::vector<std::pair<int, cudaEvent_t>> * trace, int id
 }
 
 template<typename R, int SOLVER, int STAGE>
-static void launch_stage( int nblk, cudaStream_t st, const StageArgs<R> & a,
-                          std::vector<std::pair<int, cudaEvent_t>> * trace = nullptr )
+void Engine::launch_stage( StageArgs<R> a, cudaStream_t st )
 {
-    trace_mark( trace, KERNEL_STAGE, st );
-    llg_stage<R, SOLVER, STAGE><<<nblk, 256, 0, st>>>( a );
+    trace_mark( trace_, KERNEL_STAGE, st );
+    const int k = sizeof( R ) == 8 ? 0 : spt_idx_;
+    a.blkmap    = d_sblkmap_[k];
+    a.blkcount  = d_sblkcount_[k];
+    const int n = n_sblocks_[k];
+    if( k == 0 )
+        llg_stage<R, SOLVER, STAGE, 1><<<n, 256, 0, st>>>( a );
+    else if( k == 1 )
+        llg_stage<R, SOLVER, STAGE, 2><<<n, 256, 0, st>>>( a );
+    else
+        llg_stage<R, SOLVER, STAGE, 4><<<n, 256, 0, st>>>( a );
 }
 
 template<typename R>
@@ -787,29 +847,20 @@ void Engine::launch_probe_t()
         a.h = soa<R>( field_ );
     }
     // the probe uses the solver's force definition (direct minimisation / dynamics) only
-    llg_stage<R, SOLVER_HEUN, ST_PROBE><<<n_blocks_, 256, 0, stream_>>>( a );
+    llg_stage<R, SOLVER_HEUN, ST_PROBE, 1><<<n_blocks_, 256, 0, stream_>>>( a );
     CUDA_CHECK( cudaGetLastError() );
 }
 
+// the stage kernels of one step of the current solver; with_ddi: the dipolar field of each
+// stage configuration is computed before its stage
 template<typename R>
-void Engine::launch_step_t()
+void Engine::launch_stages_t( StageArgs<R> & a, bool with_ddi )
 {
-    StageArgs<R> a{};
-    a.sd       = d_desc_;
-    a.runs     = d_runs_;
-    a.blkmap   = d_blkmap_;
-    a.blkcount = d_blkcount_;
-    a.s        = soa<R>( spins_ );
-    a.aux1     = soa<R>( aux1_ );
-    a.aux2     = soa<R>( aux2_ );
     SoA3<R> pA = soa<R>( predA_ ), pB = soa<R>( predB_ );
-    SoA3<R> hf = any_ddi_ ? soa<R>( field_ ) : SoA3<R>{ nullptr, nullptr, nullptr };
     auto field = [&]( const SoA3<R> & cfg ) {
-        if( any_ddi_ )
+        if( with_ddi && any_ddi_ )
             ddi_.run( d_desc_, d_runs_, cfg.x, cfg.y, cfg.z, field_[0], field_[1], field_[2], stream_ );
     };
-    a.h = hf;
-    const int nb = n_blocks_;
     switch( solver_ )
     {
     case SOLVER_SIB:
@@ -820,19 +871,19 @@ void Engine::launch_step_t()
         a.out = pA;
         field( a.cfg );
         if( solver_ == SOLVER_SIB )
-            launch_stage<R, SOLVER_SIB, 1>( nb, stream_, a, trace_ );
+            launch_stage<R, SOLVER_SIB, 1>( a, stream_ );
         else if( solver_ == SOLVER_HEUN )
-            launch_stage<R, SOLVER_HEUN, 1>( nb, stream_, a, trace_ );
+            launch_stage<R, SOLVER_HEUN, 1>( a, stream_ );
         else
-            launch_stage<R, SOLVER_DEPONDT, 1>( nb, stream_, a, trace_ );
+            launch_stage<R, SOLVER_DEPONDT, 1>( a, stream_ );
         a.cfg = pA;
         field( a.cfg );
         if( solver_ == SOLVER_SIB )
-            launch_stage<R, SOLVER_SIB, 2>( nb, stream_, a, trace_ );
+            launch_stage<R, SOLVER_SIB, 2>( a, stream_ );
         else if( solver_ == SOLVER_HEUN )
-            launch_stage<R, SOLVER_HEUN, 2>( nb, stream_, a, trace_ );
+            launch_stage<R, SOLVER_HEUN, 2>( a, stream_ );
         else
-            launch_stage<R, SOLVER_DEPONDT, 2>( nb, stream_, a, trace_ );
+            launch_stage<R, SOLVER_DEPONDT, 2>( a, stream_ );
         break;
     }
     case SOLVER_RK4:
@@ -840,24 +891,84 @@ void Engine::launch_step_t()
         a.cfg = a.s;
         a.out = pA;
         field( a.cfg );
-        launch_stage<R, SOLVER_RK4, 1>( nb, stream_, a, trace_ );
+        launch_stage<R, SOLVER_RK4, 1>( a, stream_ );
         a.cfg = pA;
         a.out = pB;
         field( a.cfg );
-        launch_stage<R, SOLVER_RK4, 2>( nb, stream_, a, trace_ );
+        launch_stage<R, SOLVER_RK4, 2>( a, stream_ );
         a.cfg = pB;
         a.out = pA;
         field( a.cfg );
-        launch_stage<R, SOLVER_RK4, 3>( nb, stream_, a, trace_ );
+        launch_stage<R, SOLVER_RK4, 3>( a, stream_ );
         a.cfg = pA;
         field( a.cfg );
-        launch_stage<R, SOLVER_RK4, 4>( nb, stream_, a, trace_ );
+        launch_stage<R, SOLVER_RK4, 4>( a, stream_ );
         break;
     }
     default:
         throw std::runtime_error( "solver not supported by the LLG engine" );
     }
     CUDA_CHECK( cudaGetLastError() );
+}
+
+template<typename R>
+void Engine::launch_step_t()
+{
+    StageArgs<R> a{};
+    a.sd   = d_desc_;
+    a.runs = d_runs_;
+    a.s    = soa<R>( spins_ );
+    a.aux1 = soa<R>( aux1_ );
+    a.aux2 = soa<R>( aux2_ );
+    a.h    = any_ddi_ ? soa<R>( field_ ) : SoA3<R>{ nullptr, nullptr, nullptr };
+    a.xi   = soa<R>( noise_ );
+    a.tune = 0;
+    launch_stages_t<R>( a, true );
+}
+
+// Stage-kernel autotuner: times the stage kernels of one step of the current solver for 1, 2
+// and 4 spins per thread and keeps the fastest.  Runs on scratch buffers (the state is not
+// touched) with the run state ignored; the caller resets the run state afterwards.
+template<typename R>
+void Engine::tune_stages_t()
+{
+    StageArgs<R> a{};
+    a.sd   = d_desc_;
+    a.runs = d_runs_;
+    a.s    = soa<R>( predB_ );
+    a.aux1 = soa<R>( aux1_ );
+    a.aux2 = soa<R>( aux2_ );
+    a.h    = any_ddi_ ? soa<R>( field_ ) : SoA3<R>{ nullptr, nullptr, nullptr };
+    a.xi   = soa<R>( noise_ );
+    a.tune = 1;
+    auto * saved = trace_;
+    trace_       = nullptr;
+    cudaEvent_t e0, e1;
+    CUDA_CHECK( cudaEventCreate( &e0 ) );
+    CUDA_CHECK( cudaEventCreate( &e1 ) );
+    float best = 1e30f;
+    int bi     = 0;
+    for( int k = 0; k < 3; ++k )
+    {
+        spt_idx_ = k;
+        launch_stages_t<R>( a, false );
+        CUDA_CHECK( cudaEventRecord( e0, stream_ ) );
+        for( int r = 0; r < 3; ++r )
+            launch_stages_t<R>( a, false );
+        CUDA_CHECK( cudaEventRecord( e1, stream_ ) );
+        CUDA_CHECK( cudaEventSynchronize( e1 ) );
+        float ms = 0;
+        CUDA_CHECK( cudaEventElapsedTime( &ms, e0, e1 ) );
+        if( ms < best )
+        {
+            best = ms;
+            bi   = k;
+        }
+    }
+    spt_idx_ = bi;
+    trace_   = saved;
+    CUDA_CHECK( cudaEventDestroy( e0 ) );
+    CUDA_CHECK( cudaEventDestroy( e1 ) );
 }
 
 void Engine::launch_step_kernels()
@@ -926,6 +1037,11 @@ void Engine::llg_start( int solver, const std::vector<int> & n_iterations )
         desc_[s].n_iterations = n_iterations.size() == 1 ? n_iterations[0] : n_iterations[s];
     CUDA_CHECK( cudaMemcpyAsync( d_desc_, desc_.data(), sizeof( SysDesc ) * desc_.size(), cudaMemcpyHostToDevice,
                                  stream_ ) );
+    if( !fp64_ && tuned_solver_ != solver_ )
+    {
+        tune_stages_t<float>();
+        tuned_solver_ = solver_;
+    }
     std::vector<SysRun> r( desc_.size() );
     for( auto & x : r )
     {

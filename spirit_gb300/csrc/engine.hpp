@@ -25,6 +25,9 @@ struct SystemInput
     unsigned int stream           = 0;
 };
 
+template<typename R>
+struct StageArgs;
+
 // Host-side system descriptor of one system (spin_offset 0), as the engine builds it
 void fill_system_desc( SysDesc & d, const SystemInput & in );
 
@@ -161,6 +164,12 @@ private:
     void launch_step_t();
     template<typename R>
     void launch_probe_t();
+    template<typename R, int SOLVER, int STAGE>
+    void launch_stage( StageArgs<R> a, cudaStream_t st );
+    template<typename R>
+    void launch_stages_t( StageArgs<R> & a, bool with_ddi );
+    template<typename R>
+    void tune_stages_t();
     template<typename R>
     void gradient_t( int s, double * grad_aos, double * energy, double * terms, double * per_spin );
 
@@ -179,6 +188,7 @@ private:
     void * predB_[3] = { nullptr, nullptr, nullptr };
     void * aux1_[3]  = { nullptr, nullptr, nullptr };
     void * aux2_[3]  = { nullptr, nullptr, nullptr };
+    void * noise_[3] = { nullptr, nullptr, nullptr }; // thermal field of the current iteration
     void * field_[3] = { nullptr, nullptr, nullptr };
     double * d_stage_ = nullptr; // AoS double staging for transfers
     double * d_red_   = nullptr; // reduction scratch (per-term sums)
@@ -187,6 +197,12 @@ private:
     int * d_blkcount_ = nullptr;
     int n_blocks_     = 0;
     int threads_      = 256;
+    // block maps of the stage kernels for 1, 2, 4 spins per thread; spt_idx_ picks one (tuned)
+    int2 * d_sblkmap_[3]  = { nullptr, nullptr, nullptr };
+    int * d_sblkcount_[3] = { nullptr, nullptr, nullptr };
+    int n_sblocks_[3]     = { 0, 0, 0 };
+    int spt_idx_          = 0;
+    int tuned_solver_     = -1;
     bool any_ddi_     = false;
     DDIPlan ddi_;
     int solver_       = SOLVER_HEUN;
