@@ -29,6 +29,7 @@ enum KernelId : int
     KERNEL_PASS_B_INV,
     KERNEL_PASS_A_INV,
     KERNEL_END,
+    KERNEL_PASS_BC, // fused B, C, B'
     N_KERNEL_IDS
 };
 
@@ -184,6 +185,8 @@ struct FFTDesc
     float invT_f;            // 1 / (Ma Mb Mc)
     double invT_d;
     FastDiv div_Ma, div_Mh, div_Mb, div_Mc;
+    FastDiv div_Nb, div_Nc, div_nb;
+    FastDiv div_plane; // 3 nb Mb: elements of one c-row of the fused b/c pass
 };
 
 template<>

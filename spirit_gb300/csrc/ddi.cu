@@ -37,8 +37,10 @@ struct PassArgs
     // dense real input for the dipole precompute (pass A mode 1)
     const R * dense;
     int mode; // 0: spin convolution, 1: dense forward transform
-    int g;    // lines (pass B) / columns (pass C) per block
+    int g;    // lines (pass B) / columns (pass C) per block; lines per block of pass A / A'
     FastDiv div_g;
+    int ka_major; // W1 layout: 0 [row][b][ka] (split passes B, C, B'), 1 [ka][row][b] (fused pass BC)
+    FastDiv div_gq; // (g + 1) / 2: line pairs per block of pass A
 };
 
 template<typename R>
@@ -119,14 +121,34 @@ __global__ void pass_a( PassArgs<R> p )
     }
     __syncthreads();
     const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.radix[0], tw, false );
-    cplx<R> * W1      = p.W1 + f.spec_offset + ( (size_t)row * Bin + b0 ) * Mh;
-    for( int e = threadIdx.x; e < nl * Mh; e += blockDim.x )
+    if( !p.ka_major )
     {
-        const int li      = (int)fdiv( (unsigned)e, f.div_Mh ), k = e - li * Mh;
-        const cplx<R> * z = r + ( li >> 1 ) * ls;
-        const cplx<R> zk = z[k], zm = z[k == 0 ? 0 : Ma - k];
-        W1[e]            = ( li & 1 ) ? cplx<R>{ R( 0.5 ) * ( zk.y + zm.y ), R( -0.5 ) * ( zk.x - zm.x ) }
-                                      : cplx<R>{ R( 0.5 ) * ( zk.x + zm.x ), R( 0.5 ) * ( zk.y - zm.y ) };
+        cplx<R> * W1 = p.W1 + f.spec_offset + ( (size_t)row * Bin + b0 ) * Mh;
+        for( int e = threadIdx.x; e < nl * Mh; e += blockDim.x )
+        {
+            const int li      = (int)fdiv( (unsigned)e, f.div_Mh ), k = e - li * Mh;
+            const cplx<R> * z = r + ( li >> 1 ) * ls;
+            const cplx<R> zk = z[k], zm = z[k == 0 ? 0 : Ma - k];
+            W1[e] = ( li & 1 ) ? cplx<R>{ R( 0.5 ) * ( zk.y + zm.y ), R( -0.5 ) * ( zk.x - zm.x ) }
+                               : cplx<R>{ R( 0.5 ) * ( zk.x + zm.x ), R( 0.5 ) * ( zk.y - zm.y ) };
+        }
+    }
+    else
+    {
+        // [ka][row][b]: consecutive threads -> consecutive b of one ka
+        const int G     = p.g;
+        const int rows  = 3 * nb * Cin;
+        cplx<R> * W1    = p.W1 + f.spec_offset + (size_t)row * Bin + b0;
+        for( int e = threadIdx.x; e < G * Mh; e += blockDim.x )
+        {
+            const int k = (int)fdiv( (unsigned)e, p.div_g ), li = e - k * G;
+            if( li >= nl )
+                continue;
+            const cplx<R> * z = r + ( li >> 1 ) * ls;
+            const cplx<R> zk = z[k], zm = z[k == 0 ? 0 : Ma - k];
+            W1[(size_t)k * rows * Bin + li] = ( li & 1 ) ? cplx<R>{ R( 0.5 ) * ( zk.y + zm.y ), R( -0.5 ) * ( zk.x - zm.x ) }
+                                                         : cplx<R>{ R( 0.5 ) * ( zk.x + zm.x ), R( 0.5 ) * ( zk.y - zm.y ) };
+        }
     }
 }
 
@@ -282,6 +304,94 @@ __global__ void pass_c( PassArgs<R> p )
     }
 }
 
+// ------------------------------------------------------------------ fused pass BC
+// One block per (system, ka): the whole (c, b) plane of every component in shared memory,
+// layout [c][cb][kb] (c-row = 3 nb Mb elements), twice for the Stockham ping-pong:
+//   forward along b (lines c < Nc, cb), forward along c (lines cb, kb; rows c >= Nc are zero),
+//   tensor product with Dhat (fused layout [ka][pair][6][kc][kb]), inverse along c, inverse
+//   along b; W1 [ka][row][b] in and out (row = cb Nc + c).
+template<typename R>
+__global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
+{
+    extern __shared__ unsigned char smem_raw[];
+    const int4 blk = p.blocks[blockIdx.x];
+    const int s    = blk.x;
+    if( sys_inactive( p, s ) )
+        return;
+    const FFTDesc & f = p.fd[s];
+    const int Mb = f.M[1], Mc = f.M[2], nb = f.nb;
+    const int Nb = f.N[1], Nc = f.N[2];
+    const int ncb   = 3 * nb;
+    const int plane = ncb * Mb;
+    const int vol   = Mc * plane;
+    const int ka    = blk.y;
+    cplx<R> * twb   = reinterpret_cast<cplx<R> *>( smem_raw );
+    cplx<R> * twc   = twb + Mb;
+    cplx<R> * A     = twc + Mc;
+    cplx<R> * B     = A + vol;
+    load_tw( twb, p.tw + f.tw_offset[1], Mb );
+    load_tw( twc, p.tw + f.tw_offset[2], Mc );
+    for( int e = threadIdx.x; e < 2 * vol; e += blockDim.x )
+        A[e] = { 0, 0 };
+    __syncthreads();
+    const int nin    = ncb * Nc * Nb;
+    cplx<R> * W1     = p.W1 + f.spec_offset + (size_t)ka * nin;
+    for( int e = threadIdx.x; e < nin; e += blockDim.x )
+    {
+        const int row = (int)fdiv( (unsigned)e, f.div_Nb ), b = e - row * Nb;
+        const int cb  = (int)fdiv( (unsigned)row, f.div_Nc ), c = row - cb * Nc;
+        A[c * plane + cb * Mb + b] = W1[e];
+    }
+    __syncthreads();
+    const FastDiv none = { 1, 0, 0 };
+    cplx<R> * r = sfft<R, false>( A, B, Mb, Nc * ncb, none, Mb, 1, f.radix[1], twb, false );
+    cplx<R> * o = ( r == A ) ? B : A;
+    r           = sfft<R, true>( r, o, Mc, plane, f.div_plane, 1, plane, f.radix[2], twc, false );
+    o           = ( r == A ) ? B : A;
+    // tensor product H_b1 = sum_b2 D_b1b2 . S_b2 (FFT.hpp:42-49 mult3D rows: xx xy xz | xy yy yz | xz yz zz)
+    const int npair    = nb * nb;
+    const cplx<R> * Dh = p.Dhat + f.dhat_offset + (size_t)ka * npair * 6 * Mc * Mb;
+    for( int e = threadIdx.x; e < nb * Mc * Mb; e += blockDim.x )
+    {
+        const int rest = (int)fdiv( (unsigned)e, f.div_Mb ), kb = e - rest * Mb;
+        const int kc   = (int)fdiv( (unsigned)rest, f.div_nb ), b1 = rest - kc * nb;
+        const cplx<R> * S = r + kc * plane + kb;
+        cplx<R> acc[3]    = { { 0, 0 }, { 0, 0 }, { 0, 0 } };
+        for( int b2 = 0; b2 < nb; ++b2 )
+        {
+            const cplx<R> * D = Dh + ( (size_t)( b1 * nb + b2 ) * 6 * Mc + kc ) * Mb + kb;
+            cplx<R> d[6];
+#pragma unroll
+            for( int q = 0; q < 6; ++q )
+                d[q] = D[(size_t)q * Mc * Mb];
+            const cplx<R> sx = S[( b2 * 3 + 0 ) * Mb];
+            const cplx<R> sy = S[( b2 * 3 + 1 ) * Mb];
+            const cplx<R> sz = S[( b2 * 3 + 2 ) * Mb];
+            const int rw[3][3] = { { 0, 1, 2 }, { 1, 3, 4 }, { 2, 4, 5 } };
+#pragma unroll
+            for( int c3 = 0; c3 < 3; ++c3 )
+            {
+                const cplx<R> d1 = d[rw[c3][0]], d2 = d[rw[c3][1]], d3 = d[rw[c3][2]];
+                acc[c3].x += d1.x * sx.x + d2.x * sy.x + d3.x * sz.x - d1.y * sx.y - d2.y * sy.y - d3.y * sz.y;
+                acc[c3].y += d1.x * sx.y + d2.x * sy.y + d3.x * sz.y + d1.y * sx.x + d2.y * sy.x + d3.y * sz.x;
+            }
+        }
+#pragma unroll
+        for( int c3 = 0; c3 < 3; ++c3 )
+            o[kc * plane + ( b1 * 3 + c3 ) * Mb + kb] = acc[c3];
+    }
+    __syncthreads();
+    r = sfft<R, true>( o, ( o == A ) ? B : A, Mc, plane, f.div_plane, 1, plane, f.radix[2], twc, true );
+    o = ( r == A ) ? B : A;
+    r = sfft<R, false>( r, o, Mb, Nc * ncb, none, Mb, 1, f.radix[1], twb, true );
+    for( int e = threadIdx.x; e < nin; e += blockDim.x )
+    {
+        const int row = (int)fdiv( (unsigned)e, f.div_Nb ), b = e - row * Nb;
+        const int cb  = (int)fdiv( (unsigned)row, f.div_Nc ), c = row - cb * Nc;
+        W1[e]         = r[c * plane + cb * Mb + b];
+    }
+}
+
 // ------------------------------------------------------------------ pass A': C2R along a -> field
 // Two Hermitian half spectra X, Y go through one complex inverse transform of Z = X + i Y; the
 // real part is x, the imaginary part y.  The imaginary parts of X and Y at k = 0 and k = Ma/2
@@ -305,14 +415,32 @@ __global__ void pass_a_inv( PassArgs<R> p )
     cplx<R> * a   = tw + Ma;
     cplx<R> * b   = a + nq * ls;
     load_tw( tw, p.tw + f.tw_offset[0], Ma );
-    const cplx<R> * W1 = p.W1 + f.spec_offset + ( (size_t)row * Nb + b0 ) * Mh;
-    for( int e = threadIdx.x; e < nq * Ma; e += blockDim.x )
+    // element (line li, frequency kk) of W1 in either layout
+    const size_t lstride = p.ka_major ? 1 : (size_t)Mh;
+    const size_t kstride = p.ka_major ? (size_t)3 * nb * Nc * Nb : 1;
+    const cplx<R> * W1   = p.W1 + f.spec_offset + ( p.ka_major ? (size_t)row * Nb + b0 : ( (size_t)row * Nb + b0 ) * Mh );
+    // [row][b][ka]: consecutive threads take consecutive k of a line pair; [ka][row][b]:
+    // consecutive threads take consecutive line pairs of one k (contiguous b)
+    const int gq = p.ka_major ? ( p.g + 1 ) >> 1 : nq; // line pairs of a full block
+    for( int e = threadIdx.x; e < gq * Ma; e += blockDim.x )
     {
-        const int q = (int)fdiv( (unsigned)e, f.div_Ma ), k = e - q * Ma;
+        int q, k;
+        if( p.ka_major )
+        {
+            k = (int)fdiv( (unsigned)e, p.div_gq );
+            q = e - k * gq;
+            if( q >= nq )
+                continue;
+        }
+        else
+        {
+            q = (int)fdiv( (unsigned)e, f.div_Ma );
+            k = e - q * Ma;
+        }
         const bool hi = k >= Mh;
         const int kk  = hi ? Ma - k : k;
-        cplx<R> x     = W1[( 2 * q ) * Mh + kk];
-        cplx<R> y     = 2 * q + 1 < nl ? W1[( 2 * q + 1 ) * Mh + kk] : cplx<R>{ 0, 0 };
+        cplx<R> x     = W1[( 2 * q ) * lstride + kk * kstride];
+        cplx<R> y     = 2 * q + 1 < nl ? W1[( 2 * q + 1 ) * lstride + kk * kstride] : cplx<R>{ 0, 0 };
         if( hi )
         {
             x.y = -x.y;
@@ -346,7 +474,7 @@ __global__ void pass_a_inv( PassArgs<R> p )
 
 // ------------------------------------------------------------------ Dhat re-layout
 template<typename R, typename RS>
-__global__ void dhat_relayout( const cplx<R> * W2, cplx<RS> * Dhat, int Mh, int Mb, int Mc, int npair )
+__global__ void dhat_relayout( const cplx<R> * W2, cplx<RS> * Dhat, int Mh, int Mb, int Mc, int npair, int fused )
 {
     long long total = (long long)npair * 6 * Mc * Mb * Mh;
     for( long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
@@ -357,11 +485,28 @@ __global__ void dhat_relayout( const cplx<R> * W2, cplx<RS> * Dhat, int Mh, int 
         int kc = ( e / ( (long long)Mh * Mb ) ) % Mc;
         int pc = e / ( (long long)Mh * Mb * Mc ); // pair*6 + comp6
         cplx<R> v = W2[e];
-        Dhat[( ( (size_t)kb * Mh + ka ) * npair * 6 + pc ) * Mc + kc] = { (RS)v.x, (RS)v.y };
+        if( fused ) // [ka][pair*6 + comp6][kc][kb]
+            Dhat[( ( (size_t)ka * npair * 6 + pc ) * Mc + kc ) * Mb + kb] = { (RS)v.x, (RS)v.y };
+        else        // [kb*Mh + ka][pair*6 + comp6][kc]
+            Dhat[( ( (size_t)kb * Mh + ka ) * npair * 6 + pc ) * Mc + kc] = { (RS)v.x, (RS)v.y };
     }
 }
 
 // ================================================================== host side
+static size_t smem_bc( size_t elem, const FFTDesc & f )
+{
+    return elem * ( f.M[1] + f.M[2] + 2 * (size_t)f.M[2] * 3 * f.nb * f.M[1] );
+}
+
+// largest dynamic shared memory of one block on the current device
+static size_t smem_optin()
+{
+    int dev = 0, v = 0;
+    CUDA_CHECK( cudaGetDevice( &dev ) );
+    CUDA_CHECK( cudaDeviceGetAttribute( &v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev ) );
+    return (size_t)v;
+}
+
 static void factorize( int L, int * rad )
 {
     int n = 0;
@@ -435,6 +580,10 @@ void DDIPlan::build( const std::vector<DDISystem> & systems, bool fp64, const Sy
         f.div_Mh = make_fastdiv( f.Mh );
         f.div_Mb = make_fastdiv( f.M[1] );
         f.div_Mc = make_fastdiv( f.M[2] );
+        f.div_Nb    = make_fastdiv( f.N[1] );
+        f.div_Nc    = make_fastdiv( f.N[2] );
+        f.div_nb    = make_fastdiv( f.nb );
+        f.div_plane = make_fastdiv( 3 * f.nb * f.M[1] );
         for( int d = 0; d < 3; ++d )
         {
             f.tw_offset[d] = (long long)tw_host.size() / 2;
@@ -482,6 +631,10 @@ void DDIPlan::build( const std::vector<DDISystem> & systems, bool fp64, const Sy
     d_W1       = dalloc_bytes( std::max<long long>( spec, 1 ) * elem );
     d_W2       = dalloc_bytes( std::max<long long>( spec, 1 ) * elem );
     d_Dhat     = dalloc_bytes( std::max<long long>( dhat, 1 ) * elem );
+    // fused b/c pass when every system's (c, b) plane fits into one block's shared memory
+    fused = !fds.empty();
+    for( auto & f : fds )
+        fused = fused && smem_bc( elem, f ) <= smem_optin();
     build_block_tables( systems );
     compute_dhat( systems, d_sd, stream );
 }
@@ -501,6 +654,8 @@ static size_t smem_c( size_t elem, int Mc, int ncb, int g )
 }
 
 static constexpr size_t SMEM_MAX = 200 * 1024;
+
+
 
 static void upload_table( int4 *& dst, int & n, const std::vector<int4> & t )
 {
@@ -541,6 +696,16 @@ void DDIPlan::set_tiles( int nl_a, int g_b, int g_c )
     upload_table( d_blocks[0], n_blocks[0], ta );
     upload_table( d_blocks[1], n_blocks[1], tb );
     upload_table( d_blocks[2], n_blocks[2], tc );
+    std::vector<int4> tbc;
+    smem_bc_max = 0;
+    if( fused )
+        for( size_t k = 0; k < fd_host.size(); ++k )
+        {
+            for( int ka = 0; ka < fd_host[k].Mh; ++ka )
+                tbc.push_back( make_int4( sys_index[k], ka, 0, 0 ) );
+            smem_bc_max = std::max( smem_bc_max, smem_bc( elem, fd_host[k] ) );
+        }
+    upload_table( d_blocks[3], n_blocks[3], tbc );
     tile[0] = nl_a;
     tile[1] = g_b;
     tile[2] = g_c;
@@ -587,6 +752,7 @@ static void set_smem_limits()
     CUDA_CHECK( cudaFuncSetAttribute( pass_b<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024 ) );
     CUDA_CHECK( cudaFuncSetAttribute( pass_c<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024 ) );
     CUDA_CHECK( cudaFuncSetAttribute( pass_a_inv<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024 ) );
+    CUDA_CHECK( cudaFuncSetAttribute( pass_bc<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_optin() ) );
     done = true;
 }
 
@@ -755,10 +921,10 @@ void DDIPlan::compute_dhat( const std::vector<DDISystem> & systems, const SysDes
         // W2 now holds [row][kc][kb][ka]; re-layout into Dhat[kb][ka][row][kc]
         if( fp64 )
             dhat_relayout<double, double><<<1024, 256, 0, stream>>>(
-                dW2, (cplx<double> *)d_Dhat + f.dhat_offset, Mh, Mb, Mc, npair );
+                dW2, (cplx<double> *)d_Dhat + f.dhat_offset, Mh, Mb, Mc, npair, fused ? 1 : 0 );
         else
             dhat_relayout<double, float><<<1024, 256, 0, stream>>>(
-                dW2, (cplx<float> *)d_Dhat + f.dhat_offset, Mh, Mb, Mc, npair );
+                dW2, (cplx<float> *)d_Dhat + f.dhat_offset, Mh, Mb, Mc, npair, fused ? 1 : 0 );
         CUDA_CHECK( cudaGetLastError() );
         CUDA_CHECK( cudaStreamSynchronize( stream ) );
         dfree( d_dense );
@@ -773,10 +939,13 @@ void DDIPlan::compute_dhat( const std::vector<DDISystem> & systems, const SysDes
 template<typename R>
 void DDIPlan::launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const
 {
+    a.ka_major = fused ? 1 : 0;
     switch( k )
     {
     case 0:
         a.blocks = d_blocks[0];
+        a.g      = tile[0];
+        a.div_g  = make_fastdiv( tile[0] );
         pass_a<R><<<n_blocks[0], threads[0], max_smem_a, stream>>>( a );
         break;
     case 1:
@@ -792,8 +961,15 @@ void DDIPlan::launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const
         a.div_g  = make_fastdiv( tile[2] );
         pass_c<R><<<n_blocks[2], threads[2], max_smem_c, stream>>>( a );
         break;
+    case 5:
+        a.blocks = d_blocks[3];
+        pass_bc<R><<<n_blocks[3], threads_bc, smem_bc_max, stream>>>( a );
+        break;
     default:
         a.blocks = d_blocks[0];
+        a.g      = tile[0];
+        a.div_g  = make_fastdiv( tile[0] );
+        a.div_gq = make_fastdiv( ( tile[0] + 1 ) / 2 );
         pass_a_inv<R><<<n_blocks[0], threads[0], max_smem_a, stream>>>( a );
         break;
     }
@@ -850,7 +1026,10 @@ void DDIPlan::tune_t( const SysDesc * d_sd, const R * sx, const R * sy, const R 
         return ms;
     };
     // warm-up of the whole chain (first launches pay module loading)
-    timed( { 0, 1, 2, 3, 4 } );
+    if( fused )
+        timed( { 0, 5, 4 } );
+    else
+        timed( { 0, 1, 2, 3, 4 } );
     int best[3] = { tile[0], tile[1], tile[2] };
     int bthr[3] = { threads[0], threads[1], threads[2] };
     const int thread_opts[3] = { 64, 128, 256 };
@@ -877,6 +1056,23 @@ void DDIPlan::tune_t( const SysDesc * d_sd, const R * sx, const R * sy, const R 
         }
         threads[0] = bthr[0];
     }
+    if( fused )
+    {
+        float bt = 1e30f;
+        int bthr_bc = threads_bc;
+        for( int th : { 256, 512, 1024 } )
+        {
+            threads_bc = th;
+            float t    = timed( { 5 } );
+            if( t < bt )
+            {
+                bt      = t;
+                bthr_bc = th;
+            }
+        }
+        threads_bc = bthr_bc;
+    }
+    else
     {
         float bt = 1e30f;
         for( int g : { 1, 2, 3, 4, 5, 6, 8, 10, 12, 16, 24, 32 } )
@@ -898,6 +1094,7 @@ void DDIPlan::tune_t( const SysDesc * d_sd, const R * sx, const R * sy, const R 
         }
         threads[1] = bthr[1];
     }
+    if( !fused )
     {
         float bt = 1e30f;
         for( int g : { 1, 2, 3, 4, 5, 6, 8, 10, 12, 16 } )
@@ -961,12 +1158,23 @@ void DDIPlan::run_t( const SysDesc * d_sd, const SysRun * runs, const R * sx, co
             trace->push_back( { id, e } );
         }
     };
-    for( int k = 0; k < 5; ++k )
+    if( fused )
     {
-        static const int ids[5] = { KERNEL_PASS_A, KERNEL_PASS_B, KERNEL_PASS_C, KERNEL_PASS_B_INV, KERNEL_PASS_A_INV };
-        mark( ids[k] );
-        launch_pass<R>( k, a, stream );
+        static const int ks[3]  = { 0, 5, 4 };
+        static const int ids[3] = { KERNEL_PASS_A, KERNEL_PASS_BC, KERNEL_PASS_A_INV };
+        for( int q = 0; q < 3; ++q )
+        {
+            mark( ids[q] );
+            launch_pass<R>( ks[q], a, stream );
+        }
     }
+    else
+        for( int k = 0; k < 5; ++k )
+        {
+            static const int ids[5] = { KERNEL_PASS_A, KERNEL_PASS_B, KERNEL_PASS_C, KERNEL_PASS_B_INV, KERNEL_PASS_A_INV };
+            mark( ids[k] );
+            launch_pass<R>( k, a, stream );
+        }
     CUDA_CHECK( cudaGetLastError() );
 }
 

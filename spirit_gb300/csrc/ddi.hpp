@@ -52,10 +52,13 @@ public:
     void * d_W1    = nullptr;
     void * d_W2    = nullptr;
     void * d_Dhat  = nullptr;
-    int4 * d_blocks[5] = { nullptr, nullptr, nullptr, nullptr, nullptr };
+    int4 * d_blocks[5] = { nullptr, nullptr, nullptr, nullptr, nullptr }; // A, B, C, BC
     int n_blocks[5]    = { 0, 0, 0, 0, 0 };
     int tile[3]        = { 8, 8, 8 }; // lines per block of A/A', lines per block of B/B', columns per block of C
     int threads[3]     = { 256, 256, 256 }; // threads per block of A/A', B/B', C
+    bool fused         = false; // passes B, C, B' as one kernel per (system, ka) plane
+    int threads_bc     = 1024;
+    size_t smem_bc_max = 0;
     size_t max_smem_a = 0, max_smem_b = 0, max_smem_c = 0;
     long long spec_elems = 0;
     std::vector<FFTDesc> fd_host;

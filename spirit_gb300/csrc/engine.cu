@@ -1025,7 +1025,7 @@ void Engine::profile_steps( int n, void * flush_buf, size_t flush_bytes, void * 
 int Engine::kernels_per_step() const
 {
     int stages = solver_ == SOLVER_RK4 ? 4 : 2;
-    return stages * ( 1 + ( any_ddi_ ? 5 : 0 ) );
+    return stages * ( 1 + ( any_ddi_ ? ( ddi_.fused ? 3 : 5 ) : 0 ) );
 }
 
 void Engine::llg_start( int solver, const std::vector<int> & n_iterations )

@@ -301,6 +301,204 @@ __device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int ls, int nl,
     return a;
 }
 
+// ------------------------------------------------------------------ strided line transforms
+// Stockham FFT of nl lines in shared memory whose element t of line l sits at l*ls + t*es.
+// LINE_FAST: consecutive threads take consecutive lines (for ls = 1, es > 1: a warp then touches
+// consecutive words); otherwise consecutive threads take consecutive butterflies of one line.
+// dnl = FastDiv of nl (used by LINE_FAST).  Returns the buffer that holds the result; must be
+// called by all threads of the block.
+template<typename R, int L, bool LINE_FAST>
+__device__ __forceinline__ cplx<R> * sfft_const( cplx<R> * a, cplx<R> * b, int nl, const FastDiv & dnl, int ls,
+                                                int es, const cplx<R> * tw, bool inverse )
+{
+    constexpr int lgL = ( L <= 1 ) ? 0 : ( L <= 2 ) ? 1 : ( L <= 4 ) ? 2 : ( L <= 8 ) ? 3 : ( L <= 16 ) ? 4
+                        : ( L <= 32 ) ? 5 : ( L <= 64 ) ? 6 : ( L <= 128 ) ? 7 : ( L <= 256 ) ? 8 : ( L <= 512 ) ? 9 : 10;
+#pragma unroll
+    for( int lgNs = 0; lgNs < lgL; lgNs += 2 )
+    {
+        const int lgR  = ( lgL - lgNs >= 2 ) ? 2 : 1;
+        const int lgLR = lgL - lgR;
+        const int LR   = 1 << lgLR;
+        const int Ns   = 1 << lgNs;
+        const int lgSp = lgL - lgNs - lgR;
+        for( int idx = threadIdx.x; idx < ( nl << lgLR ); idx += blockDim.x )
+        {
+            int line, j;
+            if( LINE_FAST )
+            {
+                j    = (int)fdiv( (unsigned)idx, dnl );
+                line = idx - j * nl;
+            }
+            else
+            {
+                line = idx >> lgLR;
+                j    = idx & ( LR - 1 );
+            }
+            const cplx<R> * src = a + line * ls;
+            cplx<R> * dst       = b + line * ls;
+            const int k         = j & ( Ns - 1 );
+            const int d0        = ( ( j >> lgNs ) << ( lgNs + lgR ) ) + k;
+            if( lgR == 1 )
+            {
+                cplx<R> v0 = src[j * es];
+                cplx<R> w  = tw[k << lgSp];
+                if( inverse )
+                    w = cconj( w );
+                cplx<R> v1          = cmul( src[( j + LR ) * es], w );
+                dst[d0 * es]        = { v0.x + v1.x, v0.y + v1.y };
+                dst[( d0 + Ns ) * es] = { v0.x - v1.x, v0.y - v1.y };
+            }
+            else
+            {
+                cplx<R> v0 = src[j * es];
+                cplx<R> w1 = tw[k << lgSp], w2 = tw[( 2 * k ) << lgSp], w3 = tw[( 3 * k ) << lgSp];
+                if( inverse )
+                {
+                    w1 = cconj( w1 );
+                    w2 = cconj( w2 );
+                    w3 = cconj( w3 );
+                }
+                cplx<R> v1   = cmul( src[( j + LR ) * es], w1 );
+                cplx<R> v2   = cmul( src[( j + 2 * LR ) * es], w2 );
+                cplx<R> v3   = cmul( src[( j + 3 * LR ) * es], w3 );
+                cplx<R> s02  = { v0.x + v2.x, v0.y + v2.y };
+                cplx<R> d02  = { v0.x - v2.x, v0.y - v2.y };
+                cplx<R> s13  = { v1.x + v3.x, v1.y + v3.y };
+                cplx<R> d13  = { v1.x - v3.x, v1.y - v3.y };
+                cplx<R> id13 = inverse ? cplx<R>{ -d13.y, d13.x } : cplx<R>{ d13.y, -d13.x };
+                dst[d0 * es]              = { s02.x + s13.x, s02.y + s13.y };
+                dst[( d0 + Ns ) * es]     = { d02.x + id13.x, d02.y + id13.y };
+                dst[( d0 + 2 * Ns ) * es] = { s02.x - s13.x, s02.y - s13.y };
+                dst[( d0 + 3 * Ns ) * es] = { d02.x - id13.x, d02.y - id13.y };
+            }
+        }
+        __syncthreads();
+        cplx<R> * t = a;
+        a           = b;
+        b           = t;
+        if( lgR == 1 )
+            break; // the radix-2 stage is the last one
+    }
+    return a;
+}
+
+// Mixed-radix (any L) strided Stockham: radix <= 8 butterflies, larger prime factors one output
+// per thread.  Consecutive threads take consecutive butterflies of a line.
+template<typename R>
+__device__ cplx<R> * sfft_generic( cplx<R> * a, cplx<R> * b, int L, int nl, int ls, int es, const int * rad,
+                                  const cplx<R> * tw, bool inverse )
+{
+    int Ns = 1;
+    for( int s = 0; s < 12 && rad[s] > 0; ++s )
+    {
+        const int Rr   = rad[s];
+        const int LR   = L / Rr;
+        const int span = L / ( Ns * Rr );
+        if( Rr <= 8 )
+        {
+            for( int idx = threadIdx.x; idx < nl * LR; idx += blockDim.x )
+            {
+                const int line      = idx / LR;
+                const int j         = idx - line * LR;
+                const cplx<R> * src = a + line * ls;
+                cplx<R> * dst       = b + line * ls;
+                const int k         = j % Ns;
+                cplx<R> v[8];
+#pragma unroll
+                for( int r = 0; r < 8; ++r )
+                {
+                    if( r < Rr )
+                    {
+                        cplx<R> w = tw[r * k * span];
+                        if( inverse )
+                            w = cconj( w );
+                        v[r] = r == 0 ? src[j * es] : cmul( src[( j + r * LR ) * es], w );
+                    }
+                }
+                const int d0 = ( j / Ns ) * Ns * Rr + k;
+                for( int m = 0; m < Rr; ++m )
+                {
+                    cplx<R> acc = v[0];
+                    for( int r = 1; r < Rr; ++r )
+                    {
+                        cplx<R> w = tw[( ( r * m ) % Rr ) * LR];
+                        if( inverse )
+                            w = cconj( w );
+                        cplx<R> t = cmul( v[r], w );
+                        acc.x += t.x;
+                        acc.y += t.y;
+                    }
+                    dst[( d0 + m * Ns ) * es] = acc;
+                }
+            }
+        }
+        else
+        {
+            for( int o = threadIdx.x; o < nl * L; o += blockDim.x )
+            {
+                const int line      = o / L;
+                const int q         = o - line * L;
+                const cplx<R> * src = a + line * ls;
+                const int k         = q % Ns;
+                const int m         = ( q / Ns ) % Rr;
+                const int jhi       = q / ( Ns * Rr );
+                const int j         = jhi * Ns + k;
+                cplx<R> acc         = { 0, 0 };
+                for( int r = 0; r < Rr; ++r )
+                {
+                    const int t = ( r * k * span + ( ( r * m ) % Rr ) * LR ) % L;
+                    cplx<R> w   = tw[t];
+                    if( inverse )
+                        w = cconj( w );
+                    const cplx<R> p = cmul( src[( j + r * LR ) * es], w );
+                    acc.x += p.x;
+                    acc.y += p.y;
+                }
+                b[line * ls + q * es] = acc;
+            }
+        }
+        __syncthreads();
+        cplx<R> * t = a;
+        a           = b;
+        b           = t;
+        Ns *= Rr;
+    }
+    return a;
+}
+
+template<typename R, bool LINE_FAST>
+__device__ cplx<R> * sfft( cplx<R> * a, cplx<R> * b, int L, int nl, const FastDiv & dnl, int ls, int es,
+                          const int * rad, const cplx<R> * tw, bool inverse )
+{
+    switch( L )
+    {
+    case 1:
+        return a;
+    case 2:
+        return sfft_const<R, 2, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+    case 4:
+        return sfft_const<R, 4, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+    case 8:
+        return sfft_const<R, 8, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+    case 16:
+        return sfft_const<R, 16, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+    case 32:
+        return sfft_const<R, 32, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+    case 64:
+        return sfft_const<R, 64, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+    case 128:
+        return sfft_const<R, 128, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+    case 256:
+        return sfft_const<R, 256, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+    case 512:
+        return sfft_const<R, 512, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+    case 1024:
+        return sfft_const<R, 1024, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+    default:
+        return sfft_generic<R>( a, b, L, nl, ls, es, rad, tw, inverse );
+    }
+}
+
 // shared-memory line stride for lines of length L
 __host__ __device__ inline int line_stride( int L )
 {
