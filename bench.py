@@ -144,6 +144,20 @@ def dist_env():
     return rank, world, local
 
 
+def reduce_max(v, world):
+    """Max over the ranks of one number (the timed region's milliseconds): every rank runs its own
+    replica, the slowest one sets the job time."""
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def cpu_baseline(seconds=12.0):
     """The oracle (CPU FP64 restatement of the reference path, OpenMP over all host cores) on a
     bounded sample of the same workload: as many Heun steps as fit in ~`seconds`."""
@@ -300,6 +314,92 @@ def run_batched_vs_plain(steps, warmup, plain=True, check=True):
     }
 
 
+C3_SPEC = dict(bravais="hex2d60", n_cells=[96, 96, 1], lattice_constant=1.0, mu_s=[2.0], bc=[1, 1, 0],
+               field=(1.5, (0, 0, 1)), anisotropy=(0.08, (0, 0, 1)), jij=[1.0], dij=[0.35], dm_chirality=2,
+               llg=dict(dt=1e-3, damping=0.3, temperature=0.0),
+               gneb=dict(spring_constant=1.0, force_convergence=1e-6))
+C3_IMAGES = 32
+
+
+def neel_skyrmion(pos, center, radius=8.0, width=2.0, sign=1.0):
+    """Neel skyrmion with the tanh profile theta(rho) = pi/2 (1 - tanh((rho - R) / w)), core down at
+    `center`; sign picks the radial sense of the in-plane component."""
+    d = pos[:, :2] - np.asarray(center)[:2]
+    rho = np.hypot(d[:, 0], d[:, 1])
+    th = 0.5 * np.pi * (1.0 - np.tanh((rho - radius) / width))
+    phi = np.arctan2(d[:, 1], d[:, 0])
+    return np.stack([sign * np.sin(th) * np.cos(phi), sign * np.sin(th) * np.sin(phi), np.cos(th)], axis=1)
+
+
+def run_gneb(iters_cap=150000):
+    """Batched GNEB: 32 images of a 96x96 triangular lattice between a relaxed Neel skyrmion
+    (radius 8 sites) and the ferromagnet (geodesic interpolation), spring 1, VP; 2000 plain
+    iterations, then climbing / falling images set automatically and iterations until the max
+    torque is below 1e-6 meV (or the cap).  FP32 forces, FP64 energies."""
+    from oracle.oracle import OracleSystem
+    from spirit_gb300 import chain, geometry, simulation, state, system, transition
+    from spirit_gb300.configs import write_config
+    import spirit_gb300.parameters.gneb as gneb
+    import spirit_gb300.parameters.llg as llg
+
+    p = state.setup(write_config(C3_SPEC, os.path.join(tempfile.mkdtemp(), "c3.cfg")), True)
+    simulation.set_precision(p, 32)
+    pos = np.array(geometry.get_positions(p))
+    center = 0.5 * (pos.min(axis=0) + pos.max(axis=0))
+    best = None
+    for sign in (1.0, -1.0):
+        system.get_spin_directions(p)[:] = neel_skyrmion(pos, center, sign=sign)
+        e = system.get_energy_fp64(p)
+        if best is None or e < best[0]:
+            best = (e, sign)
+    system.get_spin_directions(p)[:] = neel_skyrmion(pos, center, sign=best[1])
+    llg.set_direct_minimization(p, True)
+    llg.set_convergence(p, 1e-6)
+    simulation.start(p, simulation.METHOD_LLG, simulation.SOLVER_VP, 20000)
+    sk = np.array(system.get_spin_directions(p))
+    nos = sk.shape[0]
+    chain.image_to_clipboard(p)
+    for _ in range(1, C3_IMAGES):
+        chain.insert_image_after(p)
+    system.get_spin_directions(p, 0)[:] = sk
+    fm = np.zeros_like(sk)
+    fm[:, 2] = 1.0
+    system.get_spin_directions(p, C3_IMAGES - 1)[:] = fm
+    transition.homogeneous(p, 0, C3_IMAGES - 1)
+    gneb.set_convergence(p, 1e-6)
+    gneb.set_spring_constant(p, 1.0)
+    chain0 = np.array([np.array(system.get_spin_directions(p, i)) for i in range(C3_IMAGES)])
+    t0 = time.perf_counter()
+    info1 = simulation.start(p, simulation.METHOD_GNEB, simulation.SOLVER_VP, 2000)
+    gneb.set_image_type_automatically(p)
+    info2 = simulation.start(p, simulation.METHOD_GNEB, simulation.SOLVER_VP, iters_cap)
+    t2 = time.perf_counter()
+    mt = float(info2.max_torque)
+    E = np.array([system.get_energy_fp64(p, i) for i in range(C3_IMAGES)])
+    state.delete(p)
+    n_it = int(info1.total_iterations) + int(info2.total_iterations)
+    spins = C3_IMAGES * nos
+    # CPU: the oracle's GNEB iteration (FP64, OpenMP) on the same chain, a bounded sample
+    o = OracleSystem(C3_SPEC)
+    n_cpu = 3
+    c0 = time.perf_counter()
+    o.gneb(chain0, n_cpu, spring_constant=1.0, force_convergence=1e-6, dt=1e-3)
+    cpu_s = time.perf_counter() - c0
+    return {
+        "workload": "GNEB, 32 images of a periodic 96x96 triangular lattice (J=1, Neel D=0.35, K=0.08 meV, "
+                    "B=1.5 T), relaxed Neel skyrmion (R=8 sites, tanh profile) to ferromagnet, spring 1, VP, "
+                    "climbing image after 2000 iterations, convergence 1e-6 meV; FP32 forces, FP64 energies",
+        "n_images": C3_IMAGES, "spins_per_image": nos,
+        "iterations": n_it, "converged": bool(mt < 1e-6), "max_torque": mt,
+        "wall_s": t2 - t0, "ms_per_iteration": 1000.0 * (t2 - t0) / n_it,
+        "value": spins * n_it / (t2 - t0), "unit": "spin-updates/s",
+        "barrier_meV": float(E.max() - E[0]), "saddle_image": int(E.argmax()),
+        "timing": "wall clock of the two Simulation_GNEB_Start calls (host checks between device chunks included)",
+        "cpu_baseline": {"value": spins * n_cpu / cpu_s, "unit": "spin-updates/s", "cores": os.cpu_count(),
+                         "kind": "port", "sample": "%d GNEB iterations of the same 32-image chain (FP64, OpenMP)" % n_cpu},
+    }
+
+
 def run_gb300(args):
     import torch
 
@@ -353,11 +453,7 @@ def run_gb300(args):
             e1[k].record(stream)
         stream.synchronize()
     torch.cuda.synchronize()
-    ms = sum(a.elapsed_time(b) for a, b in zip(e0, e1))
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_max(sum(a.elapsed_time(b) for a, b in zip(e0, e1)), world)
     n_kernels = kps(p, -1, -1)
     value = NOS * args.steps * world / (ms / 1000.0)
     # --- per-kernel durations (CUDA events between launches, L2 flushed before every step)
@@ -391,6 +487,7 @@ def run_gb300(args):
     simulation.stop(p)
     state.delete(p)
     batched = run_batched_vs_plain(max(20, args.steps), max(3, args.warmup)) if args.batched else None
+    gneb_line = run_gneb() if args.gneb and rank == 0 else None
     if rank != 0:
         return
     cpu = cpu_baseline() if world == 1 else None
@@ -410,6 +507,8 @@ def run_gb300(args):
     }
     if batched is not None:
         line["batched"] = batched
+    if gneb_line is not None:
+        line["gneb"] = gneb_line
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -423,9 +522,18 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-batched", dest="batched", action="store_false",
                     help="skip the 256-system batched-vs-plain measurement")
+    ap.add_argument("--no-gneb", dest="gneb", action="store_false",
+                    help="skip the 32-image GNEB measurement")
+    ap.add_argument("--only-gneb", action="store_true", help="run and print only the GNEB measurement")
     ap.add_argument("--only-batched", action="store_true",
                     help="run and print only the 256-system batched-vs-plain measurement (profiling)")
     args = ap.parse_args()
+    if args.only_gneb:
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps(run_gneb()))
+        return
     if args.only_batched:
         import torch
 
