@@ -241,6 +241,21 @@ void Simulation_LLG_Start_Batched( State ** states, int n_states, int solver_typ
  * into the host buffers and ends the run. */
 void Simulation_LLG_Batched_Launch_Steps( State ** states, int n_states, int solver_type, int n_steps );
 void Simulation_LLG_Batched_Finish( State ** states, int n_states );
+/* EXTENSION: adjoint of a T = 0 RK4 LLG trajectory of the image (the reference has none).
+ * params = (J, D, K [meV], B [T], alpha) replace the configured first-shell exchange, first-shell
+ * DMI, anisotropy and field magnitudes (other shells / basis atoms scale with them, the field
+ * direction stays) and the damping; NULL keeps the configured values.  Runs n_steps from the
+ * image's spins; returns loss = mean_i |s_i(T) - target_i|^2 (FP64) and writes its gradient with
+ * respect to the initial spins (grad_s0, AoS [nos][3], may be NULL) and to params
+ * (grad_params[5], may be NULL); final_spins (AoS, may be NULL) receives s(T).  States are kept
+ * every `checkpoint` steps and each segment is recomputed once in the backward pass.  Device
+ * arithmetic follows Simulation_Set_Precision. */
+double Simulation_LLG_Adjoint( State * state, const double * params, int n_steps, int checkpoint,
+                               const double * target, double * grad_s0, double * grad_params, double * final_spins,
+                               int idx_image, int idx_chain );
+/* EXTENSION: the loss of the same trajectory without gradients (finite differences, timing) */
+double Simulation_LLG_Loss( State * state, const double * params, int n_steps, const double * target,
+                            double * final_spins, int idx_image, int idx_chain );
 /* EXTENSION: device arithmetic of the step loop: 32 (FP32 bulk, default) or 64 */
 void Simulation_Set_Precision( State * state, int bits );
 int Simulation_Get_Precision( State * state );

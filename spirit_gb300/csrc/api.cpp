@@ -6,6 +6,7 @@
 // (core/src/utility/Exception.cpp:70-110); unlike the reference, a CUDA error does not
 // terminate the process -- the call logs, returns its default value, and the library stays
 // usable.
+#include "adjoint.hpp"
 #include "config.hpp"
 #include "gneb.hpp"
 #include "state.hpp"
@@ -228,6 +229,93 @@ void geometry_changed( State * st )
         refresh_positions( *img );
         img->touch();
     }
+}
+
+} // namespace
+
+// adjoint driver behind Simulation_LLG_Adjoint / Simulation_LLG_Loss
+namespace
+{
+
+// first-shell / reference value of a coupling family (0 when absent)
+double first_of( const std::vector<double> & shells, const std::vector<double> & explicit_values, bool from_pairs )
+{
+    const auto & v = from_pairs ? explicit_values : shells;
+    return v.empty() ? 0.0 : v[0];
+}
+
+double run_adjoint( State * state, const double * params, int n_steps, int checkpoint, const double * target,
+                    double * grad_s0, double * grad_params, double * final_spins, int idx_image, int idx_chain,
+                    bool gradients )
+{
+    auto I            = from_indices( state, idx_image, idx_chain );
+    const Image & img = *I.img;
+    if( !target )
+        throw std::runtime_error( "target spins are required" );
+    const HamiltonianParams & h0 = img.ham;
+    const double J0 = first_of( h0.jij, h0.ex_J_in, h0.from_pairs );
+    const double D0 = first_of( h0.dij, h0.dmi_D_in, h0.from_pairs );
+    const double K0 = h0.aniso_K.empty() ? 0.0 : h0.aniso_K[0];
+    const double Jv = params ? params[0] : J0, Dv = params ? params[1] : D0, Kv = params ? params[2] : K0;
+    const double Bv = params ? params[3] : h0.B, av = params ? params[4] : img.llg.damping;
+    auto scaled = []( double v, double ref ) {
+        if( ref == 0.0 && v != 0.0 )
+            throw std::runtime_error( "a coupling absent from the configuration cannot be set by the adjoint parameters" );
+        return ref == 0.0 ? 0.0 : v / ref;
+    };
+    HamiltonianParams h = h0;
+    const double sJ = scaled( Jv, J0 ), sD = scaled( Dv, D0 ), sK = scaled( Kv, K0 );
+    for( auto & x : h.ex_J )
+        x *= sJ;
+    for( auto & x : h.dmi_D )
+        x *= sD;
+    for( auto & x : h.aniso_K )
+        x *= sK;
+    h.B = Bv;
+    // unit couplings: d/dJ of every exchange pair, d/dD of every DMI vector (same merged pair order)
+    HamiltonianParams hJ = h0, hD = h0;
+    for( size_t k = 0; k < hJ.ex_J.size(); ++k )
+        hJ.ex_J[k] = J0 != 0.0 ? h0.ex_J[k] / J0 : 0.0;
+    for( auto & x : hJ.dmi_D )
+        x = 0.0;
+    for( auto & x : hD.ex_J )
+        x = 0.0;
+    for( size_t k = 0; k < hD.dmi_D.size(); ++k )
+        hD.dmi_D[k] = D0 != 0.0 ? h0.dmi_D[k] / D0 : 0.0;
+    SystemInput in;
+    in.geom                = img.geom.get();
+    in.ham                 = &h;
+    in.dt                  = img.llg.dt;
+    in.damping             = av;
+    in.temperature         = img.llg.temperature;
+    in.direct_minimization = img.llg.direct_minimization;
+    in.force_convergence   = img.llg.force_convergence;
+    AdjointInput A;
+    A.s0         = img.spins.data();
+    A.target     = target;
+    A.n_steps    = n_steps;
+    A.checkpoint = checkpoint > 0 ? checkpoint : 100;
+    A.gradients  = gradients;
+    SystemInput iJ = in, iD = in;
+    iJ.ham         = &hJ;
+    iD.ham         = &hD;
+    fill_system_desc( A.unit_J, iJ );
+    fill_system_desc( A.unit_D, iD );
+    for( size_t k = 0; k < h0.aniso_K.size() && k < (size_t)MAX_BASIS; ++k )
+        A.unit_K[k] = K0 != 0.0 ? h0.aniso_K[k] / K0 : 0.0;
+    for( int e = 0; e < 3; ++e )
+        A.unit_B[e] = C_MU_B * h.B_normal[e];
+    Engine E( std::vector<SystemInput>{ in }, state->precision == 64 );
+    if( state->stream )
+        E.set_stream( (cudaStream_t)state->stream );
+    AdjointOutput O;
+    O.grad_s0     = grad_s0;
+    O.final_spins = final_spins;
+    const double loss = adjoint_run( E, A, O, state->precision == 64 );
+    if( grad_params )
+        for( int q = 0; q < 5; ++q )
+            grad_params[q] = O.grad_params[q];
+    return loss;
 }
 
 } // namespace
@@ -2190,6 +2278,46 @@ void Simulation_LLG_Batched_Finish( State ** states, int n_states ) noexcept
     catch( ... )
     {
         handle( first, "Simulation_LLG_Batched_Finish" );
+    }
+}
+
+// ---------------------------------------------------------------- adjoint (no reference counterpart)
+
+// Adjoint of a T = 0 RK4 LLG trajectory of the image: n_steps from the image's spins with the
+// parameters params = (J, D, K [meV], B [T], alpha) replacing the configured first-shell exchange,
+// first-shell DMI, anisotropy and field magnitudes (all shells / basis atoms scaled with them; the
+// field direction stays) and the damping (params NULL: the configured values).  Returns the loss
+// mean_i |s_i(T) - target_i|^2 (FP64); grad_s0 (AoS [nos][3]) and grad_params[5] receive its
+// gradient; final_spins (optional) s(T).  checkpoint: steps between stored states.
+double Simulation_LLG_Adjoint( State * state, const double * params, int n_steps, int checkpoint,
+                               const double * target, double * grad_s0, double * grad_params, double * final_spins,
+                               int idx_image, int idx_chain ) noexcept
+{
+    try
+    {
+        return run_adjoint( state, params, n_steps, checkpoint, target, grad_s0, grad_params, final_spins, idx_image,
+                            idx_chain, true );
+    }
+    catch( ... )
+    {
+        handle( state, "Simulation_LLG_Adjoint" );
+        return 0;
+    }
+}
+
+// The loss of the same trajectory without gradients (finite differences, forward timing).
+double Simulation_LLG_Loss( State * state, const double * params, int n_steps, const double * target,
+                            double * final_spins, int idx_image, int idx_chain ) noexcept
+{
+    try
+    {
+        return run_adjoint( state, params, n_steps, 1 << 30, target, nullptr, nullptr, final_spins, idx_image,
+                            idx_chain, false );
+    }
+    catch( ... )
+    {
+        handle( state, "Simulation_LLG_Loss" );
+        return 0;
     }
 }
 
