@@ -400,6 +400,51 @@ def run_gneb(iters_cap=150000):
     }
 
 
+C5_SPEC = dict(bravais="sc", n_cells=[128, 128, 1], lattice_constant=1.0, mu_s=[2.0], bc=[0, 0, 0],
+               field=(0.8, (0, 0, 1)), anisotropy=(0.1, (0, 0, 1)), jij=[1.0], dij=[0.3], dm_chirality=2,
+               ddi=dict(method="fft", n_periodic_images=[0, 0, 0], radius=0.0, pb_zero_padding=1),
+               llg=dict(dt=1e-3, damping=0.3, temperature=0.0))
+
+
+def run_adjoint(n_steps=2000, checkpoint=100):
+    """Adjoint workload: 128x128 open square lattice with padded dipolar FFT (256x256), RK4
+    dt=1e-3 ps, 2000 steps, loss = mean |s(T) - target|^2 against a seeded target; gradient with
+    respect to s0 and (J, D, K, B_z, alpha) by the hand-written adjoint, checkpoint every 100 steps.
+    Forward and adjoint wall times exclude the shared set-up (measured as a 0-step call)."""
+    from oracle.oracle import random_spins
+    from spirit_gb300 import adjoint, simulation, state, system
+    from spirit_gb300.configs import write_config
+
+    p = state.setup(write_config(C5_SPEC, os.path.join(tempfile.mkdtemp(), "c5.cfg")), True)
+    simulation.set_precision(p, 32)
+    nos = 128 * 128
+    system.get_spin_directions(p)[:] = random_spins(nos, 55)
+    tgt = random_spins(nos, 56)
+    prm = np.array([1.0, 0.3, 0.1, 0.8, 0.3])
+    adjoint.llg_loss(p, tgt, 2, prm)  # warm-up (module loading)
+    t0 = time.perf_counter()
+    adjoint.llg_loss(p, tgt, 0, prm)
+    setup_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss_f, _ = adjoint.llg_loss(p, tgt, n_steps, prm)
+    fwd_s = time.perf_counter() - t0 - setup_s
+    t0 = time.perf_counter()
+    loss_a, g0, gp, _ = adjoint.llg_adjoint(p, tgt, n_steps, checkpoint, prm)
+    adj_s = time.perf_counter() - t0 - setup_s
+    state.delete(p)
+    return {
+        "workload": "adjoint of RK4 LLG: 128x128 open SC 2D, DDI FFT padded 256x256, J=1, D=0.3, K=0.1 meV, "
+                    "B=0.8 T, alpha=0.3, dt=1e-3 ps, %d steps, checkpoint %d; FP32 forward and adjoint, FP64 loss"
+                    % (n_steps, checkpoint),
+        "n_spins": nos, "steps": n_steps, "forward_s": fwd_s, "adjoint_s": adj_s,
+        "adjoint_over_forward": adj_s / fwd_s,
+        "forward_value": nos * n_steps / fwd_s, "unit": "spin-updates/s", "setup_s": setup_s,
+        "loss": loss_a, "loss_forward_only": loss_f,
+        "grad_params": {k: float(v) for k, v in zip(adjoint.PARAMS, gp)},
+        "timing": "wall clock of Simulation_LLG_Loss / Simulation_LLG_Adjoint minus a 0-step call (engine set-up)",
+    }
+
+
 def run_gb300(args):
     import torch
 
@@ -488,6 +533,7 @@ def run_gb300(args):
     state.delete(p)
     batched = run_batched_vs_plain(max(20, args.steps), max(3, args.warmup)) if args.batched else None
     gneb_line = run_gneb() if args.gneb and rank == 0 else None
+    adj_line = run_adjoint() if args.adjoint and rank == 0 else None
     if rank != 0:
         return
     cpu = cpu_baseline() if world == 1 else None
@@ -509,6 +555,8 @@ def run_gb300(args):
         line["batched"] = batched
     if gneb_line is not None:
         line["gneb"] = gneb_line
+    if adj_line is not None:
+        line["adjoint"] = adj_line
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -525,9 +573,17 @@ def main():
     ap.add_argument("--no-gneb", dest="gneb", action="store_false",
                     help="skip the 32-image GNEB measurement")
     ap.add_argument("--only-gneb", action="store_true", help="run and print only the GNEB measurement")
+    ap.add_argument("--no-adjoint", dest="adjoint", action="store_false", help="skip the adjoint measurement")
+    ap.add_argument("--only-adjoint", action="store_true", help="run and print only the adjoint measurement")
     ap.add_argument("--only-batched", action="store_true",
                     help="run and print only the 256-system batched-vs-plain measurement (profiling)")
     args = ap.parse_args()
+    if args.only_adjoint:
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps(run_adjoint()))
+        return
     if args.only_gneb:
         import torch
 

@@ -61,7 +61,7 @@ struct AdjArgs
     SoA3<R> lam_next; // dLoss/ds_{n+1}
     SoA3<R> lam_s;    // dLoss/ds_n (accumulated)
     SoA3<R> lam_k[4];
-    SoA3<R> lam_Fo;
+    SoA3<R> lam_Fo[2]; // stage m uses lam_Fo[m % 2] (the next stage's is written while neighbours read this)
     SoA3<R> lam_c;
     double * pgrad; // [5][n_blocks] per-block partial parameter gradients
     int n_blocks;
@@ -173,23 +173,6 @@ __global__ void __launch_bounds__( 256 ) adj_fwd( AdjArgs<R> A )
     }
 }
 
-// ------------------------------------------------------------------ backward: the final normalisation
-template<typename R>
-__global__ void __launch_bounds__( 256 ) adj_final( AdjArgs<R> A )
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if( i >= A.sd->nos )
-        return;
-    const long long gi = A.sd->spin_offset + i;
-    const V3<R> la     = jn_t( A.acc.ld( gi ), A.lam_next.ld( gi ) );
-    const R w6 = R( 1.0 / 6.0 ), w3 = R( 1.0 / 3.0 );
-    A.lam_s.st( gi, la );
-    A.lam_k[3].st( gi, scale( la, w6 ) );
-    A.lam_k[2].st( gi, scale( la, w3 ) );
-    A.lam_k[1].st( gi, scale( la, w3 ) );
-    A.lam_k[0].st( gi, scale( la, w6 ) );
-}
-
 // per-block sums of up to 5 values into pgrad[q * n_blocks + blockIdx.x] (deterministic order)
 template<typename R>
 __device__ __forceinline__ void block_accumulate( const AdjArgs<R> & A, const R * v, int q0, int nq, double * sh )
@@ -203,10 +186,40 @@ __device__ __forceinline__ void block_accumulate( const AdjArgs<R> & A, const R 
     }
 }
 
-// ------------------------------------------------------------------ backward stage M, part 1
-// lam_k -> lam_Fo (for the transposed field), the local part of lam_c, dLoss/dalpha
-template<typename R, int M>
-__global__ void __launch_bounds__( 256 ) adj_k( AdjArgs<R> A )
+// Local part of the adjoint of stage m for one spin: from lam_k(m) to lam_Fo(m) (input of the
+// transposed field, stored in lam_Fo[m % 2]) and the local part of lam_c(m) (stored); returns the
+// spin's dLoss/dalpha contribution.
+template<typename R>
+__device__ __forceinline__ R stage_local( const AdjArgs<R> & A, const SysConst<R> & C, int m, long long gi, int ib,
+                                          V3<R> lk )
+{
+    const V3<R> cm  = A.c[m - 1].ld( gi );
+    const V3<R> fm  = A.f[m - 1].ld( gi );
+    const V3<R> Fo  = A.Fo[m - 1].ld( gi );
+    const R imu     = C.inv_mu[ib];
+    V3<R> lc        = cross( lk, fm );
+    const V3<R> lf  = cross( cm, lk );
+    const V3<R> lfc = cross( lf, cm );
+    const V3<R> lFo = { ( C.dtg * lf.x + C.dtga * lfc.x ) * imu, ( C.dtg * lf.y + C.dtga * lfc.y ) * imu,
+                        ( C.dtg * lf.z + C.dtga * lfc.z ) * imu };
+    const V3<R> Fl  = cross( Fo, lf );
+    lc.x += C.dtga * imu * Fl.x;
+    lc.y += C.dtga * imu * Fl.y;
+    lc.z += C.dtga * imu * Fl.z;
+    A.lam_Fo[m & 1].st( gi, lFo );
+    A.lam_c.st( gi, lc );
+    const R a2     = C.alpha * C.alpha;
+    const V3<R> cF = cross( cm, Fo );
+    const R sc     = C.dtg * imu / ( R( 1 ) + a2 );
+    const V3<R> da = { sc * ( R( -2 ) * C.alpha * Fo.x + ( R( 1 ) - a2 ) * cF.x ),
+                       sc * ( R( -2 ) * C.alpha * Fo.y + ( R( 1 ) - a2 ) * cF.y ),
+                       sc * ( R( -2 ) * C.alpha * Fo.z + ( R( 1 ) - a2 ) * cF.z ) };
+    return dot( lf, da );
+}
+
+// ------------------------------------------------------------------ backward: final normalisation + stage 4 local
+template<typename R>
+__global__ void __launch_bounds__( 256 ) adj_final( AdjArgs<R> A )
 {
     __shared__ SysConst<R> C;
     __shared__ double red[32];
@@ -218,30 +231,13 @@ __global__ void __launch_bounds__( 256 ) adj_k( AdjArgs<R> A )
     if( i < d.nos )
     {
         const long long gi = d.spin_offset + i;
-        const int ib       = i % d.nb;
-        const V3<R> lk     = A.lam_k[M - 1].ld( gi );
-        const V3<R> cm     = A.c[M - 1].ld( gi );
-        const V3<R> fm     = A.f[M - 1].ld( gi );
-        const V3<R> Fo     = A.Fo[M - 1].ld( gi );
-        const R imu        = C.inv_mu[ib];
-        V3<R> lc           = cross( lk, fm );
-        const V3<R> lf     = cross( cm, lk );
-        const V3<R> lfc    = cross( lf, cm );
-        const V3<R> lFo    = { ( C.dtg * lf.x + C.dtga * lfc.x ) * imu, ( C.dtg * lf.y + C.dtga * lfc.y ) * imu,
-                               ( C.dtg * lf.z + C.dtga * lfc.z ) * imu };
-        const V3<R> Fl     = cross( Fo, lf );
-        lc.x += C.dtga * imu * Fl.x;
-        lc.y += C.dtga * imu * Fl.y;
-        lc.z += C.dtga * imu * Fl.z;
-        A.lam_Fo.st( gi, lFo );
-        A.lam_c.st( gi, lc );
-        const R a2     = C.alpha * C.alpha;
-        const V3<R> cF = cross( cm, Fo );
-        const R sc     = C.dtg * imu / ( R( 1 ) + a2 );
-        const V3<R> da = { sc * ( R( -2 ) * C.alpha * Fo.x + ( R( 1 ) - a2 ) * cF.x ),
-                           sc * ( R( -2 ) * C.alpha * Fo.y + ( R( 1 ) - a2 ) * cF.y ),
-                           sc * ( R( -2 ) * C.alpha * Fo.z + ( R( 1 ) - a2 ) * cF.z ) };
-        galpha = dot( lf, da );
+        const V3<R> la     = jn_t( A.acc.ld( gi ), A.lam_next.ld( gi ) );
+        const R w6 = R( 1.0 / 6.0 ), w3 = R( 1.0 / 3.0 );
+        A.lam_s.st( gi, la );
+        A.lam_k[2].st( gi, scale( la, w3 ) );
+        A.lam_k[1].st( gi, scale( la, w3 ) );
+        A.lam_k[0].st( gi, scale( la, w6 ) );
+        galpha = stage_local( A, C, 4, gi, i % d.nb, scale( la, w6 ) );
     }
     block_accumulate( A, &galpha, 4, 1, red );
 }
@@ -263,11 +259,11 @@ __global__ void __launch_bounds__( 256 ) adj_c( AdjArgs<R> A )
     int ib, a, b, c;
     cell_of( GS, valid ? i : 0, ib, a, b, c );
     const int smode = warp_stencil_mode( GS, a, b, c, valid );
-    R gp[4]         = { 0, 0, 0, 0 }; // J, D, K, B
+    R gp[5]         = { 0, 0, 0, 0, 0 }; // J, D, K, B, alpha (of stage M - 1)
     if( valid )
     {
         const long long gi = GS.off + i;
-        const V3<R> lF     = A.lam_Fo.ld( gi );
+        const V3<R> lF     = A.lam_Fo[M & 1].ld( gi );
         const V3<R> cm     = A.c[M - 1].ld( gi );
         V3<R> Ll           = { 0, 0, 0 }; // -L lam_Fo
         // anisotropy
@@ -302,7 +298,7 @@ __global__ void __launch_bounds__( 256 ) adj_c( AdjArgs<R> A )
                 j = pair_index( GS, a, b, c, P.j, P.da, P.db, P.dc );
             if( j < 0 )
                 continue;
-            const V3<R> lj = A.lam_Fo.ld( j );
+            const V3<R> lj = A.lam_Fo[M & 1].ld( j );
             const V3<R> cj = A.c[M - 1].ld( j );
             const V3<R> D  = { P.Dx, P.Dy, P.Dz };
             const V3<R> lx = cross( lj, D );
@@ -337,13 +333,14 @@ __global__ void __launch_bounds__( 256 ) adj_c( AdjArgs<R> A )
             lk.x += w * lp.x;
             lk.y += w * lp.y;
             lk.z += w * lp.z;
-            A.lam_k[M - 2].st( gi, lk );
+            // stage M - 1 starts here: its lam_k is final
+            gp[4] = stage_local( A, C, M - 1, gi, ib, lk );
         }
         else
             ls = operator_add( ls, lc );
         A.lam_s.st( gi, ls );
     }
-    block_accumulate( A, gp, 0, 4, red );
+    block_accumulate( A, gp, 0, M > 1 ? 5 : 4, red );
 }
 
 // ================================================================== host driver
@@ -363,7 +360,7 @@ struct AdjPlan
     static constexpr int SLOTS = 16;
     void * pool  = nullptr; // [k][SLOTS][3][total]
     void * work  = nullptr; // unrecorded forward: c0..c3, acc, s_out (6 slots) + adjoint: lam_next, lam_s,
-                            // lam_k0..3, lam_Fo, lam_c (8 slots)
+                            // lam_k0..3, lam_Fo (2), lam_c (9 slots)
     void * ckpt  = nullptr; // [n_ckpt][3][total]
     double * pgrad = nullptr;
 
@@ -400,8 +397,9 @@ struct AdjPlan
         A.lam_s    = soa_at<R>( work, total, 7 );
         for( int m = 0; m < 4; ++m )
             A.lam_k[m] = soa_at<R>( work, total, 8 + m );
-        A.lam_Fo = soa_at<R>( work, total, 12 );
-        A.lam_c  = soa_at<R>( work, total, 13 );
+        A.lam_Fo[0] = soa_at<R>( work, total, 12 );
+        A.lam_Fo[1] = soa_at<R>( work, total, 14 );
+        A.lam_c     = soa_at<R>( work, total, 13 );
         return A;
     }
 };
@@ -443,25 +441,21 @@ static void backward_step( Engine & E, AdjArgs<R> A, int nblk, cudaStream_t st )
 {
     void * hf[3] = { E.field_ptr( 0 ), E.field_ptr( 1 ), E.field_ptr( 2 ) };
     A.h          = E.has_ddi() ? SoA3<R>{ (R *)hf[0], (R *)hf[1], (R *)hf[2] } : SoA3<R>{ nullptr, nullptr, nullptr };
-    auto field   = [&]() {
+    auto field   = [&]( int m ) {
         if( E.has_ddi() )
         {
-            void * cp[3] = { A.lam_Fo.x, A.lam_Fo.y, A.lam_Fo.z };
+            void * cp[3] = { A.lam_Fo[m & 1].x, A.lam_Fo[m & 1].y, A.lam_Fo[m & 1].z };
             E.run_ddi( cp, nullptr );
         }
     };
     adj_final<R><<<nblk, 256, 0, st>>>( A );
-    adj_k<R, 4><<<nblk, 256, 0, st>>>( A );
-    field();
+    field( 4 );
     adj_c<R, 4><<<nblk, 256, 0, st>>>( A );
-    adj_k<R, 3><<<nblk, 256, 0, st>>>( A );
-    field();
+    field( 3 );
     adj_c<R, 3><<<nblk, 256, 0, st>>>( A );
-    adj_k<R, 2><<<nblk, 256, 0, st>>>( A );
-    field();
+    field( 2 );
     adj_c<R, 2><<<nblk, 256, 0, st>>>( A );
-    adj_k<R, 1><<<nblk, 256, 0, st>>>( A );
-    field();
+    field( 1 );
     adj_c<R, 1><<<nblk, 256, 0, st>>>( A );
     CUDA_CHECK( cudaGetLastError() );
 }
@@ -496,8 +490,8 @@ static double run_t( Engine & E, const AdjointInput & in, AdjointOutput & out )
     AdjPlan<R> P;
     P.total    = total;
     P.n_blocks = nblk;
-    P.pool     = dalloc_bytes( (size_t)K * AdjPlan<R>::SLOTS * 3 * total * sizeof( R ) );
-    P.work     = dalloc_bytes( (size_t)14 * 3 * total * sizeof( R ) );
+    P.pool     = in.gradients ? dalloc_bytes( (size_t)K * AdjPlan<R>::SLOTS * 3 * total * sizeof( R ) ) : nullptr;
+    P.work     = dalloc_bytes( (size_t)15 * 3 * total * sizeof( R ) );
     P.ckpt     = dalloc_bytes( (size_t)n_ckpt * 3 * total * sizeof( R ) );
     P.pgrad    = dalloc<double>( (size_t)5 * nblk );
     const AdjUnits<R> u  = make_units<R>( in );
@@ -512,13 +506,26 @@ static double run_t( Engine & E, const AdjointInput & in, AdjointOutput & out )
                 soa[e * total + d.spin_offset + i] = (R)in.s0[3 * (size_t)i + e];
         AdjArgs<R> W = P.step_args( d_sd, u, 0, false );
         CUDA_CHECK( cudaMemcpyAsync( W.c[0].x, soa.data(), 3 * total * sizeof( R ), cudaMemcpyHostToDevice, st ) );
-        // forward with checkpoints
+        // forward with checkpoints; with gradients, the last segment is recorded right away (the
+        // backward pass then recomputes every segment but that one)
+        const int last0 = in.n_steps > 0 ? ( ( in.n_steps - 1 ) / K ) * K : 0;
         for( int n = 0; n < in.n_steps; ++n )
         {
             if( n % K == 0 )
                 copy3( soa_at<R>( P.ckpt, total, n / K ), W.c[0], total, st );
-            forward_step<R>( E, W, nblk, st );
-            copy3( W.c[0], W.s_out, total, st );
+            if( in.gradients && n >= last0 )
+            {
+                AdjArgs<R> A = P.step_args( d_sd, u, n - last0, true );
+                if( n == last0 )
+                    copy3( A.c[0], W.c[0], total, st );
+                A.s_out = n + 1 < in.n_steps ? P.step_args( d_sd, u, n + 1 - last0, true ).c[0] : W.c[0];
+                forward_step<R>( E, A, nblk, st );
+            }
+            else
+            {
+                forward_step<R>( E, W, nblk, st );
+                copy3( W.c[0], W.s_out, total, st );
+            }
         }
         std::vector<R> fin( 3 * total );
         CUDA_CHECK( cudaMemcpyAsync( fin.data(), W.c[0].x, 3 * total * sizeof( R ), cudaMemcpyDeviceToHost, st ) );
@@ -543,9 +550,10 @@ static double run_t( Engine & E, const AdjointInput & in, AdjointOutput & out )
             for( int seg = ( in.n_steps - 1 ) / K; seg >= 0; --seg )
             {
                 const int n0 = seg * K, n1 = std::min( in.n_steps, n0 + K );
-                // recompute the segment, recording every stage of its steps
-                copy3( P.step_args( d_sd, u, 0, true ).c[0], soa_at<R>( P.ckpt, total, seg ), total, st );
-                for( int n = n0; n < n1; ++n )
+                // recompute the segment, recording every stage of its steps (the last one is recorded)
+                if( n0 != last0 )
+                    copy3( P.step_args( d_sd, u, 0, true ).c[0], soa_at<R>( P.ckpt, total, seg ), total, st );
+                for( int n = n0; n < n1 && n0 != last0; ++n )
                 {
                     AdjArgs<R> A = P.step_args( d_sd, u, n - n0, true );
                     if( n + 1 < n1 )

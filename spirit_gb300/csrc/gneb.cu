@@ -507,8 +507,9 @@ public:
         size_t el = eng->fp64() ? sizeof( double ) : sizeof( float );
         for( int k = 0; k < 3; ++k )
         {
-            CUDA_CHECK( cudaMemset( F[k], 0, eng->total_spins() * el ) );
-            CUDA_CHECK( cudaMemset( V[k], 0, eng->total_spins() * el ) );
+            // on the engine's (non-blocking) stream, ordered before the iterations
+            CUDA_CHECK( cudaMemsetAsync( F[k], 0, eng->total_spins() * el, eng->stream() ) );
+            CUDA_CHECK( cudaMemsetAsync( V[k], 0, eng->total_spins() * el, eng->stream() ) );
         }
         if( graph )
         {

@@ -30,7 +30,10 @@ inline void * dalloc_bytes( size_t bytes )
     if( bytes == 0 )
         bytes = 16;
     CUDA_CHECK( cudaMalloc( &p, bytes ) );
+    // zero-filled before any stream may use it: cudaMemset runs on the legacy stream and returns
+    // early, and the engine streams are non-blocking (they would not wait for it)
     CUDA_CHECK( cudaMemset( p, 0, bytes ) );
+    CUDA_CHECK( cudaStreamSynchronize( nullptr ) );
     return p;
 }
 
@@ -51,12 +54,16 @@ inline void dfree( T *& p )
 template<typename T>
 inline void h2d( T * d, const T * h, size_t n )
 {
+    // complete before return: later work runs on non-blocking streams, which a pageable copy's
+    // outstanding DMA on the legacy stream would not order
     CUDA_CHECK( cudaMemcpy( d, h, n * sizeof( T ), cudaMemcpyHostToDevice ) );
+    CUDA_CHECK( cudaStreamSynchronize( nullptr ) );
 }
 
 inline void h2d_bytes( void * d, const void * h, size_t n )
 {
     CUDA_CHECK( cudaMemcpy( d, h, n, cudaMemcpyHostToDevice ) );
+    CUDA_CHECK( cudaStreamSynchronize( nullptr ) );
 }
 
 template<typename T>
