@@ -331,7 +331,7 @@ def neel_skyrmion(pos, center, radius=8.0, width=2.0, sign=1.0):
     return np.stack([sign * np.sin(th) * np.cos(phi), sign * np.sin(th) * np.sin(phi), np.cos(th)], axis=1)
 
 
-def run_gneb(iters_cap=150000):
+def run_gneb(iters_cap=60000):
     """Batched GNEB: 32 images of a 96x96 triangular lattice between a relaxed Neel skyrmion
     (radius 8 sites) and the ferromagnet (geodesic interpolation), spring 1, VP; 2000 plain
     iterations, then climbing / falling images set automatically and iterations until the max
