@@ -187,6 +187,7 @@ struct FFTDesc
     FastDiv div_Ma, div_Mh, div_Mb, div_Mc;
     FastDiv div_Nb, div_Nc, div_nb;
     FastDiv div_plane; // 3 nb Mb: elements of one c-row of the fused b/c pass
+    FastDiv div_crow;  // 3 nb Mb / K: one c-row of a block of the clustered b/c pass
 };
 
 template<>

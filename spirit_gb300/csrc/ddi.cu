@@ -10,6 +10,8 @@
 #include "fft.cuh"
 #include "util.hpp"
 
+#include <cooperative_groups.h>
+
 #include <cmath>
 #include <vector>
 
@@ -392,6 +394,127 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
     }
 }
 
+// ------------------------------------------------------------------ fused pass BC on a cluster
+// The (c, b) plane of one ka split over a cluster of K blocks.  b-phase: block r owns the c-rows
+// [r cq, r cq + nc) (cq = ceil(Nc / K)), layout [c_local][cb][kb]; c-phase: block r owns the kb
+// range [r kq, (r + 1) kq) (kq = Mb / K) for every c (Mc rows, rows >= Nc zero), layout
+// [c][cb][kb_local].  The two transposes between the phases go through distributed shared memory.
+// Block table: (system, ka, rank, 0), the K blocks of a plane consecutive.
+template<typename R>
+__global__ void __launch_bounds__( 512 ) pass_bc_cl( PassArgs<R> p, int K )
+{
+    namespace cg = cooperative_groups;
+    extern __shared__ unsigned char smem_raw[];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank            = (int)cluster.block_rank();
+    const int4 blk            = p.blocks[blockIdx.x];
+    const int s               = blk.x;
+    if( sys_inactive( p, s ) ) // uniform over the cluster: its blocks share the system
+        return;
+    const FFTDesc & f = p.fd[s];
+    const int Mb = f.M[1], Mc = f.M[2], nb = f.nb;
+    const int Nb = f.N[1], Nc = f.N[2];
+    const int ncb = 3 * nb;
+    const int ka  = blk.y;
+    const int cq  = ( Nc + K - 1 ) / K;
+    const int c0  = rank * cq;
+    const int nc  = max( 0, min( cq, Nc - c0 ) );
+    const int kq  = Mb / K;
+    const int kb0 = rank * kq;
+    const int lb  = cq * ncb * Mb;  // b-phase buffer
+    const int lc  = Mc * ncb * kq;  // c-phase buffer
+    const int crow = ncb * kq;      // elements of one c-row in the c-phase
+    cplx<R> * twb = reinterpret_cast<cplx<R> *>( smem_raw );
+    cplx<R> * twc = twb + Mb;
+    cplx<R> * Bb0 = twc + Mc;
+    cplx<R> * Bb1 = Bb0 + lb;
+    cplx<R> * Bc0 = Bb1 + lb;
+    cplx<R> * Bc1 = Bc0 + lc;
+    load_tw( twb, p.tw + f.tw_offset[1], Mb );
+    load_tw( twc, p.tw + f.tw_offset[2], Mc );
+    for( int e = threadIdx.x; e < lb; e += blockDim.x )
+        Bb0[e] = { 0, 0 };
+    for( int e = threadIdx.x; e < lc; e += blockDim.x )
+        Bc0[e] = { 0, 0 };
+    __syncthreads();
+    const int nin    = ncb * Nc * Nb;
+    cplx<R> * W1     = p.W1 + f.spec_offset + (size_t)ka * nin;
+    for( int e = threadIdx.x; e < ncb * nc * Nb; e += blockDim.x )
+    {
+        const int rest = (int)fdiv( (unsigned)e, f.div_Nb ), b = e - rest * Nb;
+        const int cb = rest / nc, cl = rest - cb * nc;
+        Bb0[( cl * ncb + cb ) * Mb + b] = W1[( (size_t)cb * Nc + c0 + cl ) * Nb + b];
+    }
+    // every block's c-phase buffer is zero before any block writes into it
+    cluster.sync();
+    const FastDiv none = { 1, 0, 0 };
+    cplx<R> * r = sfft<R, false>( Bb0, Bb1, Mb, nc * ncb, none, Mb, 1, f.radix[1], twb, false );
+    // transpose 1: rows (c0 + cl, cb), all kb -> owner of kb
+    for( int e = threadIdx.x; e < nc * ncb * Mb; e += blockDim.x )
+    {
+        const int l = (int)fdiv( (unsigned)e, f.div_Mb ), kb = e - l * Mb;
+        const int cl = l / ncb, cb = l - cl * ncb;
+        const int d = kb / kq, kbl = kb - d * kq;
+        cplx<R> * dst = cluster.map_shared_rank( Bc0, d );
+        dst[( c0 + cl ) * crow + cb * kq + kbl] = r[l * Mb + kb];
+    }
+    cluster.sync();
+    const FastDiv dcrow = f.div_crow;
+    r           = sfft<R, true>( Bc0, Bc1, Mc, crow, dcrow, 1, crow, f.radix[2], twc, false );
+    cplx<R> * o = ( r == Bc0 ) ? Bc1 : Bc0;
+    // tensor product at (kc, kb0 + kbl)
+    const int npair    = nb * nb;
+    const cplx<R> * Dh = p.Dhat + f.dhat_offset + (size_t)ka * npair * 6 * Mc * Mb;
+    for( int e = threadIdx.x; e < nb * Mc * kq; e += blockDim.x )
+    {
+        const int rest = e / kq, kbl = e - rest * kq;
+        const int kc = rest / nb, b1 = rest - kc * nb;
+        const cplx<R> * S = r + kc * crow + kbl;
+        cplx<R> acc[3]    = { { 0, 0 }, { 0, 0 }, { 0, 0 } };
+        for( int b2 = 0; b2 < nb; ++b2 )
+        {
+            const cplx<R> * D = Dh + ( (size_t)( b1 * nb + b2 ) * 6 * Mc + kc ) * Mb + kb0 + kbl;
+            cplx<R> dd[6];
+#pragma unroll
+            for( int q = 0; q < 6; ++q )
+                dd[q] = D[(size_t)q * Mc * Mb];
+            const cplx<R> sx = S[( b2 * 3 + 0 ) * kq];
+            const cplx<R> sy = S[( b2 * 3 + 1 ) * kq];
+            const cplx<R> sz = S[( b2 * 3 + 2 ) * kq];
+            const int rw[3][3] = { { 0, 1, 2 }, { 1, 3, 4 }, { 2, 4, 5 } };
+#pragma unroll
+            for( int c3 = 0; c3 < 3; ++c3 )
+            {
+                const cplx<R> d1 = dd[rw[c3][0]], d2 = dd[rw[c3][1]], d3 = dd[rw[c3][2]];
+                acc[c3].x += d1.x * sx.x + d2.x * sy.x + d3.x * sz.x - d1.y * sx.y - d2.y * sy.y - d3.y * sz.y;
+                acc[c3].y += d1.x * sx.y + d2.x * sy.y + d3.x * sz.y + d1.y * sx.x + d2.y * sy.x + d3.y * sz.x;
+            }
+        }
+#pragma unroll
+        for( int c3 = 0; c3 < 3; ++c3 )
+            o[kc * crow + ( b1 * 3 + c3 ) * kq + kbl] = acc[c3];
+    }
+    __syncthreads();
+    r = sfft<R, true>( o, ( o == Bc0 ) ? Bc1 : Bc0, Mc, crow, dcrow, 1, crow, f.radix[2], twc, true );
+    // transpose 2: rows c < Nc of the kb range -> owner of row c (its b-phase buffers are free)
+    for( int e = threadIdx.x; e < Nc * ncb * kq; e += blockDim.x )
+    {
+        const int l = e / kq, kbl = e - l * kq;
+        const int c = l / ncb, cb = l - c * ncb;
+        const int d = c / cq, cl = c - d * cq;
+        cplx<R> * dst = cluster.map_shared_rank( Bb0, d );
+        dst[( cl * ncb + cb ) * Mb + kb0 + kbl] = r[c * crow + cb * kq + kbl];
+    }
+    cluster.sync();
+    r = sfft<R, false>( Bb0, Bb1, Mb, nc * ncb, none, Mb, 1, f.radix[1], twb, true );
+    for( int e = threadIdx.x; e < ncb * nc * Nb; e += blockDim.x )
+    {
+        const int rest = (int)fdiv( (unsigned)e, f.div_Nb ), b = e - rest * Nb;
+        const int cb = rest / nc, cl = rest - cb * nc;
+        W1[( (size_t)cb * Nc + c0 + cl ) * Nb + b] = r[( cl * ncb + cb ) * Mb + b];
+    }
+}
+
 // ------------------------------------------------------------------ pass A': C2R along a -> field
 // Two Hermitian half spectra X, Y go through one complex inverse transform of Z = X + i Y; the
 // real part is x, the imaginary part y.  The imaginary parts of X and Y at k = 0 and k = Ma/2
@@ -496,6 +619,13 @@ __global__ void dhat_relayout( const cplx<R> * W2, cplx<RS> * Dhat, int Mh, int 
 static size_t smem_bc( size_t elem, const FFTDesc & f )
 {
     return elem * ( f.M[1] + f.M[2] + 2 * (size_t)f.M[2] * 3 * f.nb * f.M[1] );
+}
+
+// fused pass split over a cluster of K blocks (pass_bc_cl)
+static size_t smem_bcl( size_t elem, const FFTDesc & f, int K )
+{
+    const size_t cq = ( f.N[2] + K - 1 ) / K, kq = f.M[1] / K, ncb = 3 * f.nb;
+    return elem * ( f.M[1] + f.M[2] + 2 * cq * ncb * f.M[1] + 2 * (size_t)f.M[2] * ncb * kq );
 }
 
 // largest dynamic shared memory of one block on the current device
@@ -609,7 +739,8 @@ void DDIPlan::build( const std::vector<DDISystem> & systems, bool fp64, const Sy
     int n_batch = 0;
     for( auto & S : systems )
         n_batch = std::max( n_batch, S.sys + 1 );
-    std::vector<FFTDesc> fd_by_sys( std::max( n_batch, 1 ) );
+    n_fd_slots = std::max( n_batch, 1 );
+    std::vector<FFTDesc> fd_by_sys( n_fd_slots );
     for( size_t k = 0; k < systems.size(); ++k )
         fd_by_sys[systems[k].sys] = fds[k];
     d_fd = dalloc<FFTDesc>( fd_by_sys.size() );
@@ -699,12 +830,22 @@ void DDIPlan::set_tiles( int nl_a, int g_b, int g_c )
     std::vector<int4> tbc;
     smem_bc_max = 0;
     if( fused )
+    {
         for( size_t k = 0; k < fd_host.size(); ++k )
         {
             for( int ka = 0; ka < fd_host[k].Mh; ++ka )
-                tbc.push_back( make_int4( sys_index[k], ka, 0, 0 ) );
-            smem_bc_max = std::max( smem_bc_max, smem_bc( elem, fd_host[k] ) );
+                for( int r = 0; r < cluster_k; ++r )
+                    tbc.push_back( make_int4( sys_index[k], ka, r, 0 ) );
+            smem_bc_max = std::max( smem_bc_max, cluster_k == 1 ? smem_bc( elem, fd_host[k] )
+                                                                : smem_bcl( elem, fd_host[k], cluster_k ) );
+            fd_host[k].div_crow = make_fastdiv( 3 * fd_host[k].nb * fd_host[k].M[1] / cluster_k );
         }
+        // FFTDesc table indexed by the batch's system index
+        std::vector<FFTDesc> by_sys( n_fd_slots );
+        for( size_t k = 0; k < fd_host.size(); ++k )
+            by_sys[sys_index[k]] = fd_host[k];
+        h2d( d_fd, by_sys.data(), by_sys.size() );
+    }
     upload_table( d_blocks[3], n_blocks[3], tbc );
     tile[0] = nl_a;
     tile[1] = g_b;
@@ -753,6 +894,7 @@ static void set_smem_limits()
     CUDA_CHECK( cudaFuncSetAttribute( pass_c<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024 ) );
     CUDA_CHECK( cudaFuncSetAttribute( pass_a_inv<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024 ) );
     CUDA_CHECK( cudaFuncSetAttribute( pass_bc<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_optin() ) );
+    CUDA_CHECK( cudaFuncSetAttribute( pass_bc_cl<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_optin() ) );
     done = true;
 }
 
@@ -963,7 +1105,24 @@ void DDIPlan::launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const
         break;
     case 5:
         a.blocks = d_blocks[3];
-        pass_bc<R><<<n_blocks[3], threads_bc, smem_bc_max, stream>>>( a );
+        if( cluster_k == 1 )
+            pass_bc<R><<<n_blocks[3], threads_bc, smem_bc_max, stream>>>( a );
+        else
+        {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim            = dim3( n_blocks[3] );
+            cfg.blockDim           = dim3( std::min( threads_bc, 512 ) );
+            cfg.dynamicSmemBytes   = smem_bc_max;
+            cfg.stream             = stream;
+            cudaLaunchAttribute at[1];
+            at[0].id               = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = cluster_k;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs              = at;
+            cfg.numAttrs           = 1;
+            CUDA_CHECK( cudaLaunchKernelEx( &cfg, pass_bc_cl<R>, a, cluster_k ) );
+        }
         break;
     default:
         a.blocks = d_blocks[0];
@@ -1058,19 +1217,35 @@ void DDIPlan::tune_t( const SysDesc * d_sd, const R * sx, const R * sy, const R 
     }
     if( fused )
     {
+        // cluster size K (the plane split over K blocks) and threads per block; K = 1 is the
+        // single-block kernel.  The arithmetic of every line is the same for every K.
         float bt = 1e30f;
-        int bthr_bc = threads_bc;
-        for( int th : { 256, 512, 1024 } )
+        int bthr_bc = threads_bc, bk = 1;
+        for( int K : { 1, 2, 4 } )
         {
-            threads_bc = th;
-            float t    = timed( { 5 } );
-            if( t < bt )
+            bool ok = true;
+            for( auto & f : fd_host )
+                ok = ok && ( K == 1 || ( f.M[1] % K == 0 && f.N[2] >= K && smem_bcl( elem, f, K ) <= smem_optin() ) );
+            if( !ok )
+                continue;
+            cluster_k = K;
+            set_tiles( best[0], best[1], best[2] );
+            for( int th : { 256, 512, 1024 } )
             {
-                bt      = t;
-                bthr_bc = th;
+                if( K > 1 && th > 512 )
+                    continue;
+                threads_bc = th;
+                float t    = timed( { 5 } );
+                if( t < bt )
+                {
+                    bt      = t;
+                    bthr_bc = th;
+                    bk      = K;
+                }
             }
         }
         threads_bc = bthr_bc;
+        cluster_k  = bk;
     }
     else
     {

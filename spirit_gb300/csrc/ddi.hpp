@@ -58,6 +58,8 @@ public:
     int threads[3]     = { 256, 256, 256 }; // threads per block of A/A', B/B', C
     bool fused         = false; // passes B, C, B' as one kernel per (system, ka) plane
     int threads_bc     = 1024;
+    int cluster_k      = 1; // blocks per (system, ka) plane of the fused pass (cluster size)
+    int n_fd_slots     = 1;
     size_t smem_bc_max = 0;
     size_t max_smem_a = 0, max_smem_b = 0, max_smem_c = 0;
     long long spec_elems = 0;

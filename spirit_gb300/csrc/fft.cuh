@@ -38,6 +38,183 @@ __device__ __forceinline__ cplx<R> cconj( cplx<R> a )
     return { a.x, -a.y };
 }
 
+// ------------------------------------------------------------------ register DFTs (radix 2..16)
+// In-register DFT of N = 2, 4, 8, 16 points, X_m = sum_r v_r w^(r m), w = exp(-/+ 2 pi i / N).
+// Constants are cos / sin of multiples of pi / 8.
+template<typename R>
+__device__ __forceinline__ cplx<R> mul_mi( cplx<R> a, bool inverse ) // a * (-i) forward, a * (+i) inverse
+{
+    return inverse ? cplx<R>{ -a.y, a.x } : cplx<R>{ a.y, -a.x };
+}
+
+template<typename R>
+__device__ __forceinline__ void dft4( cplx<R> & v0, cplx<R> & v1, cplx<R> & v2, cplx<R> & v3, bool inverse )
+{
+    const cplx<R> s02 = { v0.x + v2.x, v0.y + v2.y }, d02 = { v0.x - v2.x, v0.y - v2.y };
+    const cplx<R> s13 = { v1.x + v3.x, v1.y + v3.y }, d13 = { v1.x - v3.x, v1.y - v3.y };
+    const cplx<R> id13 = mul_mi( d13, inverse );
+    v0 = { s02.x + s13.x, s02.y + s13.y };
+    v1 = { d02.x + id13.x, d02.y + id13.y };
+    v2 = { s02.x - s13.x, s02.y - s13.y };
+    v3 = { d02.x - id13.x, d02.y - id13.y };
+}
+
+// w16^k for k = 0..9 (forward sign), applied as multiplication (conjugated for the inverse)
+template<typename R>
+__device__ __forceinline__ cplx<R> w16( int k, bool inverse )
+{
+    const R c1 = R( 0.92387953251128675613 ), s1 = R( 0.38268343236508977173 ), c2 = R( 0.70710678118654752440 );
+    cplx<R> w;
+    switch( k )
+    {
+    case 0: w = { R( 1 ), R( 0 ) }; break;
+    case 1: w = { c1, -s1 }; break;
+    case 2: w = { c2, -c2 }; break;
+    case 3: w = { s1, -c1 }; break;
+    case 4: w = { R( 0 ), R( -1 ) }; break;
+    case 6: w = { -c2, -c2 }; break;
+    default: w = { -c1, s1 }; break; // k = 9
+    }
+    if( inverse )
+        w.y = -w.y;
+    return w;
+}
+
+template<typename R, int N>
+__device__ __forceinline__ void dft_reg( cplx<R> * v, bool inverse )
+{
+    if constexpr( N == 2 )
+    {
+        const cplx<R> a = v[0], b = v[1];
+        v[0] = { a.x + b.x, a.y + b.y };
+        v[1] = { a.x - b.x, a.y - b.y };
+    }
+    else if constexpr( N == 4 )
+        dft4( v[0], v[1], v[2], v[3], inverse );
+    else if constexpr( N == 8 )
+    {
+        // two 4-point DFTs (even, odd inputs), then X_m = E_m + w8^m O_m, X_{m+4} = E_m - w8^m O_m
+        cplx<R> e[4] = { v[0], v[2], v[4], v[6] }, o[4] = { v[1], v[3], v[5], v[7] };
+        dft4( e[0], e[1], e[2], e[3], inverse );
+        dft4( o[0], o[1], o[2], o[3], inverse );
+        const R c2 = R( 0.70710678118654752440 );
+        const cplx<R> t0 = o[0];
+        const cplx<R> t1 = inverse ? cplx<R>{ c2 * ( o[1].x - o[1].y ), c2 * ( o[1].x + o[1].y ) }
+                                   : cplx<R>{ c2 * ( o[1].x + o[1].y ), c2 * ( o[1].y - o[1].x ) };
+        const cplx<R> t2 = mul_mi( o[2], inverse );
+        const cplx<R> t3 = inverse ? cplx<R>{ -c2 * ( o[3].x + o[3].y ), c2 * ( o[3].x - o[3].y ) }
+                                   : cplx<R>{ c2 * ( o[3].y - o[3].x ), -c2 * ( o[3].x + o[3].y ) };
+        const cplx<R> t[4] = { t0, t1, t2, t3 };
+#pragma unroll
+        for( int m = 0; m < 4; ++m )
+        {
+            v[m]     = { e[m].x + t[m].x, e[m].y + t[m].y };
+            v[m + 4] = { e[m].x - t[m].x, e[m].y - t[m].y };
+        }
+    }
+    else
+    {
+        static_assert( N == 16, "radix 2, 4, 8 or 16" );
+        // r = r1 + 4 r2:  Y[r1][m2] = DFT4_r2 v[r1 + 4 r2],  Y *= w16^(r1 m2),  X[m2 + 4 m1] = DFT4_r1 Y
+        cplx<R> y[16];
+#pragma unroll
+        for( int r1 = 0; r1 < 4; ++r1 )
+        {
+            cplx<R> a0 = v[r1], a1 = v[r1 + 4], a2 = v[r1 + 8], a3 = v[r1 + 12];
+            dft4( a0, a1, a2, a3, inverse );
+            y[r1 * 4 + 0] = a0;
+            y[r1 * 4 + 1] = r1 == 0 ? a1 : cmul( a1, w16<R>( r1, inverse ) );
+            y[r1 * 4 + 2] = r1 == 0 ? a2 : cmul( a2, w16<R>( 2 * r1, inverse ) );
+            y[r1 * 4 + 3] = r1 == 0 ? a3 : cmul( a3, w16<R>( 3 * r1, inverse ) );
+        }
+#pragma unroll
+        for( int m2 = 0; m2 < 4; ++m2 )
+        {
+            cplx<R> b0 = y[0 * 4 + m2], b1 = y[1 * 4 + m2], b2 = y[2 * 4 + m2], b3 = y[3 * 4 + m2];
+            dft4( b0, b1, b2, b3, inverse );
+            v[m2]      = b0;
+            v[m2 + 4]  = b1;
+            v[m2 + 8]  = b2;
+            v[m2 + 12] = b3;
+        }
+    }
+}
+
+// One Stockham stage of radix 2^LGR on lines of length 2^LGL (Ns = 2^LGNS), lines at l*ls,
+// elements at t*es.  Twiddles: tw[t] = exp(-2 pi i t / L).
+template<typename R, int LGL, int LGNS, int LGR, bool LINE_FAST>
+__device__ __forceinline__ void stockham_stage( const cplx<R> * a, cplx<R> * b, int nl, const FastDiv & dnl, int ls,
+                                               int es, const cplx<R> * tw, bool inverse )
+{
+    constexpr int RR   = 1 << LGR;
+    constexpr int LGLR = LGL - LGR;
+    constexpr int LR   = 1 << LGLR;
+    constexpr int NS   = 1 << LGNS;
+    constexpr int LGSP = LGL - LGNS - LGR;
+    for( int idx = threadIdx.x; idx < ( nl << LGLR ); idx += blockDim.x )
+    {
+        int line, j;
+        if( LINE_FAST )
+        {
+            j    = (int)fdiv( (unsigned)idx, dnl );
+            line = idx - j * nl;
+        }
+        else
+        {
+            line = idx >> LGLR;
+            j    = idx & ( LR - 1 );
+        }
+        const cplx<R> * src = a + line * ls;
+        cplx<R> * dst       = b + line * ls;
+        const int k         = j & ( NS - 1 );
+        cplx<R> v[RR];
+#pragma unroll
+        for( int r = 0; r < RR; ++r )
+        {
+            const cplx<R> x = src[( j + r * LR ) * es];
+            if( r == 0 || LGNS == 0 )
+                v[r] = x;
+            else
+            {
+                cplx<R> w = tw[( r * k ) << LGSP];
+                if( inverse )
+                    w.y = -w.y;
+                v[r] = cmul( x, w );
+            }
+        }
+        dft_reg<R, RR>( v, inverse );
+        const int d0 = ( ( j >> LGNS ) << ( LGNS + LGR ) ) + k;
+#pragma unroll
+        for( int m = 0; m < RR; ++m )
+            dst[( d0 + m * NS ) * es] = v[m];
+    }
+}
+
+// Stockham FFT of length 2^LGL with radix-2^MAXLG register stages (the last stage takes the
+// remainder).  Returns the buffer holding the result.
+template<typename R, int LGL, int LGNS, int MAXLG, bool LINE_FAST>
+__device__ __forceinline__ cplx<R> * stockham_reg( cplx<R> * a, cplx<R> * b, int nl, const FastDiv & dnl, int ls,
+                                                  int es, const cplx<R> * tw, bool inverse )
+{
+    if constexpr( LGNS >= LGL )
+        return a;
+    else
+    {
+        constexpr int LGR = ( LGL - LGNS ) >= MAXLG ? MAXLG : ( LGL - LGNS );
+        stockham_stage<R, LGL, LGNS, LGR, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        __syncthreads();
+        return stockham_reg<R, LGL, LGNS + LGR, MAXLG, LINE_FAST>( b, a, nl, dnl, ls, es, tw, inverse );
+    }
+}
+
+// radix 16 stages in FP32, radix 8 in FP64 (register budget)
+template<typename R>
+struct MaxRadix
+{
+    static constexpr int LG = sizeof( R ) == 4 ? 4 : 3;
+};
+
+
 // Power-of-two lines: radix-4 stages (and one radix-2 stage if log2 L is odd) with shift/mask
 // index arithmetic.
 template<typename R>
@@ -184,17 +361,17 @@ __device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int ls, int nl,
     case 1:
         return a;
     case 16:
-        return block_fft_const<R, 16>( a, b, ls, nl, tw, inverse );
+        return stockham_reg<R, 4, 0, MaxRadix<R>::LG, false>( a, b, nl, FastDiv{ 1, 0, 0 }, ls, 1, tw, inverse );
     case 32:
-        return block_fft_const<R, 32>( a, b, ls, nl, tw, inverse );
+        return stockham_reg<R, 5, 0, MaxRadix<R>::LG, false>( a, b, nl, FastDiv{ 1, 0, 0 }, ls, 1, tw, inverse );
     case 64:
-        return block_fft_const<R, 64>( a, b, ls, nl, tw, inverse );
+        return stockham_reg<R, 6, 0, MaxRadix<R>::LG, false>( a, b, nl, FastDiv{ 1, 0, 0 }, ls, 1, tw, inverse );
     case 128:
-        return block_fft_const<R, 128>( a, b, ls, nl, tw, inverse );
+        return stockham_reg<R, 7, 0, MaxRadix<R>::LG, false>( a, b, nl, FastDiv{ 1, 0, 0 }, ls, 1, tw, inverse );
     case 256:
-        return block_fft_const<R, 256>( a, b, ls, nl, tw, inverse );
+        return stockham_reg<R, 8, 0, MaxRadix<R>::LG, false>( a, b, nl, FastDiv{ 1, 0, 0 }, ls, 1, tw, inverse );
     case 512:
-        return block_fft_const<R, 512>( a, b, ls, nl, tw, inverse );
+        return stockham_reg<R, 9, 0, MaxRadix<R>::LG, false>( a, b, nl, FastDiv{ 1, 0, 0 }, ls, 1, tw, inverse );
     default:
         break;
     }
@@ -481,19 +658,19 @@ __device__ cplx<R> * sfft( cplx<R> * a, cplx<R> * b, int L, int nl, const FastDi
     case 8:
         return sfft_const<R, 8, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 16:
-        return sfft_const<R, 16, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 4, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 32:
-        return sfft_const<R, 32, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 5, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 64:
-        return sfft_const<R, 64, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 6, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 128:
-        return sfft_const<R, 128, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 7, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 256:
-        return sfft_const<R, 256, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 8, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 512:
-        return sfft_const<R, 512, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 9, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 1024:
-        return sfft_const<R, 1024, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 10, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     default:
         return sfft_generic<R>( a, b, L, nl, ls, es, rad, tw, inverse );
     }
