@@ -64,7 +64,7 @@ struct FastDiv
     unsigned long long m;
 };
 
-inline FastDiv make_fastdiv( unsigned int d )
+__host__ __device__ inline FastDiv make_fastdiv( unsigned int d )
 {
     FastDiv f;
     f.d   = d;

@@ -46,13 +46,6 @@ struct PassArgs
 };
 
 template<typename R>
-__device__ __forceinline__ void load_tw( cplx<R> * dst, const cplx<R> * src, int L )
-{
-    for( int t = threadIdx.x; t < L; t += blockDim.x )
-        dst[t] = src[t];
-}
-
-template<typename R>
 __device__ __forceinline__ bool sys_inactive( const PassArgs<R> & p, int s )
 {
     return p.runs && !p.runs[s].active;

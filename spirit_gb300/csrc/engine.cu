@@ -55,6 +55,196 @@ enum
 // spins per thread of the FP32 stage kernels (index = Engine::spt_idx_); FP64 uses 1
 static const int SPT_OPTIONS[3] = { 1, 2, 4 };
 
+// Per-spin part of a stage after the field g of configuration ci is known: thermal field, virtual
+// force and the solver's update (Solver_SIB.hpp, Solver_Heun.hpp, Solver_Depondt.hpp,
+// Solver_RK4.hpp); t2 takes the max squared torque.
+template<typename R, int SOLVER, int STAGE>
+__device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysConst<R> & C, const SysDesc & d,
+                                              long long gi, int i, int ib, V3<R> ci, V3<R> g, int iteration,
+                                              float & t2 )
+{
+    constexpr bool PROBE = STAGE == ST_PROBE;
+    V3<R> xi             = { 0, 0, 0 };
+    if( C.thermal )
+    {
+        // drawn once per iteration (Prepare_Thermal_Field, Method_LLG.cpp:65-110) by the first
+        // stage and kept for the later stages of the same iteration
+        if( PROBE || STAGE == 1 )
+        {
+            const R sc = C.noise[ib];
+            V3<R> z = gauss3<R>( d.seed, d.stream, PROBE ? 0xFFFFFFFFu : (unsigned int)iteration, (unsigned int)i );
+            xi      = { sc * z.x, sc * z.y, sc * z.z };
+            if( STAGE == 1 )
+                A.xi.st( gi, xi );
+        }
+        else
+            xi = A.xi.ld( gi );
+    }
+    V3<R> fv = virtual_force<R>( C, ci, g, C.inv_mu[ib], xi );
+    if( PROBE )
+    {
+        t2 = fmaxf( t2, (float)torque2( fv, ci ) );
+    }
+    else if( SOLVER == SOLVER_SIB )
+    {
+        const V3<R> si = ( STAGE == 1 ) ? ci : A.s.ld( gi );
+        if( STAGE == 1 )
+        {
+            V3<R> p = sib( si, fv );
+            p.x += si.x;
+            p.y += si.y;
+            p.z += si.z;
+            p.x *= R( 0.5 );
+            p.y *= R( 0.5 );
+            p.z *= R( 0.5 );
+            A.out.st( gi, p );
+            A.aux1.st( gi, fv );
+        }
+        else
+        {
+            V3<R> sn = sib( si, fv );
+            // SIB preserves |s| only in exact arithmetic; in FP32 the rounding drift is removed
+            if( sizeof( R ) == 4 )
+                sn = normalized( sn );
+            A.s.st( gi, sn );
+            t2 = fmaxf( t2, (float)torque2( A.aux1.ld( gi ), sn ) );
+        }
+    }
+    else if( SOLVER == SOLVER_HEUN )
+    {
+        if( STAGE == 1 )
+        {
+            V3<R> cr = cross( ci, fv );
+            V3<R> p  = { ci.x + R( -1 ) * cr.x, ci.y + R( -1 ) * cr.y, ci.z + R( -1 ) * cr.z };
+            A.out.st( gi, normalized( p ) );
+            A.aux1.st( gi, fv );
+        }
+        else
+        {
+            const V3<R> si  = A.s.ld( gi );
+            const V3<R> fv1 = A.aux1.ld( gi );
+            V3<R> c1        = cross( si, fv1 );
+            V3<R> t1        = { R( -1 ) * c1.x, R( -1 ) * c1.y, R( -1 ) * c1.z };
+            V3<R> c2        = cross( ci, fv );
+            V3<R> t         = { t1.x * R( 0.5 ), t1.y * R( 0.5 ), t1.z * R( 0.5 ) };
+            t.x += si.x;
+            t.y += si.y;
+            t.z += si.z;
+            t.x += R( 0.5 ) * ( R( -1 ) * c2.x );
+            t.y += R( 0.5 ) * ( R( -1 ) * c2.y );
+            t.z += R( 0.5 ) * ( R( -1 ) * c2.z );
+            V3<R> sn = normalized( t );
+            A.s.st( gi, sn );
+            t2 = fmaxf( t2, (float)torque2( fv1, sn ) );
+        }
+    }
+    else if( SOLVER == SOLVER_DEPONDT )
+    {
+        if( STAGE == 1 )
+        {
+            R ang    = sqrt( dot( fv, fv ) );
+            V3<R> ax = normalized( fv );
+            A.out.st( gi, rotate( ci, ax, ang ) );
+            A.aux1.st( gi, fv );
+        }
+        else
+        {
+            const V3<R> si  = A.s.ld( gi );
+            const V3<R> fv1 = A.aux1.ld( gi );
+            V3<R> ax        = { R( 0.5 ) * fv1.x, R( 0.5 ) * fv1.y, R( 0.5 ) * fv1.z };
+            ax.x += R( 0.5 ) * fv.x;
+            ax.y += R( 0.5 ) * fv.y;
+            ax.z += R( 0.5 ) * fv.z;
+            R ang    = sqrt( dot( ax, ax ) );
+            V3<R> sn = rotate( si, normalized( ax ), ang );
+            // a rotation preserves |s| only in exact arithmetic; in FP32 the rounding drift is removed
+            if( sizeof( R ) == 4 )
+                sn = normalized( sn );
+            A.s.st( gi, sn );
+            t2 = fmaxf( t2, (float)torque2( fv1, sn ) );
+        }
+    }
+    else if( SOLVER == SOLVER_RK4 )
+    {
+        // k_m = -(cfg_m x fv_m); cfg_{m+1} = normalize(s + w k_m); running sum acc = s + k1/6 + k2/3 + ...
+        V3<R> cr = cross( ci, fv );
+        V3<R> k  = { R( -1 ) * cr.x, R( -1 ) * cr.y, R( -1 ) * cr.z };
+        const V3<R> si = ( STAGE == 1 ) ? ci : A.s.ld( gi );
+        if( STAGE == 1 )
+        {
+            A.aux1.st( gi, fv );
+            V3<R> acc = si;
+            R w6      = R( 1.0 / 6.0 );
+            acc.x += w6 * k.x;
+            acc.y += w6 * k.y;
+            acc.z += w6 * k.z;
+            A.aux2.st( gi, acc );
+            V3<R> p = { si.x + R( 0.5 ) * k.x, si.y + R( 0.5 ) * k.y, si.z + R( 0.5 ) * k.z };
+            A.out.st( gi, normalized( p ) );
+        }
+        else if( STAGE == 2 || STAGE == 3 )
+        {
+            V3<R> acc = A.aux2.ld( gi );
+            R w3      = R( 1.0 / 3.0 );
+            acc.x += w3 * k.x;
+            acc.y += w3 * k.y;
+            acc.z += w3 * k.z;
+            A.aux2.st( gi, acc );
+            R wn    = STAGE == 2 ? R( 0.5 ) : R( 1 );
+            V3<R> p = { si.x + wn * k.x, si.y + wn * k.y, si.z + wn * k.z };
+            A.out.st( gi, normalized( p ) );
+        }
+        else
+        {
+            V3<R> acc = A.aux2.ld( gi );
+            R w6      = R( 1.0 / 6.0 );
+            acc.x += w6 * k.x;
+            acc.y += w6 * k.y;
+            acc.z += w6 * k.z;
+            V3<R> sn = normalized( acc );
+            A.s.st( gi, sn );
+            t2 = fmaxf( t2, (float)torque2( A.aux1.ld( gi ), sn ) );
+        }
+    }
+}
+
+// End of the final stage (or of the probe): energy of the evaluated configuration and max torque
+// of the step per system (warp sums in the working precision, FP64 across the warps of the block);
+// the last block of the system closes the iteration.
+template<typename R, bool PROBE>
+__device__ __forceinline__ void stage_finalize( const StageArgs<R> & A, SysRun * run, int s, const SysDesc & d, R e,
+                                               float t2, double * red_d, float * red_f, int & is_last )
+{
+    double es = block_sum_w( e, red_d );
+    float tm  = block_max( t2, red_f );
+    if( threadIdx.x == 0 )
+    {
+        atomicAdd( &run->energy_acc, es );
+        atomicMax( &run->torque_bits, __float_as_uint( tm ) );
+        __threadfence();
+        unsigned int prev = atomicAdd( &run->blocks_done, 1u );
+        is_last           = ( prev == (unsigned int)A.blkcount[s] - 1 );
+    }
+    __syncthreads();
+    if( is_last && threadIdx.x == 0 )
+    {
+        __threadfence();
+        volatile SysRun * vr = run;
+        float mt             = sqrtf( __uint_as_float( vr->torque_bits ) );
+        vr->max_torque       = mt;
+        vr->energy           = vr->energy_acc;
+        vr->energy_acc       = 0;
+        vr->torque_bits      = 0;
+        vr->blocks_done      = 0;
+        if( !A.tune )
+        {
+            int it        = vr->iteration + ( PROBE ? 0 : 1 );
+            vr->iteration = it;
+            vr->active    = ( it < d.n_iterations ) && !( mt < (float)d.force_convergence );
+        }
+    }
+}
+
 // SOLVER / STAGE are compile-time; STAGE 0 is the constructor probe (initial torque + energy).
 // A block of 256 threads covers SPT * 256 consecutive spins of one system (thread t: spins
 // t, t + 256, ...), so the per-block set-up and reductions are shared by SPT spins per thread.
@@ -98,182 +288,12 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
         R ek               = 0;
         V3<R> g            = gradient_at<R>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu, ek, smode );
         e += ek;
-        V3<R> xi           = { 0, 0, 0 };
-        if( C.thermal )
-        {
-            // drawn once per iteration (Prepare_Thermal_Field, Method_LLG.cpp:65-110) by the first
-            // stage and kept for the later stages of the same iteration
-            if( PROBE || STAGE == 1 )
-            {
-                const R sc = C.noise[ib];
-                V3<R> z = gauss3<R>( d.seed, d.stream, PROBE ? 0xFFFFFFFFu : (unsigned int)iteration, (unsigned int)i );
-                xi      = { sc * z.x, sc * z.y, sc * z.z };
-                if( STAGE == 1 )
-                    A.xi.st( gi, xi );
-            }
-            else
-                xi = A.xi.ld( gi );
-        }
-        V3<R> fv = virtual_force<R>( C, ci, g, C.inv_mu[ib], xi );
-        if( PROBE )
-        {
-            t2 = fmaxf( t2, (float)torque2( fv, ci ) );
-        }
-        else if( SOLVER == SOLVER_SIB )
-        {
-            const V3<R> si = ( STAGE == 1 ) ? ci : A.s.ld( gi );
-            if( STAGE == 1 )
-            {
-                V3<R> p = sib( si, fv );
-                p.x += si.x;
-                p.y += si.y;
-                p.z += si.z;
-                p.x *= R( 0.5 );
-                p.y *= R( 0.5 );
-                p.z *= R( 0.5 );
-                A.out.st( gi, p );
-                A.aux1.st( gi, fv );
-            }
-            else
-            {
-                V3<R> sn = sib( si, fv );
-                // SIB preserves |s| only in exact arithmetic; in FP32 the rounding drift is removed
-                if( sizeof( R ) == 4 )
-                    sn = normalized( sn );
-                A.s.st( gi, sn );
-                t2 = fmaxf( t2, (float)torque2( A.aux1.ld( gi ), sn ) );
-            }
-        }
-        else if( SOLVER == SOLVER_HEUN )
-        {
-            if( STAGE == 1 )
-            {
-                V3<R> cr = cross( ci, fv );
-                V3<R> p  = { ci.x + R( -1 ) * cr.x, ci.y + R( -1 ) * cr.y, ci.z + R( -1 ) * cr.z };
-                A.out.st( gi, normalized( p ) );
-                A.aux1.st( gi, fv );
-            }
-            else
-            {
-                const V3<R> si  = A.s.ld( gi );
-                const V3<R> fv1 = A.aux1.ld( gi );
-                V3<R> c1        = cross( si, fv1 );
-                V3<R> t1        = { R( -1 ) * c1.x, R( -1 ) * c1.y, R( -1 ) * c1.z };
-                V3<R> c2        = cross( ci, fv );
-                V3<R> t         = { t1.x * R( 0.5 ), t1.y * R( 0.5 ), t1.z * R( 0.5 ) };
-                t.x += si.x;
-                t.y += si.y;
-                t.z += si.z;
-                t.x += R( 0.5 ) * ( R( -1 ) * c2.x );
-                t.y += R( 0.5 ) * ( R( -1 ) * c2.y );
-                t.z += R( 0.5 ) * ( R( -1 ) * c2.z );
-                V3<R> sn = normalized( t );
-                A.s.st( gi, sn );
-                t2 = fmaxf( t2, (float)torque2( fv1, sn ) );
-            }
-        }
-        else if( SOLVER == SOLVER_DEPONDT )
-        {
-            if( STAGE == 1 )
-            {
-                R ang    = sqrt( dot( fv, fv ) );
-                V3<R> ax = normalized( fv );
-                A.out.st( gi, rotate( ci, ax, ang ) );
-                A.aux1.st( gi, fv );
-            }
-            else
-            {
-                const V3<R> si  = A.s.ld( gi );
-                const V3<R> fv1 = A.aux1.ld( gi );
-                V3<R> ax        = { R( 0.5 ) * fv1.x, R( 0.5 ) * fv1.y, R( 0.5 ) * fv1.z };
-                ax.x += R( 0.5 ) * fv.x;
-                ax.y += R( 0.5 ) * fv.y;
-                ax.z += R( 0.5 ) * fv.z;
-                R ang    = sqrt( dot( ax, ax ) );
-                V3<R> sn = rotate( si, normalized( ax ), ang );
-                // a rotation preserves |s| only in exact arithmetic; in FP32 the rounding drift is removed
-                if( sizeof( R ) == 4 )
-                    sn = normalized( sn );
-                A.s.st( gi, sn );
-                t2 = fmaxf( t2, (float)torque2( fv1, sn ) );
-            }
-        }
-        else if( SOLVER == SOLVER_RK4 )
-        {
-            // k_m = -(cfg_m x fv_m); cfg_{m+1} = normalize(s + w k_m); running sum acc = s + k1/6 + k2/3 + ...
-            V3<R> cr = cross( ci, fv );
-            V3<R> k  = { R( -1 ) * cr.x, R( -1 ) * cr.y, R( -1 ) * cr.z };
-            const V3<R> si = ( STAGE == 1 ) ? ci : A.s.ld( gi );
-            if( STAGE == 1 )
-            {
-                A.aux1.st( gi, fv );
-                V3<R> acc = si;
-                R w6      = R( 1.0 / 6.0 );
-                acc.x += w6 * k.x;
-                acc.y += w6 * k.y;
-                acc.z += w6 * k.z;
-                A.aux2.st( gi, acc );
-                V3<R> p = { si.x + R( 0.5 ) * k.x, si.y + R( 0.5 ) * k.y, si.z + R( 0.5 ) * k.z };
-                A.out.st( gi, normalized( p ) );
-            }
-            else if( STAGE == 2 || STAGE == 3 )
-            {
-                V3<R> acc = A.aux2.ld( gi );
-                R w3      = R( 1.0 / 3.0 );
-                acc.x += w3 * k.x;
-                acc.y += w3 * k.y;
-                acc.z += w3 * k.z;
-                A.aux2.st( gi, acc );
-                R wn    = STAGE == 2 ? R( 0.5 ) : R( 1 );
-                V3<R> p = { si.x + wn * k.x, si.y + wn * k.y, si.z + wn * k.z };
-                A.out.st( gi, normalized( p ) );
-            }
-            else
-            {
-                V3<R> acc = A.aux2.ld( gi );
-                R w6      = R( 1.0 / 6.0 );
-                acc.x += w6 * k.x;
-                acc.y += w6 * k.y;
-                acc.z += w6 * k.z;
-                V3<R> sn = normalized( acc );
-                A.s.st( gi, sn );
-                t2 = fmaxf( t2, (float)torque2( A.aux1.ld( gi ), sn ) );
-            }
-        }
+        stage_update<R, SOLVER, STAGE>( A, C, d, gi, i, ib, ci, g, iteration, t2 );
     }
     }
     if( !( FINAL || PROBE ) )
         return;
-    // energy of the evaluated configuration and max torque of the step, per system: warp sums in
-    // the working precision, FP64 only across the warps of the block
-    double es = block_sum_w( e, red_d );
-    float tm  = block_max( t2, red_f );
-    if( threadIdx.x == 0 )
-    {
-        atomicAdd( &run->energy_acc, es );
-        atomicMax( &run->torque_bits, __float_as_uint( tm ) );
-        __threadfence();
-        unsigned int prev = atomicAdd( &run->blocks_done, 1u );
-        is_last           = ( prev == (unsigned int)A.blkcount[s] - 1 );
-    }
-    __syncthreads();
-    if( is_last && threadIdx.x == 0 )
-    {
-        __threadfence();
-        volatile SysRun * vr = run;
-        float mt             = sqrtf( __uint_as_float( vr->torque_bits ) );
-        vr->max_torque       = mt;
-        vr->energy           = vr->energy_acc;
-        vr->energy_acc       = 0;
-        vr->torque_bits      = 0;
-        vr->blocks_done      = 0;
-        if( !A.tune )
-        {
-            int it        = vr->iteration + ( PROBE ? 0 : 1 );
-            vr->iteration = it;
-            vr->active    = ( it < d.n_iterations ) && !( mt < (float)d.force_convergence );
-        }
-    }
+    stage_finalize<R, PROBE>( A, run, s, d, e, t2, red_d, red_f, is_last );
 }
 
 // ------------------------------------------------------------------ evaluation kernel

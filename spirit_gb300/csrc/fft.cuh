@@ -676,6 +676,14 @@ __device__ cplx<R> * sfft( cplx<R> * a, cplx<R> * b, int L, int nl, const FastDi
     }
 }
 
+// copy a twiddle table into shared memory (all threads)
+template<typename R>
+__device__ __forceinline__ void load_tw( cplx<R> * dst, const cplx<R> * src, int L )
+{
+    for( int t = threadIdx.x; t < L; t += blockDim.x )
+        dst[t] = src[t];
+}
+
 // shared-memory line stride for lines of length L
 __host__ __device__ inline int line_stride( int L )
 {
