@@ -500,6 +500,12 @@ def run_gb300(args):
     torch.cuda.synchronize()
     ms = reduce_max(sum(a.elapsed_time(b) for a, b in zip(e0, e1)), world)
     n_kernels = kps(p, -1, -1)
+    tun = (ctypes.c_int * 16)()
+    ntun = fn("Simulation_Get_Tuning", [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int], ctypes.c_int)(p, tun, 16, -1, -1)
+    tuned = dict(zip(["stage_spins_per_thread", "fft_a_lines", "fft_a_threads", "fft_b_lines", "fft_b_threads",
+                      "fft_c_columns", "fft_c_threads", "fused_bc", "bc_cluster", "bc_threads", "ddi"],
+                     [int(tun[k]) for k in range(ntun)]))
     value = NOS * args.steps * world / (ms / 1000.0)
     # --- per-kernel durations (CUDA events between launches, L2 flushed before every step)
     kms = (ctypes.c_double * 16)()
@@ -548,6 +554,7 @@ def run_gb300(args):
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_ms},
         "kernel_share": {k: round(v[0] / total, 4) for k, v in per.items()},
+        "autotuned": tuned,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
     }

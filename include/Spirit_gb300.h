@@ -256,6 +256,12 @@ double Simulation_LLG_Adjoint( State * state, const double * params, int n_steps
 /* EXTENSION: the loss of the same trajectory without gradients (finite differences, timing) */
 double Simulation_LLG_Loss( State * state, const double * params, int n_steps, const double * target,
                             double * final_spins, int idx_image, int idx_chain );
+/* EXTENSION: the autotuned launch parameters of the image's started LLG run, in this order:
+ * spins per thread of the stage kernels; lines and threads per block of FFT pass A / A'; lines
+ * and threads of pass B / B'; columns and threads of pass C; 1 if the fused b/c pass is used;
+ * its cluster size and threads per block; 1 if the run has a dipolar term.  Writes at most n
+ * values; returns the number the engine reports (0 without a started run). */
+int Simulation_Get_Tuning( State * state, int * values, int n, int idx_image, int idx_chain );
 /* EXTENSION: device arithmetic of the step loop: 32 (FP32 bulk, default) or 64 */
 void Simulation_Set_Precision( State * state, int bits );
 int Simulation_Get_Precision( State * state );

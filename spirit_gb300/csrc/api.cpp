@@ -2219,6 +2219,21 @@ int Simulation_Get_Kernels_Per_Step( State * state, int idx_image, int idx_chain
     }
 }
 
+// Tuned launch parameters of the image's LLG engine (see include/Spirit_gb300.h); returns how many
+// values the engine reports (0 before a start).
+int Simulation_Get_Tuning( State * state, int * values, int n, int idx_image, int idx_chain ) noexcept
+{
+    try
+    {
+        auto I = from_indices( state, idx_image, idx_chain );
+        return I.img->run && values ? I.img->run->tuning( values, n ) : 0;
+    }
+    catch( ... )
+    {
+        return 0;
+    }
+}
+
 void Simulation_Set_Precision( State * state, int bits ) noexcept
 {
     if( bits == 32 || bits == 64 )

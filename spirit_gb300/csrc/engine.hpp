@@ -103,6 +103,9 @@ public:
     // nullptr returns to the engine's own stream
     void set_stream( cudaStream_t s );
     int kernels_per_step() const;
+    // tuned launch parameters: spins per thread of the stage kernels, lines / threads per block of
+    // the FFT passes A, B, C, fused b/c pass (1 fused, 0 split), its cluster size and threads
+    int tuning( int * out, int n ) const;
     // n steps launched kernel by kernel with CUDA events between launches on the engine stream;
     // before every step `flush_buf` is overwritten and `read_buf` read back (an L2 flush that
     // leaves clean lines; both may be null).
