@@ -167,6 +167,39 @@ void Chain_Setup_Data( State * state, int idx_chain );                          
 /* ================================================================ Transitions (core/include/Spirit/Transitions.h) */
 void Transition_Homogeneous( State * state, int idx_1, int idx_2, int idx_chain );        /* :29 */
 
+/* ================================================================ Parameters_MC (core/include/Spirit/Parameters_MC.h) */
+void Parameters_MC_Set_Output_Tag( State * state, const char * tag, int idx_image, int idx_chain );       /* :30 */
+void Parameters_MC_Set_Output_Folder( State * state, const char * folder, int idx_image, int idx_chain ); /* :34 */
+void Parameters_MC_Set_Output_General( State * state, bool any, bool initial, bool final, int idx_image,
+                                       int idx_chain );                                                    /* :37 */
+void Parameters_MC_Set_Output_Energy( State * state, bool energy_step, bool energy_archive, bool energy_spin_resolved,
+                                      bool energy_divide_by_nos, bool energy_add_readability_lines, int idx_image,
+                                      int idx_chain );                                                     /* :49 */
+void Parameters_MC_Set_Output_Configuration( State * state, bool configuration_step, bool configuration_archive,
+                                             int configuration_filetype, int idx_image, int idx_chain );   /* :60 */
+void Parameters_MC_Set_N_Iterations( State * state, int n_iterations, int n_iterations_log, int idx_image,
+                                     int idx_chain );                                                      /* :70 */
+void Parameters_MC_Set_Temperature( State * state, float T, int idx_image, int idx_chain );                /* :79 */
+void Parameters_MC_Set_Metropolis_Cone( State * state, bool cone, float cone_angle, bool adaptive_cone,
+                                        float target_acceptance_ratio, int idx_image, int idx_chain );    /* :89 */
+/* random_sample is stored; the device sweeps are colour-ordered in every case */
+void Parameters_MC_Set_Random_Sample( State * state, bool random_sample, int idx_image, int idx_chain );  /* :94 */
+const char * Parameters_MC_Get_Output_Tag( State * state, int idx_image, int idx_chain );                /* :103 */
+const char * Parameters_MC_Get_Output_Folder( State * state, int idx_image, int idx_chain );             /* :106 */
+void Parameters_MC_Get_Output_General( State * state, bool * any, bool * initial, bool * final, int idx_image,
+                                       int idx_chain );                                                   /* :109 */
+void Parameters_MC_Get_Output_Energy( State * state, bool * energy_step, bool * energy_archive,
+                                      bool * energy_spin_resolved, bool * energy_divide_by_nos,
+                                      bool * energy_add_readability_lines, int idx_image, int idx_chain ); /* :113 */
+void Parameters_MC_Get_Output_Configuration( State * state, bool * configuration_step, bool * configuration_archive,
+                                             int * configuration_filetype, int idx_image, int idx_chain ); /* :118 */
+void Parameters_MC_Get_N_Iterations( State * state, int * iterations, int * iterations_log, int idx_image,
+                                     int idx_chain );                                                     /* :123 */
+float Parameters_MC_Get_Temperature( State * state, int idx_image, int idx_chain );                       /* :132 */
+void Parameters_MC_Get_Metropolis_Cone( State * state, bool * cone, float * cone_angle, bool * adaptive_cone,
+                                        float * target_acceptance_ratio, int idx_image, int idx_chain );  /* :142 */
+bool Parameters_MC_Get_Random_Sample( State * state, int idx_image, int idx_chain );                      /* :147 */
+
 /* ================================================================ Parameters_LLG (core/include/Spirit/Parameters_LLG.h) */
 void Parameters_LLG_Set_Output_General( State * state, bool any, bool initial, bool final, int idx_image,
                                         int idx_chain );                                  /* :37 (accepted, no files written) */
@@ -210,6 +243,9 @@ int Parameters_GNEB_Get_N_Energy_Interpolations( State * state, int idx_chain );
 
 /* ================================================================ Simulation (core/include/Spirit/Simulation.h) */
 void free_run_info( Simulation_Run_Info info );                                           /* :73 */
+/* Monte Carlo: colour-ordered Metropolis sweeps on the device */
+void Simulation_MC_Start( State * state, int n_iterations, int n_iterations_log, bool singleshot,
+                          Simulation_Run_Info * info, int idx_image, int idx_chain );               /* :81 */
 void Simulation_LLG_Start( State * state, int solver_type, int n_iterations, int n_iterations_log, bool singleshot,
                            Simulation_Run_Info * info, int idx_image, int idx_chain );    /* :86 */
 void Simulation_GNEB_Start( State * state, int solver_type, int n_iterations, int n_iterations_log, bool singleshot,

@@ -64,6 +64,10 @@ def lib():
         L.og_philox4x32.argtypes = [P(ctypes.c_uint32), P(ctypes.c_uint32), P(ctypes.c_uint32)]
         L.og_llg_run.argtypes = [vp, vp, i, i, P(d), P(d), P(d)]
         L.og_gneb_run.argtypes = [vp, vp, i, i, P(d), P(i), P(d), P(d), P(d)]
+        L.og_mc_colors.argtypes = [vp, P(i)]
+        L.og_mc_colors.restype = i
+        L.og_mc_run.argtypes = [vp, vp, i, P(d), P(d), P(d)]
+        L.og_mc_run.restype = i
         L.og_gneb_image_types_auto.argtypes = [i, P(d), P(i)]
         L.og_transition_homogeneous.argtypes = [i, i, P(d), i, i]
         _lib = L
@@ -91,6 +95,18 @@ class GNEBParams(ctypes.Structure):
         ("spring_constant", ctypes.c_double),
         ("force_convergence", ctypes.c_double),
         ("dt", ctypes.c_double),
+    ]
+
+
+class MCParams(ctypes.Structure):
+    _fields_ = [
+        ("temperature", ctypes.c_double),
+        ("cone", ctypes.c_int),
+        ("cone_angle_deg", ctypes.c_double),
+        ("adaptive", ctypes.c_int),
+        ("acceptance_target", ctypes.c_double),
+        ("seed", ctypes.c_uint64),
+        ("stream", ctypes.c_uint32),
     ]
 
 
@@ -266,6 +282,22 @@ class OracleSystem:
         it = lib().og_llg_run(self.h, ctypes.byref(p), solver_id, int(n_iter), _p(s), ctypes.byref(E),
                               ctypes.byref(mt))
         return s, {"iterations": it, "energy": E.value, "max_torque": mt.value}
+
+    def mc_colors(self):
+        """Greedy colouring of the interaction graph (the Monte Carlo sweep order)."""
+        c = np.zeros(self.nos, dtype=np.int32)
+        n = lib().og_mc_colors(self.h, _p(c, ctypes.c_int))
+        return c, n
+
+    def mc(self, spins, n_sweeps, temperature=0.0, cone=True, cone_angle=30.0, adaptive=True, target=0.5,
+           seed=2006, stream=0):
+        """Metropolis sweeps (Method_MC with colour-ordered sweeps and Philox draws); returns
+        (spins, {"cone_angle": deg, "acceptance": ratio})."""
+        s = np.ascontiguousarray(spins, dtype=np.float64).copy()
+        p = MCParams(temperature, int(cone), cone_angle, int(adaptive), target, seed, stream)
+        ca, ac = ctypes.c_double(), ctypes.c_double()
+        lib().og_mc_run(self.h, ctypes.byref(p), int(n_sweeps), _p(s), ctypes.byref(ca), ctypes.byref(ac))
+        return s, {"cone_angle": ca.value, "acceptance": ac.value}
 
     def gneb(self, chain, n_iter, image_type=None, spring_constant=1.0, force_convergence=1e-6, dt=1e-3):
         c = np.ascontiguousarray(chain, dtype=np.float64).copy()

@@ -1762,3 +1762,193 @@ void og_transition_homogeneous( int nos, int noi, double * chain, int idx_1, int
         }
     }
 }
+
+/* ================================================================ Monte Carlo */
+/* Neighbours of spin i over the exchange and DMI pair lists (both redundant), -1 skipped. */
+static int mc_neighbours( const og_system * s, int i, int * out, int cap )
+{
+    int n  = 0;
+    int ib = i % s->n_cell_atoms;
+    for( int p = 0; p < s->n_ex && n < cap; ++p )
+        if( s->ex_pairs[p].i == ib )
+        {
+            int j = idx_from_pair( s, i, &s->ex_pairs[p] );
+            if( j >= 0 )
+                out[n++] = j;
+        }
+    for( int p = 0; p < s->n_dmi && n < cap; ++p )
+        if( s->dmi_pairs[p].i == ib )
+        {
+            int j = idx_from_pair( s, i, &s->dmi_pairs[p] );
+            if( j >= 0 )
+                out[n++] = j;
+        }
+    return n;
+}
+
+/* greedy colouring in spin order: the smallest colour no already coloured neighbour has */
+int og_mc_colors( const og_system * s, int * colors )
+{
+    int nc = 0;
+    int nbr[512];
+    for( int i = 0; i < s->nos; ++i )
+        colors[i] = -1;
+    for( int i = 0; i < s->nos; ++i )
+    {
+        int n      = mc_neighbours( s, i, nbr, 512 );
+        int c      = 0;
+        int change = 1;
+        while( change )
+        {
+            change = 0;
+            for( int k = 0; k < n; ++k )
+                if( nbr[k] != i && colors[nbr[k]] == c )
+                {
+                    ++c;
+                    change = 1;
+                }
+        }
+        colors[i] = c;
+        if( c + 1 > nc )
+            nc = c + 1;
+    }
+    return nc;
+}
+
+/* Energy_Single_Spin (Hamiltonian_Heisenberg.cpp:559-668, OpenMP build) of spin i set to v, the
+ * other spins fixed: Zeeman, anisotropy, exchange and DMI pairs with pair.i == basis(i); no DDI.
+ * The pair terms are written -v . h with h = sum_p (J_p s_j + D_p s_j x n_p). */
+static double mc_energy_single( const og_system * s, const double * spins, int i, const double * v, const double * h )
+{
+    int ib   = i % s->n_cell_atoms;
+    double E = 0;
+    if( has_zeeman( s ) )
+        E -= s->mu_s[i] * s->field_mag * dot3( s->field_normal, v );
+    for( int k = 0; k < s->n_aniso; ++k )
+        if( s->aniso_idx[k] == ib )
+        {
+            double d = dot3( s->aniso_normal[k], v );
+            E -= s->aniso_mag[k] * d * d;
+        }
+    E -= dot3( v, h );
+    (void)spins;
+    return E;
+}
+
+static void mc_pair_field( const og_system * s, const double * spins, int i, double * h )
+{
+    int ib = i % s->n_cell_atoms;
+    h[0] = h[1] = h[2] = 0;
+    for( int p = 0; p < s->n_ex; ++p )
+        if( s->ex_pairs[p].i == ib )
+        {
+            int j = idx_from_pair( s, i, &s->ex_pairs[p] );
+            if( j >= 0 )
+                for( int e = 0; e < 3; ++e )
+                    h[e] += s->ex_mag[p] * spins[3 * j + e];
+        }
+    for( int p = 0; p < s->n_dmi; ++p )
+        if( s->dmi_pairs[p].i == ib )
+        {
+            int j = idx_from_pair( s, i, &s->dmi_pairs[p] );
+            if( j >= 0 )
+            {
+                double c[3];
+                cross3( spins + 3 * j, s->dmi_normal + 3 * p, c );
+                for( int e = 0; e < 3; ++e )
+                    h[e] += s->dmi_mag[p] * c[e];
+            }
+        }
+}
+
+int og_mc_run( og_system * s, const og_mc_params * p, int n_sweeps, double * spins, double * cone_out, double * acc_out )
+{
+    int * colors = (int *)malloc( sizeof( int ) * (size_t)s->nos );
+    int nc       = og_mc_colors( s, colors );
+    double cone  = C_PI * p->cone_angle_deg / 180.0;
+    double acc   = p->acceptance_target;
+    long n_rej   = 0;
+    const double kT  = C_K_B * p->temperature;
+    const double dif = 0.01;
+    uint32_t key[2]  = { (uint32_t)p->seed, (uint32_t)( p->seed >> 32 ) };
+    for( int it = 0; it < n_sweeps; ++it )
+    {
+        /* cone angle feedback from the previous sweep's rejections (Method_MC.cpp:73-89) */
+        if( p->cone && p->adaptive )
+        {
+            acc = 1.0 - (double)n_rej / (double)s->nos;
+            if( acc < p->acceptance_target && cone > dif )
+                cone -= dif;
+            if( acc > p->acceptance_target && cone < C_PI - dif )
+                cone += dif;
+        }
+        n_rej                 = 0;
+        const double cos_cone = cos( cone );
+        for( int c = 0; c < nc; ++c )
+        {
+#pragma omp parallel for reduction( + : n_rej )
+            for( int i = 0; i < s->nos; ++i )
+            {
+                if( colors[i] != c )
+                    continue;
+                uint32_t ctr[4] = { (uint32_t)i, (uint32_t)it, p->stream, 0x4D435300u };
+                uint32_t x[4];
+                og_philox4x32( ctr, key, x );
+                const double sc = 1.0 / 8388608.0;
+                const double u0 = ( (double)( x[0] >> 9 ) + 0.5 ) * sc;
+                const double u1 = ( (double)( x[1] >> 9 ) + 0.5 ) * sc;
+                const double u2 = ( (double)( x[2] >> 9 ) + 0.5 ) * sc;
+                double * so     = spins + 3 * i;
+                double e0[3] = { 1, 0, 0 }, e1[3] = { 0, 1, 0 }, e2[3] = { 0, 0, 1 };
+                double ct;
+                if( p->cone )
+                {
+                    /* local basis with the spin as third axis (Method_MC.cpp:113-123) */
+                    if( so[2] < 1 - 1e-10 )
+                    {
+                        const double ez[3] = { 0, 0, 1 };
+                        e2[0] = so[0];
+                        e2[1] = so[1];
+                        e2[2] = so[2];
+                        cross3( e2, ez, e0 );
+                        normalize3( e0 );
+                        cross3( e2, e0, e1 );
+                    }
+                    ct = 1 - ( 1 - cos_cone ) * u0;
+                }
+                else
+                    ct = u0; /* the reference samples cos(theta) in [0, 1) here */
+                const double st  = sqrt( 1 - ct * ct );
+                const double phi = 2 * C_PI * u1;
+                const double l[3] = { st * cos( phi ), st * sin( phi ), ct };
+                double v[3];
+                for( int e = 0; e < 3; ++e )
+                    v[e] = e0[e] * l[0] + e1[e] * l[1] + e2[e] * l[2];
+                double h[3];
+                mc_pair_field( s, spins, i, h );
+                const double Eold = mc_energy_single( s, spins, i, so, h );
+                const double Enew = mc_energy_single( s, spins, i, v, h );
+                const double dE   = Enew - Eold;
+                int reject        = 0;
+                if( dE > 1e-14 )
+                {
+                    if( p->temperature < 1e-12 )
+                        reject = 1;
+                    else if( exp( -dE / kT ) < u2 )
+                        reject = 1;
+                }
+                if( reject )
+                    ++n_rej;
+                else
+                    for( int e = 0; e < 3; ++e )
+                        so[e] = v[e];
+            }
+        }
+    }
+    if( cone_out )
+        *cone_out = cone * 180.0 / C_PI;
+    if( acc_out )
+        *acc_out = acc;
+    free( colors );
+    return n_sweeps;
+}

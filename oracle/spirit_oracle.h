@@ -114,6 +114,27 @@ void og_gneb_image_types_auto( int noi, const double * energies, int * image_typ
 /* Transition_Homogeneous (geodesic interpolation between images idx_1 and idx_2) */
 void og_transition_homogeneous( int nos, int noi, double * chain, int idx_1, int idx_2 );
 
+/* Monte Carlo (Method_MC, core/src/engine/Method_MC.cpp): Metropolis sweeps with cone sampling
+ * and the adaptive cone.  A sweep visits the spins colour by colour (greedy colouring of the
+ * interaction graph in spin order: spins of one colour never interact), drawing per spin and
+ * sweep one Philox4x32-10 block (counter (i, sweep, stream, 0x4D435300), key = seed): u0 for
+ * cos(theta), u1 for phi, u2 for the Metropolis test. */
+typedef struct og_mc_params
+{
+    double temperature;
+    int cone;
+    double cone_angle_deg;
+    int adaptive;
+    double acceptance_target;
+    uint64_t seed;
+    uint32_t stream;
+} og_mc_params;
+/* colour of every spin (colors[nos]); returns the number of colours */
+int og_mc_colors( const og_system * s, int * colors );
+/* n_sweeps sweeps, spins in/out; cone_angle_deg_out / acceptance_out: state after the run */
+int og_mc_run( og_system * s, const og_mc_params * p, int n_sweeps, double * spins, double * cone_angle_deg_out,
+               double * acceptance_out );
+
 #ifdef __cplusplus
 }
 #endif

@@ -9,6 +9,7 @@
 #include "adjoint.hpp"
 #include "config.hpp"
 #include "gneb.hpp"
+#include "mc.hpp"
 #include "state.hpp"
 #include "util.hpp"
 
@@ -232,6 +233,86 @@ void geometry_changed( State * st )
 }
 
 } // namespace
+
+// Monte Carlo run of one image: its own engine (precision of the State) and colouring
+struct MCImageRun
+{
+    std::unique_ptr<Engine> eng;
+    std::unique_ptr<MCRun> mc;
+    long version = -1;
+    bool fp64    = false;
+};
+
+MCImageRun & mc_image_run( State * st, Image & img )
+{
+    const bool fp64 = st->precision == 64;
+    auto * r        = static_cast<MCImageRun *>( img.mc_run.get() );
+    if( !r || r->version != img.version || r->fp64 != fp64 )
+    {
+        auto nr     = std::make_shared<MCImageRun>();
+        nr->eng     = std::make_unique<Engine>( std::vector<SystemInput>{ input_of( img, 0 ) }, fp64 );
+        nr->mc      = std::make_unique<MCRun>( *nr->eng );
+        nr->version = img.version;
+        nr->fp64    = fp64;
+        img.mc_run  = nr;
+        r           = nr.get();
+    }
+    r->eng->set_stream( (cudaStream_t)st->stream );
+    return *r;
+}
+
+MCSettings mc_settings_of( const Image & img )
+{
+    MCSettings m;
+    m.temperature       = img.mc.temperature;
+    m.cone              = img.mc.step_cone;
+    m.cone_angle_deg    = img.mc.cone_angle;
+    m.adaptive          = img.mc.cone_adaptive;
+    m.acceptance_target = img.mc.acceptance_target;
+    m.seed              = (unsigned long long)(unsigned)img.mc.rng_seed;
+    m.stream            = 0;
+    m.n_iterations      = (int)img.mc.n_iterations;
+    m.rng_offset        = img.mc_sweeps_drawn;
+    return m;
+}
+
+void finish_mc( Image & img, MCImageRun & R )
+{
+    auto st = R.mc->status()[0];
+    R.eng->get_spins( 0, img.spins.data() );
+    img.mc_sweeps_drawn += (unsigned)( st.iteration - img.info.iteration );
+    img.info.iteration = st.iteration;
+    // the cone angle adapts during the run and is kept (Method_MC.cpp:85)
+    if( img.mc.step_cone && img.mc.cone_adaptive )
+        img.mc.cone_angle = st.cone_angle_deg;
+    // the energy of the final state (Method_MC::Message_End -> UpdateEnergy)
+    update_data( img );
+    auto now         = std::chrono::steady_clock::now();
+    img.info.wall_ms = std::chrono::duration_cast<std::chrono::milliseconds>( now - img.info.t_start ).count();
+    img.info.ips     = img.info.wall_ms > 0 ? 1000.0 * st.iteration / img.info.wall_ms : 0.0;
+}
+
+// Method::Iterate for MC: sweeps in device chunks, host checks in between
+void iterate_mc( Image & img, MCImageRun & R )
+{
+    int chunk = 8;
+    auto t0   = std::chrono::steady_clock::now();
+    while( true )
+    {
+        auto s = R.mc->status()[0];
+        if( s.iteration >= img.mc.n_iterations || !img.iteration_allowed.load() || stop_file_present() )
+            break;
+        if( img.mc.max_walltime_sec > 0 )
+        {
+            double el = std::chrono::duration<double>( std::chrono::steady_clock::now() - t0 ).count();
+            if( el > img.mc.max_walltime_sec )
+                break;
+        }
+        R.mc->launch( chunk );
+        chunk = std::min( 512, chunk * 2 );
+    }
+    finish_mc( img, R );
+}
 
 // adjoint driver behind Simulation_LLG_Adjoint / Simulation_LLG_Loss
 namespace
@@ -1795,6 +1876,47 @@ void free_run_info( Simulation_Run_Info info ) noexcept
 }
 
 // Simulation_LLG_Start (core/src/Spirit/Simulation.cpp:134-217)
+// Simulation_MC_Start (core/src/Spirit/Simulation.cpp:77-132)
+void Simulation_MC_Start( State * state, int n_iterations, int n_iterations_log, bool singleshot,
+                          Simulation_Run_Info * info, int idx_image, int idx_chain ) noexcept
+{
+    try
+    {
+        auto I     = from_indices( state, idx_image, idx_chain );
+        auto & img = *I.img;
+        std::lock_guard<std::recursive_mutex> lk( img.mtx );
+        if( img.iteration_allowed || I.chain->iteration_allowed )
+        {
+            log_msg( state, 2, "Tried to use Simulation_Start on an image, but there is already a simulation running." );
+            return;
+        }
+        if( n_iterations > 0 )
+            img.mc.n_iterations = n_iterations;
+        if( n_iterations_log > 0 )
+            img.mc.n_iterations_log = n_iterations_log;
+        img.iteration_allowed  = true;
+        img.singleshot_allowed = singleshot;
+        img.info               = MethodInfo{};
+        img.info.method        = "MC";
+        img.info.solver        = "None";
+        img.info.solver_id     = -1;
+        img.info.n_iterations  = (int)img.mc.n_iterations;
+        img.info.t_start       = std::chrono::steady_clock::now();
+        MCImageRun & R         = mc_image_run( state, img );
+        R.eng->set_spins( 0, img.spins.data() );
+        R.mc->start( { mc_settings_of( img ) } );
+        if( singleshot )
+            return;
+        iterate_mc( img, R );
+        img.iteration_allowed = false;
+        fill_run_info( info, img.info );
+    }
+    catch( ... )
+    {
+        handle( state, "Simulation_MC_Start" );
+    }
+}
+
 void Simulation_LLG_Start( State * state, int solver_type, int n_iterations, int n_iterations_log, bool singleshot,
                            Simulation_Run_Info * info, int idx_image, int idx_chain ) noexcept
 {
@@ -1873,6 +1995,19 @@ void Simulation_N_Shot( State * state, int N, int idx_image, int idx_chain ) noe
         if( !( img.iteration_allowed && img.singleshot_allowed ) )
         {
             log_msg( state, 2, "Tried to use Simulation_SingleShot but no SingleShot simulation has been started." );
+            return;
+        }
+        if( img.info.method == "MC" )
+        {
+            MCImageRun & R = mc_image_run( state, img );
+            R.eng->set_spins( 0, img.spins.data() );
+            R.mc->launch( N );
+            finish_mc( img, R );
+            if( img.info.iteration >= img.mc.n_iterations || stop_file_present() )
+            {
+                img.iteration_allowed  = false;
+                img.singleshot_allowed = false;
+            }
             return;
         }
         if( img.info.solver_id == SOLVER_VP )
@@ -2335,6 +2470,151 @@ double Simulation_LLG_Loss( State * state, const double * params, int n_steps, c
         return 0;
     }
 }
+
+// ============================================================== Parameters_MC (core/include/Spirit/Parameters_MC.h)
+#define MC_IMG( fn_name, body )                                                                                        \
+    try                                                                                                                \
+    {                                                                                                                  \
+        auto I   = from_indices( state, idx_image, idx_chain );                                                        \
+        auto & M = I.img->mc;                                                                                          \
+        body;                                                                                                          \
+    }                                                                                                                  \
+    catch( ... )                                                                                                       \
+    {                                                                                                                  \
+        handle( state, fn_name );                                                                                      \
+    }
+
+void Parameters_MC_Set_Output_Tag( State * state, const char * tag, int idx_image, int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Set_Output_Tag", M.output_tag = tag ? tag : "" )
+}
+void Parameters_MC_Set_Output_Folder( State * state, const char * folder, int idx_image, int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Set_Output_Folder", M.output_folder = folder ? folder : "" )
+}
+void Parameters_MC_Set_Output_General( State * state, bool any, bool initial, bool final, int idx_image,
+                                       int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Set_Output_General", M.output_any = any; M.output_initial = initial; M.output_final = final )
+}
+void Parameters_MC_Set_Output_Energy( State * state, bool energy_step, bool energy_archive, bool energy_spin_resolved,
+                                      bool energy_divide_by_nos, bool energy_add_readability_lines, int idx_image,
+                                      int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Set_Output_Energy", M.output_energy_step = energy_step;
+            M.output_energy_archive = energy_archive; M.output_energy_spin_resolved = energy_spin_resolved;
+            M.output_energy_divide_by_nspins = energy_divide_by_nos;
+            M.output_energy_add_readability_lines = energy_add_readability_lines )
+}
+void Parameters_MC_Set_Output_Configuration( State * state, bool configuration_step, bool configuration_archive,
+                                             int configuration_filetype, int idx_image, int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Set_Output_Configuration", M.output_configuration_step = configuration_step;
+            M.output_configuration_archive = configuration_archive;
+            M.output_configuration_filetype = configuration_filetype )
+}
+void Parameters_MC_Set_N_Iterations( State * state, int n_iterations, int n_iterations_log, int idx_image,
+                                     int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Set_N_Iterations", M.n_iterations = n_iterations; M.n_iterations_log = n_iterations_log )
+}
+void Parameters_MC_Set_Temperature( State * state, float T, int idx_image, int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Set_Temperature", M.temperature = T )
+}
+void Parameters_MC_Set_Metropolis_Cone( State * state, bool cone, float cone_angle, bool adaptive_cone,
+                                        float target_acceptance_ratio, int idx_image, int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Set_Metropolis_Cone", M.step_cone = cone; M.cone_angle = cone_angle;
+            M.cone_adaptive = adaptive_cone; M.acceptance_target = target_acceptance_ratio )
+}
+void Parameters_MC_Set_Random_Sample( State * state, bool random_sample, int idx_image, int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Set_Random_Sample", M.random_sample = random_sample )
+}
+const char * Parameters_MC_Get_Output_Tag( State * state, int idx_image, int idx_chain ) noexcept
+{
+    try
+    {
+        return from_indices( state, idx_image, idx_chain ).img->mc.output_tag.c_str();
+    }
+    catch( ... )
+    {
+        handle( state, "Parameters_MC_Get_Output_Tag" );
+        return "";
+    }
+}
+const char * Parameters_MC_Get_Output_Folder( State * state, int idx_image, int idx_chain ) noexcept
+{
+    try
+    {
+        return from_indices( state, idx_image, idx_chain ).img->mc.output_folder.c_str();
+    }
+    catch( ... )
+    {
+        handle( state, "Parameters_MC_Get_Output_Folder" );
+        return "";
+    }
+}
+void Parameters_MC_Get_Output_General( State * state, bool * any, bool * initial, bool * final, int idx_image,
+                                       int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Get_Output_General", *any = M.output_any; *initial = M.output_initial;
+            *final = M.output_final )
+}
+void Parameters_MC_Get_Output_Energy( State * state, bool * energy_step, bool * energy_archive,
+                                      bool * energy_spin_resolved, bool * energy_divide_by_nos,
+                                      bool * energy_add_readability_lines, int idx_image, int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Get_Output_Energy", *energy_step = M.output_energy_step;
+            *energy_archive = M.output_energy_archive; *energy_spin_resolved = M.output_energy_spin_resolved;
+            *energy_divide_by_nos = M.output_energy_divide_by_nspins;
+            *energy_add_readability_lines = M.output_energy_add_readability_lines )
+}
+void Parameters_MC_Get_Output_Configuration( State * state, bool * configuration_step, bool * configuration_archive,
+                                             int * configuration_filetype, int idx_image, int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Get_Output_Configuration", *configuration_step = M.output_configuration_step;
+            *configuration_archive = M.output_configuration_archive;
+            *configuration_filetype = M.output_configuration_filetype )
+}
+void Parameters_MC_Get_N_Iterations( State * state, int * iterations, int * iterations_log, int idx_image,
+                                     int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Get_N_Iterations", *iterations = (int)M.n_iterations;
+            *iterations_log = (int)M.n_iterations_log )
+}
+float Parameters_MC_Get_Temperature( State * state, int idx_image, int idx_chain ) noexcept
+{
+    try
+    {
+        return (float)from_indices( state, idx_image, idx_chain ).img->mc.temperature;
+    }
+    catch( ... )
+    {
+        handle( state, "Parameters_MC_Get_Temperature" );
+        return 0;
+    }
+}
+void Parameters_MC_Get_Metropolis_Cone( State * state, bool * cone, float * cone_angle, bool * adaptive_cone,
+                                        float * target_acceptance_ratio, int idx_image, int idx_chain ) noexcept
+{
+    MC_IMG( "Parameters_MC_Get_Metropolis_Cone", *cone = M.step_cone; *cone_angle = (float)M.cone_angle;
+            *adaptive_cone = M.cone_adaptive; *target_acceptance_ratio = (float)M.acceptance_target )
+}
+bool Parameters_MC_Get_Random_Sample( State * state, int idx_image, int idx_chain ) noexcept
+{
+    try
+    {
+        return from_indices( state, idx_image, idx_chain ).img->mc.random_sample;
+    }
+    catch( ... )
+    {
+        handle( state, "Parameters_MC_Get_Random_Sample" );
+        return false;
+    }
+}
+#undef MC_IMG
 
 // ============================================================== System (core/include/Spirit/System.h)
 int System_Get_Index( State * state ) noexcept

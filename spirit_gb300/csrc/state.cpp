@@ -263,6 +263,18 @@ std::shared_ptr<Image> make_image_from_config( const std::string & path, State &
             L.max_walltime_sec = parse_walltime( wt );
         cf.get( "llg_output_folder", L.output_folder );
         cf.get( "output_file_tag", L.output_tag );
+        // ---- MC (Parameters_Method_MC_from_Config, core/src/io/Configparser.cpp:910-990)
+        MCParams & M = img->mc;
+        cf.get( "mc_seed", M.rng_seed );
+        cf.get( "mc_n_iterations", M.n_iterations );
+        cf.get( "mc_n_iterations_log", M.n_iterations_log );
+        cf.get( "mc_temperature", M.temperature );
+        cf.get( "mc_acceptance_ratio", M.acceptance_target );
+        std::string mwt;
+        if( cf.get( "mc_max_walltime", mwt ) )
+            M.max_walltime_sec = parse_walltime( mwt );
+        cf.get( "mc_output_folder", M.output_folder );
+        cf.get( "output_file_tag", M.output_tag );
     }
     else
     {
@@ -305,6 +317,7 @@ std::shared_ptr<Image> clone_image( const Image & src )
     img->geom      = src.geom; // geometry is shared by all images of a chain
     img->ham       = src.ham;
     img->llg       = src.llg;
+    img->mc        = src.mc;
     img->spins     = src.spins;
     img->eff_field = src.eff_field;
     img->positions = src.positions;

@@ -33,6 +33,28 @@ struct LLGParams
     std::string output_tag    = "<time>";
 };
 
+// Parameters_Method_MC (core/include/data/Parameters_Method_MC.hpp) and the generic method part
+struct MCParams
+{
+    double temperature            = 0;
+    int rng_seed                  = 2006;
+    bool random_sample            = true;
+    bool step_cone                = true;
+    bool cone_adaptive            = true;
+    double cone_angle             = 30; // degrees
+    double acceptance_target      = 0.5;
+    long n_iterations             = 1000000;
+    long n_iterations_log         = 1000;
+    long max_walltime_sec         = 0;
+    std::string output_folder     = "output";
+    std::string output_tag        = "<time>";
+    bool output_any = false, output_initial = false, output_final = false;
+    bool output_energy_step = false, output_energy_archive = false, output_energy_spin_resolved = false;
+    bool output_energy_divide_by_nspins = true, output_energy_add_readability_lines = false;
+    bool output_configuration_step = false, output_configuration_archive = false;
+    int output_configuration_filetype = 3;
+};
+
 struct GNEBParams
 {
     double spring_constant          = 1;
@@ -69,6 +91,7 @@ struct Image
     std::shared_ptr<Geometry> geom;
     HamiltonianParams ham;
     LLGParams llg;
+    MCParams mc;
     std::vector<double> spins;     // API mirror, AoS
     std::vector<double> eff_field; // AoS
     std::vector<double> positions; // AoS
@@ -87,6 +110,8 @@ struct Image
     long run_version  = -1;
     bool run_fp64     = false;
     std::shared_ptr<void> vp_run; // single-shot LLG run with the VP solver
+    std::shared_ptr<void> mc_run; // Monte Carlo run (engine + colouring) of this image
+    unsigned int mc_sweeps_drawn = 0; // Monte Carlo sweeps done so far (position in the random stream)
 
     int nos() const
     {

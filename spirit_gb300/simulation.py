@@ -55,10 +55,17 @@ _Set_Precision = fn("Simulation_Set_Precision", [_vp, _i])
 _Get_Precision = fn("Simulation_Get_Precision", [_vp], _i)
 
 
+_MC_Start = fn("Simulation_MC_Start", [_vp, _i, _i, _b, ctypes.c_void_p, _i, _i])
+
+
 def start(p_state, method_type, solver_type=None, n_iterations=-1, n_iterations_log=-1, single_shot=False,
           idx_image=-1, idx_chain=-1):
     info = simulation_run_info()
-    if method_type == METHOD_LLG:
+    if method_type == METHOD_MC:
+        spiritlib.wrap_function(_MC_Start, [_vp(p_state), _i(n_iterations), _i(n_iterations_log), _b(single_shot),
+                                            ctypes.cast(ctypes.pointer(info), ctypes.c_void_p), _i(idx_image),
+                                            _i(idx_chain)])
+    elif method_type == METHOD_LLG:
         spiritlib.wrap_function(_LLG_Start, [_vp(p_state), _i(solver_type), _i(n_iterations), _i(n_iterations_log),
                                              _b(single_shot), ctypes.pointer(info), _i(idx_image), _i(idx_chain)])
     elif method_type == METHOD_GNEB:
