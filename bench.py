@@ -445,6 +445,42 @@ def run_adjoint(n_steps=2000, checkpoint=100):
     }
 
 
+def run_mc(sweeps=200):
+    """Monte Carlo on the C2 lattice (SC 128x128x16; the single-spin energy has no dipolar term):
+    Metropolis sweeps at T = 10 K with the adaptive cone, FP32, timed by wall clock around
+    Simulation_MC_Start after a warm-up run; CPU: the oracle's sweep (FP64, OpenMP) on a sample."""
+    from oracle.oracle import OracleSystem, random_spins
+    from spirit_gb300 import simulation, state, system
+    from spirit_gb300.configs import write_config
+    import spirit_gb300.parameters.mc as mc
+
+    spec = dict(SPEC)
+    spec.pop("ddi", None)
+    p = state.setup(write_config(spec, os.path.join(tempfile.mkdtemp(), "mc.cfg")), True)
+    simulation.set_precision(p, 32)
+    system.get_spin_directions(p)[:] = random_spins(NOS, 5)
+    mc.set_temperature(p, 10.0)
+    simulation.start(p, simulation.METHOD_MC, n_iterations=16)
+    t0 = time.perf_counter()
+    info = simulation.start(p, simulation.METHOD_MC, n_iterations=sweeps)
+    dt = time.perf_counter() - t0
+    state.delete(p)
+    o = OracleSystem(spec)
+    s = random_spins(NOS, 5)
+    c0 = time.perf_counter()
+    o.mc(s, 3, temperature=10.0)
+    cpu_s = time.perf_counter() - c0
+    return {
+        "workload": "Metropolis Monte Carlo, SC 128x128x16 (J=1, D=0.2, K=0.05 meV, B=0.5 T), T=10 K, adaptive cone, "
+                    "colour-ordered sweeps, FP32",
+        "sweeps": int(info.total_iterations), "wall_s": dt, "value": NOS * int(info.total_iterations) / dt,
+        "unit": "spin-updates/s",
+        "timing": "wall clock of Simulation_MC_Start (host checks between device chunks included)",
+        "cpu_baseline": {"value": NOS * 3 / cpu_s, "unit": "spin-updates/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": "3 sweeps of the same lattice (FP64, OpenMP)"},
+    }
+
+
 def run_gb300(args):
     import torch
 
@@ -540,6 +576,7 @@ def run_gb300(args):
     batched = run_batched_vs_plain(max(20, args.steps), max(3, args.warmup)) if args.batched else None
     gneb_line = run_gneb() if args.gneb and rank == 0 else None
     adj_line = run_adjoint() if args.adjoint and rank == 0 else None
+    mc_line = run_mc() if args.mc and rank == 0 else None
     if rank != 0:
         return
     cpu = cpu_baseline() if world == 1 else None
@@ -564,6 +601,8 @@ def run_gb300(args):
         line["gneb"] = gneb_line
     if adj_line is not None:
         line["adjoint"] = adj_line
+    if mc_line is not None:
+        line["mc"] = mc_line
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -581,6 +620,7 @@ def main():
                     help="skip the 32-image GNEB measurement")
     ap.add_argument("--only-gneb", action="store_true", help="run and print only the GNEB measurement")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false", help="skip the adjoint measurement")
+    ap.add_argument("--no-mc", dest="mc", action="store_false", help="skip the Monte Carlo measurement")
     ap.add_argument("--only-adjoint", action="store_true", help="run and print only the adjoint measurement")
     ap.add_argument("--only-batched", action="store_true",
                     help="run and print only the 256-system batched-vs-plain measurement (profiling)")

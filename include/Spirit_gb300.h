@@ -167,6 +167,30 @@ void Chain_Setup_Data( State * state, int idx_chain );                          
 /* ================================================================ Transitions (core/include/Spirit/Transitions.h) */
 void Transition_Homogeneous( State * state, int idx_1, int idx_2, int idx_chain );        /* :29 */
 
+/* ================================================================ IO (core/include/Spirit/IO.h)
+ * OVF 2.0 files; format: 0 binary in the API precision (8 bytes), 1 binary 4, 2 binary 8, 3 text,
+ * 4 CSV (IO.h:26-38).  Segments written here carry the image's random-stream positions (LLG noise
+ * iterations, Metropolis sweeps) in a Desc line; reading such a segment restores them, so a run
+ * resumed from the file continues the same Philox streams. */
+#define IO_Fileformat_OVF_bin 0
+#define IO_Fileformat_OVF_bin4 1
+#define IO_Fileformat_OVF_bin8 2
+#define IO_Fileformat_OVF_text 3
+#define IO_Fileformat_OVF_csv 4
+void IO_Positions_Write( State * state, const char * file, int format, const char * comment, int idx_image,
+                         int idx_chain );                                                  /* :50 */
+int IO_N_Images_In_File( State * state, const char * file, int idx_image, int idx_chain ); /* :60 */
+void IO_Image_Read( State * state, const char * file, int idx_image_infile, int idx_image_inchain,
+                    int idx_chain );                                                       /* :63 */
+void IO_Image_Write( State * state, const char * file, int format, const char * comment, int idx_image,
+                     int idx_chain );                                                      /* :67 */
+void IO_Image_Append( State * state, const char * file, int format, const char * comment, int idx_image,
+                      int idx_chain );                                                     /* :72 */
+void IO_Chain_Read( State * state, const char * file, int start_image_infile, int end_image_infile, int insert_idx,
+                    int idx_chain );                                                       /* :87 */
+void IO_Chain_Write( State * state, const char * file, int format, const char * comment, int idx_chain ); /* :92 */
+void IO_Chain_Append( State * state, const char * file, int format, const char * comment, int idx_chain ); /* :97 */
+
 /* ================================================================ Parameters_MC (core/include/Spirit/Parameters_MC.h) */
 void Parameters_MC_Set_Output_Tag( State * state, const char * tag, int idx_image, int idx_chain );       /* :30 */
 void Parameters_MC_Set_Output_Folder( State * state, const char * folder, int idx_image, int idx_chain ); /* :34 */

@@ -10,6 +10,7 @@
 #include "config.hpp"
 #include "gneb.hpp"
 #include "mc.hpp"
+#include "ovf.hpp"
 #include "state.hpp"
 #include "util.hpp"
 
@@ -91,6 +92,7 @@ SystemInput input_of( const Image & img, unsigned int stream )
     in.direct_minimization = img.llg.direct_minimization;
     in.seed                = (unsigned long long)(unsigned)img.llg.rng_seed;
     in.stream              = stream;
+    in.noise_offset        = img.llg_noise_drawn;
     return in;
 }
 
@@ -138,6 +140,8 @@ void finish_llg( Image & img, Engine & E )
     auto stv = E.status();
     E.get_spins( 0, img.spins.data() );
     auto & s            = stv[0];
+    if( img.llg.temperature > 0 )
+        img.llg_noise_drawn += (unsigned)( s.iteration - img.info.iteration );
     img.E               = s.energy;
     img.info.iteration  = s.iteration;
     img.info.max_torque = s.max_torque;
@@ -233,6 +237,59 @@ void geometry_changed( State * st )
 }
 
 } // namespace
+
+// OVF segment of an image (OVF_Segment(Spin_System), core/src/io/OVF_File.cpp: nodes
+// (Na nb, Nb, Nc), bounds and step sizes in nm); the description carries the positions of the
+// image's random streams so a run read back from the file continues them.
+OvfSegment image_segment( const Image & img, const std::vector<double> & data, const char * comment )
+{
+    OvfSegment seg;
+    const Geometry & g = *img.geom;
+    seg.title          = std::string( "SPIRIT Version " ) + "2.2.0 (spirit_gb300)";
+    seg.desc           = std::string( comment ? comment : "-" ) + "\nspirit_gb300 llg_noise_drawn=" +
+               std::to_string( img.llg_noise_drawn ) + " mc_sweeps_drawn=" + std::to_string( img.mc_sweeps_drawn );
+    seg.nodes          = { g.n_cells[0] * g.nb(), g.n_cells[1], g.n_cells[2] };
+    const Vec3 lo = g.bounds_min(), hi = g.bounds_max();
+    for( int e = 0; e < 3; ++e )
+    {
+        seg.bounds_min[e] = lo[e] * 0.1;
+        seg.bounds_max[e] = hi[e] * 0.1;
+        seg.base[e]       = 0;
+        seg.step[e]       = g.lattice_constant * g.bravais[e][e] * 0.1;
+    }
+    seg.data = data;
+    return seg;
+}
+
+// random-stream positions written by image_segment (absent in files of other writers)
+void restore_streams( Image & img, const std::string & desc )
+{
+    auto grab = [&]( const char * key, unsigned int & out ) {
+        size_t p = desc.find( key );
+        if( p != std::string::npos )
+            out = (unsigned int)std::stoul( desc.substr( p + std::strlen( key ) ) );
+    };
+    if( desc.find( "spirit_gb300" ) == std::string::npos )
+        return;
+    grab( "llg_noise_drawn=", img.llg_noise_drawn );
+    grab( "mc_sweeps_drawn=", img.mc_sweeps_drawn );
+}
+
+// IO_Image_Read (core/src/Spirit/IO.cpp:186-292): copy min(N, nos) spins, normalise, vacancies -> +z
+void read_image( Image & img, const OvfSegment & seg )
+{
+    if( seg.valuedim != 3 )
+        throw std::runtime_error( "the OVF segment should have 3 columns, but has " + std::to_string( seg.valuedim ) );
+    const size_t n = std::min( seg.data.size() / 3, (size_t)img.nos() );
+    for( size_t i = 0; i < n; ++i )
+    {
+        double v[3] = { seg.data[3 * i], seg.data[3 * i + 1], seg.data[3 * i + 2] };
+        double nn   = std::sqrt( v[0] * v[0] + v[1] * v[1] + v[2] * v[2] );
+        for( int e = 0; e < 3; ++e )
+            img.spins[3 * i + e] = nn < 1e-5 ? ( e == 2 ? 1.0 : 0.0 ) : v[e] / nn;
+    }
+    restore_streams( img, seg.desc );
+}
 
 // Monte Carlo run of one image: its own engine (precision of the State) and colouring
 struct MCImageRun
@@ -2468,6 +2525,163 @@ double Simulation_LLG_Loss( State * state, const double * params, int n_steps, c
     {
         handle( state, "Simulation_LLG_Loss" );
         return 0;
+    }
+}
+
+// ============================================================== IO (core/include/Spirit/IO.h)
+int IO_N_Images_In_File( State * state, const char * file, int idx_image, int idx_chain ) noexcept
+{
+    (void)idx_image;
+    (void)idx_chain;
+    try
+    {
+        return ovf_count( file ? file : "" );
+    }
+    catch( ... )
+    {
+        handle( state, "IO_N_Images_In_File" );
+        return 0;
+    }
+}
+
+void IO_Image_Read( State * state, const char * file, int idx_image_infile, int idx_image_inchain,
+                    int idx_chain ) noexcept
+{
+    try
+    {
+        auto I = from_indices( state, idx_image_inchain, idx_chain );
+        std::lock_guard<std::recursive_mutex> lk( I.img->mtx );
+        read_image( *I.img, ovf_read( file ? file : "", idx_image_infile ) );
+    }
+    catch( ... )
+    {
+        handle( state, "IO_Image_Read" );
+    }
+}
+
+static void write_image( State * state, const char * file, int format, const char * comment, int idx_image,
+                         int idx_chain, bool append )
+{
+    auto I = from_indices( state, idx_image, idx_chain );
+    if( format < 0 || format > 4 )
+        throw std::runtime_error( "Invalid file format index " + std::to_string( format ) );
+    ovf_write( file ? file : "", image_segment( *I.img, I.img->spins, comment ), format, append );
+}
+
+void IO_Image_Write( State * state, const char * file, int format, const char * comment, int idx_image,
+                     int idx_chain ) noexcept
+{
+    try
+    {
+        write_image( state, file, format, comment, idx_image, idx_chain, false );
+    }
+    catch( ... )
+    {
+        handle( state, "IO_Image_Write" );
+    }
+}
+
+void IO_Image_Append( State * state, const char * file, int format, const char * comment, int idx_image,
+                      int idx_chain ) noexcept
+{
+    try
+    {
+        write_image( state, file, format, comment, idx_image, idx_chain, true );
+    }
+    catch( ... )
+    {
+        handle( state, "IO_Image_Append" );
+    }
+}
+
+void IO_Positions_Write( State * state, const char * file, int format, const char * comment, int idx_image,
+                         int idx_chain ) noexcept
+{
+    try
+    {
+        auto I   = from_indices( state, idx_image, idx_chain );
+        auto seg = image_segment( *I.img, I.img->positions, comment );
+        seg.valuelabels = "position_x position_y position_z";
+        seg.valueunits  = "Angstrom Angstrom Angstrom";
+        ovf_write( file ? file : "", seg, format, false );
+    }
+    catch( ... )
+    {
+        handle( state, "IO_Positions_Write" );
+    }
+}
+
+// IO_Chain_Read (core/src/Spirit/IO.cpp): segments [start, end] of the file into images
+// insert_idx, insert_idx + 1, ... of the chain, appending images where the chain is too short
+void IO_Chain_Read( State * state, const char * file, int start_image_infile, int end_image_infile, int insert_idx,
+                    int idx_chain ) noexcept
+{
+    try
+    {
+        auto I         = from_indices( state, -1, idx_chain );
+        auto & ch      = *I.chain;
+        std::lock_guard<std::recursive_mutex> lk( ch.mtx );
+        const int nseg = ovf_count( file ? file : "" );
+        if( nseg == 0 )
+            throw std::runtime_error( std::string( "no OVF segments in \"" ) + ( file ? file : "" ) + "\"" );
+        if( insert_idx < 0 )
+            insert_idx = state->idx_active_image;
+        if( end_image_infile < 0 || end_image_infile >= nseg )
+            end_image_infile = nseg - 1;
+        for( int k = start_image_infile; k <= end_image_infile; ++k )
+        {
+            const int dst = insert_idx + ( k - start_image_infile );
+            while( (int)ch.images.size() <= dst )
+            {
+                auto img  = clone_image( *ch.images.back() );
+                img->geom = ch.images[0]->geom;
+                ch.images.push_back( img );
+            }
+            read_image( *ch.images[dst], ovf_read( file, k ) );
+        }
+        ch.Rx.assign( ch.images.size(), 0.0 );
+    }
+    catch( ... )
+    {
+        handle( state, "IO_Chain_Read" );
+    }
+}
+
+static void write_chain( State * state, const char * file, int format, const char * comment, int idx_chain,
+                         bool append )
+{
+    auto I = from_indices( state, -1, idx_chain );
+    if( format < 0 || format > 4 )
+        throw std::runtime_error( "Invalid file format index " + std::to_string( format ) );
+    bool first = !append;
+    for( auto & img : I.chain->images )
+    {
+        ovf_write( file ? file : "", image_segment( *img, img->spins, comment ), format, !first );
+        first = false;
+    }
+}
+
+void IO_Chain_Write( State * state, const char * file, int format, const char * comment, int idx_chain ) noexcept
+{
+    try
+    {
+        write_chain( state, file, format, comment, idx_chain, false );
+    }
+    catch( ... )
+    {
+        handle( state, "IO_Chain_Write" );
+    }
+}
+
+void IO_Chain_Append( State * state, const char * file, int format, const char * comment, int idx_chain ) noexcept
+{
+    try
+    {
+        write_chain( state, file, format, comment, idx_chain, true );
+    }
+    catch( ... )
+    {
+        handle( state, "IO_Chain_Append" );
     }
 }
 

@@ -129,6 +129,7 @@ struct SysDesc
     double force_convergence;
     unsigned long long seed;
     unsigned int stream;
+    unsigned int noise_offset; // iterations drawn by earlier runs: the noise counter continues there
     int n_iterations;
     // DDI
     int ddi;                    // 0 none, 1 FFT

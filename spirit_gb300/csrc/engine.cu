@@ -72,7 +72,8 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
         if( PROBE || STAGE == 1 )
         {
             const R sc = C.noise[ib];
-            V3<R> z = gauss3<R>( d.seed, d.stream, PROBE ? 0xFFFFFFFFu : (unsigned int)iteration, (unsigned int)i );
+            V3<R> z = gauss3<R>( d.seed, d.stream, PROBE ? 0xFFFFFFFFu : (unsigned int)iteration + d.noise_offset,
+                                 (unsigned int)i );
             xi      = { sc * z.x, sc * z.y, sc * z.z };
             if( STAGE == 1 )
                 A.xi.st( gi, xi );
@@ -522,6 +523,7 @@ static void fill_desc( SysDesc & d, const SystemInput & in )
     d.force_convergence   = in.force_convergence;
     d.seed                = in.seed;
     d.stream              = in.stream;
+    d.noise_offset        = in.noise_offset;
     d.n_iterations        = 0;
     d.ddi                 = ( h.ddi_method == 1 ) ? 1 : 0;
     fill_consts( d );
@@ -679,6 +681,7 @@ void Engine::set_params( int s, const SystemInput & in )
     d.force_convergence   = in.force_convergence;
     d.seed                = in.seed;
     d.stream              = in.stream;
+    d.noise_offset        = in.noise_offset;
     fill_consts( d );
     CUDA_CHECK( cudaMemcpyAsync( d_desc_ + s, &d, sizeof( SysDesc ), cudaMemcpyHostToDevice, stream_ ) );
     CUDA_CHECK( cudaStreamSynchronize( stream_ ) );

@@ -23,6 +23,7 @@ struct SystemInput
     bool direct_minimization      = false;
     unsigned long long seed       = 2006;
     unsigned int stream           = 0;
+    unsigned int noise_offset     = 0; // thermal-noise iterations drawn before this run
 };
 
 template<typename R>

@@ -888,6 +888,7 @@ static Engine & batched_prepare( State ** states, int n_states, int solver, int 
         s.direct_minimization = ims[k]->llg.direct_minimization;
         s.seed                = (unsigned long long)(unsigned)ims[k]->llg.rng_seed;
         s.stream              = (unsigned)k;
+        s.noise_offset        = ims[k]->llg_noise_drawn;
         E.set_params( k, s );
         ims[k]->info           = MethodInfo{};
         ims[k]->info.method    = "LLG";
@@ -918,6 +919,8 @@ static void batched_finish( Engine & E, const std::vector<Image *> & ims )
         std::memcpy( ims[k]->spins.data(), C.pinned + o, ims[k]->spins.size() * sizeof( double ) );
         o += ims[k]->spins.size();
         ims[k]->E               = stv[k].energy;
+        if( ims[k]->llg.temperature > 0 )
+            ims[k]->llg_noise_drawn += (unsigned)stv[k].iteration;
         ims[k]->info.iteration  = stv[k].iteration;
         ims[k]->info.max_torque = stv[k].max_torque;
         ims[k]->info.time_ps    = stv[k].iteration * ims[k]->llg.dt;

@@ -112,6 +112,7 @@ struct Image
     std::shared_ptr<void> vp_run; // single-shot LLG run with the VP solver
     std::shared_ptr<void> mc_run; // Monte Carlo run (engine + colouring) of this image
     unsigned int mc_sweeps_drawn = 0; // Monte Carlo sweeps done so far (position in the random stream)
+    unsigned int llg_noise_drawn = 0; // LLG iterations whose thermal noise was drawn (noise stream position)
 
     int nos() const
     {
