@@ -281,12 +281,18 @@ def run_batched_vs_plain(steps, warmup, plain=True, check=True):
     stream.synchronize()
     batched_ms = a.elapsed_time(b)
     simulation.batched_finish(states)
-    # accuracy after 1000 steps: 8 smallest systems, batched FP32 vs the FP64 oracle
+    for p in states:
+        state.delete(p)
+    # accuracy after 1000 steps: 8 smallest systems in fresh States (Philox streams from their
+    # start), batched FP32 vs the FP64 oracle
     small = sorted(range(len(specs)), key=lambda k: nos[k])[:8 if check else 0]
-    sub = [states[k] for k in small]
+    sub = []
     s0 = [random_spins(nos[k], 5000 + k) for k in small]
-    for p, s in zip(sub, s0):
+    for k, s in zip(small, s0):
+        p = state.setup(write_config(specs[k], os.path.join(tmp, "c4_%d.cfg" % k)), True)
         system.get_spin_directions(p)[:] = s
+        simulation.set_precision(p, 32)
+        sub.append(p)
     if sub:
         simulation.start_batched(sub, simulation.SOLVER_SIB, 1000)
     dm = 0.0 if sub else None
@@ -297,7 +303,7 @@ def run_batched_vs_plain(steps, warmup, plain=True, check=True):
                        seed=sp["llg"]["seed"], stream=j)
         got = np.array(system.get_spin_directions(sub[j]))
         dm = max(dm, float(np.abs(got - ref).max()))
-    for p in states:
+    for p in sub:
         state.delete(p)
     bv = total * steps / (batched_ms / 1000.0)
     pv = total * steps / (plain_ms / 1000.0)

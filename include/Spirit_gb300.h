@@ -47,6 +47,8 @@ typedef struct Simulation_Run_Info
 #define Solver_Depondt 2
 #define Solver_Heun 3
 #define Solver_RungeKutta4 4
+#define Solver_LBFGS_OSO 5 /* Simulation.h:48 (direct minimisation, LLG and GNEB) */
+#define Solver_VP_OSO 7    /* Simulation.h:54 */
 
 /* ================================================================ State (core/include/Spirit/State.h) */
 State * State_Setup( const char * config_file, bool quiet );                  /* State.h:71 */

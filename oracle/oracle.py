@@ -64,6 +64,7 @@ def lib():
         L.og_philox4x32.argtypes = [P(ctypes.c_uint32), P(ctypes.c_uint32), P(ctypes.c_uint32)]
         L.og_llg_run.argtypes = [vp, vp, i, i, P(d), P(d), P(d)]
         L.og_gneb_run.argtypes = [vp, vp, i, i, P(d), P(i), P(d), P(d), P(d)]
+        L.og_gneb_run_solver.argtypes = [vp, vp, i, i, i, P(d), P(i), P(d), P(d), P(d)]
         L.og_mc_colors.argtypes = [vp, P(i)]
         L.og_mc_colors.restype = i
         L.og_mc_run.argtypes = [vp, vp, i, P(d), P(d), P(d)]
@@ -120,7 +121,7 @@ BRAVAIS = {
     "hex2d120": [[0.5, -0.5 * np.sqrt(3), 0], [0.5, 0.5 * np.sqrt(3), 0], [0, 0, 1]],
 }
 
-SOLVER = {"VP": 0, "SIB": 1, "Depondt": 2, "Heun": 3, "RK4": 4}
+SOLVER = {"VP": 0, "SIB": 1, "Depondt": 2, "Heun": 3, "RK4": 4, "LBFGS_OSO": 5, "VP_OSO": 7}
 
 
 def bravais_of(spec):
@@ -299,7 +300,8 @@ class OracleSystem:
         lib().og_mc_run(self.h, ctypes.byref(p), int(n_sweeps), _p(s), ctypes.byref(ca), ctypes.byref(ac))
         return s, {"cone_angle": ca.value, "acceptance": ac.value}
 
-    def gneb(self, chain, n_iter, image_type=None, spring_constant=1.0, force_convergence=1e-6, dt=1e-3):
+    def gneb(self, chain, n_iter, image_type=None, spring_constant=1.0, force_convergence=1e-6, dt=1e-3,
+             solver="VP"):
         c = np.ascontiguousarray(chain, dtype=np.float64).copy()
         noi = c.shape[0]
         types = np.zeros(noi, dtype=np.int32) if image_type is None else np.asarray(image_type, dtype=np.int32)
@@ -307,8 +309,9 @@ class OracleSystem:
         Rx = np.zeros(noi)
         mt = ctypes.c_double()
         p = GNEBParams(spring_constant, force_convergence, dt)
-        it = lib().og_gneb_run(self.h, ctypes.byref(p), noi, int(n_iter), _p(c), _p(types, ctypes.c_int), _p(E),
-                               _p(Rx), ctypes.byref(mt))
+        solver_id = SOLVER[solver] if isinstance(solver, str) else int(solver)
+        it = lib().og_gneb_run_solver(self.h, ctypes.byref(p), solver_id, noi, int(n_iter), _p(c),
+                                      _p(types, ctypes.c_int), _p(E), _p(Rx), ctypes.byref(mt))
         return c, {"iterations": it, "energies": E, "Rx": Rx, "max_torque": mt.value}
 
 

@@ -1166,7 +1166,14 @@ static void force_virtual(
     double a   = p->damping;
     double dtg = p->dt * C_GAMMA / C_MU_B / ( 1 + a * a );
     int thermal = p->temperature > 0;
-    if( p->direct_minimization || solver == 0 )
+    if( solver == 5 ) /* LBFGS_OSO: s x F (Method_LLG.cpp:161-164) */
+    {
+#pragma omp parallel for
+        for( int i = 0; i < s->nos; ++i )
+            cross3( spins + 3 * i, F + 3 * i, fv + 3 * i );
+        return;
+    }
+    if( p->direct_minimization || solver == 0 || solver == 7 )
     {
         double d = p->dt * C_GAMMA / C_MU_B;
 #pragma omp parallel for
@@ -1412,6 +1419,236 @@ static double llg_iteration(
     return E;
 }
 
+static double vdot( int n3, const double * a, const double * b )
+{
+    double r = 0;
+#pragma omp parallel for reduction( + : r )
+    for( int k = 0; k < n3; ++k )
+        r += a[k] * b[k];
+    return r;
+}
+
+/* ---------------------------------------------------------------- OSO direct minimisers
+ * Orthogonal spin optimisation (A. Ivanov et al., arXiv:1904.02669) as the reference writes it,
+ * in its coordinates: the "gradient" of an image is g = T (-s x f) with the signed permutation
+ * T = [[0,0,1],[0,-1,0],[1,0,0]] (oso_calc_gradients, Solver_Kernels.cpp:50-60), a search
+ * direction sd is applied as the rotation matrix of oso_rotate (Solver_Kernels.cpp:62-95), and
+ * the step is limited to an rms angle of maxmove = pi/200 (maximum_rotation, :97-105).
+ * VP_OSO: Solver_VP_OSO.hpp:28-114.  LBFGS_OSO: Solver_LBFGS_OSO.hpp:13-85 with
+ * lbfgs_get_searchdir (Solver_Kernels.hpp:44-189), memory 3. */
+typedef struct oso_state
+{
+    int noi, nos, solver;
+    size_t n3;
+    double *grad, *grad_pr, *v, *sd, *q;
+    double *da[3], *dg[3];
+    double rho[3], alpha[3];
+    int local_iter;
+} oso_state;
+
+static void oso_init( oso_state * o, int solver, int noi, int nos )
+{
+    memset( o, 0, sizeof( *o ) );
+    o->solver = solver;
+    o->noi    = noi;
+    o->nos    = nos;
+    o->n3     = (size_t)3 * nos;
+    size_t n  = noi * o->n3;
+    o->grad    = (double *)calloc( n, sizeof( double ) );
+    o->grad_pr = (double *)calloc( n, sizeof( double ) );
+    o->v       = (double *)calloc( n, sizeof( double ) );
+    o->sd      = (double *)calloc( n, sizeof( double ) );
+    o->q       = (double *)calloc( n, sizeof( double ) );
+    for( int k = 0; k < 3; ++k )
+    {
+        o->da[k] = (double *)calloc( n, sizeof( double ) );
+        o->dg[k] = (double *)calloc( n, sizeof( double ) );
+    }
+}
+
+static void oso_free( oso_state * o )
+{
+    free( o->grad );
+    free( o->grad_pr );
+    free( o->v );
+    free( o->sd );
+    free( o->q );
+    for( int k = 0; k < 3; ++k )
+    {
+        free( o->da[k] );
+        free( o->dg[k] );
+    }
+}
+
+/* g = T (-s x f) */
+static void oso_gradient( int nos, const double * spins, const double * f, double * g )
+{
+#pragma omp parallel for
+    for( int i = 0; i < nos; ++i )
+    {
+        double c[3];
+        cross3( spins + 3 * i, f + 3 * i, c );
+        g[3 * i + 0] = -c[2];
+        g[3 * i + 1] = c[1];
+        g[3 * i + 2] = -c[0];
+    }
+}
+
+static void oso_rotate( int nos, double * spins, const double * sd )
+{
+#pragma omp parallel for
+    for( int i = 0; i < nos; ++i )
+    {
+        const double * d = sd + 3 * i;
+        double * sp      = spins + 3 * i;
+        double theta     = norm3( d );
+        if( !( theta > 1.0e-20 ) )
+            continue;
+        double q = cos( theta ), w = 1 - q, sn = sin( theta );
+        double x = -d[0] / theta, y = -d[1] / theta, z = -d[2] / theta;
+        double a = -y * z * w, b = x * z * w, c = -x * y * w;
+        double p1 = x * sn, p2 = y * sn, p3 = z * sn;
+        double t1 = ( q + z * z * w ) * sp[0] + ( a + p1 ) * sp[1] + ( b + p2 ) * sp[2];
+        double t2 = ( a - p1 ) * sp[0] + ( q + y * y * w ) * sp[1] + ( c + p3 ) * sp[2];
+        double t3 = ( b - p2 ) * sp[0] + ( c - p3 ) * sp[1] + ( q + x * x * w ) * sp[2];
+        sp[0] = t1;
+        sp[1] = t2;
+        sp[2] = t3;
+    }
+}
+
+/* VP_OSO iteration on forces F (noi images) */
+static void oso_vp_iteration( oso_state * o, double * chain, const double * F, double dt )
+{
+    const double m = 1.0;
+    size_t n       = o->noi * o->n3;
+    memcpy( o->grad_pr, o->grad, n * sizeof( double ) );
+    for( int img = 0; img < o->noi; ++img )
+    {
+        double * g = o->grad + img * o->n3;
+        oso_gradient( o->nos, chain + img * o->n3, F + img * o->n3, g );
+        for( size_t k = 0; k < o->n3; ++k )
+            g[k] *= -1.0;
+    }
+    double proj = 0, fn2 = 0;
+    for( int img = 0; img < o->noi; ++img )
+    {
+        double * g  = o->grad + img * o->n3;
+        double * gp = o->grad_pr + img * o->n3;
+        double * v  = o->v + img * o->n3;
+        for( size_t k = 0; k < o->n3; ++k )
+            v[k] += 0.5 / m * ( gp[k] + g[k] );
+        proj += vdot( (int)o->n3, v, g );
+        fn2 += vdot( (int)o->n3, g, g );
+    }
+    for( int img = 0; img < o->noi; ++img )
+    {
+        double * g  = o->grad + img * o->n3;
+        double * v  = o->v + img * o->n3;
+        double * sd = o->sd + img * o->n3;
+        double ratio = proj / fn2;
+        if( proj <= 0 )
+            memset( v, 0, o->n3 * sizeof( double ) );
+        else
+            for( size_t k = 0; k < o->n3; ++k )
+                v[k] = g[k] * ratio;
+        for( size_t k = 0; k < o->n3; ++k )
+            sd[k] = dt * v[k] + 0.5 / m * dt * g[k];
+    }
+    for( int img = 0; img < o->noi; ++img )
+        oso_rotate( o->nos, chain + img * o->n3, o->sd + img * o->n3 );
+}
+
+static double chain_dot( const oso_state * o, const double * a, const double * b )
+{
+    double r = 0;
+    for( int img = 0; img < o->noi; ++img )
+        r += vdot( (int)o->n3, a + img * o->n3, b + img * o->n3 );
+    return r;
+}
+
+static void lbfgs_searchdir( oso_state * o )
+{
+    const int M     = 3;
+    const double eps = 1e-300;
+    size_t n        = o->noi * o->n3;
+    int m           = o->local_iter % M;
+    if( o->local_iter == 0 )
+    {
+        memcpy( o->grad_pr, o->grad, n * sizeof( double ) );
+        for( size_t k = 0; k < n; ++k )
+            o->sd[k] = -o->grad[k];
+        for( int i = 0; i < M; ++i )
+        {
+            o->rho[i] = 0;
+            memset( o->da[i], 0, n * sizeof( double ) );
+            memset( o->dg[i], 0, n * sizeof( double ) );
+        }
+        o->local_iter++;
+        return;
+    }
+    for( size_t k = 0; k < n; ++k )
+    {
+        o->da[m][k] = o->sd[k];
+        o->dg[m][k] = o->grad[k] - o->grad_pr[k];
+    }
+    double rinv = chain_dot( o, o->dg[m], o->da[m] );
+    if( rinv > eps )
+        o->rho[m] = 1.0 / rinv;
+    else
+    {
+        o->local_iter = 0;
+        lbfgs_searchdir( o );
+        return;
+    }
+    memcpy( o->q, o->grad, n * sizeof( double ) );
+    for( int k = M - 1; k > -1; --k )
+    {
+        int c       = ( k + m + 1 ) % M;
+        o->alpha[c] = o->rho[c] * chain_dot( o, o->da[c], o->q );
+        for( size_t j = 0; j < n; ++j )
+            o->q[j] += -o->alpha[c] * o->dg[c][j];
+    }
+    double dy2    = chain_dot( o, o->dg[m], o->dg[m] );
+    double rhody2 = dy2 * o->rho[m];
+    double inv    = rhody2 > eps ? 1.0 / rhody2 : 1.0 / eps;
+    for( size_t j = 0; j < n; ++j )
+        o->sd[j] = inv * o->q[j];
+    for( int k = 0; k < M; ++k )
+    {
+        int c         = o->local_iter < M ? k : ( k + m + 1 ) % M;
+        double rhopdg = o->rho[c] * chain_dot( o, o->dg[c], o->sd );
+        for( size_t j = 0; j < n; ++j )
+            o->sd[j] += ( o->alpha[c] - rhopdg ) * o->da[c][j];
+    }
+    for( size_t j = 0; j < n; ++j )
+    {
+        o->grad_pr[j] = o->grad[j];
+        o->sd[j]      = -o->sd[j];
+    }
+    o->local_iter++;
+}
+
+/* LBFGS_OSO iteration on forces F */
+static void oso_lbfgs_iteration( oso_state * o, double * chain, const double * F )
+{
+    const double maxmove = 3.14159265358979323846 / 200.0;
+    for( int img = 0; img < o->noi; ++img )
+        oso_gradient( o->nos, chain + img * o->n3, F + img * o->n3, o->grad + img * o->n3 );
+    lbfgs_searchdir( o );
+    double scaling = 1;
+    for( int img = 0; img < o->noi; ++img )
+    {
+        double th = sqrt( vdot( (int)o->n3, o->sd + img * o->n3, o->sd + img * o->n3 ) / o->nos );
+        double sc = th > maxmove ? maxmove / th : 1.0;
+        scaling   = fmin( sc, scaling );
+    }
+    for( size_t k = 0; k < o->noi * o->n3; ++k )
+        o->sd[k] *= scaling;
+    for( int img = 0; img < o->noi; ++img )
+        oso_rotate( o->nos, chain + img * o->n3, o->sd + img * o->n3 );
+}
+
 /* Method::Iterate (Method.cpp:57-113) + Method_LLG ctor (Method_LLG.cpp:22-63) and
  * Hook_Post_Iteration (247-301): the constructor evaluates the initial max torque, the loop
  * runs while iteration < n_iter and max_torque >= force_convergence. */
@@ -1433,6 +1670,25 @@ int og_llg_run(
     force_virtual( s, p, solver, spins, work, xi, fv1 );
     double mt = max_torque( nos, spins, fv1 );
     int it    = 0;
+    if( solver == 5 || solver == 7 )
+    {
+        /* direct minimisers: the force of the configuration before the step, its virtual force
+         * (LBFGS_OSO: s x F; VP_OSO: dt gamma/mu_B s x F) for the torque after the step */
+        oso_state o;
+        oso_init( &o, solver, 1, nos );
+        for( it = 0; it < n_iter && !( mt < p->force_convergence ); ++it )
+        {
+            E = calc_force( s, spins, work );
+            force_virtual( s, p, solver, spins, work, xi, fv1 );
+            if( solver == 7 )
+                oso_vp_iteration( &o, spins, work, p->dt );
+            else
+                oso_lbfgs_iteration( &o, spins, work );
+            mt = max_torque( nos, spins, fv1 );
+        }
+        oso_free( &o );
+        goto done;
+    }
     for( it = 0; it < n_iter && !( mt < p->force_convergence ); ++it )
     {
         if( p->temperature > 0 )
@@ -1440,6 +1696,7 @@ int og_llg_run(
         E  = llg_iteration( s, p, solver, spins, xi, fv1, work );
         mt = max_torque( nos, spins, fv1 );
     }
+done:
     if( energy )
         *energy = E;
     if( max_torque_out )
@@ -1455,15 +1712,6 @@ int og_llg_run(
  * Geodesic_Tangent 78-113, Tangents 115-215, project_orthogonal 31-38, invert_parallel 40-47,
  * normalize 224-229.  Method_GNEB.cpp:88-357 (Calculate_Force, no spring-force ratio, no path
  * shortening, fixed endpoints), Solver_VP.hpp:28-114, Hook_Post_Iteration 411-456. */
-static double vdot( int n3, const double * a, const double * b )
-{
-    double r = 0;
-#pragma omp parallel for reduction( + : r )
-    for( int k = 0; k < n3; ++k )
-        r += a[k] * b[k];
-    return r;
-}
-
 static double dist_geodesic( int nos, const double * a, const double * b )
 {
     double d = 0;
@@ -1579,130 +1827,162 @@ static void tangents( int nos, int noi, const double * chain, const double * ene
     }
 }
 
-int og_gneb_run(
-    og_system * s, const og_gneb_params * p, int noi, int n_iter, double * chain, const int * image_type,
+/* Method_GNEB::Calculate_Force (Method_GNEB.cpp:88-357): gradient forces, energies, Rx,
+ * tangents and total forces Ft (zero at the end points).  Returns 1 when two images coincide. */
+static int gneb_forces(
+    og_system * s, const og_gneb_params * p, int noi, const double * chain, const int * image_type, double * energies,
+    double * Rx, double * Fg, double * T, double * Ft )
+{
+    int nos     = s->nos;
+    size_t n3   = (size_t)3 * nos;
+    int aborted = 0;
+    for( int img = 0; img < noi; ++img )
+    {
+        double * g    = Fg + img * n3;
+        energies[img] = og_gradient_and_energy( s, chain + img * n3, g );
+        for( size_t k = 0; k < n3; ++k )
+            g[k] *= -1;
+        if( img == 0 )
+            Rx[0] = 0;
+        else
+        {
+            Rx[img] = Rx[img - 1] + dist_geodesic( nos, chain + img * n3, chain + ( img - 1 ) * n3 );
+            if( Rx[img] - Rx[img - 1] < 1e-10 )
+                aborted = 1;
+        }
+    }
+    if( aborted )
+        return 1;
+    tangents( nos, noi, chain, energies, T );
+    for( int img = 1; img < noi - 1; ++img )
+    {
+        double * g  = Fg + img * n3;
+        double * t  = T + img * n3;
+        double * ft = Ft + img * n3;
+        project_tangential( nos, g, chain + img * n3 );
+        if( image_type[img] == 1 )
+        {
+            double x = vdot( (int)n3, g, t );
+            for( size_t k = 0; k < n3; ++k )
+                g[k] -= 2 * x * t[k];
+            memcpy( ft, g, sizeof( double ) * n3 );
+        }
+        else if( image_type[img] == 2 )
+            memcpy( ft, g, sizeof( double ) * n3 );
+        else if( image_type[img] == 0 )
+        {
+            double x = vdot( (int)n3, g, t );
+            for( size_t k = 0; k < n3; ++k )
+                g[k] -= x * t[k];
+            double d = p->spring_constant * ( Rx[img + 1] - 2 * Rx[img] + Rx[img - 1] );
+            for( size_t k = 0; k < n3; ++k )
+            {
+                double v = g[k];
+                v += d * t[k];
+                ft[k] = v;
+            }
+        }
+        else
+            memset( ft, 0, sizeof( double ) * n3 );
+    }
+    return 0;
+}
+
+/* max over images of max_i |P_perp F_total| (Method_GNEB::Hook_Post_Iteration, 411-430) */
+static double gneb_max_torque( int nos, int noi, const double * chain, double * Ft )
+{
+    size_t n3 = (size_t)3 * nos;
+    double mt = 0;
+    for( int img = 0; img < noi; ++img )
+    {
+        double * ft = Ft + img * n3;
+        project_tangential( nos, ft, chain + img * n3 );
+        double m2 = 0;
+        for( int i = 0; i < nos; ++i )
+        {
+            double n2 = dot3( ft + 3 * i, ft + 3 * i );
+            if( n2 > m2 )
+                m2 = n2;
+        }
+        if( sqrt( m2 ) > mt )
+            mt = sqrt( m2 );
+    }
+    return mt;
+}
+
+int og_gneb_run_solver(
+    og_system * s, const og_gneb_params * p, int solver, int noi, int n_iter, double * chain, const int * image_type,
     double * energies, double * Rx, double * max_torque_out )
 {
     int nos   = s->nos;
     size_t n3 = (size_t)3 * nos;
-    double * F      = (double *)calloc( noi * n3, sizeof( double ) ); /* forces */
-    double * Fp     = (double *)calloc( noi * n3, sizeof( double ) ); /* forces_previous */
-    double * V      = (double *)calloc( noi * n3, sizeof( double ) );
-    double * Fg     = (double *)calloc( noi * n3, sizeof( double ) ); /* F_gradient */
-    double * Ft     = (double *)calloc( noi * n3, sizeof( double ) ); /* F_total */
-    double * T      = (double *)calloc( noi * n3, sizeof( double ) );
-    const double m  = 1.0;
-    double mt       = p->force_convergence + 1.0;
+    double * F  = (double *)calloc( noi * n3, sizeof( double ) ); /* forces (VP: F_total projected) */
+    double * Fp = (double *)calloc( noi * n3, sizeof( double ) ); /* forces_previous */
+    double * V  = (double *)calloc( noi * n3, sizeof( double ) );
+    double * Fg = (double *)calloc( noi * n3, sizeof( double ) ); /* F_gradient */
+    double * Ft = (double *)calloc( noi * n3, sizeof( double ) ); /* F_total */
+    double * T  = (double *)calloc( noi * n3, sizeof( double ) );
+    oso_state o;
+    oso_init( &o, solver, solver == 0 ? 1 : noi, solver == 0 ? 1 : nos );
+    const double m = 1.0;
+    double mt      = p->force_convergence + 1.0;
     int it;
     for( it = 0; it < n_iter && !( mt < p->force_convergence ); ++it )
     {
-        memcpy( Fp, F, sizeof( double ) * noi * n3 );
-        /* Calculate_Force */
-        int aborted = 0;
-        for( int img = 0; img < noi; ++img )
-        {
-            double * g = Fg + img * n3;
-            energies[img] = og_gradient_and_energy( s, chain + img * n3, g );
-            for( size_t k = 0; k < n3; ++k )
-                g[k] *= -1;
-            if( img == 0 )
-                Rx[0] = 0;
-            else
-            {
-                Rx[img] = Rx[img - 1] + dist_geodesic( nos, chain + img * n3, chain + ( img - 1 ) * n3 );
-                if( Rx[img] - Rx[img - 1] < 1e-10 )
-                    aborted = 1;
-            }
-        }
-        if( aborted )
+        if( solver == 0 )
+            memcpy( Fp, F, sizeof( double ) * noi * n3 );
+        if( gneb_forces( s, p, noi, chain, image_type, energies, Rx, Fg, T, Ft ) )
             break;
-        tangents( nos, noi, chain, energies, T );
-        for( int img = 1; img < noi - 1; ++img )
+        if( solver == 7 )
+            oso_vp_iteration( &o, chain, Ft, p->dt );
+        else if( solver == 5 )
+            oso_lbfgs_iteration( &o, chain, Ft );
+        else
         {
-            double * g  = Fg + img * n3;
-            double * t  = T + img * n3;
-            double * ft = Ft + img * n3;
-            project_tangential( nos, g, chain + img * n3 );
-            if( image_type[img] == 1 )
+            for( int img = 1; img < noi - 1; ++img )
+                memcpy( F + img * n3, Ft + img * n3, sizeof( double ) * n3 );
+            /* Solver_VP::Iteration */
+            double proj = 0, fn2 = 0;
+            for( int img = 0; img < noi; ++img )
             {
-                double x = vdot( (int)n3, g, t );
+                double * f  = F + img * n3;
+                double * fp = Fp + img * n3;
+                double * v  = V + img * n3;
                 for( size_t k = 0; k < n3; ++k )
-                    g[k] -= 2 * x * t[k];
-                memcpy( ft, g, sizeof( double ) * n3 );
+                    v[k] += 0.5 / m * ( fp[k] + f[k] );
+                proj += vdot( (int)n3, v, f );
+                fn2 += vdot( (int)n3, f, f );
             }
-            else if( image_type[img] == 2 )
-                memcpy( ft, g, sizeof( double ) * n3 );
-            else if( image_type[img] == 0 )
+            for( int img = 0; img < noi; ++img )
             {
-                double x = vdot( (int)n3, g, t );
-                for( size_t k = 0; k < n3; ++k )
-                    g[k] -= x * t[k];
-                double d = p->spring_constant * ( Rx[img + 1] - 2 * Rx[img] + Rx[img - 1] );
-                for( size_t k = 0; k < n3; ++k )
+                double * f  = F + img * n3;
+                double * v  = V + img * n3;
+                double * sp = chain + img * n3;
+                double ratio = proj / fn2;
+                if( proj <= 0 )
+                    memset( v, 0, sizeof( double ) * n3 );
+                else
+                    for( size_t k = 0; k < n3; ++k )
+                        v[k] = f[k] * ratio;
+                for( int i = 0; i < nos; ++i )
                 {
-                    double v = g[k];
-                    v += d * t[k];
-                    ft[k] = v;
+                    double c[3];
+                    for( int e = 0; e < 3; ++e )
+                        c[e] = sp[3 * i + e] + p->dt * v[3 * i + e] + 0.5 / m * p->dt * f[3 * i + e];
+                    normalize3( c );
+                    memcpy( sp + 3 * i, c, sizeof( c ) );
                 }
             }
-            else
-                memset( ft, 0, sizeof( double ) * n3 );
-            memcpy( F + img * n3, ft, sizeof( double ) * n3 );
+            /* the post-iteration hook also projects the stored forces onto the new tangent
+             * planes in place (Method_GNEB.cpp:428); VP reuses them as forces_previous */
+            for( int img = 0; img < noi; ++img )
+                project_tangential( nos, F + img * n3, chain + img * n3 );
         }
-        /* Solver_VP::Iteration */
-        double proj = 0, fn2 = 0;
-        for( int img = 0; img < noi; ++img )
-        {
-            double * f  = F + img * n3;
-            double * fp = Fp + img * n3;
-            double * v  = V + img * n3;
-            for( size_t k = 0; k < n3; ++k )
-                v[k] += 0.5 / m * ( fp[k] + f[k] );
-            proj += vdot( (int)n3, v, f );
-            fn2 += vdot( (int)n3, f, f );
-        }
-        for( int img = 0; img < noi; ++img )
-        {
-            double * f  = F + img * n3;
-            double * v  = V + img * n3;
-            double * sp = chain + img * n3;
-            double ratio = proj / fn2;
-            if( proj <= 0 )
-                memset( v, 0, sizeof( double ) * n3 );
-            else
-                for( size_t k = 0; k < n3; ++k )
-                    v[k] = f[k] * ratio;
-            for( int i = 0; i < nos; ++i )
-            {
-                double c[3];
-                for( int e = 0; e < 3; ++e )
-                    c[e] = sp[3 * i + e] + p->dt * v[3 * i + e] + 0.5 / m * p->dt * f[3 * i + e];
-                normalize3( c );
-                memcpy( sp + 3 * i, c, sizeof( c ) );
-            }
-        }
-        /* Hook_Post_Iteration: max over images of max_i |P_perp F_total|; it also projects the
-         * stored forces onto the new tangent planes in place (Method_GNEB.cpp:428), which the VP
-         * solver then reuses as forces_previous */
-        mt = 0;
-        for( int img = 0; img < noi; ++img )
-        {
-            double * ft = Ft + img * n3;
-            project_tangential( nos, ft, chain + img * n3 );
-            project_tangential( nos, F + img * n3, chain + img * n3 );
-            double m2 = 0;
-            for( int i = 0; i < nos; ++i )
-            {
-                double n2 = dot3( ft + 3 * i, ft + 3 * i );
-                if( n2 > m2 )
-                    m2 = n2;
-            }
-            if( sqrt( m2 ) > mt )
-                mt = sqrt( m2 );
-        }
+        mt = gneb_max_torque( nos, noi, chain, Ft );
     }
     if( max_torque_out )
         *max_torque_out = mt;
+    oso_free( &o );
     free( F );
     free( Fp );
     free( V );
@@ -1710,6 +1990,13 @@ int og_gneb_run(
     free( Ft );
     free( T );
     return it;
+}
+
+int og_gneb_run(
+    og_system * s, const og_gneb_params * p, int noi, int n_iter, double * chain, const int * image_type,
+    double * energies, double * Rx, double * max_torque_out )
+{
+    return og_gneb_run_solver( s, p, 0, noi, n_iter, chain, image_type, energies, Rx, max_torque_out );
 }
 
 void og_gneb_image_types_auto( int noi, const double * E, int * type )

@@ -91,6 +91,7 @@ typedef struct og_llg_params
 } og_llg_params;
 
 /* Runs up to n_iter iterations (stops earlier on convergence, like Method::Iterate).
+ * solver: 0 VP, 1 SIB, 2 Depondt, 3 Heun, 4 RK4, 5 LBFGS_OSO, 7 VP_OSO (Simulation.h ids).
  * spins in/out.  Returns the number of iterations done; energy = energy of the last force
  * evaluation (Spin_System::E after the run), max_torque as Simulation_Get_MaxTorqueNorm. */
 int og_llg_run(
@@ -109,6 +110,10 @@ typedef struct og_gneb_params
 int og_gneb_run(
     og_system * s, const og_gneb_params * p, int noi, int n_iter, double * chain, const int * image_type,
     double * energies, double * Rx, double * max_torque );
+/* GNEB with solver 0 (VP), 5 (LBFGS_OSO) or 7 (VP_OSO): Method_GNEB<solver> */
+int og_gneb_run_solver(
+    og_system * s, const og_gneb_params * p, int solver, int noi, int n_iter, double * chain,
+    const int * image_type, double * energies, double * Rx, double * max_torque );
 /* Parameters_GNEB_Set_Image_Type_Automatically */
 void og_gneb_image_types_auto( int noi, const double * energies, int * image_type );
 /* Transition_Homogeneous (geodesic interpolation between images idx_1 and idx_2) */

@@ -130,6 +130,10 @@ const char * solver_name( int s )
         return "Heun";
     case 4:
         return "RK4";
+    case 5:
+        return "LBFGS_OSO";
+    case 7:
+        return "VP_OSO";
     default:
         return "None";
     }
@@ -1988,7 +1992,8 @@ void Simulation_LLG_Start( State * state, int solver_type, int n_iterations, int
             return;
         }
         if( solver_type != SOLVER_SIB && solver_type != SOLVER_HEUN && solver_type != SOLVER_DEPONDT
-            && solver_type != SOLVER_RK4 && solver_type != SOLVER_VP )
+            && solver_type != SOLVER_RK4 && solver_type != SOLVER_VP && solver_type != SOLVER_VP_OSO
+            && solver_type != SOLVER_LBFGS_OSO )
         {
             log_msg( state, 2, "Invalid solver_type " + std::to_string( solver_type ) );
             return;
@@ -2005,10 +2010,11 @@ void Simulation_LLG_Start( State * state, int solver_type, int n_iterations, int
         img.info.solver_id     = solver_type;
         img.info.n_iterations  = (int)img.llg.n_iterations;
         img.info.t_start       = std::chrono::steady_clock::now();
-        if( solver_type == SOLVER_VP )
+        if( solver_type == SOLVER_VP || solver_type == SOLVER_VP_OSO || solver_type == SOLVER_LBFGS_OSO )
         {
-            // VP on a single image: the chain-global projection over one image (Solver_VP.hpp:28-114)
-            llg_vp_run( state, img, singleshot );
+            // direct minimisers on a single image: the chain-global projection / L-BFGS memory over
+            // one image (Solver_VP.hpp:28-114, Solver_VP_OSO.hpp, Solver_LBFGS_OSO.hpp)
+            llg_vp_run( state, img, solver_type, singleshot );
             if( !singleshot )
                 fill_run_info( info, img.info );
             return;
@@ -2067,7 +2073,8 @@ void Simulation_N_Shot( State * state, int N, int idx_image, int idx_chain ) noe
             }
             return;
         }
-        if( img.info.solver_id == SOLVER_VP )
+        if( img.info.solver_id == SOLVER_VP || img.info.solver_id == SOLVER_VP_OSO
+            || img.info.solver_id == SOLVER_LBFGS_OSO )
         {
             llg_vp_shot( state, img, N );
             return;
@@ -2295,16 +2302,17 @@ void Simulation_GNEB_Start( State * state, int solver_type, int n_iterations, in
             log_msg( state, 1, "There are less than 2 images in the specified chain!" );
             return;
         }
-        if( solver_type != SOLVER_VP )
+        if( solver_type != SOLVER_VP && solver_type != SOLVER_VP_OSO && solver_type != SOLVER_LBFGS_OSO )
         {
-            log_msg( state, 2, "Simulation_GNEB_Start: this engine runs GNEB with the VP solver" );
+            log_msg( state, 2,
+                     "Simulation_GNEB_Start: this engine runs GNEB with the VP, VP_OSO and LBFGS_OSO solvers" );
             return;
         }
         if( n_iterations > 0 )
             I.chain->gneb.n_iterations = n_iterations;
         if( n_iterations_log > 0 )
             I.chain->gneb.n_iterations_log = n_iterations_log;
-        gneb_start( state, *I.chain, singleshot );
+        gneb_start( state, *I.chain, solver_type, singleshot );
         if( !singleshot )
             fill_run_info( info, I.chain->info );
     }

@@ -33,14 +33,17 @@ enum KernelId : int
     N_KERNEL_IDS
 };
 
-// LLG solver ids (core/include/Spirit/Simulation.h): VP=0, SIB=1, Depondt=2, Heun=3, RK4=4
+// Solver ids (core/include/Spirit/Simulation.h:33-53): VP=0, SIB=1, Depondt=2, Heun=3, RK4=4,
+// LBFGS_OSO=5, VP_OSO=7 (LBFGS_Atlas=6 is not provided)
 enum Solver : int
 {
-    SOLVER_VP      = 0,
-    SOLVER_SIB     = 1,
-    SOLVER_DEPONDT = 2,
-    SOLVER_HEUN    = 3,
-    SOLVER_RK4     = 4,
+    SOLVER_VP        = 0,
+    SOLVER_SIB       = 1,
+    SOLVER_DEPONDT   = 2,
+    SOLVER_HEUN      = 3,
+    SOLVER_RK4       = 4,
+    SOLVER_LBFGS_OSO = 5,
+    SOLVER_VP_OSO    = 7,
 };
 
 // One interaction pair of basis atom i with atom j in the cell translated by (da, db, dc).

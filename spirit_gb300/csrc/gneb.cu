@@ -14,6 +14,23 @@
 //               in-place projection of the stored forces; the last block finalises the iteration
 // Reductions are FP64 atomics of per-block partial sums.  The iteration counter and the
 // convergence flag live on the device, so iterations replay from a CUDA graph.
+//
+// The exponential-transform minimisers replace K4/K5 (orthogonal spin optimisation,
+// Solver_VP_OSO.hpp, Solver_LBFGS_OSO.hpp).  The reference writes them in permuted coordinates
+// (g = T(-s x f) with the signed permutation T of oso_calc_gradients, Solver_Kernels.cpp:50-60,
+// and the matching rotation matrix of oso_rotate, :62-95); T is orthogonal and applied to every
+// vector alike, so here they run in physical coordinates: the search direction is the rotation
+// vector itself and dot products are unchanged.
+//   VP_OSO     K4' torque g = s x F, v += (g_prev + g)/2m, chain-global v.g and g.g;
+//              K5' v = (v.g / g.g) g or 0, rotate s by dt v + dt g/2m
+//   LBFGS_OSO  K4' gradient -(s x F), new difference dg[m], and the per-image Gram matrix of the
+//              7 vectors {grad, da[0..2], dg[0..2]};
+//              K6  one thread: the two-loop recursion of lbfgs_get_searchdir
+//              (Solver_Kernels.hpp:44-189) on coefficients over those 7 vectors (every dot product
+//              it needs is a Gram entry), and the rms-angle limit (maximum_rotation, :97-105)
+//              from the per-image Grams;
+//              K5' sd = sum c_j b_j, kept as the next da, rotate s by sd
+// so one L-BFGS iteration reads the memory twice instead of once per recursion step.
 #include "gneb.hpp"
 #include "kernels.cuh"
 #include "util.hpp"
@@ -22,6 +39,7 @@
 #include <chrono>
 #include <cstring>
 #include <fstream>
+#include <type_traits>
 
 namespace sg
 {
@@ -38,15 +56,23 @@ struct GnebImage
 
 struct GnebCtl
 {
-    int iteration, active, n_iterations, mode; // mode 0: GNEB, 1: LLG with VP (single image)
-    int noi, nos, aborted, pad;
+    int iteration, active, n_iterations, mode; // mode 0: GNEB, 1: LLG direct minimisation (single image)
+    int noi, nos, aborted, solver;             // solver: SOLVER_VP, SOLVER_LBFGS_OSO, SOLVER_VP_OSO
     double force_convergence, m, proj, fn2;
     double hm; // 0.5 / m
     float max_torque;
     unsigned int blocks_done;
     unsigned int torque_bits;
-    int pad2;
+    int fv_unit; // LLG virtual force s x F without the dt gamma / mu_B factor (LBFGS_OSO)
+    // L-BFGS memory (3 pairs) and the coefficients of this iteration's search direction
+    int local_iter, lb_store, pad3[2];
+    double eps, maxmove;
+    double rho[3], alpha[3], coef[7];
 };
+
+constexpr int LB_MEM  = 3;
+constexpr int LB_VEC  = 1 + 2 * LB_MEM;                // grad, da[0..2], dg[0..2]
+constexpr int LB_GRAM = LB_VEC * ( LB_VEC + 1 ) / 2;  // upper triangle
 
 template<typename R>
 struct GArgs
@@ -55,6 +81,8 @@ struct GArgs
     const int2 * blkmap;
     int nblocks;
     SoA3<R> s, F, V, T, G, h;
+    SoA3<R> Gb, DA[LB_MEM], DG[LB_MEM]; // L-BFGS: gradient, step and gradient-difference memory
+    double * gram;                       // L-BFGS: per-image Gram matrices [noi][LB_GRAM]
     GnebImage * img;
     GnebCtl * ctl;
     double spring_constant;
@@ -107,16 +135,21 @@ __global__ void __launch_bounds__( 256 ) gneb_eval( GArgs<R> A, int probe )
         }
         if( A.ctl->mode == 1 )
         {
-            // LLG-VP: virtual force of the direct minimisation fv = dt gamma/mu_B (s x F), kept in T
-            R k      = C.kdm;
+            // direct minimisation: virtual force fv = dt gamma/mu_B (s x F) (VP, VP_OSO) or s x F
+            // (LBFGS_OSO; Method_LLG.cpp:161-168), kept in T for the torque
+            R k      = A.ctl->fv_unit ? R( 1 ) : C.kdm;
             V3<R> cr = cross( si, f );
             V3<R> fv = { k * cr.x, k * cr.y, k * cr.z };
             A.T.st( gi, fv );
             if( probe )
             {
-                // constructor: initial forces projected onto the tangent planes (Hook_Post_Iteration)
-                R dd = dot( f, si );
-                A.F.st( gi, V3<R>{ f.x - dd * si.x, f.y - dd * si.y, f.z - dd * si.z } );
+                // constructor: initial forces projected onto the tangent planes (Hook_Post_Iteration);
+                // VP reuses them as its previous forces, the OSO solvers start from zero
+                if( A.ctl->solver == SOLVER_VP )
+                {
+                    R dd = dot( f, si );
+                    A.F.st( gi, V3<R>{ f.x - dd * si.x, f.y - dd * si.y, f.z - dd * si.z } );
+                }
                 float t2 = (float)torque2( fv, si );
                 atomicMax( &A.img[im].torque_bits, __float_as_uint( t2 ) );
             }
@@ -309,6 +342,33 @@ __global__ void __launch_bounds__( 256 ) gneb_force( GArgs<R> A )
     }
 }
 
+// last block of an iteration: per-image and maximum torques, iteration counter, convergence
+template<typename R>
+__device__ void finish_iteration( const GArgs<R> & A )
+{
+    __threadfence();
+    volatile GnebCtl * vc   = A.ctl;
+    volatile GnebImage * vi = A.img;
+    float mt                = 0;
+    for( int k = 0; k < vc->noi; ++k )
+    {
+        float tk          = sqrtf( __uint_as_float( vi[k].torque_bits ) );
+        vi[k].torque      = tk;
+        vi[k].torque_bits = 0;
+        mt                = fmaxf( mt, tk );
+    }
+    vc->blocks_done = 0;
+    if( vc->aborted )
+    {
+        vc->active = 0;
+        return;
+    }
+    vc->max_torque = mt;
+    int it         = vc->iteration + 1;
+    vc->iteration  = it;
+    vc->active     = ( it < vc->n_iterations ) && !( mt < (float)vc->force_convergence );
+}
+
 // K5: VP step, torques, projection of the stored forces, finalisation
 template<typename R>
 __global__ void __launch_bounds__( 256 ) gneb_update( GArgs<R> A )
@@ -361,33 +421,331 @@ __global__ void __launch_bounds__( 256 ) gneb_update( GArgs<R> A )
     }
     __syncthreads();
     if( is_last && threadIdx.x == 0 )
+        finish_iteration( A );
+}
+
+// total force of an image's spin for the minimisers: GNEB climbing / falling / normal force
+// (Method_GNEB.cpp:176-256; zero at the end points), LLG the gradient force
+template<typename R>
+__device__ __forceinline__ V3<R> total_force( const GArgs<R> & A, int im, long long gi )
+{
+    V3<R> fnew    = { 0, 0, 0 };
+    const int noi = A.ctl->noi;
+    if( A.ctl->mode == 1 )
+        fnew = A.G.ld( gi );
+    else if( im > 0 && im < noi - 1 )
     {
-        __threadfence();
-        volatile GnebCtl * vc  = ctl;
-        volatile GnebImage * vi = A.img;
-        float mt               = 0;
-        for( int k = 0; k < vc->noi; ++k )
+        const GnebImage & I = A.img[im];
+        const R inv         = R( 1 ) / sqrt( (R)I.tt );
+        V3<R> t             = A.T.ld( gi );
+        t                   = { t.x * inv, t.y * inv, t.z * inv };
+        R ftn               = (R)I.ft * inv;
+        V3<R> f             = A.G.ld( gi );
+        if( I.type == 1 )
+            fnew = { f.x - R( 2 ) * ftn * t.x, f.y - R( 2 ) * ftn * t.y, f.z - R( 2 ) * ftn * t.z };
+        else if( I.type == 2 )
+            fnew = f;
+        else if( I.type == 0 )
         {
-            float tk        = sqrtf( __uint_as_float( vi[k].torque_bits ) );
-            vi[k].torque    = tk;
-            vi[k].torque_bits = 0;
-            mt              = fmaxf( mt, tk );
+            R sp = (R)I.spring;
+            fnew = { f.x - ftn * t.x, f.y - ftn * t.y, f.z - ftn * t.z };
+            fnew.x += sp * t.x;
+            fnew.y += sp * t.y;
+            fnew.z += sp * t.z;
         }
-        vc->blocks_done = 0;
-        if( vc->aborted )
+    }
+    return fnew;
+}
+
+// K4' (VP_OSO, LBFGS_OSO)
+template<typename R>
+__global__ void __launch_bounds__( 256 ) oso_force( GArgs<R> A )
+{
+    __shared__ double red[8 * LB_GRAM];
+    __shared__ double red1[32];
+    GnebCtl * ctl = A.ctl;
+    if( !ctl->active || ctl->aborted )
+        return;
+    const int2 bm     = A.blkmap[blockIdx.x];
+    const int im      = bm.x;
+    const SysDesc & d = A.sd[im];
+    const int i       = bm.y + threadIdx.x;
+    const bool lbfgs  = ctl->solver == SOLVER_LBFGS_OSO;
+    double vf = 0, ff = 0;
+    double b[LB_VEC][3];
+#pragma unroll
+    for( int k = 0; k < LB_VEC; ++k )
+        b[k][0] = b[k][1] = b[k][2] = 0;
+    if( i < d.nos )
+    {
+        const long long gi = d.spin_offset + i;
+        const V3<R> fnew   = total_force( A, im, gi );
+        if( ctl->mode == 0 )
+            A.T.st( gi, fnew ); // F_total, for the torque after the step
+        const V3<R> c = cross( A.s.ld( gi ), fnew );
+        if( !lbfgs )
         {
-            vc->active = 0;
-            return;
+            const V3<R> gp = A.F.ld( gi );
+            V3<R> v        = A.V.ld( gi );
+            const R hm     = (R)ctl->hm;
+            v.x += hm * ( gp.x + c.x );
+            v.y += hm * ( gp.y + c.y );
+            v.z += hm * ( gp.z + c.z );
+            A.V.st( gi, v );
+            A.F.st( gi, c );
+            vf = (double)v.x * c.x + (double)v.y * c.y + (double)v.z * c.z;
+            ff = (double)c.x * c.x + (double)c.y * c.y + (double)c.z * c.z;
         }
-        vc->max_torque = mt;
-        int it         = vc->iteration + 1;
-        vc->iteration  = it;
-        vc->active     = ( it < vc->n_iterations ) && !( mt < (float)vc->force_convergence );
+        else
+        {
+            const V3<R> gr = { -c.x, -c.y, -c.z };
+            const int m    = ctl->local_iter % LB_MEM;
+            const bool upd = ctl->local_iter > 0;
+            V3<R> dgm      = { 0, 0, 0 };
+            if( upd )
+            {
+                // dg[m] = grad - grad_prev; da[m] already holds the previous step
+                const V3<R> go = A.Gb.ld( gi );
+                dgm            = { gr.x - go.x, gr.y - go.y, gr.z - go.z };
+                A.DG[m].st( gi, dgm );
+            }
+            A.Gb.st( gi, gr );
+            b[0][0] = gr.x;
+            b[0][1] = gr.y;
+            b[0][2] = gr.z;
+#pragma unroll
+            for( int k = 0; k < LB_MEM; ++k )
+            {
+                const V3<R> a = A.DA[k].ld( gi );
+                const V3<R> g = ( upd && k == m ) ? dgm : A.DG[k].ld( gi );
+                b[1 + k][0] = a.x;
+                b[1 + k][1] = a.y;
+                b[1 + k][2] = a.z;
+                b[4 + k][0] = g.x;
+                b[4 + k][1] = g.y;
+                b[4 + k][2] = g.z;
+            }
+        }
+    }
+    if( !lbfgs )
+    {
+        double a  = block_sum( vf, red1 );
+        double bb = block_sum( ff, red1 );
+        if( threadIdx.x == 0 )
+        {
+            atomicAdd( &ctl->proj, a );
+            atomicAdd( &ctl->fn2, bb );
+        }
+        return;
+    }
+    // per-block Gram partial sums (warp shuffles, then across the warps)
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int k = 0;
+#pragma unroll
+    for( int p = 0; p < LB_VEC; ++p )
+#pragma unroll
+        for( int q = p; q < LB_VEC; ++q )
+        {
+            double x = b[p][0] * b[q][0] + b[p][1] * b[q][1] + b[p][2] * b[q][2];
+#pragma unroll
+            for( int o = 16; o > 0; o >>= 1 )
+                x += __shfl_xor_sync( 0xffffffffu, x, o );
+            if( lane == 0 )
+                red[w * LB_GRAM + k] = x;
+            ++k;
+        }
+    __syncthreads();
+    if( threadIdx.x < LB_GRAM )
+    {
+        double t = 0;
+        for( int j = 0; j < (int)( blockDim.x >> 5 ); ++j )
+            t += red[j * LB_GRAM + threadIdx.x];
+        if( t != 0 )
+            atomicAdd( &A.gram[(size_t)im * LB_GRAM + threadIdx.x], t );
     }
 }
 
-// clear the per-iteration accumulators (E, dist2, tt, ft) -- one block
-__global__ void gneb_clear( GnebImage * img, GnebCtl * ctl )
+// K6 (LBFGS_OSO): search-direction coefficients over {grad, da[0..2], dg[0..2]} -- one thread
+__global__ void lbfgs_dir( GnebCtl * ctl, const double * gram )
+{
+    if( threadIdx.x != 0 || blockIdx.x != 0 || !ctl->active || ctl->aborted )
+        return;
+    const int noi = ctl->noi;
+    double G[LB_VEC][LB_VEC];
+    for( int p = 0; p < LB_VEC; ++p )
+        for( int q = 0; q < LB_VEC; ++q )
+            G[p][q] = 0;
+    for( int im = 0; im < noi; ++im )
+    {
+        int k = 0;
+        for( int p = 0; p < LB_VEC; ++p )
+            for( int q = p; q < LB_VEC; ++q, ++k )
+                G[p][q] += gram[(size_t)im * LB_GRAM + k];
+    }
+    for( int p = 0; p < LB_VEC; ++p )
+        for( int q = 0; q < p; ++q )
+            G[p][q] = G[q][p];
+    const double eps = ctl->eps;
+    int li           = ctl->local_iter;
+    const int m      = li % LB_MEM;
+    double sc[LB_VEC] = { 0, 0, 0, 0, 0, 0, 0 };
+    bool gd           = li == 0;
+    if( !gd )
+    {
+        const double rinv = G[4 + m][1 + m]; // dg[m] . da[m]
+        if( rinv > eps )
+            ctl->rho[m] = 1.0 / rinv;
+        else
+            gd = true; // restart from steepest descent
+    }
+    if( gd )
+    {
+        for( int k = 0; k < LB_MEM; ++k )
+            ctl->rho[k] = 0;
+        sc[0] = -1;
+        li    = 1;
+    }
+    else
+    {
+        double qc[LB_VEC] = { 1, 0, 0, 0, 0, 0, 0 };
+        for( int k = LB_MEM - 1; k > -1; --k )
+        {
+            const int c = ( k + m + 1 ) % LB_MEM;
+            double x    = 0;
+            for( int j = 0; j < LB_VEC; ++j )
+                x += qc[j] * G[1 + c][j];
+            const double a = ctl->rho[c] * x;
+            ctl->alpha[c]  = a;
+            qc[4 + c] -= a;
+        }
+        const double rhody2 = G[4 + m][4 + m] * ctl->rho[m];
+        const double inv    = rhody2 > eps ? 1.0 / rhody2 : 1.0 / eps;
+        for( int j = 0; j < LB_VEC; ++j )
+            sc[j] = inv * qc[j];
+        for( int k = 0; k < LB_MEM; ++k )
+        {
+            const int c = li < LB_MEM ? k : ( k + m + 1 ) % LB_MEM;
+            double x    = 0;
+            for( int j = 0; j < LB_VEC; ++j )
+                x += sc[j] * G[4 + c][j];
+            sc[1 + c] += ctl->alpha[c] - ctl->rho[c] * x;
+        }
+        for( int j = 0; j < LB_VEC; ++j )
+            sc[j] = -sc[j];
+        ++li;
+    }
+    // rms rotation angle of every image, limited to maxmove
+    double scaling = 1;
+    for( int im = 0; im < noi; ++im )
+    {
+        double th2 = 0;
+        int k      = 0;
+        for( int p = 0; p < LB_VEC; ++p )
+            for( int q = p; q < LB_VEC; ++q, ++k )
+                th2 += ( p == q ? 1.0 : 2.0 ) * sc[p] * sc[q] * gram[(size_t)im * LB_GRAM + k];
+        const double th = sqrt( fmax( th2, 0.0 ) / ctl->nos );
+        const double f  = th > ctl->maxmove ? ctl->maxmove / th : 1.0;
+        scaling         = fmin( f, scaling );
+    }
+    for( int j = 0; j < LB_VEC; ++j )
+        ctl->coef[j] = scaling * sc[j];
+    ctl->local_iter = li;
+    ctl->lb_store   = li % LB_MEM;
+}
+
+// rotation of s about the vector sd by |sd| (Rodrigues); no-op below 1e-20 (oso_rotate)
+template<typename R>
+__device__ __forceinline__ V3<R> rotate_by( V3<R> s, V3<R> sd )
+{
+    const R th = sqrt( dot( sd, sd ) );
+    if( !( th > R( 1e-20 ) ) )
+        return s;
+    const R inv = R( 1 ) / th;
+    const V3<R> u = { sd.x * inv, sd.y * inv, sd.z * inv };
+    R sn, cs;
+    if constexpr( std::is_same<R, float>::value )
+        sincosf( th, &sn, &cs );
+    else
+        sincos( th, &sn, &cs );
+    const V3<R> x = cross( u, s );
+    const R ud    = dot( u, s ) * ( R( 1 ) - cs );
+    return { s.x * cs + x.x * sn + u.x * ud, s.y * cs + x.y * sn + u.y * ud, s.z * cs + x.z * sn + u.z * ud };
+}
+
+// K5' (VP_OSO, LBFGS_OSO): step, rotation, torques, finalisation
+template<typename R>
+__global__ void __launch_bounds__( 256 ) oso_update( GArgs<R> A )
+{
+    __shared__ float red[32];
+    __shared__ int is_last;
+    GnebCtl * ctl = A.ctl;
+    if( !ctl->active )
+        return;
+    const int2 bm     = A.blkmap[blockIdx.x];
+    const int im      = bm.x;
+    const SysDesc & d = A.sd[im];
+    const int i       = bm.y + threadIdx.x;
+    float t2          = 0;
+    const bool abort  = ctl->aborted != 0;
+    if( i < d.nos && !abort )
+    {
+        const long long gi = d.spin_offset + i;
+        V3<R> sd;
+        if( ctl->solver == SOLVER_VP_OSO )
+        {
+            const V3<R> g = A.F.ld( gi );
+            V3<R> v;
+            if( ctl->proj <= 0 )
+                v = { 0, 0, 0 };
+            else
+            {
+                const R ratio = (R)( ctl->proj / ctl->fn2 );
+                v             = { g.x * ratio, g.y * ratio, g.z * ratio };
+            }
+            A.V.st( gi, v );
+            const R dt   = sys_const<R>( d ).dt;
+            const R hmdt = (R)ctl->hm * dt;
+            sd           = { dt * v.x + hmdt * g.x, dt * v.y + hmdt * g.y, dt * v.z + hmdt * g.z };
+        }
+        else
+        {
+            R c[LB_VEC];
+#pragma unroll
+            for( int j = 0; j < LB_VEC; ++j )
+                c[j] = (R)ctl->coef[j];
+            const V3<R> g = A.Gb.ld( gi );
+            sd            = { c[0] * g.x, c[0] * g.y, c[0] * g.z };
+#pragma unroll
+            for( int k = 0; k < LB_MEM; ++k )
+            {
+                const V3<R> a = A.DA[k].ld( gi );
+                const V3<R> e = A.DG[k].ld( gi );
+                sd.x += c[1 + k] * a.x + c[4 + k] * e.x;
+                sd.y += c[1 + k] * a.y + c[4 + k] * e.y;
+                sd.z += c[1 + k] * a.z + c[4 + k] * e.z;
+            }
+            A.DA[ctl->lb_store].st( gi, sd ); // the step becomes the next da
+        }
+        const V3<R> sn = rotate_by( A.s.ld( gi ), sd );
+        A.s.st( gi, sn );
+        // max torque: GNEB |P_perp F_total|, LLG |P_perp fv| (both kept in T)
+        t2 = (float)torque2( A.T.ld( gi ), sn );
+    }
+    float tm = block_max( t2, red );
+    if( threadIdx.x == 0 )
+    {
+        atomicMax( &A.img[im].torque_bits, __float_as_uint( tm ) );
+        __threadfence();
+        unsigned int prev = atomicAdd( &ctl->blocks_done, 1u );
+        is_last           = ( prev == (unsigned int)A.nblocks - 1 );
+    }
+    __syncthreads();
+    if( is_last && threadIdx.x == 0 )
+        finish_iteration( A );
+}
+
+// clear the per-iteration accumulators (E, dist2, tt, ft; the L-BFGS Grams) -- one block
+__global__ void gneb_clear( GnebImage * img, GnebCtl * ctl, double * gram )
 {
     if( !ctl->active )
         return;
@@ -398,6 +756,9 @@ __global__ void gneb_clear( GnebImage * img, GnebCtl * ctl )
         img[k].tt    = 0;
         img[k].ft    = 0;
     }
+    if( gram )
+        for( int k = threadIdx.x; k < ctl->noi * LB_GRAM; k += blockDim.x )
+            gram[k] = 0;
 }
 
 // LLG-VP has no chain scalars; only the global sums are reset
@@ -424,7 +785,7 @@ __global__ void vp_probe_finish( GnebImage * img, GnebCtl * ctl )
 class GnebRun
 {
 public:
-    GnebRun( const std::vector<Image *> & images, bool fp64, int mode ) : mode_( mode )
+    GnebRun( const std::vector<Image *> & images, bool fp64, int mode, int solver ) : mode_( mode ), solver_( solver )
     {
         std::vector<SystemInput> in;
         for( auto * im : images )
@@ -448,6 +809,19 @@ public:
         }
         d_img = dalloc<GnebImage>( noi );
         d_ctl = dalloc<GnebCtl>( 1 );
+        if( solver_ == SOLVER_LBFGS_OSO )
+        {
+            for( int c = 0; c < 3; ++c )
+            {
+                Gb[c] = dalloc_bytes( eng->total_spins() * el );
+                for( int k = 0; k < LB_MEM; ++k )
+                {
+                    DA[k][c] = dalloc_bytes( eng->total_spins() * el );
+                    DG[k][c] = dalloc_bytes( eng->total_spins() * el );
+                }
+            }
+            d_gram = dalloc<double>( (size_t)noi * LB_GRAM );
+        }
     }
     ~GnebRun()
     {
@@ -462,6 +836,19 @@ public:
         }
         dfree( d_img );
         dfree( d_ctl );
+        if( d_gram )
+        {
+            for( int c = 0; c < 3; ++c )
+            {
+                dfree( Gb[c] );
+                for( int k = 0; k < LB_MEM; ++k )
+                {
+                    dfree( DA[k][c] );
+                    dfree( DG[k][c] );
+                }
+            }
+            dfree( d_gram );
+        }
     }
 
     template<typename R>
@@ -479,6 +866,16 @@ public:
         a.h       = eng->has_ddi() ? SoA3<R>{ (R *)eng->field_ptr( 0 ), (R *)eng->field_ptr( 1 ),
                                             (R *)eng->field_ptr( 2 ) }
                                    : SoA3<R>{ nullptr, nullptr, nullptr };
+        if( d_gram )
+        {
+            a.Gb = { (R *)Gb[0], (R *)Gb[1], (R *)Gb[2] };
+            for( int k = 0; k < LB_MEM; ++k )
+            {
+                a.DA[k] = { (R *)DA[k][0], (R *)DA[k][1], (R *)DA[k][2] };
+                a.DG[k] = { (R *)DG[k][0], (R *)DG[k][1], (R *)DG[k][2] };
+            }
+        }
+        a.gram    = d_gram;
         a.img     = d_img;
         a.ctl     = d_ctl;
         a.spring_constant = spring;
@@ -503,6 +900,10 @@ public:
         c.m                 = 1.0;
         c.hm                = 0.5 / c.m;
         c.active            = 1;
+        c.solver            = solver_;
+        c.fv_unit           = mode_ == 1 && solver_ == SOLVER_LBFGS_OSO;
+        c.eps               = eng->fp64() ? 1e-300 : 1e-30; // lbfgs_get_searchdir epsilon
+        c.maxmove           = 3.14159265358979323846 / 200.0;
         h2d( d_ctl, &c, 1 );
         size_t el = eng->fp64() ? sizeof( double ) : sizeof( float );
         for( int k = 0; k < 3; ++k )
@@ -510,6 +911,15 @@ public:
             // on the engine's (non-blocking) stream, ordered before the iterations
             CUDA_CHECK( cudaMemsetAsync( F[k], 0, eng->total_spins() * el, eng->stream() ) );
             CUDA_CHECK( cudaMemsetAsync( V[k], 0, eng->total_spins() * el, eng->stream() ) );
+            if( d_gram )
+            {
+                CUDA_CHECK( cudaMemsetAsync( Gb[k], 0, eng->total_spins() * el, eng->stream() ) );
+                for( int j = 0; j < LB_MEM; ++j )
+                {
+                    CUDA_CHECK( cudaMemsetAsync( DA[j][k], 0, eng->total_spins() * el, eng->stream() ) );
+                    CUDA_CHECK( cudaMemsetAsync( DG[j][k], 0, eng->total_spins() * el, eng->stream() ) );
+                }
+            }
         }
         if( graph )
         {
@@ -533,7 +943,7 @@ public:
         auto a  = args<R>();
         auto st = eng->stream();
         eng->run_ddi( eng_spins(), nullptr );
-        gneb_clear<<<1, 64, 0, st>>>( d_img, d_ctl );
+        gneb_clear<<<1, 64, 0, st>>>( d_img, d_ctl, d_gram );
         gneb_eval<R><<<eng->n_blocks(), 256, 0, st>>>( a, 1 );
         vp_probe_finish<<<1, 1, 0, st>>>( d_img, d_ctl );
         CUDA_CHECK( cudaGetLastError() );
@@ -554,7 +964,7 @@ public:
         auto st = eng->stream();
         int nb  = eng->n_blocks();
         eng->run_ddi( eng_spins(), nullptr );
-        gneb_clear<<<1, 64, 0, st>>>( d_img, d_ctl );
+        gneb_clear<<<1, 256, 0, st>>>( d_img, d_ctl, d_gram );
         gneb_eval<R><<<nb, 256, 0, st>>>( a, 0 );
         if( mode_ == 0 )
         {
@@ -563,8 +973,18 @@ public:
         }
         else
             gneb_scalars_vp<<<1, 32, 0, st>>>( d_ctl );
-        gneb_force<R><<<nb, 256, 0, st>>>( a );
-        gneb_update<R><<<nb, 256, 0, st>>>( a );
+        if( solver_ == SOLVER_VP )
+        {
+            gneb_force<R><<<nb, 256, 0, st>>>( a );
+            gneb_update<R><<<nb, 256, 0, st>>>( a );
+        }
+        else
+        {
+            oso_force<R><<<nb, 256, 0, st>>>( a );
+            if( solver_ == SOLVER_LBFGS_OSO )
+                lbfgs_dir<<<1, 32, 0, st>>>( d_ctl, d_gram );
+            oso_update<R><<<nb, 256, 0, st>>>( a );
+        }
         CUDA_CHECK( cudaGetLastError() );
     }
 
@@ -615,8 +1035,11 @@ public:
     std::unique_ptr<Engine> eng;
     int noi;
     int mode_;
+    int solver_;
     double spring = 1;
     void * F[3] = {}, *V[3] = {}, *T[3] = {}, *G[3] = {};
+    void * Gb[3] = {}, *DA[LB_MEM][3] = {}, *DG[LB_MEM][3] = {};
+    double * d_gram = nullptr;
     GnebImage * d_img = nullptr;
     GnebCtl * d_ctl   = nullptr;
     cudaGraphExec_t graph = nullptr;
@@ -677,7 +1100,7 @@ static void finish_chain( State * st, Chain & chain, GnebRun & R )
         log_msg( st, 1, "The geodesic distance between two images is zero! Stopping..." );
 }
 
-void gneb_start( State * st, Chain & chain, bool singleshot )
+void gneb_start( State * st, Chain & chain, int solver, bool singleshot )
 {
     std::vector<Image *> ims;
     std::vector<int> types;
@@ -686,14 +1109,14 @@ void gneb_start( State * st, Chain & chain, bool singleshot )
         ims.push_back( im.get() );
         types.push_back( im->gneb_type );
     }
-    auto R = std::make_shared<GnebRun>( ims, st->precision == 64, 0 );
+    auto R = std::make_shared<GnebRun>( ims, st->precision == 64, 0, solver );
     for( int k = 0; k < R->noi; ++k )
         R->eng->set_spins( k, ims[k]->spins.data() );
     R->start( types, (int)chain.gneb.n_iterations, chain.gneb.force_convergence, chain.gneb.spring_constant );
     chain.info              = MethodInfo{};
     chain.info.method       = "GNEB";
-    chain.info.solver       = "VP";
-    chain.info.solver_id    = SOLVER_VP;
+    chain.info.solver       = solver == SOLVER_VP ? "VP" : ( solver == SOLVER_VP_OSO ? "VP_OSO" : "LBFGS_OSO" );
+    chain.info.solver_id    = solver;
     chain.info.n_iterations = (int)chain.gneb.n_iterations;
     chain.info.t_start      = std::chrono::steady_clock::now();
     chain.iteration_allowed  = true;
@@ -769,9 +1192,9 @@ static void finish_vp( Image & img, GnebRun & R )
     img.info.ips     = img.info.wall_ms > 0 ? 1000.0 * c.iteration / img.info.wall_ms : 0;
 }
 
-void llg_vp_run( State * st, Image & img, bool singleshot )
+void llg_vp_run( State * st, Image & img, int solver, bool singleshot )
 {
-    auto R = std::make_shared<GnebRun>( std::vector<Image *>{ &img }, st->precision == 64, 1 );
+    auto R = std::make_shared<GnebRun>( std::vector<Image *>{ &img }, st->precision == 64, 1, solver );
     R->eng->set_spins( 0, img.spins.data() );
     R->start( { 0 }, (int)img.llg.n_iterations, img.llg.force_convergence, 1.0 );
     if( singleshot )

@@ -1,4 +1,5 @@
-// GNEB (chain of images, VP solver) and the VP / batched LLG drivers behind the C API.
+// GNEB (chain of images; VP, VP_OSO or LBFGS_OSO) and the direct-minimisation / batched LLG
+// drivers behind the C API.
 #pragma once
 #include "state.hpp"
 
@@ -7,13 +8,14 @@
 namespace sg
 {
 
-void gneb_start( State * st, Chain & chain, bool singleshot );
+void gneb_start( State * st, Chain & chain, int solver, bool singleshot );
 void gneb_n_shot( State * st, Chain & chain, int n );
 void gneb_update_rx( Chain & chain );
 const std::vector<double> & gneb_torques( Chain & chain );
 
-// LLG with the VP solver on one image (direct minimisation; Solver_VP.hpp:28-114 with Method_LLG)
-void llg_vp_run( State * st, Image & img, bool singleshot );
+// LLG direct minimisation on one image with VP (Solver_VP.hpp:28-114), VP_OSO or LBFGS_OSO
+// (Solver_VP_OSO.hpp, Solver_LBFGS_OSO.hpp) under Method_LLG
+void llg_vp_run( State * st, Image & img, int solver, bool singleshot );
 void llg_vp_shot( State * st, Image & img, int n );
 
 // batched LLG over the active images of several States (one device batch)

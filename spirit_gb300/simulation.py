@@ -16,6 +16,8 @@ SOLVER_SIB = 1
 SOLVER_DEPONDT = 2
 SOLVER_HEUN = 3
 SOLVER_RK4 = 4
+SOLVER_LBFGS_OSO = 5
+SOLVER_VP_OSO = 7
 
 
 class simulation_run_info(ctypes.Structure):

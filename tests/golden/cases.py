@@ -103,6 +103,11 @@ LLG_CASES = [
     ("sc3d_ddi", "Heun", 3, 50),
     ("open2d_ddi", "RK4", 4, 50),
     ("hex2d", "SIB", 1, 100),
+    # direct minimisers with exponential transforms (Solver_VP_OSO.hpp, Solver_LBFGS_OSO.hpp)
+    ("sq_c1", "VP_OSO", 7, 50),  # VP projections switch branch on rounding after ~100
+    ("sq_c1", "LBFGS_OSO", 5, 200),
+    ("sc3d_ddi", "LBFGS_OSO", 5, 60),
+    ("open2d_ddi", "VP_OSO", 7, 60),
 ]
 
 SPIN_SEED = {"sq_c1": 11, "sc3d_ddi": 12, "hex2d": 13, "open2d_ddi": 14, "ddi_irregular": 15,

@@ -6,7 +6,9 @@ generated here from fixed seeds and injected through System_Get_Spin_Directions,
 its outputs into small .npz files.  Needs the reference sources (only in the build
 container); the fixtures it writes are committed and the tests read only those.
 
-    make -C oracle/ref -j8 && python tests/golden/make_golden.py
+    make -C oracle/ref -j8 && python tests/golden/make_golden.py [--only SUBSTRING]
+
+--only regenerates just the fixtures whose name contains SUBSTRING.
 """
 import os
 import subprocess
@@ -52,11 +54,17 @@ def nos_of(spec):
     return n[0] * n[1] * n[2] * len(spec.get("basis", [[0, 0, 0]]))
 
 
-def main():
+def main(only=None):
     tmp = tempfile.mkdtemp(prefix="golden_")
     out = {}
+
+    def want(tag):
+        return only is None or only in tag
+
     # --- neighbour / DMI pair lists
     for name, spec in PAIR_GEOMETRIES.items():
+        if not want("pairs_" + name):
+            continue
         cfg = write_config(spec, os.path.join(tmp, name + ".cfg"))
         run(["pairs", cfg, os.path.join(tmp, name)], tmp)
         ex = np.loadtxt(os.path.join(tmp, name + "_exchange.txt"), ndmin=2)
@@ -70,6 +78,8 @@ def main():
         out[name] = (len(ex), len(dm))
     # --- gradients and energies
     for name, spec in GRAD_CASES.items():
+        if not want("grad_" + name):
+            continue
         cfg = write_config(spec, os.path.join(tmp, name + ".cfg"))
         nos = nos_of(spec)
         spins = random_spins(nos, SPIN_SEED[name])
@@ -96,6 +106,8 @@ def main():
         out[name] = E["total"]
     # --- LLG trajectories (T = 0)
     for case, sname, sid, n_iter in LLG_CASES:
+        if not want("llg_%s_%s" % (case, sname)):
+            continue
         spec = GRAD_CASES[case]
         cfg = write_config(spec, os.path.join(tmp, case + ".cfg"))
         nos = nos_of(spec)
@@ -131,16 +143,21 @@ def main():
     chain.tofile(cp)
     # VP with a chain-global velocity projection switches branches on rounding-level differences,
     # so step-by-step parity is pinned over a short run; the converged run pins the saddle.
-    for tag_name, n1, n2 in (("gneb_vp", 20, 0), ("gneb_vp_ci", 20, 20), ("gneb_converged", 20000, 200000)):
+    # The OSO solvers (VP_OSO = 7, LBFGS_OSO = 5) are pinned the same way over short runs.
+    for tag_name, sid, n1, n2 in (("gneb_vp", 0, 20, 0), ("gneb_vp_ci", 0, 20, 20),
+                                  ("gneb_converged", 0, 20000, 200000), ("gneb_vp_oso", 7, 20, 0),
+                                  ("gneb_lbfgs_oso", 5, 20, 0), ("gneb_lbfgs_oso_ci", 5, 20, 20)):
+        if not want(tag_name):
+            continue
         tag = os.path.join(tmp, tag_name)
-        run(["gneb", cfg, cp, tag, str(noi), "0", str(n1), str(n2)], tmp)
+        run(["gneb", cfg, cp, tag, str(noi), str(sid), str(n1), str(n2)], tmp)
         rows = [l.split() for l in open(tag + "_result.txt")]
         img = [r_ for r_ in rows if r_[0] == "image"]
         np.savez_compressed(
             os.path.join(HERE, "%s.npz" % tag_name), config=config_text(spec), chain_in=chain,
             chain_out=load_bin(tag + "_chain.bin", (noi, nos, 3)),
             energies=np.array([float(r_[3]) for r_ in img]), Rx=np.array([float(r_[5]) for r_ in img]),
-            image_type=np.array([int(r_[7]) for r_ in img]), n_iter=n1, n_iter_ci=n2,
+            image_type=np.array([int(r_[7]) for r_ in img]), n_iter=n1, n_iter_ci=n2, solver=sid,
             max_torque=float([r_ for r_ in rows if r_[0] == "max_torque"][0][1]),
         )
         out[tag_name] = [float(r_[3]) for r_ in img]
@@ -149,4 +166,8 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    import argparse
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", default=None)
+    main(ap.parse_args().only)

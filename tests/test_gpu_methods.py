@@ -25,20 +25,21 @@ def _load_chain(p, chain_in):
         system.get_spin_directions(p, i)[:] = chain_in[i]
 
 
-@pytest.mark.parametrize("tag", ["gneb_vp", "gneb_vp_ci"])
+@pytest.mark.parametrize("tag", ["gneb_vp", "gneb_vp_ci", "gneb_vp_oso", "gneb_lbfgs_oso", "gneb_lbfgs_oso_ci"])
 def test_gneb_short_fp64(tag):
     from spirit_gb300 import chain, simulation, system
     import spirit_gb300.parameters.gneb as gneb
 
     f = golden("%s.npz" % tag)
+    sid = int(f["solver"]) if "solver" in f else simulation.SOLVER_VP
     with make_state(SOLVERS, precision=64) as p:
         _load_chain(p, f["chain_in"])
-        simulation.start(p, simulation.METHOD_GNEB, simulation.SOLVER_VP, int(f["n_iter"]))
+        simulation.start(p, simulation.METHOD_GNEB, sid, int(f["n_iter"]))
         if int(f["n_iter_ci"]) > 0:
             gneb.set_image_type_automatically(p)
             types = [gneb.get_climbing_falling(p, i) for i in range(9)]
             assert types == list(f["image_type"])
-            simulation.start(p, simulation.METHOD_GNEB, simulation.SOLVER_VP, int(f["n_iter_ci"]))
+            simulation.start(p, simulation.METHOD_GNEB, sid, int(f["n_iter_ci"]))
         out = np.stack([spins_of(p, i) for i in range(9)])
         E = np.array([system.get_energy_fp64(p, i) for i in range(9)])
         Rx = np.array([system.get_rx(p, i) for i in range(9)])
@@ -48,10 +49,12 @@ def test_gneb_short_fp64(tag):
 
 
 @pytest.mark.parametrize("precision", [64, 32])
-def test_gneb_converged_saddle(precision):
-    """Skyrmion collapse on the reference solver-test system: VP, then climbing image until the
-    max torque is below the convergence threshold (1e-6 meV FP64, 1e-4 FP32 as the reference's
-    float build uses); the saddle energy matches the reference within 1e-5 (FP64) / 5e-3 (FP32)."""
+@pytest.mark.parametrize("solver", [0, 5, 7])
+def test_gneb_converged_saddle(solver, precision):
+    """Skyrmion collapse on the reference solver-test system (core/test/test_solvers.cpp:73-133,
+    solvers VP, LBFGS_OSO, VP_OSO): 20000 iterations, then climbing image until the max torque is
+    below the convergence threshold (1e-6 meV FP64, 1e-4 FP32 as the reference's float build
+    uses); the saddle energy matches the reference within 1e-5 (FP64) / 5e-3 (FP32)."""
     from spirit_gb300 import simulation, system
     import spirit_gb300.parameters.gneb as gneb
 
@@ -60,9 +63,9 @@ def test_gneb_converged_saddle(precision):
     with make_state(SOLVERS, precision=precision) as p:
         gneb.set_convergence(p, conv)
         _load_chain(p, f["chain_in"])
-        simulation.start(p, simulation.METHOD_GNEB, simulation.SOLVER_VP, 20000)
+        simulation.start(p, simulation.METHOD_GNEB, solver, 20000)
         gneb.set_image_type_automatically(p)
-        simulation.start(p, simulation.METHOD_GNEB, simulation.SOLVER_VP, 200000)
+        simulation.start(p, simulation.METHOD_GNEB, solver, 200000)
         E = np.array([system.get_energy_fp64(p, i) for i in range(9)])
         mt = simulation.get_max_torque_norm(p)
     assert mt < conv
@@ -72,7 +75,7 @@ def test_gneb_converged_saddle(precision):
 
 
 @pytest.mark.parametrize("precision", [64, 32])
-@pytest.mark.parametrize("solver", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("solver", [0, 1, 2, 3, 4, 5, 7])
 def test_direct_minimisation_skyrmion(solver, precision):
     """core/test/test_solvers.cpp:18-70: plus-z with a skyrmion of radius 5 (order 1, phase -90),
     direct minimisation to convergence; E = -5849.69140625 meV, m = (0, 0, 2*0.79977)."""

@@ -94,6 +94,25 @@ def test_gneb_vp_short(tag):
     np.testing.assert_allclose(r["Rx"], f["Rx"], rtol=1e-11, atol=1e-12)
 
 
+@pytest.mark.parametrize("tag", ["gneb_vp_oso", "gneb_lbfgs_oso", "gneb_lbfgs_oso_ci"])
+def test_gneb_oso_short(tag):
+    """GNEB with the exponential-transform solvers (Method_GNEB<VP_OSO>, Method_GNEB<LBFGS_OSO>)
+    against the reference's own runs; a second start (climbing image) restarts the L-BFGS memory."""
+    f = golden("%s.npz" % tag)
+    o = OracleSystem(SOLVERS)
+    sid = int(f["solver"])
+    c, r = o.gneb(f["chain_in"], int(f["n_iter"]), spring_constant=1.0, force_convergence=1e-6, dt=1e-3, solver=sid)
+    if int(f["n_iter_ci"]) > 0:
+        t = image_types_auto(r["energies"], np.zeros(9))
+        assert np.array_equal(t, f["image_type"])
+        c, r = o.gneb(c, int(f["n_iter_ci"]), image_type=t, spring_constant=1.0, force_convergence=1e-6, dt=1e-3,
+                      solver=sid)
+    assert np.abs(c - f["chain_out"]).max() <= 1e-11
+    np.testing.assert_allclose(r["energies"], f["energies"], rtol=1e-13)
+    np.testing.assert_allclose(r["Rx"], f["Rx"], rtol=1e-11, atol=1e-12)
+    assert abs(r["max_torque"] - float(f["max_torque"])) <= 1e-9 * float(f["max_torque"])
+
+
 @pytest.mark.slow
 def test_gneb_converged_saddle():
     """Converged skyrmion-collapse saddle; the reference test asserts -5811.5244140625 meV
