@@ -653,7 +653,10 @@ __global__ void lbfgs_dir( GnebCtl * ctl, const double * gram )
     ctl->lb_store   = li % LB_MEM;
 }
 
-// rotation of s about the vector sd by |sd| (Rodrigues); no-op below 1e-20 (oso_rotate)
+// rotation of s about the vector sd by |sd| (Rodrigues); no-op below 1e-20 (oso_rotate).  A
+// rotation keeps |s| = 1 in exact arithmetic; in FP32 the rounding of the update (relative 6e-8
+// per step) makes |s| drift over 1e5 iterations enough to move a saddle energy by 1e-2 meV, so
+// the FP32 result is renormalised.  FP64 keeps the reference's arithmetic (no renormalisation).
 template<typename R>
 __device__ __forceinline__ V3<R> rotate_by( V3<R> s, V3<R> sd )
 {
@@ -669,7 +672,11 @@ __device__ __forceinline__ V3<R> rotate_by( V3<R> s, V3<R> sd )
         sincos( th, &sn, &cs );
     const V3<R> x = cross( u, s );
     const R ud    = dot( u, s ) * ( R( 1 ) - cs );
-    return { s.x * cs + x.x * sn + u.x * ud, s.y * cs + x.y * sn + u.y * ud, s.z * cs + x.z * sn + u.z * ud };
+    const V3<R> r = { s.x * cs + x.x * sn + u.x * ud, s.y * cs + x.y * sn + u.y * ud, s.z * cs + x.z * sn + u.z * ud };
+    if constexpr( std::is_same<R, float>::value )
+        return normalized( r );
+    else
+        return r;
 }
 
 // K5' (VP_OSO, LBFGS_OSO): step, rotation, torques, finalisation
