@@ -65,6 +65,8 @@ def lib():
         L.og_llg_run.argtypes = [vp, vp, i, i, P(d), P(d), P(d)]
         L.og_gneb_run.argtypes = [vp, vp, i, i, P(d), P(i), P(d), P(d), P(d)]
         L.og_gneb_run_solver.argtypes = [vp, vp, i, i, i, P(d), P(i), P(d), P(d), P(d)]
+        L.og_htst.argtypes = [vp, P(d), P(d), i, i, vp, P(d), P(d), P(d), P(d), P(d)]
+        L.og_htst.restype = i
         L.og_mc_colors.argtypes = [vp, P(i)]
         L.og_mc_colors.restype = i
         L.og_mc_run.argtypes = [vp, vp, i, P(d), P(d), P(d)]
@@ -300,6 +302,11 @@ class OracleSystem:
         lib().og_mc_run(self.h, ctypes.byref(p), int(n_sweeps), _p(s), ctypes.byref(ca), ctypes.byref(ac))
         return s, {"cone_angle": ca.value, "acceptance": ac.value}
 
+    def htst(self, spins_min, spins_sp, sparse=False, n_keep=-1):
+        """HTST prefactor of the transition minimum -> saddle point (HTST_Calculate); dict of the
+        HTST_Info fields (+ eigenvalues / eigenvectors [mode][2N] / velocities when dense)."""
+        return _htst(self, spins_min, spins_sp, sparse, n_keep)
+
     def gneb(self, chain, n_iter, image_type=None, spring_constant=1.0, force_convergence=1e-6, dt=1e-3,
              solver="VP"):
         c = np.ascontiguousarray(chain, dtype=np.float64).copy()
@@ -313,6 +320,31 @@ class OracleSystem:
         it = lib().og_gneb_run_solver(self.h, ctypes.byref(p), solver_id, noi, int(n_iter), _p(c),
                                       _p(types, ctypes.c_int), _p(E), _p(Rx), ctypes.byref(mt))
         return c, {"iterations": it, "energies": E, "Rx": Rx, "max_torque": mt.value}
+
+
+class HTSTInfo(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in ("temperature_exponent", "me", "Omega_0", "s", "volume_min",
+                                               "volume_sp", "prefactor_dynamical", "prefactor", "det_min",
+                                               "det_sp")] + [("n_eigenmodes_keep", ctypes.c_int),
+                                                             ("status", ctypes.c_int)]
+
+
+def _htst(system, spins_min, spins_sp, sparse=False, n_keep=-1):
+    nos = system.nos
+    a = np.ascontiguousarray(spins_min, dtype=np.float64)
+    b = np.ascontiguousarray(spins_sp, dtype=np.float64)
+    n2 = 2 * nos
+    keep = n2 if n_keep < 0 else min(n_keep, n2)
+    em, es = np.zeros(n2), np.zeros(n2)
+    vm, vs = np.zeros((max(keep, 1), n2)), np.zeros((max(keep, 1), n2))
+    vel = np.zeros(n2)
+    info = HTSTInfo()
+    lib().og_htst(system.h, _p(a), _p(b), int(sparse), int(n_keep), ctypes.byref(info), _p(em), _p(es), _p(vm),
+                  _p(vs), _p(vel))
+    out = {k: getattr(info, k) for k, _ in HTSTInfo._fields_}
+    if not sparse:
+        out.update(evalues_min=em, evalues_sp=es, evectors_min=vm[:keep], evectors_sp=vs[:keep], velocities=vel)
+    return out
 
 
 def image_types_auto(energies, image_type):

@@ -13,11 +13,14 @@
 //   golden_harness direct  <cfg> <spins.bin> <out>         same, after switching DDI to the direct sum
 //   golden_harness llg     <cfg> <spins.bin> <out> <solver> <n_iter>
 //   golden_harness gneb    <cfg> <chain.bin> <out> <noi> <solver> <n_iter> [<n_iter_ci>]
+//   golden_harness htst    <cfg> <chain.bin> <out> <noi> <idx_min> <idx_sp> <sparse> <n_keep>
+//                                                        HTST_Calculate on two images of a chain
 //
 // Binary files are little-endian float64 arrays; text outputs are whitespace separated.
 #include <Spirit/Chain.h>
 #include <Spirit/Configurations.h>
 #include <Spirit/Geometry.h>
+#include <Spirit/HTST.h>
 #include <Spirit/Hamiltonian.h>
 #include <Spirit/Parameters_GNEB.h>
 #include <Spirit/Parameters_LLG.h>
@@ -215,6 +218,50 @@ int main( int argc, char ** argv )
         std::fprintf( f, "max_torque %.17g\n", (double)s->method_chain->getTorqueMaxNorm() );
         std::fprintf( f, "iterations %d\n", s->method_chain->getNIterations() );
         std::fclose( f );
+    }
+    else if( op == "htst" )
+    {
+        auto chain_in   = read_bin( argv[3] );
+        std::string out = argv[4];
+        int noi         = std::atoi( argv[5] );
+        int idx_min     = std::atoi( argv[6] );
+        int idx_sp      = std::atoi( argv[7] );
+        bool sparse     = std::atoi( argv[8] ) != 0;
+        int n_keep      = std::atoi( argv[9] );
+        Chain_Image_to_Clipboard( s );
+        for( int i = 1; i < noi; ++i )
+            Chain_Insert_Image_After( s );
+        int nos = System_Get_NOS( s );
+        for( int i = 0; i < noi; ++i )
+        {
+            double * d = System_Get_Spin_Directions( s, i );
+            std::memcpy( d, chain_in.data() + (size_t)3 * nos * i, sizeof( double ) * 3 * nos );
+        }
+        float pf    = HTST_Calculate( s, idx_min, idx_sp, n_keep, sparse );
+        auto & info = s->chain->htst_info;
+        FILE * f    = std::fopen( ( out + "_result.txt" ).c_str(), "w" );
+        std::fprintf( f, "prefactor_float %.9g\n", (double)pf );
+        std::fprintf( f, "temperature_exponent %.17g\n", (double)info.temperature_exponent );
+        std::fprintf( f, "me %.17g\n", (double)info.me );
+        std::fprintf( f, "Omega_0 %.17g\n", (double)info.Omega_0 );
+        std::fprintf( f, "s %.17g\n", (double)info.s );
+        std::fprintf( f, "volume_min %.17g\n", (double)info.volume_min );
+        std::fprintf( f, "volume_sp %.17g\n", (double)info.volume_sp );
+        std::fprintf( f, "prefactor_dynamical %.17g\n", (double)info.prefactor_dynamical );
+        std::fprintf( f, "prefactor %.17g\n", (double)info.prefactor );
+        std::fprintf( f, "det_min %.17g\n", (double)info.det_min );
+        std::fprintf( f, "det_sp %.17g\n", (double)info.det_sp );
+        std::fprintf( f, "n_eigenmodes_keep %d\n", info.n_eigenmodes_keep );
+        std::fclose( f );
+        if( !sparse )
+        {
+            write_bin( out + "_evalues_min.bin", info.eigenvalues_min.data(), info.eigenvalues_min.size() );
+            write_bin( out + "_evalues_sp.bin", info.eigenvalues_sp.data(), info.eigenvalues_sp.size() );
+            write_bin( out + "_evectors_min.bin", info.eigenvectors_min.data(), info.eigenvectors_min.size() );
+            write_bin( out + "_evectors_sp.bin", info.eigenvectors_sp.data(), info.eigenvectors_sp.size() );
+            write_bin(
+                out + "_velocities.bin", info.perpendicular_velocity.data(), info.perpendicular_velocity.size() );
+        }
     }
     State_Delete( s );
     return 0;

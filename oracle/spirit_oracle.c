@@ -2239,3 +2239,477 @@ int og_mc_run( og_system * s, const og_mc_params * p, int n_sweeps, double * spi
     free( colors );
     return n_sweeps;
 }
+
+/* ---------------------------------------------------------------- HTST
+ * Harmonic transition-state theory prefactor (core/src/engine/HTST.cpp:29-346 dense,
+ * Sparse_HTST.cpp:246-533 sparse), with Hamiltonian_Heisenberg::Hessian
+ * (Hamiltonian_Heisenberg.cpp:1119-1275; the anisotropy term puts its beta sum on the diagonal as
+ * the reference writes it), hessian_bordered_3N (HTST.cpp:484-503), tangent_basis_spherical
+ * (Manifoldmath.cpp:254-287), Calculate_Dynamical_Matrix (HTST.cpp:425-482) and
+ * Calculate_Zero_Volume (HTST.cpp:348-410).  The symmetric eigenproblems are solved by cyclic
+ * Jacobi rotations; the sparse variant's log-determinants, lowest modes and linear solve are
+ * evaluated from the same full decomposition (equal up to rounding). */
+#define C_HBAR 0.6582119514
+#define C_G_E 2.00231930436182
+
+/* Hessian (3N x 3N row-major); the sparse variant's Sparse_Hessian (Hamiltonian_Heisenberg.cpp:
+ * 1277-1371) has no dipolar block */
+static void htst_hessian( const og_system * s, double * H, int with_ddi )
+{
+    int nos  = s->nos;
+    size_t n = (size_t)3 * nos;
+    int N    = s->n_cell_atoms;
+    memset( H, 0, sizeof( double ) * n * n );
+    for( int icell = 0; icell < s->n_cells_total; ++icell )
+        for( int k = 0; k < s->n_aniso; ++k )
+        {
+            int i = icell * N + s->aniso_idx[k];
+            for( int a = 0; a < 3; ++a )
+                for( int b = 0; b < 3; ++b )
+                    H[( 3 * i + a ) * n + 3 * i + a]
+                        += -2.0 * s->aniso_mag[k] * s->aniso_normal[k][a] * s->aniso_normal[k][b];
+        }
+    for( int icell = 0; icell < s->n_cells_total; ++icell )
+        for( int p = 0; p < s->n_ex; ++p )
+        {
+            int i = s->ex_pairs[p].i + icell * N;
+            int j = idx_from_pair( s, i, &s->ex_pairs[p] );
+            if( j < 0 )
+                continue;
+            for( int a = 0; a < 3; ++a )
+                H[( 3 * i + a ) * n + 3 * j + a] += -s->ex_mag[p];
+        }
+    for( int icell = 0; icell < s->n_cells_total; ++icell )
+        for( int p = 0; p < s->n_dmi; ++p )
+        {
+            int i = s->dmi_pairs[p].i + icell * N;
+            int j = idx_from_pair( s, i, &s->dmi_pairs[p] );
+            if( j < 0 )
+                continue;
+            const double d = s->dmi_mag[p], * nn = s->dmi_normal + 3 * p;
+            size_t r = 3 * (size_t)i, c = 3 * (size_t)j;
+            H[( r + 2 ) * n + c + 1] += d * nn[0];
+            H[( r + 1 ) * n + c + 2] += -d * nn[0];
+            H[( r + 0 ) * n + c + 2] += d * nn[1];
+            H[( r + 2 ) * n + c + 0] += -d * nn[1];
+            H[( r + 1 ) * n + c + 0] += d * nn[2];
+            H[( r + 0 ) * n + c + 1] += -d * nn[2];
+        }
+    if( s->ddi_method != 0 && with_ddi )
+    {
+        const double mult = C_MU_0 * C_MU_B * C_MU_B / ( 4 * C_PI * 1e-30 );
+        for( int i = 0; i < nos; ++i )
+            for( int j = 0; j < nos; ++j )
+            {
+                double d[3];
+                for( int e = 0; e < 3; ++e )
+                    d[e] = s->positions[3 * j + e] - s->positions[3 * i + e];
+                double r = norm3( d );
+                double D[3][3] = { { 0 } };
+                if( r > 1e-10 )
+                {
+                    double r3 = r * r * r, r5 = r3 * r * r;
+                    for( int a = 0; a < 3; ++a )
+                        for( int b = 0; b < 3; ++b )
+                            D[a][b] = mult * ( 3 * d[a] * d[b] / r5 - ( a == b ? 1 / r3 : 0 ) );
+                }
+                double m = s->mu_s[i] * s->mu_s[j];
+                for( int a = 0; a < 3; ++a )
+                    for( int b = 0; b < 3; ++b )
+                        H[( 3 * i + a ) * n + 3 * j + b] += -m * D[a][b];
+            }
+    }
+}
+
+/* columns 2i, 2i+1 of the tangent basis at spin i */
+static void htst_basis( const double * sp, double e1[3], double e2[3] )
+{
+    double t1[3], t2[3];
+    if( sp[2] > 1 - 1e-8 )
+    {
+        double a[3] = { 1, 0, 0 }, b[3] = { 0, 1, 0 };
+        memcpy( t1, a, sizeof( a ) );
+        memcpy( t2, b, sizeof( b ) );
+    }
+    else if( sp[2] < -1 + 1e-8 )
+    {
+        double a[3] = { 1, 0, 0 }, b[3] = { 0, -1, 0 };
+        memcpy( t1, a, sizeof( a ) );
+        memcpy( t2, b, sizeof( b ) );
+    }
+    else
+    {
+        double rxy = sqrt( 1 - sp[2] * sp[2] ), z = sp[2] / rxy;
+        double a[3] = { sp[0] * z, sp[1] * z, -rxy }, b[3] = { -sp[1] / rxy, sp[0] / rxy, 0 };
+        memcpy( t1, a, sizeof( a ) );
+        memcpy( t2, b, sizeof( b ) );
+    }
+    double d1 = dot3( t1, sp ), d2 = dot3( t2, sp );
+    for( int e = 0; e < 3; ++e )
+    {
+        e1[e] = t1[e] - d1 * sp[e];
+        e2[e] = t2[e] - d2 * sp[e];
+    }
+    normalize3( e1 );
+    normalize3( e2 );
+}
+
+/* out (2N x 2N) = B^T M B for a 3N x 3N row-major M */
+static void htst_project( int nos, const double * B /* nos x 2 x 3 */, const double * M, double * out )
+{
+    size_t n3 = (size_t)3 * nos, n2 = (size_t)2 * nos;
+#pragma omp parallel for
+    for( int i = 0; i < nos; ++i )
+        for( int j = 0; j < nos; ++j )
+            for( int a = 0; a < 2; ++a )
+                for( int b = 0; b < 2; ++b )
+                {
+                    double v = 0;
+                    for( int x = 0; x < 3; ++x )
+                        for( int y = 0; y < 3; ++y )
+                            v += B[6 * i + 3 * a + x] * M[( 3 * i + x ) * n3 + 3 * j + y] * B[6 * j + 3 * b + y];
+                    out[( 2 * i + a ) * n2 + 2 * j + b] = v;
+                }
+}
+
+/* cyclic Jacobi eigen-decomposition of a symmetric n x n matrix (destroyed); eigenvalues ascending,
+ * eigenvectors as columns of V (row-major n x n) */
+static void htst_eigh( int n, double * A, double * w, double * V )
+{
+    for( int i = 0; i < n; ++i )
+        for( int j = 0; j < n; ++j )
+            V[(size_t)i * n + j] = i == j;
+    for( int sweep = 0; sweep < 100; ++sweep )
+    {
+        double off = 0, tot = 0;
+        for( int i = 0; i < n; ++i )
+            for( int j = 0; j < n; ++j )
+            {
+                double x = A[(size_t)i * n + j] * A[(size_t)i * n + j];
+                tot += x;
+                if( i != j )
+                    off += x;
+            }
+        if( off <= 1e-30 * tot || off == 0 )
+            break;
+        for( int p = 0; p < n - 1; ++p )
+            for( int q = p + 1; q < n; ++q )
+            {
+                double apq = A[(size_t)p * n + q];
+                if( apq == 0 )
+                    continue;
+                double app = A[(size_t)p * n + p], aqq = A[(size_t)q * n + q];
+                double th = ( aqq - app ) / ( 2 * apq );
+                double t  = ( th >= 0 ? 1.0 : -1.0 ) / ( fabs( th ) + sqrt( th * th + 1 ) );
+                double c = 1 / sqrt( t * t + 1 ), sn = t * c;
+                for( int k = 0; k < n; ++k )
+                {
+                    double akp = A[(size_t)k * n + p], akq = A[(size_t)k * n + q];
+                    A[(size_t)k * n + p] = c * akp - sn * akq;
+                    A[(size_t)k * n + q] = sn * akp + c * akq;
+                }
+                for( int k = 0; k < n; ++k )
+                {
+                    double apk = A[(size_t)p * n + k], aqk = A[(size_t)q * n + k];
+                    A[(size_t)p * n + k] = c * apk - sn * aqk;
+                    A[(size_t)q * n + k] = sn * apk + c * aqk;
+                }
+                for( int k = 0; k < n; ++k )
+                {
+                    double vkp = V[(size_t)k * n + p], vkq = V[(size_t)k * n + q];
+                    V[(size_t)k * n + p] = c * vkp - sn * vkq;
+                    V[(size_t)k * n + q] = sn * vkp + c * vkq;
+                }
+            }
+    }
+    /* sort ascending (selection sort, swapping columns) */
+    for( int i = 0; i < n; ++i )
+        w[i] = A[(size_t)i * n + i];
+    for( int i = 0; i < n; ++i )
+    {
+        int m = i;
+        for( int j = i + 1; j < n; ++j )
+            if( w[j] < w[m] )
+                m = j;
+        if( m != i )
+        {
+            double t = w[i];
+            w[i]     = w[m];
+            w[m]     = t;
+            for( int k = 0; k < n; ++k )
+            {
+                double x             = V[(size_t)k * n + i];
+                V[(size_t)k * n + i] = V[(size_t)k * n + m];
+                V[(size_t)k * n + m] = x;
+            }
+        }
+    }
+}
+
+/* geodesic (bordered, tangent-projected) Hessian of an image; returns max torque of the gradient */
+static double htst_geodesic(
+    og_system * s, const double * spins, double * H3, double * B, double * H2, double * g, int with_ddi )
+{
+    int nos  = s->nos;
+    size_t n = (size_t)3 * nos;
+    og_gradient( s, spins, g );
+    double fm = 0;
+    for( int i = 0; i < nos; ++i )
+    {
+        double f[3] = { g[3 * i], g[3 * i + 1], g[3 * i + 2] };
+        double d    = dot3( f, spins + 3 * i );
+        for( int e = 0; e < 3; ++e )
+            f[e] -= d * spins[3 * i + e];
+        fm = fmax( fm, norm3( f ) );
+    }
+    htst_hessian( s, H3, with_ddi );
+    for( int i = 0; i < nos; ++i )
+    {
+        double u[3] = { spins[3 * i], spins[3 * i + 1], spins[3 * i + 2] };
+        normalize3( u );
+        double lam = dot3( u, g + 3 * i );
+        for( int e = 0; e < 3; ++e )
+            H3[( 3 * i + e ) * n + 3 * i + e] -= lam;
+        htst_basis( spins + 3 * i, B + 6 * i, B + 6 * i + 3 );
+    }
+    htst_project( nos, B, H3, H2 );
+    return fm;
+}
+
+/* Calculate_Zero_Volume */
+static double htst_zero_volume( const og_system * s, const double * spins )
+{
+    int nos = s->nos, dim = 0;
+    double len[3] = { 0, 0, 0 };
+    double * sh   = (double *)malloc( sizeof( double ) * 3 * nos );
+    for( int ib = 0; ib < 3; ++ib )
+    {
+        if( !( s->bc[ib] && s->n_cells[ib] > 1 ) )
+            continue;
+        int shift = ib == 0 ? s->n_cell_atoms
+                            : ( ib == 1 ? s->n_cell_atoms * s->n_cells[0] : s->n_cell_atoms * s->n_cells[0] * s->n_cells[1] );
+        for( int i = 0; i < nos; ++i )
+            memcpy( sh + 3 * ( ( i + shift ) % nos ), spins + 3 * i, sizeof( double ) * 3 );
+        len[ib] = dist_geodesic( nos, spins, sh );
+        ++dim;
+    }
+    free( sh );
+    double b[3][3];
+    for( int k = 0; k < 3; ++k )
+    {
+        memcpy( b[k], s->bravais[k], sizeof( b[k] ) );
+        normalize3( b[k] );
+    }
+    double c[3];
+    cross3( b[0], b[1], c );
+    if( dim == 1 )
+        return len[0];
+    if( dim == 2 )
+        return len[0] * len[1] * norm3( c );
+    if( dim == 3 )
+        return len[0] * len[1] * len[2] * fabs( dot3( c, b[2] ) );
+    return 1;
+}
+
+/* w = (B^T V B)^T q with V the dynamical matrix of the bordered Hessian H3 (Calculate_Dynamical_Matrix) */
+static void htst_velocity_T( const og_system * s, const double * spins, const double * H3, const double * B,
+                             const double * q, double * w )
+{
+    int nos  = s->nos;
+    size_t n = (size_t)3 * nos;
+    double * V = (double *)calloc( n * n, sizeof( double ) );
+    for( int i = 0; i < nos; ++i )
+    {
+        const double * si = spins + 3 * i;
+        double beff[3]    = { 0, 0, 0 };
+        for( size_t c = 0; c < n; ++c )
+        {
+            double h[3] = { H3[( 3 * i ) * n + c], H3[( 3 * i + 1 ) * n + c], H3[( 3 * i + 2 ) * n + c] };
+            V[( 3 * i ) * n + c]     = si[1] * h[2] - si[2] * h[1];
+            V[( 3 * i + 1 ) * n + c] = si[2] * h[0] - si[0] * h[2];
+            V[( 3 * i + 2 ) * n + c] = si[0] * h[1] - si[1] * h[0];
+        }
+        for( int j = 0; j < nos; ++j )
+            for( int a = 0; a < 3; ++a )
+                for( int b = 0; b < 3; ++b )
+                    beff[a] -= H3[( 3 * i + a ) * n + 3 * j + b] * spins[3 * j + b];
+        V[( 3 * i ) * n + 3 * i + 1] -= beff[2];
+        V[( 3 * i ) * n + 3 * i + 2] += beff[1];
+        V[( 3 * i + 1 ) * n + 3 * i] += beff[2];
+        V[( 3 * i + 1 ) * n + 3 * i + 2] -= beff[0];
+        V[( 3 * i + 2 ) * n + 3 * i] -= beff[1];
+        V[( 3 * i + 2 ) * n + 3 * i + 1] += beff[0];
+        for( int a = 0; a < 3; ++a )
+            for( size_t c = 0; c < n; ++c )
+                V[( 3 * i + a ) * n + c] /= s->mu_s[i];
+    }
+    double * V2 = (double *)malloc( sizeof( double ) * 4 * nos * nos );
+    htst_project( nos, B, V, V2 );
+    size_t n2 = (size_t)2 * nos;
+    for( size_t c = 0; c < n2; ++c )
+    {
+        double x = 0;
+        for( size_t r = 0; r < n2; ++r )
+            x += V2[r * n2 + c] * q[r];
+        w[c] = x;
+    }
+    free( V );
+    free( V2 );
+}
+
+int og_htst(
+    og_system * s, const double * spins_min, const double * spins_sp, int sparse, int n_keep, og_htst_info * info,
+    double * evalues_min, double * evalues_sp, double * evectors_min, double * evectors_sp, double * velocities )
+{
+    const double eps = 1e-4, eps_force = 1e-8;
+    int nos = s->nos, n2 = 2 * nos;
+    size_t n = (size_t)3 * nos;
+    memset( info, 0, sizeof( *info ) );
+    if( n_keep < 0 )
+        n_keep = n2;
+    n_keep                  = n_keep < n2 ? n_keep : n2;
+    info->n_eigenmodes_keep = sparse ? 0 : n_keep;
+    double * H3 = (double *)malloc( sizeof( double ) * n * n );
+    double * B  = (double *)malloc( sizeof( double ) * 6 * nos );
+    double * H2 = (double *)malloc( sizeof( double ) * n2 * n2 );
+    double * Q  = (double *)malloc( sizeof( double ) * n2 * n2 );
+    double * ws = (double *)malloc( sizeof( double ) * n2 );
+    double * wm = (double *)malloc( sizeof( double ) * n2 );
+    double * g  = (double *)malloc( sizeof( double ) * n );
+    double * q0 = (double *)malloc( sizeof( double ) * n2 );
+    double * a  = (double *)malloc( sizeof( double ) * n2 );
+    int status  = 0;
+    if( htst_geodesic( s, spins_min, H3, B, H2, g, !sparse ) > eps_force )
+    {
+        status = 1; /* minimum not converged */
+        goto out;
+    }
+    if( htst_geodesic( s, spins_sp, H3, B, H2, g, !sparse ) > eps_force )
+    {
+        status = 2; /* saddle point not converged */
+        goto out;
+    }
+    /* saddle point (H3, B, H2 hold the saddle point's matrices) */
+    htst_eigh( n2, H2, ws, Q );
+    if( ws[0] > -eps )
+    {
+        status = 3;
+        goto out;
+    }
+    {
+        int n_neg = 0, lim = sparse ? ( n2 < 6 ? n2 : 6 ) : n2;
+        for( int i = 0; i < lim; ++i )
+            n_neg += ws[i] < -eps;
+        if( n_neg > 1 )
+        {
+            status = 4;
+            goto out;
+        }
+    }
+    for( int r = 0; r < n2; ++r )
+        q0[r] = Q[(size_t)r * n2];
+    htst_velocity_T( s, spins_sp, H3, B, q0, a ); /* a = V2^T q0 */
+    int n0_sp = 0;
+    {
+        int lim = sparse ? ( n2 < 6 ? n2 : 6 ) : n2;
+        for( int i = 0; i < lim; ++i )
+            n0_sp += fabs( ws[i] ) <= eps;
+    }
+    info->volume_sp = n0_sp > 0 ? htst_zero_volume( s, spins_sp ) : 1;
+    if( !sparse )
+    {
+        /* perpendicular velocities a_k = (V2^T q0) . q_k */
+        for( int k = 0; k < n2; ++k )
+        {
+            double x = 0;
+            for( int r = 0; r < n2; ++r )
+                x += a[r] * Q[(size_t)r * n2 + k];
+            velocities[k] = x;
+        }
+        double s2 = 0;
+        for( int i = n0_sp + 1; i < n2; ++i )
+            s2 += velocities[i] * velocities[i] / ws[i];
+        info->s = sqrt( s2 );
+        memcpy( evalues_sp, ws, sizeof( double ) * n2 );
+        for( int k = 0; k < n_keep; ++k )
+            for( int r = 0; r < n2; ++r )
+                evectors_sp[(size_t)k * n2 + r] = Q[(size_t)r * n2 + k];
+    }
+    else
+    {
+        /* s^2 = b . H^-1 b with b = V2^T q0; log|det| minus the unstable mode */
+        double s2 = 0, ld = 0;
+        for( int k = 0; k < n2; ++k )
+        {
+            double x = 0;
+            for( int r = 0; r < n2; ++r )
+                x += a[r] * Q[(size_t)r * n2 + k];
+            s2 += x * x / ws[k];
+            ld += log( fabs( ws[k] ) );
+        }
+        info->s      = sqrt( s2 );
+        info->det_sp = ld - log( -ws[0] );
+    }
+    /* minimum */
+    htst_geodesic( s, spins_min, H3, B, H2, g, !sparse );
+    htst_eigh( n2, H2, wm, Q );
+    if( !sparse && wm[0] < -eps )
+    {
+        status = 5;
+        goto out;
+    }
+    int n0_min = 0;
+    {
+        int lim = sparse ? ( n2 < 6 ? n2 : 6 ) : n2;
+        for( int i = 0; i < lim; ++i )
+            n0_min += fabs( wm[i] ) <= eps;
+    }
+    info->volume_min = n0_min > 0 ? htst_zero_volume( s, spins_min ) : 1;
+    info->temperature_exponent = 0.5 * ( n0_min - n0_sp );
+    info->me                   = pow( 2 * C_PI * C_K_B, info->temperature_exponent );
+    if( !sparse )
+    {
+        memcpy( evalues_min, wm, sizeof( double ) * n2 );
+        for( int k = 0; k < n_keep; ++k )
+            for( int r = 0; r < n2; ++r )
+                evectors_min[(size_t)k * n2 + r] = Q[(size_t)r * n2 + k];
+        double om = 1;
+        if( n0_min > n0_sp + 1 )
+            for( int i = n0_sp + 1; i < n0_min; ++i )
+                om /= sqrt( ws[i] );
+        else if( n0_min < n0_sp + 1 )
+            for( int i = n0_min; i < n0_sp + 1; ++i )
+                om *= sqrt( wm[i] );
+        for( int i = ( n0_min > n0_sp + 1 ? n0_min : n0_sp + 1 ); i < n2; ++i )
+            om *= sqrt( wm[i] / ws[i] );
+        info->Omega_0 = om;
+    }
+    else
+    {
+        double ld = 0;
+        for( int k = 0; k < n2; ++k )
+            ld += log( fabs( wm[k] ) );
+        info->det_min = ld;
+        double om     = sqrt( exp( info->det_min - info->det_sp ) );
+        double zf     = 1;
+        for( int i = 0; i < n0_min; ++i )
+            zf /= fabs( wm[i] );
+        for( int i = 0; i < n0_sp; ++i )
+            zf *= fabs( ws[i + 1] );
+        info->Omega_0 = om * sqrt( zf );
+    }
+    info->prefactor_dynamical = info->me * info->volume_sp / info->volume_min * info->s;
+    info->prefactor = C_G_E / ( C_HBAR * 1e-12 ) * info->Omega_0 * info->prefactor_dynamical / ( 2 * C_PI );
+out:
+    info->status = status;
+    free( H3 );
+    free( B );
+    free( H2 );
+    free( Q );
+    free( ws );
+    free( wm );
+    free( g );
+    free( q0 );
+    free( a );
+    return status;
+}

@@ -119,6 +119,21 @@ void og_gneb_image_types_auto( int noi, const double * energies, int * image_typ
 /* Transition_Homogeneous (geodesic interpolation between images idx_1 and idx_2) */
 void og_transition_homogeneous( int nos, int noi, double * chain, int idx_1, int idx_2 );
 
+/* HTST prefactor (HTST_Calculate, core/src/engine/HTST.cpp, Sparse_HTST.cpp).  Returns 0 or the
+ * check that failed: 1 minimum / 2 saddle point not converged (torque > 1e-8), 3 no negative mode
+ * at the saddle point, 4 higher-order saddle point, 5 negative mode at the minimum (dense only).
+ * Dense (sparse = 0): evalues_* [2N] ascending, evectors_* [n_keep][2N] (mode-major),
+ * velocities [2N]; sparse: those outputs are not written. */
+typedef struct og_htst_info
+{
+    double temperature_exponent, me, Omega_0, s, volume_min, volume_sp, prefactor_dynamical, prefactor;
+    double det_min, det_sp;
+    int n_eigenmodes_keep, status;
+} og_htst_info;
+int og_htst(
+    og_system * s, const double * spins_min, const double * spins_sp, int sparse, int n_keep, og_htst_info * info,
+    double * evalues_min, double * evalues_sp, double * evectors_min, double * evectors_sp, double * velocities );
+
 /* Monte Carlo (Method_MC, core/src/engine/Method_MC.cpp): Metropolis sweeps with cone sampling
  * and the adaptive cone.  A sweep visits the spins colour by colour (greedy colouring of the
  * interaction graph in spin order: spins of one colour never interact), drawing per spin and

@@ -112,3 +112,25 @@ LLG_CASES = [
 
 SPIN_SEED = {"sq_c1": 11, "sc3d_ddi": 12, "hex2d": 13, "open2d_ddi": 14, "ddi_irregular": 15,
              "periodic_ddi": 16, "fd_pairs": 17}
+
+# HTST (HTST_Calculate) on converged minimum / first-order saddle pairs: an open chain (coherent
+# reversal), an open 2D patch with DMI, and an open 2D patch with a tilted anisotropy axis and the
+# dipolar interaction.  The field is tilted off the anisotropy axis so no continuous symmetry gives
+# zero modes.  (name, spec, rng seed)
+_HTST_BASE = dict(bravais="sc", lattice_constant=1.0, mu_s=[2.0], bc=[0, 0, 0], jij=[1.0], dm_chirality=2,
+                  llg=dict(dt=1e-3, damping=0.3, temperature=0.0, force_convergence=1e-12),
+                  gneb=dict(spring_constant=1.0, force_convergence=1e-11))
+HTST_CASES = [
+    ("chain8", dict(_HTST_BASE, n_cells=[8, 1, 1], field=(4.0, (0.2, 0.0, -1.0)), anisotropy=(0.5, (0, 0, 1)),
+                    dij=[0.0]), 3),
+    ("dmi5x4", dict(_HTST_BASE, n_cells=[5, 4, 1], field=(3.0, (0.2, 0.0, -1.0)), anisotropy=(0.5, (0, 0, 1)),
+                    dij=[0.3]), 3),
+    ("ddi4x3", dict(_HTST_BASE, n_cells=[4, 3, 1], lattice_constant=3.0, field=(3.0, (0.2, 0.1, -1.0)),
+                    anisotropy=(0.5, (0, 0, 1.0)), dij=[0.2],
+                    ddi=dict(method="fft", n_periodic_images=[0, 0, 0], radius=0.0, pb_zero_padding=1)), 5),
+    # tilted anisotropy axis: the reference's Hessian puts the anisotropy's beta sum on the diagonal
+    # (Hamiltonian_Heisenberg.cpp:1136-1146), which no longer matches the gradient for a tilted
+    # axis; its HTST then sees a higher-order saddle and stops.  Pins that the same Hessian is used.
+    ("tilted8", dict(_HTST_BASE, n_cells=[8, 1, 1], lattice_constant=3.0, field=(4.0, (0.2, 0.1, -1.0)),
+                     anisotropy=(0.5, (0.1, 0.2, 1.0)), dij=[0.0]), 5),
+]

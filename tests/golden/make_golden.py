@@ -22,11 +22,13 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
-from cases import GRAD_CASES, LLG_CASES, PAIR_GEOMETRIES, SOLVERS, SPIN_SEED  # noqa: E402
-from oracle.oracle import OracleSystem, random_spins, transition_homogeneous  # noqa: E402
+from cases import GRAD_CASES, HTST_CASES, LLG_CASES, PAIR_GEOMETRIES, SOLVERS, SPIN_SEED  # noqa: E402
+from oracle.oracle import OracleSystem, image_types_auto, random_spins, transition_homogeneous  # noqa: E402
 from spirit_gb300.configs import config_text, write_config  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "golden_harness")
+HTST_KEYS = ["temperature_exponent", "me", "Omega_0", "s", "volume_min", "volume_sp", "prefactor_dynamical",
+             "prefactor", "det_min", "det_sp"]
 
 
 def run(args, cwd):
@@ -161,6 +163,53 @@ def main(only=None):
             max_torque=float([r_ for r_ in rows if r_[0] == "max_torque"][0][1]),
         )
         out[tag_name] = [float(r_[3]) for r_ in img]
+    # --- HTST: converged minimum and saddle point from the oracle's minimisers (LBFGS_OSO, GNEB with
+    # climbing image, torque < 1e-11), then the reference's HTST_Calculate (dense and sparse)
+    for name, spec, seed in HTST_CASES:
+        if not want("htst_" + name):
+            continue
+        o = OracleSystem(spec)
+        nos = o.nos
+        rng = np.random.default_rng(seed)
+        ends = []
+        for sgn in (1.0, -1.0):
+            x = np.tile([0.05, 0.0, sgn], (nos, 1)) + 0.05 * rng.normal(size=(nos, 3))
+            x /= np.linalg.norm(x, axis=1, keepdims=True)
+            ends.append(o.llg(x, "LBFGS_OSO", 20000, force_convergence=1e-12)[0])
+        noi = 9
+        chain = np.zeros((noi, nos, 3))
+        chain[0], chain[-1] = ends
+        chain = transition_homogeneous(chain, 0, noi - 1)
+        for k in range(1, noi - 1):
+            chain[k] += 0.1 * rng.normal(size=(nos, 3))
+            chain[k] /= np.linalg.norm(chain[k], axis=1, keepdims=True)
+        chain, r = o.gneb(chain, 3000, solver="LBFGS_OSO", force_convergence=1e-11)
+        types = image_types_auto(r["energies"], np.zeros(noi))
+        chain, r = o.gneb(chain, 100000, image_type=types, solver="VP_OSO", force_convergence=1e-11)
+        sp = int(np.argmax(types == 1))
+        cfg = write_config(spec, os.path.join(tmp, "htst_%s.cfg" % name))
+        cp = os.path.join(tmp, "htst_%s_chain.bin" % name)
+        chain.tofile(cp)
+        res = {}
+        for sparse in (0, 1):
+            tag = os.path.join(tmp, "htst_%s_%d" % (name, sparse))
+            run(["htst", cfg, cp, tag, str(noi), "0", str(sp), str(sparse), "-1"], tmp)
+            res[sparse] = load_kv(tag + "_result.txt")
+        tag = os.path.join(tmp, "htst_%s_0" % name)
+        n2 = 2 * nos
+        # the reference stops (no eigen output) when a check fails, e.g. a higher-order saddle point
+        done = os.path.getsize(tag + "_evalues_min.bin") > 0
+        ev = (lambda suffix, shape=None: load_bin(tag + suffix, shape)) if done else (lambda suffix, shape=None: np.zeros(0))
+        np.savez_compressed(
+            os.path.join(HERE, "htst_%s.npz" % name), config=config_text(spec), spins_min=chain[0], spins_sp=chain[sp],
+            sp_index=sp, gneb_max_torque=r["max_torque"],
+            dense=np.array([res[0][k] for k in HTST_KEYS]), sparse=np.array([res[1][k] for k in HTST_KEYS]),
+            keys=np.array(HTST_KEYS),
+            completed=done, evalues_min=ev("_evalues_min.bin"), evalues_sp=ev("_evalues_sp.bin"),
+            evectors_min=ev("_evectors_min.bin", (n2, n2)), evectors_sp=ev("_evectors_sp.bin", (n2, n2)),
+            velocities=ev("_velocities.bin"),
+        )
+        out["htst_" + name] = (res[0]["prefactor"], res[1]["prefactor"])
     for k, v in out.items():
         print(k, v)
 

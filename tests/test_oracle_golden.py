@@ -8,7 +8,7 @@ trajectories follow the same operations in the same order.
 import numpy as np
 import pytest
 
-from cases import GRAD_CASES, LLG_CASES, PAIR_GEOMETRIES, SOLVERS
+from cases import GRAD_CASES, HTST_CASES, LLG_CASES, PAIR_GEOMETRIES, SOLVERS
 from conftest import golden
 from oracle.oracle import OracleSystem, image_types_auto, philox4x32
 
@@ -142,3 +142,36 @@ def test_thermal_noise_statistics():
     sigma = eps * np.sqrt(10.0 / 2.0)
     z = xs / sigma
     assert abs(z.mean()) < 0.02 and abs(z.std() - 1) < 0.02
+
+
+@pytest.mark.parametrize("name", [c[0] for c in HTST_CASES])
+def test_htst_vs_reference(name):
+    """HTST_Calculate of the reference (dense and sparse) on converged minimum / saddle pairs:
+    prefactor constituents, full spectra, eigenvectors up to sign, perpendicular velocities."""
+    f = golden("htst_%s.npz" % name)
+    spec = [c[1] for c in HTST_CASES if c[0] == name][0]
+    o = OracleSystem(spec)
+    keys = [str(k) for k in f["keys"]]
+    for sparse, ref in ((False, f["dense"]), (True, f["sparse"])):
+        r = o.htst(f["spins_min"], f["spins_sp"], sparse=sparse)
+        if not bool(f["completed"]):
+            assert r["status"] == 4 and r["prefactor"] == 0  # higher-order saddle point: stops
+            continue
+        assert r["status"] == 0
+        for k, v in zip(keys, ref):
+            if sparse or k not in ("det_min", "det_sp"):
+                assert abs(r[k] - v) <= 1e-10 * max(abs(v), 1.0), (sparse, k, r[k], v)
+        if sparse:
+            continue
+        np.testing.assert_allclose(r["evalues_min"], f["evalues_min"], rtol=0, atol=1e-12)
+        np.testing.assert_allclose(r["evalues_sp"], f["evalues_sp"], rtol=0, atol=1e-12)
+        # eigenvectors: reference stores them column-major [2N][2N] -> mode k is row k of the file
+        # array read as (2N, 2N); compare up to sign where the eigenvalue is simple
+        for which in ("min", "sp"):
+            ev, ref_v = r["evectors_" + which], f["evectors_" + which]
+            w = f["evalues_" + which]
+            for k in range(len(w)):
+                gap = min(abs(w[k] - w[j]) for j in range(len(w)) if j != k)
+                if gap > 1e-6:
+                    assert min(np.abs(ev[k] - ref_v[k]).max(), np.abs(ev[k] + ref_v[k]).max()) < 1e-8
+        np.testing.assert_allclose(np.abs(r["velocities"]), np.abs(f["velocities"]), rtol=0, atol=1e-10)
