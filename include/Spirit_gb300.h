@@ -169,6 +169,28 @@ void Chain_Setup_Data( State * state, int idx_chain );                          
 /* ================================================================ Transitions (core/include/Spirit/Transitions.h) */
 void Transition_Homogeneous( State * state, int idx_1, int idx_2, int idx_chain );        /* :29 */
 
+/* ================================================================ HTST (core/include/Spirit/HTST.h)
+ * The Hessians and all eigenpairs are computed on the device in FP64 (parallel Jacobi); sparse =
+ * true reports what the reference's sparse variant reports (log-determinants, no eigen output). */
+float HTST_Calculate( State * state, int idx_image_minimum, int idx_image_sp, int n_eigenmodes_keep, bool sparse,
+                      int idx_chain );                                                               /* :37 */
+void HTST_Get_Info( State * state, float * temperature_exponent, float * me, float * Omega_0, float * s,
+                    float * volume_min, float * volume_sp, float * prefactor_dynamical, float * prefactor,
+                    int * n_eigenmodes_keep, int idx_chain );                                        /* :52 */
+void HTST_Get_Eigenvalues_Min( State * state, float * eigenvalues_min, int idx_chain );             /* :61 */
+void HTST_Get_Eigenvectors_Min( State * state, float * eigenvectors_min, int idx_chain );           /* :67 */
+void HTST_Get_Eigenvalues_SP( State * state, float * eigenvalues_sp, int idx_chain );               /* :73 */
+void HTST_Get_Eigenvectors_SP( State * state, float * eigenvectors_sp, int idx_chain );             /* :79 */
+void HTST_Get_Velocities( State * state, float * velocities, int idx_chain );                       /* :86 */
+/* EXTENSION: FP64 copy of the last HTST result.  info[10] = temperature_exponent, me, Omega_0, s,
+ * volume_min, volume_sp, prefactor_dynamical, prefactor, det_min, det_sp; eigenvalues [2N];
+ * eigenvectors [n_eigenmodes_keep][2N]; velocities [2N] (NULL pointers are skipped).  Returns 0
+ * when the calculation completed, 1-5 for the check that stopped it (1 minimum / 2 saddle point
+ * not converged, 3 no negative mode, 4 higher-order saddle point, 5 negative mode at the
+ * minimum), -1 when there is no result. */
+int HTST_Get_Result_FP64( State * state, double * info, double * eigenvalues_min, double * eigenvalues_sp,
+                          double * eigenvectors_min, double * eigenvectors_sp, double * velocities, int idx_chain );
+
 /* ================================================================ IO (core/include/Spirit/IO.h)
  * OVF 2.0 files; format: 0 binary in the API precision (8 bytes), 1 binary 4, 2 binary 8, 3 text,
  * 4 CSV (IO.h:26-38).  Segments written here carry the image's random-stream positions (LLG noise

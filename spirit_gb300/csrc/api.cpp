@@ -9,6 +9,7 @@
 #include "adjoint.hpp"
 #include "config.hpp"
 #include "gneb.hpp"
+#include "htst.hpp"
 #include "mc.hpp"
 #include "ovf.hpp"
 #include "state.hpp"
@@ -2533,6 +2534,226 @@ double Simulation_LLG_Loss( State * state, const double * params, int n_steps, c
     {
         handle( state, "Simulation_LLG_Loss" );
         return 0;
+    }
+}
+
+// ============================================================== HTST (core/include/Spirit/HTST.h)
+static std::vector<double> fp64_gradient( Image & img )
+{
+    std::vector<double> g( 3 * (size_t)img.nos() );
+    Engine & E = eval_engine( img );
+    E.set_spins( 0, img.spins.data() );
+    double Et = 0;
+    E.gradient( 0, g.data(), &Et, nullptr );
+    return g;
+}
+
+float HTST_Calculate( State * state, int idx_image_minimum, int idx_image_sp, int n_eigenmodes_keep, bool sparse,
+                      int idx_chain ) noexcept
+{
+    try
+    {
+        auto Im = from_indices( state, idx_image_minimum, idx_chain );
+        auto Is = from_indices( state, idx_image_sp, idx_chain );
+        std::lock_guard<std::recursive_mutex> lk( Im.chain->mtx );
+        Im.chain->htst.reset();
+        auto gm = fp64_gradient( *Im.img );
+        auto gs = fp64_gradient( *Is.img );
+        cudaStream_t st;
+        CUDA_CHECK( cudaStreamCreateWithFlags( &st, cudaStreamNonBlocking ) );
+        std::shared_ptr<HtstResult> R;
+        try
+        {
+            R = std::make_shared<HtstResult>( htst_calculate( *Im.img->geom, Im.img->ham, Im.img->spins, gm,
+                                                              Is.img->ham, Is.img->spins, gs, sparse,
+                                                              n_eigenmodes_keep, st ) );
+        }
+        catch( ... )
+        {
+            cudaStreamDestroy( st );
+            throw;
+        }
+        CUDA_CHECK( cudaStreamDestroy( st ) );
+        static const char * why[] = { "",
+                                      "HTST: the initial configuration is not a converged minimum, its max. torque "
+                                      "is above the threshold (1e-8)!",
+                                      "HTST: the transition configuration is not a converged saddle point, its max. "
+                                      "torque is above the threshold (1e-8)!",
+                                      "HTST: the transition configuration is not a saddle point, its lowest "
+                                      "eigenvalue is above the threshold (-1e-4)!",
+                                      "HTST: the image you passed is a higher order saddle point!",
+                                      "HTST: the initial configuration is not a minimum, its lowest eigenvalue is "
+                                      "below the threshold (-1e-4)!" };
+        if( R->status > 0 && R->status < 6 )
+            log_msg( state, 1, why[R->status] );
+        Im.chain->htst = R;
+        return (float)R->prefactor;
+    }
+    catch( ... )
+    {
+        handle( state, "HTST_Calculate" );
+        return 0;
+    }
+}
+
+static std::shared_ptr<HtstResult> htst_of( State * state, int idx_chain, const char * who, bool eigen )
+{
+    auto I = from_indices( state, -1, idx_chain );
+    auto R = std::static_pointer_cast<HtstResult>( I.chain->htst );
+    if( !R )
+        throw std::runtime_error( std::string( who ) + ": HTST_Calculate has not been called" );
+    if( eigen && R->sparse )
+    {
+        log_msg( state, 1,
+                 std::string( who )
+                     + ": You tried to call this function after performing a sparse calculation. This is not allowed." );
+        return nullptr;
+    }
+    return R;
+}
+
+void HTST_Get_Info( State * state, float * temperature_exponent, float * me, float * Omega_0, float * s,
+                    float * volume_min, float * volume_sp, float * prefactor_dynamical, float * prefactor,
+                    int * n_eigenmodes_keep, int idx_chain ) noexcept
+{
+    try
+    {
+        auto R = htst_of( state, idx_chain, "HTST_Get_Info", false );
+        auto put = []( float * p, double v ) {
+            if( p )
+                *p = (float)v;
+        };
+        put( temperature_exponent, R->temperature_exponent );
+        put( me, R->me );
+        put( Omega_0, R->Omega_0 );
+        put( s, R->s );
+        put( volume_min, R->volume_min );
+        put( volume_sp, R->volume_sp );
+        put( prefactor_dynamical, R->prefactor_dynamical );
+        put( prefactor, R->prefactor );
+        if( n_eigenmodes_keep )
+            *n_eigenmodes_keep = R->n_keep;
+    }
+    catch( ... )
+    {
+        handle( state, "HTST_Get_Info" );
+    }
+}
+
+static void htst_copy( State * state, float * out, int idx_chain, const char * who, int which )
+{
+    auto R = htst_of( state, idx_chain, who, true );
+    if( !R )
+        return;
+    if( !out )
+    {
+        log_msg( state, 1, std::string( who ) + ": you passed a null pointer" );
+        return;
+    }
+    const std::vector<double> & v = which == 0 ? R->evalues_min
+                                  : which == 1 ? R->evectors_min
+                                  : which == 2 ? R->evalues_sp
+                                  : which == 3 ? R->evectors_sp
+                                               : R->velocities;
+    for( size_t i = 0; i < v.size(); ++i )
+        out[i] = (float)v[i];
+}
+
+void HTST_Get_Eigenvalues_Min( State * state, float * eigenvalues_min, int idx_chain ) noexcept
+{
+    try
+    {
+        htst_copy( state, eigenvalues_min, idx_chain, "HTST_Get_Eigenvalues_Min", 0 );
+    }
+    catch( ... )
+    {
+        handle( state, "HTST_Get_Eigenvalues_Min" );
+    }
+}
+
+void HTST_Get_Eigenvectors_Min( State * state, float * eigenvectors_min, int idx_chain ) noexcept
+{
+    try
+    {
+        htst_copy( state, eigenvectors_min, idx_chain, "HTST_Get_Eigenvectors_Min", 1 );
+    }
+    catch( ... )
+    {
+        handle( state, "HTST_Get_Eigenvectors_Min" );
+    }
+}
+
+void HTST_Get_Eigenvalues_SP( State * state, float * eigenvalues_sp, int idx_chain ) noexcept
+{
+    try
+    {
+        htst_copy( state, eigenvalues_sp, idx_chain, "HTST_Get_Eigenvalues_SP", 2 );
+    }
+    catch( ... )
+    {
+        handle( state, "HTST_Get_Eigenvalues_SP" );
+    }
+}
+
+void HTST_Get_Eigenvectors_SP( State * state, float * eigenvectors_sp, int idx_chain ) noexcept
+{
+    try
+    {
+        htst_copy( state, eigenvectors_sp, idx_chain, "HTST_Get_Eigenvectors_SP", 3 );
+    }
+    catch( ... )
+    {
+        handle( state, "HTST_Get_Eigenvectors_SP" );
+    }
+}
+
+void HTST_Get_Velocities( State * state, float * velocities, int idx_chain ) noexcept
+{
+    try
+    {
+        htst_copy( state, velocities, idx_chain, "HTST_Get_Velocities", 4 );
+    }
+    catch( ... )
+    {
+        handle( state, "HTST_Get_Velocities" );
+    }
+}
+
+// FP64 copy of the last result: info[10] = temperature_exponent, me, Omega_0, s, volume_min,
+// volume_sp, prefactor_dynamical, prefactor, det_min, det_sp; spectra / eigenvectors [n_keep][2N] /
+// velocities as the float getters (NULL pointers skipped).  Returns the status (0 done, 1-5 the
+// check that stopped the calculation, -1 none).
+int HTST_Get_Result_FP64( State * state, double * info, double * eigenvalues_min, double * eigenvalues_sp,
+                          double * eigenvectors_min, double * eigenvectors_sp, double * velocities,
+                          int idx_chain ) noexcept
+{
+    try
+    {
+        auto I = from_indices( state, -1, idx_chain );
+        auto R = std::static_pointer_cast<HtstResult>( I.chain->htst );
+        if( !R )
+            return -1;
+        if( info )
+        {
+            const double v[10] = { R->temperature_exponent, R->me, R->Omega_0, R->s, R->volume_min, R->volume_sp,
+                                   R->prefactor_dynamical, R->prefactor, R->det_min, R->det_sp };
+            std::memcpy( info, v, sizeof( v ) );
+        }
+        auto cp = []( double * o, const std::vector<double> & v ) {
+            if( o && !v.empty() )
+                std::memcpy( o, v.data(), v.size() * sizeof( double ) );
+        };
+        cp( eigenvalues_min, R->evalues_min );
+        cp( eigenvalues_sp, R->evalues_sp );
+        cp( eigenvectors_min, R->evectors_min );
+        cp( eigenvectors_sp, R->evectors_sp );
+        cp( velocities, R->velocities );
+        return R->status;
+    }
+    catch( ... )
+    {
+        handle( state, "HTST_Get_Result_FP64" );
+        return -1;
     }
 }
 

@@ -135,6 +135,7 @@ struct Chain
     std::recursive_mutex mtx;
     std::shared_ptr<void> gneb_run; // GNEB engine of a running/singleshot chain method
     std::vector<double> torques;    // per-image max torque of the last GNEB iteration
+    std::shared_ptr<void> htst;     // result of the last HTST_Calculate (HtstResult)
 };
 
 struct State
