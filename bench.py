@@ -487,6 +487,71 @@ def run_mc(sweeps=200):
     }
 
 
+def htst_spec(L):
+    """Skyrmion-collapse system of the reference's solver test (core/test/input/solvers.cfg
+    parameters: SC, J=10, Bloch D=6 meV, B=25 T, periodic in-plane) on an L x L lattice."""
+    return dict(bravais="sc", n_cells=[L, L, 1], lattice_constant=1.0, mu_s=[2.0], bc=[1, 1, 0],
+                field=(25.0, (0, 0, 1)), anisotropy=(0.0, (0, 0, 1)), jij=[10.0], dij=[6.0], dm_chirality=1,
+                llg=dict(dt=1e-3, damping=0.3, temperature=0.0, force_convergence=1e-10),
+                gneb=dict(spring_constant=1.0, force_convergence=1e-9))
+
+
+def run_htst(sizes=(16, 32), cpu_size=16):
+    """HTST prefactor of skyrmion collapse: FP64 minimum (LBFGS_OSO to 1e-10) and saddle point
+    (GNEB, 9 images, VP_OSO + climbing image to 1e-9) prepared on the device, then HTST_Calculate
+    (dense: all eigenpairs of both 2N x 2N geodesic Hessians) timed by wall clock; CPU: the oracle's
+    HTST (FP64, serial cyclic Jacobi) on the smallest size."""
+    from oracle.oracle import OracleSystem
+    from spirit_gb300 import chain, configuration, htst, simulation, state, system, transition
+    from spirit_gb300.configs import write_config
+    import spirit_gb300.parameters.gneb as gneb
+
+    out = {"workload": "HTST of skyrmion collapse, SC L x L periodic, J=10, Bloch D=6 meV, B=25 T; minimum "
+                       "LBFGS_OSO to 1e-10, saddle point GNEB (9 images, VP_OSO + climbing image) to 1e-9 meV, "
+                       "FP64; dense HTST_Calculate (all eigenpairs of both 2N x 2N geodesic Hessians)",
+           "timing": "wall clock of HTST_Calculate (gradients, Hessian assembly, two eigen-decompositions, "
+                     "velocities)", "sizes": []}
+    for L in sizes:
+        spec = htst_spec(L)
+        p = state.setup(write_config(spec, os.path.join(tempfile.mkdtemp(), "htst.cfg")), True)
+        simulation.set_precision(p, 64)
+        configuration.plus_z(p)
+        configuration.skyrmion(p, 5, phase=-90)
+        simulation.start(p, simulation.METHOD_LLG, simulation.SOLVER_LBFGS_OSO, 200000)
+        noi = 9
+        chain.image_to_clipboard(p)
+        for _ in range(1, noi):
+            chain.insert_image_after(p)
+        configuration.plus_z(p, idx_image=noi - 1)
+        transition.homogeneous(p, 0, noi - 1)
+        simulation.start(p, simulation.METHOD_GNEB, simulation.SOLVER_VP_OSO, 5000)
+        gneb.set_image_type_automatically(p)
+        simulation.start(p, simulation.METHOD_GNEB, simulation.SOLVER_VP_OSO, 400000)
+        E = [system.get_energy_fp64(p, i) for i in range(noi)]
+        sp = int(np.argmax(E[1:-1])) + 1
+        smin = np.array(system.get_spin_directions(p, 0))
+        ssp = np.array(system.get_spin_directions(p, sp))
+        htst.calculate(p, 0, sp, 0, False)  # warm-up (module load, allocations)
+        t0 = time.perf_counter()
+        pf = htst.calculate(p, 0, sp, 0, False)
+        dt = time.perf_counter() - t0
+        r = htst.get_result_fp64(p)
+        entry = {"L": L, "n_spins": L * L, "matrix_order": 2 * L * L, "status": r["status"], "wall_s": dt,
+                 "prefactor": r["prefactor"], "Omega_0": r["Omega_0"], "s": r["s"],
+                 "barrier_meV": E[sp] - E[0], "max_torque_gneb": simulation.get_max_torque_norm(p)}
+        state.delete(p)
+        if L == cpu_size:
+            o = OracleSystem(spec)
+            c0 = time.perf_counter()
+            ro = o.htst(smin, ssp, n_keep=0)
+            cdt = time.perf_counter() - c0
+            entry["cpu_baseline"] = {"value": cdt, "unit": "s", "cores": 1, "kind": "port",
+                                     "sample": "the oracle's dense HTST of the same pair (serial Jacobi)",
+                                     "prefactor": ro["prefactor"], "status": ro["status"]}
+        out["sizes"].append(entry)
+    return out
+
+
 def run_gb300(args):
     import torch
 
@@ -583,6 +648,7 @@ def run_gb300(args):
     gneb_line = run_gneb() if args.gneb and rank == 0 else None
     adj_line = run_adjoint() if args.adjoint and rank == 0 else None
     mc_line = run_mc() if args.mc and rank == 0 else None
+    htst_line = run_htst() if args.htst and rank == 0 else None
     if rank != 0:
         return
     cpu = cpu_baseline() if world == 1 else None
@@ -609,6 +675,8 @@ def run_gb300(args):
         line["adjoint"] = adj_line
     if mc_line is not None:
         line["mc"] = mc_line
+    if htst_line is not None:
+        line["htst"] = htst_line
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -627,6 +695,8 @@ def main():
     ap.add_argument("--only-gneb", action="store_true", help="run and print only the GNEB measurement")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false", help="skip the adjoint measurement")
     ap.add_argument("--no-mc", dest="mc", action="store_false", help="skip the Monte Carlo measurement")
+    ap.add_argument("--no-htst", dest="htst", action="store_false", help="skip the HTST measurement")
+    ap.add_argument("--only-htst", action="store_true", help="run and print only the HTST measurement")
     ap.add_argument("--only-adjoint", action="store_true", help="run and print only the adjoint measurement")
     ap.add_argument("--only-batched", action="store_true",
                     help="run and print only the 256-system batched-vs-plain measurement (profiling)")
@@ -636,6 +706,12 @@ def main():
 
         torch.cuda.set_device(0)
         print(json.dumps(run_adjoint()))
+        return
+    if args.only_htst:
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps(run_htst()))
         return
     if args.only_gneb:
         import torch
