@@ -215,4 +215,18 @@ __host__ __device__ inline double fft_invT<double>( const FFTDesc & f )
     return f.invT_d;
 }
 
+#ifdef __CUDACC__
+// griddepcontrol (sm_90+): wait for the programmatic predecessor grid (completed, writes visible);
+// allow the dependent grid to be launched.  Both are no-ops for a kernel launched without the
+// programmatic-serialization attribute.
+__device__ __forceinline__ void pdl_wait()
+{
+    asm volatile( "griddepcontrol.wait;" ::: "memory" );
+}
+__device__ __forceinline__ void pdl_trigger()
+{
+    asm volatile( "griddepcontrol.launch_dependents;" ::: "memory" );
+}
+#endif
+
 } // namespace sg

@@ -66,8 +66,6 @@ __global__ void pass_a( PassArgs<R> p )
     extern __shared__ unsigned char smem_raw[];
     const int4 blk = p.blocks[blockIdx.x];
     const int s    = blk.x;
-    if( sys_inactive( p, s ) )
-        return;
     const FFTDesc & f = p.fd[s];
     const int Ma = f.M[0], Mh = f.Mh, nb = f.nb;
     const int Cin = p.mode ? f.M[2] : f.N[2];
@@ -80,6 +78,10 @@ __global__ void pass_a( PassArgs<R> p )
     cplx<R> * a   = tw + Ma;
     cplx<R> * b   = a + nq * ls;
     load_tw( tw, p.tw + f.tw_offset[0], Ma );
+    pdl_wait();
+    pdl_trigger();
+    if( sys_inactive( p, s ) )
+        return;
     if( p.mode == 0 )
     {
         const int cb = row / Cin, c = row - cb * Cin;
@@ -311,8 +313,6 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
     extern __shared__ unsigned char smem_raw[];
     const int4 blk = p.blocks[blockIdx.x];
     const int s    = blk.x;
-    if( sys_inactive( p, s ) )
-        return;
     const FFTDesc & f = p.fd[s];
     const int Mb = f.M[1], Mc = f.M[2], nb = f.nb;
     const int Nb = f.N[1], Nc = f.N[2];
@@ -329,6 +329,10 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
     for( int e = threadIdx.x; e < 2 * vol; e += blockDim.x )
         A[e] = { 0, 0 };
     __syncthreads();
+    pdl_wait();
+    pdl_trigger();
+    if( sys_inactive( p, s ) )
+        return;
     const int nin    = ncb * Nc * Nb;
     cplx<R> * W1     = p.W1 + f.spec_offset + (size_t)ka * nin;
     for( int e = threadIdx.x; e < nin; e += blockDim.x )
@@ -402,8 +406,6 @@ __global__ void __launch_bounds__( 512 ) pass_bc_cl( PassArgs<R> p, int K )
     const int rank            = (int)cluster.block_rank();
     const int4 blk            = p.blocks[blockIdx.x];
     const int s               = blk.x;
-    if( sys_inactive( p, s ) ) // uniform over the cluster: its blocks share the system
-        return;
     const FFTDesc & f = p.fd[s];
     const int Mb = f.M[1], Mc = f.M[2], nb = f.nb;
     const int Nb = f.N[1], Nc = f.N[2];
@@ -430,6 +432,10 @@ __global__ void __launch_bounds__( 512 ) pass_bc_cl( PassArgs<R> p, int K )
     for( int e = threadIdx.x; e < lc; e += blockDim.x )
         Bc0[e] = { 0, 0 };
     __syncthreads();
+    pdl_wait();
+    pdl_trigger();
+    if( sys_inactive( p, s ) ) // uniform over the cluster: its blocks share the system
+        return;
     const int nin    = ncb * Nc * Nb;
     cplx<R> * W1     = p.W1 + f.spec_offset + (size_t)ka * nin;
     for( int e = threadIdx.x; e < ncb * nc * Nb; e += blockDim.x )
@@ -518,8 +524,6 @@ __global__ void pass_a_inv( PassArgs<R> p )
     extern __shared__ unsigned char smem_raw[];
     const int4 blk = p.blocks[blockIdx.x];
     const int s    = blk.x;
-    if( sys_inactive( p, s ) )
-        return;
     const FFTDesc & f = p.fd[s];
     const SysDesc & d = p.sd[s];
     const int Ma = f.M[0], Mh = f.Mh, nb = f.nb;
@@ -531,6 +535,10 @@ __global__ void pass_a_inv( PassArgs<R> p )
     cplx<R> * a   = tw + Ma;
     cplx<R> * b   = a + nq * ls;
     load_tw( tw, p.tw + f.tw_offset[0], Ma );
+    pdl_wait();
+    pdl_trigger();
+    if( sys_inactive( p, s ) )
+        return;
     // element (line li, frequency kk) of W1 in either layout
     const size_t lstride = p.ka_major ? 1 : (size_t)Mh;
     const size_t kstride = p.ka_major ? (size_t)3 * nb * Nc * Nb : 1;
@@ -1081,7 +1089,7 @@ void DDIPlan::launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const
         a.blocks = d_blocks[0];
         a.g      = tile[0];
         a.div_g  = make_fastdiv( tile[0] );
-        pass_a<R><<<n_blocks[0], threads[0], max_smem_a, stream>>>( a );
+        launch_pdl( pass_a<R>, dim3( n_blocks[0] ), dim3( threads[0] ), max_smem_a, stream, 1, a );
         break;
     case 1:
     case 3:
@@ -1099,30 +1107,17 @@ void DDIPlan::launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const
     case 5:
         a.blocks = d_blocks[3];
         if( cluster_k == 1 )
-            pass_bc<R><<<n_blocks[3], threads_bc, smem_bc_max, stream>>>( a );
+            launch_pdl( pass_bc<R>, dim3( n_blocks[3] ), dim3( threads_bc ), smem_bc_max, stream, 1, a );
         else
-        {
-            cudaLaunchConfig_t cfg = {};
-            cfg.gridDim            = dim3( n_blocks[3] );
-            cfg.blockDim           = dim3( std::min( threads_bc, 512 ) );
-            cfg.dynamicSmemBytes   = smem_bc_max;
-            cfg.stream             = stream;
-            cudaLaunchAttribute at[1];
-            at[0].id               = cudaLaunchAttributeClusterDimension;
-            at[0].val.clusterDim.x = cluster_k;
-            at[0].val.clusterDim.y = 1;
-            at[0].val.clusterDim.z = 1;
-            cfg.attrs              = at;
-            cfg.numAttrs           = 1;
-            CUDA_CHECK( cudaLaunchKernelEx( &cfg, pass_bc_cl<R>, a, cluster_k ) );
-        }
+            launch_pdl( pass_bc_cl<R>, dim3( n_blocks[3] ), dim3( std::min( threads_bc, 512 ) ), smem_bc_max, stream,
+                        cluster_k, a, cluster_k );
         break;
     default:
         a.blocks = d_blocks[0];
         a.g      = tile[0];
         a.div_g  = make_fastdiv( tile[0] );
         a.div_gq = make_fastdiv( ( tile[0] + 1 ) / 2 );
-        pass_a_inv<R><<<n_blocks[0], threads[0], max_smem_a, stream>>>( a );
+        launch_pdl( pass_a_inv<R>, dim3( n_blocks[0] ), dim3( threads[0] ), max_smem_a, stream, 1, a );
         break;
     }
 }

@@ -261,13 +261,15 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
     const int2 bm = A.blkmap[blockIdx.x];
     const int s   = bm.x;
     SysRun * run  = A.runs + s;
-    if( !A.tune && !run->active )
-        return;
     const SysDesc & d = A.sd[s];
     load_pairs_smem( pairs, d );
     load_const( C, d );
     load_geo( GS, d );
     __syncthreads();
+    pdl_wait(); // everything below reads what earlier kernels wrote
+    pdl_trigger();
+    if( !A.tune && !run->active )
+        return;
     constexpr bool FINAL = ( SOLVER == SOLVER_RK4 ) ? ( STAGE == 4 ) : ( STAGE == 2 );
     constexpr bool PROBE = STAGE == ST_PROBE;
     const int iteration  = run->iteration;
@@ -846,11 +848,11 @@ void Engine::launch_stage( StageArgs<R> a, cudaStream_t st )
     a.blkcount  = d_sblkcount_[k];
     const int n = n_sblocks_[k];
     if( k == 0 )
-        llg_stage<R, SOLVER, STAGE, 1><<<n, 256, 0, st>>>( a );
+        launch_pdl( llg_stage<R, SOLVER, STAGE, 1>, dim3( n ), dim3( 256 ), 0, st, 1, a );
     else if( k == 1 )
-        llg_stage<R, SOLVER, STAGE, 2><<<n, 256, 0, st>>>( a );
+        launch_pdl( llg_stage<R, SOLVER, STAGE, 2>, dim3( n ), dim3( 256 ), 0, st, 1, a );
     else
-        llg_stage<R, SOLVER, STAGE, 4><<<n, 256, 0, st>>>( a );
+        launch_pdl( llg_stage<R, SOLVER, STAGE, 4>, dim3( n ), dim3( 256 ), 0, st, 1, a );
 }
 
 template<typename R>

@@ -4,8 +4,10 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstdlib>
 #include <stdexcept>
 #include <string>
+#include <utility>
 
 namespace sg
 {
@@ -70,6 +72,50 @@ template<typename T>
 inline void d2h( T * h, const T * d, size_t n )
 {
     CUDA_CHECK( cudaMemcpy( h, d, n * sizeof( T ), cudaMemcpyDeviceToHost ) );
+}
+
+// Programmatic dependent launch: the kernel may be launched while its predecessor in the stream
+// is still running, so launch latency and its set-up (constants, twiddles, pair tables into
+// shared memory) overlap the predecessor's tail; the kernel executes pdl_wait() (griddepcontrol
+// .wait: the predecessor has completed and its writes are visible) before touching data an
+// earlier kernel produced.  SPIRIT_GB300_PDL=0 launches without the attribute.
+inline bool pdl_enabled()
+{
+    static const bool on = [] {
+        const char * e = std::getenv( "SPIRIT_GB300_PDL" );
+        return !( e && e[0] == '0' );
+    }();
+    return on;
+}
+
+template<typename... KArgs, typename... Args>
+inline void launch_pdl( void ( *kern )( KArgs... ), dim3 grid, dim3 block, size_t smem, cudaStream_t st, int cluster,
+                        Args &&... args )
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim            = grid;
+    cfg.blockDim           = block;
+    cfg.dynamicSmemBytes   = smem;
+    cfg.stream             = st;
+    cudaLaunchAttribute at[2];
+    unsigned na = 0;
+    if( pdl_enabled() )
+    {
+        at[na].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[na].val.programmaticStreamSerializationAllowed = 1;
+        ++na;
+    }
+    if( cluster > 1 )
+    {
+        at[na].id               = cudaLaunchAttributeClusterDimension;
+        at[na].val.clusterDim.x = cluster;
+        at[na].val.clusterDim.y = 1;
+        at[na].val.clusterDim.z = 1;
+        ++na;
+    }
+    cfg.attrs    = na ? at : nullptr;
+    cfg.numAttrs = na;
+    CUDA_CHECK( cudaLaunchKernelEx( &cfg, kern, std::forward<Args>( args )... ) );
 }
 
 } // namespace sg
