@@ -53,18 +53,20 @@ KERNELS = ["stage", "fft_pass_a", "fft_pass_b", "fft_pass_c_tensor", "fft_pass_b
            "fft_pass_bc_tensor"]
 
 
-def algorithmic_bytes(kernel, stage):
+def algorithmic_bytes(kernel, stage, rows=False):
     """Algorithmic HBM bytes of one launch at the workload size, FP32 (SoA spins 12 B/spin,
     complex 8 B).  Stage 1 of Heun reads s and h, writes predictor and fv1 (48 B/spin); stage 2
     reads predictor, s, fv1, h and writes s (60 B/spin).  FFT passes read and write their
-    half-spectrum arrays once; pass C also reads the 6-component dipole spectrum."""
+    half-spectrum arrays once; pass C also reads the 6-component dipole spectrum.  Row-fused
+    stages (rows=True) read the field spectrum and write the next configuration's instead of
+    reading h: stage bytes - 12 B/spin + 2 W1."""
     Mh, Mb, Mc, Nb, Nc = 65, 128, 32, 128, 16
     W1 = 3 * Nc * Nb * Mh * 8
     W2 = 3 * Nc * Mb * Mh * 8
     D = 6 * Mc * Mb * Mh * 8
     S = 12 * NOS
     return {
-        "stage": (48 if stage == 1 else 60) * NOS,
+        "stage": (48 if stage == 1 else 60) * NOS + ((2 * W1 - 12 * NOS) if rows else 0),
         "fft_pass_a": S + W1,
         "fft_pass_b": W1 + W2,
         "fft_pass_c_tensor": 2 * W2 + D,
@@ -207,28 +209,34 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def c4_specs(n=256, seed=4):
+def c4_specs(n=256, seed=4, ddi=False):
     """The batched uneven ensemble: n periodic square lattices with edge lengths log-uniform in
     [32, 256] and per-system J, D (Neel), K, B_z, T drawn from the given seed; SIB, alpha 0.2,
-    dt 1e-3 ps, mu_s 2 mu_B."""
+    dt 1e-3 ps, mu_s 2 mu_B.  ddi=True: the dipolar variant -- open boundaries, DDI by FFT
+    (zero-padded 2L x 2L, no periodic images), lattice constant 4 A."""
     rng = np.random.default_rng(seed)
     specs = []
     for k in range(n):
         L = int(round(np.exp(rng.uniform(np.log(32), np.log(256)))))
         J, D, K = rng.uniform(0.5, 1.5), rng.uniform(0.0, 0.4), rng.uniform(0.0, 0.2)
         B, T = rng.uniform(0.0, 2.0), rng.uniform(0.0, 50.0)
-        specs.append(dict(bravais="sc", n_cells=[L, L, 1], lattice_constant=1.0, mu_s=[2.0], bc=[1, 1, 0],
-                          field=(B, (0, 0, 1)), anisotropy=(K, (0, 0, 1)), jij=[J], dij=[D], dm_chirality=2,
-                          llg=dict(dt=1e-3, damping=0.2, temperature=T, seed=1000 + k)))
+        sp = dict(bravais="sc", n_cells=[L, L, 1], lattice_constant=1.0, mu_s=[2.0], bc=[1, 1, 0],
+                  field=(B, (0, 0, 1)), anisotropy=(K, (0, 0, 1)), jij=[J], dij=[D], dm_chirality=2,
+                  llg=dict(dt=1e-3, damping=0.2, temperature=T, seed=1000 + k))
+        if ddi:
+            sp.update(bc=[0, 0, 0], lattice_constant=4.0,
+                      ddi=dict(method="fft", n_periodic_images=[0, 0, 0], radius=0.0, pb_zero_padding=1))
+        specs.append(sp)
     return specs
 
 
-def run_batched_vs_plain(steps, warmup, plain=True, check=True):
+def run_batched_vs_plain(steps, warmup, plain=True, check=True, ddi=False):
     """256 uneven systems: spin-updates/s of the batched path (all systems in one launch per SIB
     stage, CUDA graphs) against the plain path (every system its own engine and launches, on the
     same stream), both FP32 and device-timed with CUDA events; the ensemble's arrays (~290 MB)
     exceed L2.  Accuracy: the 8 smallest systems run 1000 batched FP32 steps against the FP64
-    oracle consuming the same Philox streams."""
+    oracle consuming the same Philox streams.  ddi=True: the dipolar variant of the ensemble
+    (c4_specs), one batched FFT plan over all 256 systems."""
     import torch
 
     from oracle.oracle import OracleSystem, random_spins
@@ -237,7 +245,7 @@ def run_batched_vs_plain(steps, warmup, plain=True, check=True):
     from spirit_gb300.spiritlib import fn
 
     launch = fn("Simulation_Launch_Steps", [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int])
-    specs = c4_specs()
+    specs = c4_specs(ddi=ddi)
     tmp = tempfile.mkdtemp()
     states, nos = [], []
     for k, sp in enumerate(specs):
@@ -307,13 +315,21 @@ def run_batched_vs_plain(steps, warmup, plain=True, check=True):
         state.delete(p)
     bv = total * steps / (batched_ms / 1000.0)
     pv = total * steps / (plain_ms / 1000.0)
+    if ddi:
+        workload = ("256 uneven open SC 2D systems with the dipolar interaction (DDI FFT, zero-padded 2L x 2L, "
+                    "a = 4 A), L log-uniform in [32,256] (seed 4), per-system J, D, K, B_z, T in U[0,50] K; "
+                    "stochastic SIB alpha=0.2 dt=1e-3 ps, FP32")
+        plain_desc = "one engine per system (its own FFT plan), 2 stages x (DDI passes + stage) per step, same stream"
+    else:
+        workload = ("256 uneven periodic SC 2D systems, L log-uniform in [32,256] (seed 4), per-system J, D, K, "
+                    "B_z, T in U[0,50] K; stochastic SIB alpha=0.2 dt=1e-3 ps, FP32")
+        plain_desc = "one engine per system, 2 launches per system per step (1-step CUDA graph), same stream"
     return {
-        "workload": "256 uneven periodic SC 2D systems, L log-uniform in [32,256] (seed 4), per-system J, D, K, "
-                    "B_z, T in U[0,50] K; stochastic SIB alpha=0.2 dt=1e-3 ps, FP32",
+        "workload": workload,
         "n_systems": len(specs), "n_spins": total, "steps": steps, "warmup": warmup,
         "value": bv, "unit": "spin-updates/s", "ms_per_step": batched_ms / steps,
         "plain_value": pv, "plain_ms_per_step": plain_ms / steps, "ratio_batched_vs_plain": bv / pv,
-        "plain": "one engine per system, 2 launches per system per step (1-step CUDA graph), same stream",
+        "plain": plain_desc,
         "l2": "not flushed: the ensemble's 6 x 3 FP32 arrays (%.0f MB) exceed the 129 MB L2" % (total * 72 / 1e6),
         "max_dm_vs_fp64_oracle": dm,
         "accuracy_check": "8 smallest systems, 1000 batched FP32 steps vs the FP64 oracle on the same Philox streams",
@@ -611,8 +627,10 @@ def run_gb300(args):
     ntun = fn("Simulation_Get_Tuning", [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int], ctypes.c_int)(p, tun, 16, -1, -1)
     tuned = dict(zip(["stage_spins_per_thread", "fft_a_lines", "fft_a_threads", "fft_b_lines", "fft_b_threads",
-                      "fft_c_columns", "fft_c_threads", "fused_bc", "bc_cluster", "bc_threads", "ddi"],
+                      "fft_c_columns", "fft_c_threads", "fused_bc", "bc_cluster", "bc_threads", "ddi",
+                      "row_fused_stages"],
                      [int(tun[k]) for k in range(ntun)]))
+    rows = bool(tuned.get("row_fused_stages", 0))
     value = NOS * args.steps * world / (ms / 1000.0)
     # --- per-kernel durations (CUDA events between launches, L2 flushed before every step)
     kms = (ctypes.c_double * 16)()
@@ -626,7 +644,7 @@ def run_gb300(args):
     avg_ms = per[dom][0] / per[dom][1]
     if dom == "stage":
         # both Heun stages share the kernel name; average their algorithmic bytes
-        alg = 0.5 * (algorithmic_bytes("stage", 1) + algorithmic_bytes("stage", 2))
+        alg = 0.5 * (algorithmic_bytes("stage", 1, rows) + algorithmic_bytes("stage", 2, rows))
     else:
         alg = algorithmic_bytes(dom, 1)
     peak, peak_kind = measured_peaks()
@@ -645,6 +663,8 @@ def run_gb300(args):
     simulation.stop(p)
     state.delete(p)
     batched = run_batched_vs_plain(max(20, args.steps), max(3, args.warmup)) if args.batched else None
+    batched_ddi = (run_batched_vs_plain(max(20, args.steps), max(3, args.warmup), ddi=True)
+                   if args.batched and args.batched_ddi else None)
     gneb_line = run_gneb() if args.gneb and rank == 0 else None
     adj_line = run_adjoint() if args.adjoint and rank == 0 else None
     mc_line = run_mc() if args.mc and rank == 0 else None
@@ -669,6 +689,8 @@ def run_gb300(args):
     }
     if batched is not None:
         line["batched"] = batched
+    if batched_ddi is not None:
+        line["batched_ddi"] = batched_ddi
     if gneb_line is not None:
         line["gneb"] = gneb_line
     if adj_line is not None:
@@ -696,6 +718,10 @@ def main():
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false", help="skip the adjoint measurement")
     ap.add_argument("--no-mc", dest="mc", action="store_false", help="skip the Monte Carlo measurement")
     ap.add_argument("--no-htst", dest="htst", action="store_false", help="skip the HTST measurement")
+    ap.add_argument("--no-batched-ddi", dest="batched_ddi", action="store_false",
+                    help="skip the dipolar variant of the 256-system batched measurement")
+    ap.add_argument("--only-batched-ddi", action="store_true",
+                    help="run and print only the dipolar batched-vs-plain measurement")
     ap.add_argument("--only-htst", action="store_true", help="run and print only the HTST measurement")
     ap.add_argument("--only-adjoint", action="store_true", help="run and print only the adjoint measurement")
     ap.add_argument("--only-batched", action="store_true",
@@ -706,6 +732,12 @@ def main():
 
         torch.cuda.set_device(0)
         print(json.dumps(run_adjoint()))
+        return
+    if args.only_batched_ddi:
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps(run_batched_vs_plain(max(20, args.steps), max(3, args.warmup), ddi=True)))
         return
     if args.only_htst:
         import torch

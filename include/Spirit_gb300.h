@@ -343,7 +343,8 @@ double Simulation_LLG_Loss( State * state, const double * params, int n_steps, c
 /* EXTENSION: the autotuned launch parameters of the image's started LLG run, in this order:
  * spins per thread of the stage kernels; lines and threads per block of FFT pass A / A'; lines
  * and threads of pass B / B'; columns and threads of pass C; 1 if the fused b/c pass is used;
- * its cluster size and threads per block; 1 if the run has a dipolar term.  Writes at most n
+ * its cluster size and threads per block; 1 if the run has a dipolar term; 1 if the stage kernels
+ * do the passes along a themselves (row-fused stages).  Writes at most n
  * values; returns the number the engine reports (0 without a started run). */
 int Simulation_Get_Tuning( State * state, int * values, int n, int idx_image, int idx_chain );
 /* EXTENSION: device arithmetic of the step loop: 32 (FP32 bulk, default) or 64 */

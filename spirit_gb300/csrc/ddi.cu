@@ -1303,7 +1303,7 @@ void DDIPlan::tune( const SysDesc * d_sd, const void * sx, const void * sy, cons
 
 template<typename R>
 void DDIPlan::run_t( const SysDesc * d_sd, const SysRun * runs, const R * sx, const R * sy, const R * sz, R * hx,
-                     R * hy, R * hz, cudaStream_t stream ) const
+                     R * hy, R * hz, cudaStream_t stream, int only ) const
 {
     if( n_sys == 0 )
         return;
@@ -1327,7 +1327,13 @@ void DDIPlan::run_t( const SysDesc * d_sd, const SysRun * runs, const R * sx, co
             trace->push_back( { id, e } );
         }
     };
-    if( fused )
+    if( only >= 0 )
+    {
+        // one pass alone (the row-fused stage kernels do A and A' themselves)
+        mark( only == 0 ? KERNEL_PASS_A : KERNEL_PASS_BC );
+        launch_pass<R>( only, a, stream );
+    }
+    else if( fused )
     {
         static const int ks[3]  = { 0, 5, 4 };
         static const int ids[3] = { KERNEL_PASS_A, KERNEL_PASS_BC, KERNEL_PASS_A_INV };
@@ -1348,14 +1354,14 @@ void DDIPlan::run_t( const SysDesc * d_sd, const SysRun * runs, const R * sx, co
 }
 
 void DDIPlan::run( const SysDesc * d_sd, const SysRun * runs, const void * sx, const void * sy, const void * sz,
-                   void * hx, void * hy, void * hz, cudaStream_t stream ) const
+                   void * hx, void * hy, void * hz, cudaStream_t stream, int only ) const
 {
     if( fp64 )
         run_t<double>( d_sd, runs, (const double *)sx, (const double *)sy, (const double *)sz, (double *)hx,
-                       (double *)hy, (double *)hz, stream );
+                       (double *)hy, (double *)hz, stream, only );
     else
         run_t<float>( d_sd, runs, (const float *)sx, (const float *)sy, (const float *)sz, (float *)hx, (float *)hy,
-                      (float *)hz, stream );
+                      (float *)hz, stream, only );
 }
 
 } // namespace sg

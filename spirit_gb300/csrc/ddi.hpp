@@ -33,9 +33,10 @@ class DDIPlan
 public:
     ~DDIPlan();
     void build( const std::vector<DDISystem> & systems, bool fp64, const SysDesc * d_sd, cudaStream_t stream );
-    // h = D * (mu s) for every DDI system of the batch whose SysRun is active (runs may be null)
+    // h = D * (mu s) for every DDI system of the batch whose SysRun is active (runs may be null);
+    // only >= 0 launches that pass alone (0: A, the spectrum of s; 5: the fused b/c pass)
     void run( const SysDesc * d_sd, const SysRun * runs, const void * sx, const void * sy, const void * sz,
-              void * hx, void * hy, void * hz, cudaStream_t stream ) const;
+              void * hx, void * hy, void * hz, cudaStream_t stream, int only = -1 ) const;
     void release();
     // measure and keep the fastest lines (columns) per block of every pass (outside stream capture)
     void tune( const SysDesc * d_sd, const void * sx, const void * sy, const void * sz, void * hx, void * hy,
@@ -76,7 +77,7 @@ private:
     void launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const;
     template<typename R>
     void run_t( const SysDesc * d_sd, const SysRun * runs, const R * sx, const R * sy, const R * sz, R * hx, R * hy,
-                R * hz, cudaStream_t stream ) const;
+                R * hz, cudaStream_t stream, int only ) const;
 };
 
 // Padded FFT extent per axis (Prepare_DDI, Hamiltonian_Heisenberg.cpp:1510-1518): doubled when the

@@ -19,11 +19,13 @@
 //   RK4                   core/include/engine/Solver_RK4.hpp:40-147
 //   max torque            core/include/engine/Method_Solver.hpp:225-230, Method_LLG.cpp:247-301
 #include "engine.hpp"
+#include "fft.cuh"
 #include "kernels.cuh"
 #include "util.hpp"
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 namespace sg
@@ -297,6 +299,177 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
     if( !( FINAL || PROBE ) )
         return;
     stage_finalize<R, PROBE>( A, run, s, d, e, t2, red_d, red_f, is_last );
+}
+
+// ------------------------------------------------------------------ row-fused stage kernel
+// For systems whose dipolar spectrum is kept ka-major (fused b/c pass): a block owns whole rows
+// along a -- (system, c, b0 .. b0+nr-1), every basis atom and component -- and does the passes
+// along a itself:
+//   prologue  the dipolar field of its rows: C2R along a of the spectrum after the b/c pass
+//             (pass A' arithmetic, the same line pairs (b0 even): the field is bit for bit the one
+//             pass A' writes);
+//   main      the stage (gradient with that field, thermal field, solver update) as llg_stage;
+//   epilogue  R2C along a of the configuration the next field evaluation needs (the predictor,
+//             or the new state after the last stage) into the spectrum (pass A arithmetic).
+// So one field evaluation is the b/c pass and this kernel: two launches instead of four, and the
+// field arrays are neither written nor read.
+template<typename R>
+struct RowArgs
+{
+    const FFTDesc * fd; // per system
+    const cplx<R> * tw; // twiddle tables
+    cplx<R> * W1;       // ka-major spectra [ka][cb][c][b]
+    const int4 * map;   // (system, c, first b, rows)
+};
+
+constexpr int ROW_SPT = 4; // spins per thread the row kernel holds (rows * row length <= 1024)
+
+template<typename R, int SOLVER, int STAGE>
+__global__ void __launch_bounds__( 256 ) llg_stage_rows( StageArgs<R> A, RowArgs<R> F )
+{
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ PairR<R> pairs[MAX_PAIRS];
+    __shared__ SysConst<R> C;
+    __shared__ Geo GS;
+    __shared__ double red_d[32];
+    __shared__ float red_f[32];
+    __shared__ int is_last;
+    const int4 bm     = F.map[blockIdx.x];
+    const int s       = bm.x, cc = bm.y, b0 = bm.z, nr = bm.w;
+    SysRun * run      = A.runs + s;
+    const SysDesc & d = A.sd[s];
+    const FFTDesc & f = F.fd[s];
+    const int Ma = f.M[0], Mh = f.Mh, nb = f.nb, Na = f.N[0], Nb = f.N[1], Nc = f.N[2];
+    const int ncb    = 3 * nb;
+    const int nrq    = ( nr + 1 ) >> 1; // line pairs per component row
+    const int nq     = ncb * nrq;       // complex lines of the block
+    const int ls     = line_stride( Ma );
+    const int rowlen = nb * Na;
+    cplx<R> * tw     = reinterpret_cast<cplx<R> *>( smem_raw );
+    cplx<R> * ba     = tw + Ma;
+    cplx<R> * bb     = ba + nq * ls;
+    load_pairs_smem( pairs, d );
+    load_const( C, d );
+    load_geo( GS, d );
+    load_tw( tw, F.tw + f.tw_offset[0], Ma );
+    __syncthreads();
+    pdl_wait(); // everything below reads what earlier kernels wrote
+    pdl_trigger();
+    if( !A.tune && !run->active )
+        return;
+    constexpr bool FINAL = ( SOLVER == SOLVER_RK4 ) ? ( STAGE == 4 ) : ( STAGE == 2 );
+    const size_t kstride = (size_t)ncb * Nc * Nb;
+    cplx<R> * W1         = F.W1 + f.spec_offset;
+    // ---- prologue: C2R along a (pass_a_inv, ka-major branch)
+    for( int e = threadIdx.x; e < nq * Ma; e += blockDim.x )
+    {
+        const int q = (int)fdiv( (unsigned)e, f.div_Ma ), k = e - q * Ma;
+        const int cb = q / nrq, bl = 2 * ( q - cb * nrq );
+        const bool hi  = k >= Mh;
+        const int kk   = hi ? Ma - k : k;
+        const size_t o = (size_t)kk * kstride + ( (size_t)cb * Nc + cc ) * Nb + b0 + bl;
+        cplx<R> x      = W1[o];
+        cplx<R> y      = bl + 1 < nr ? W1[o + 1] : cplx<R>{ 0, 0 };
+        if( hi )
+        {
+            x.y = -x.y;
+            y.y = -y.y;
+        }
+        if( k == 0 || 2 * k == Ma )
+        {
+            x.y = 0;
+            y.y = 0;
+        }
+        ba[q * ls + k] = { x.x - y.y, x.y + y.x };
+    }
+    __syncthreads();
+    const cplx<R> * hr = block_fft( ba, bb, Ma, ls, nq, f.radix[0], tw, true );
+    const R invT       = fft_invT<R>( f );
+    // ---- main: the stage on the block's spins
+    const int i0        = rowlen * ( b0 + Nb * cc ); // first local spin of the block
+    const int n_spins   = nr * rowlen;
+    const int iteration = run->iteration;
+    R e                 = 0;
+    float t2            = 0;
+    V3<R> nx[ROW_SPT];
+#pragma unroll
+    for( int k = 0; k < ROW_SPT; ++k )
+    {
+        const int el     = threadIdx.x + k * 256;
+        const bool valid = el < n_spins;
+        const int i      = i0 + ( valid ? el : 0 );
+        int ib, a, b, c;
+        cell_of( GS, i, ib, a, b, c );
+        const int smode = warp_stencil_mode( GS, a, b, c, valid );
+        nx[k]           = { 0, 0, 0 };
+        if( valid )
+        {
+            const long long gi = GS.off + i;
+            const R mu         = C.mu[ib];
+            const V3<R> ci     = A.cfg.ld( gi );
+            const int lr       = b - b0;
+            V3<R> hv;
+            {
+                const int qb      = lr >> 1;
+                const bool odd    = lr & 1;
+                const cplx<R> vx  = hr[( ( 3 * ib + 0 ) * nrq + qb ) * ls + a];
+                const cplx<R> vy  = hr[( ( 3 * ib + 1 ) * nrq + qb ) * ls + a];
+                const cplx<R> vz  = hr[( ( 3 * ib + 2 ) * nrq + qb ) * ls + a];
+                hv                = { ( odd ? vx.y : vx.x ) * invT, ( odd ? vy.y : vy.x ) * invT,
+                       ( odd ? vz.y : vz.x ) * invT };
+            }
+            R ek    = 0;
+            V3<R> g = gradient_at<R>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu, ek, smode, &hv );
+            e += ek;
+            stage_update<R, SOLVER, STAGE>( A, C, d, gi, i, ib, ci, g, iteration, t2 );
+            const V3<R> v = FINAL ? A.s.ld( gi ) : A.out.ld( gi ); // this thread's own store
+            nx[k]         = { mu * v.x, mu * v.y, mu * v.z };
+        }
+    }
+    __syncthreads(); // the field buffer is free
+    // ---- epilogue: R2C along a of the next configuration (pass_a, ka-major branch)
+#pragma unroll
+    for( int k = 0; k < ROW_SPT; ++k )
+    {
+        const int el = threadIdx.x + k * 256;
+        if( el < n_spins )
+        {
+            const int lr = el / rowlen, rem = el - lr * rowlen;
+            const int a = rem / nb, ib = rem - a * nb;
+            const int qb = lr >> 1;
+            R * px       = reinterpret_cast<R *>( ba + ( ( 3 * ib + 0 ) * nrq + qb ) * ls + a ) + ( lr & 1 );
+            R * py       = reinterpret_cast<R *>( ba + ( ( 3 * ib + 1 ) * nrq + qb ) * ls + a ) + ( lr & 1 );
+            R * pz       = reinterpret_cast<R *>( ba + ( ( 3 * ib + 2 ) * nrq + qb ) * ls + a ) + ( lr & 1 );
+            *px          = nx[k].x;
+            *py          = nx[k].y;
+            *pz          = nx[k].z;
+        }
+    }
+    // zero padding along a, and the second line of an unpaired last row
+    for( int e2 = threadIdx.x; e2 < nq * Ma; e2 += blockDim.x )
+    {
+        const int q = (int)fdiv( (unsigned)e2, f.div_Ma ), t = e2 - q * Ma;
+        const int bl = 2 * ( q % nrq );
+        if( t >= Na )
+            ba[q * ls + t] = { 0, 0 };
+        else if( bl + 1 >= nr )
+            ba[q * ls + t].y = 0;
+    }
+    __syncthreads();
+    const cplx<R> * r = block_fft( ba, bb, Ma, ls, nq, f.radix[0], tw, false );
+    for( int e2 = threadIdx.x; e2 < ncb * nr * Mh; e2 += blockDim.x )
+    {
+        const int lr = e2 % nr, rest = e2 / nr;
+        const int cb = rest % ncb, k = rest / ncb;
+        const cplx<R> * z = r + ( cb * nrq + ( lr >> 1 ) ) * ls;
+        const cplx<R> zk = z[k], zm = z[k == 0 ? 0 : Ma - k];
+        W1[(size_t)k * kstride + ( (size_t)cb * Nc + cc ) * Nb + b0 + lr]
+            = ( lr & 1 ) ? cplx<R>{ R( 0.5 ) * ( zk.y + zm.y ), R( -0.5 ) * ( zk.x - zm.x ) }
+                         : cplx<R>{ R( 0.5 ) * ( zk.x + zm.x ), R( 0.5 ) * ( zk.y - zm.y ) };
+    }
+    if( !FINAL )
+        return;
+    stage_finalize<R, false>( A, run, s, d, e, t2, red_d, red_f, is_last );
 }
 
 // ------------------------------------------------------------------ evaluation kernel
@@ -573,6 +746,8 @@ Engine::~Engine()
         dfree( d_sblkmap_[k] );
         dfree( d_sblkcount_[k] );
     }
+    dfree( d_rowmap_ );
+    dfree( d_rowcount_ );
     if( own_stream_ )
         cudaStreamDestroy( own_stream_ );
 }
@@ -670,11 +845,70 @@ void Engine::build_systems( const std::vector<SystemInput> & systems )
             field_[c] = dalloc_bytes( total_ * elem_ );
         ddi_.build( ddis, fp64_, d_desc_, stream_ );
         ddi_.tune( d_desc_, spins_[0], spins_[1], spins_[2], field_[0], field_[1], field_[2], stream_ );
+        build_row_map( (int)ddis.size() );
     }
+}
+
+// Row-fused stages (llg_stage_rows), selected by SPIRIT_GB300_ROWS=1, when every system has the
+// dipolar interaction on the fused (ka-major) b/c path and a block of whole rows fits: rows per
+// block even (the line pairs of pass A / A'), rows * row length <= 1024 spins, the line buffers
+// within the shared memory.  Not the default: on the 128x128x16 Heun workload the fused kernel
+// (0.143 ms/step at 512 spins per block; 0.151 at 256, 0.171 at 1024) is slower than the
+// separate passes (0.112 ms/step) -- each block runs its C2R, stage and R2C phases one after
+// another with few lines to transform, where the separate kernels each fill the GPU.
+void Engine::build_row_map( int n_ddi )
+{
+    rows_ = false;
+    const char * env = std::getenv( "SPIRIT_GB300_ROWS" );
+    if( !( env && env[0] == '1' ) )
+        return;
+    if( n_ddi != (int)desc_.size() || !ddi_.fused )
+        return;
+    std::vector<int4> m;
+    size_t smem = 0;
+    for( size_t s = 0; s < desc_.size(); ++s )
+    {
+        const FFTDesc & f = ddi_.fd_host[s];
+        const int rowlen  = f.nb * f.N[0];
+        int nr            = 2;
+        const char * want = std::getenv( "SPIRIT_GB300_ROW_SPINS" ); // spins per block (experiments)
+        const int target  = want ? std::atoi( want ) : 512;
+        while( nr * 2 * rowlen <= target )
+            nr *= 2;
+        if( nr * rowlen > 256 * 4 )
+            return;
+        const int nq = 3 * f.nb * ( ( nr + 1 ) / 2 );
+        smem         = std::max( smem, elem_ * 2 * ( f.M[0] + 2 * (size_t)nq * line_stride( f.M[0] ) ) );
+        for( int c = 0; c < f.N[2]; ++c )
+            for( int b0 = 0; b0 < f.N[1]; b0 += nr )
+                m.push_back( make_int4( (int)s, c, b0, std::min( nr, f.N[1] - b0 ) ) );
+    }
+    if( smem > 96 * 1024 )
+        return;
+    std::vector<int> cnt( desc_.size(), 0 );
+    for( auto & x : m )
+        ++cnt[x.x];
+    d_rowmap_   = dalloc<int4>( m.size() );
+    d_rowcount_ = dalloc<int>( cnt.size() );
+    h2d( d_rowmap_, m.data(), m.size() );
+    h2d( d_rowcount_, cnt.data(), cnt.size() );
+    n_rowblocks_ = (int)m.size();
+    rows_smem_   = smem;
+    rows_        = true;
+}
+
+// the spectrum must hold the current state's before the first b/c pass of a step sequence
+void Engine::ensure_spectrum()
+{
+    if( !rows_ || w1_valid_ )
+        return;
+    ddi_.run( d_desc_, d_runs_, spins_[0], spins_[1], spins_[2], field_[0], field_[1], field_[2], stream_, 0 );
+    w1_valid_ = true;
 }
 
 void Engine::set_params( int s, const SystemInput & in )
 {
+    w1_valid_   = false;
     SysDesc & d = desc_[s];
     d.dt                  = in.dt;
     d.damping             = in.damping;
@@ -697,6 +931,7 @@ static SoA3<R> soa( void * const * p )
 
 void Engine::set_spins( int s, const double * aos )
 {
+    w1_valid_         = false;
     const SysDesc & d = desc_[s];
     CUDA_CHECK( cudaMemcpyAsync( d_stage_, aos, sizeof( double ) * 3 * d.nos, cudaMemcpyHostToDevice, stream_ ) );
     int grid = std::min( 1024, ( d.nos + 255 ) / 256 );
@@ -723,6 +958,7 @@ void Engine::get_spins( int s, double * aos )
 
 void Engine::set_all_spins( const double * aos )
 {
+    w1_valid_ = false;
     // one host->device copy of the concatenated systems, then per-system conversion kernels
     size_t n = 0;
     for( auto & d : desc_ )
@@ -765,6 +1001,7 @@ void Engine::gradient_t( int s, double * grad_aos, double * energy, double * ter
     if( d.ddi )
     {
         ddi_.run( d_desc_, nullptr, spins_[0], spins_[1], spins_[2], field_[0], field_[1], field_[2], stream_ );
+        w1_valid_ = false;
         h = soa<R>( field_ );
     }
     CUDA_CHECK( cudaMemsetAsync( d_red_, 0, sizeof( double ) * N_TERMS, stream_ ) );
@@ -819,6 +1056,7 @@ void Engine::ddi_field( int s, double * h_aos )
         return;
     }
     ddi_.run( d_desc_, nullptr, spins_[0], spins_[1], spins_[2], field_[0], field_[1], field_[2], stream_ );
+    w1_valid_ = false;
     int grid = std::min( 1024, ( d.nos + 255 ) / 256 );
     if( fp64_ )
         soa_to_aos<double><<<grid, 256, 0, stream_>>>( soa<double>( field_ ), d.spin_offset, d.nos, d_stage_ );
@@ -840,8 +1078,33 @@ static void trace_mark( std::vector<std::pair<int, cudaEvent_t>> * trace, int id
 }
 
 template<typename R, int SOLVER, int STAGE>
+void Engine::launch_stage_rows( StageArgs<R> a, cudaStream_t st )
+{
+    trace_mark( trace_, KERNEL_STAGE, st );
+    static bool attr = false;
+    if( !attr )
+    {
+        CUDA_CHECK( cudaFuncSetAttribute( llg_stage_rows<R, SOLVER, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          96 * 1024 ) );
+        attr = true;
+    }
+    a.blkcount = d_rowcount_;
+    RowArgs<R> F;
+    F.fd  = ddi_.d_fd;
+    F.tw  = (const cplx<R> *)ddi_.d_tw;
+    F.W1  = (cplx<R> *)ddi_.d_W1;
+    F.map = d_rowmap_;
+    launch_pdl( llg_stage_rows<R, SOLVER, STAGE>, dim3( n_rowblocks_ ), dim3( 256 ), rows_smem_, st, 1, a, F );
+}
+
+template<typename R, int SOLVER, int STAGE>
 void Engine::launch_stage( StageArgs<R> a, cudaStream_t st )
 {
+    if( rows_ && a.h.x )
+    {
+        launch_stage_rows<R, SOLVER, STAGE>( a, st );
+        return;
+    }
     trace_mark( trace_, KERNEL_STAGE, st );
     const int k = sizeof( R ) == 8 ? 0 : spt_idx_;
     a.blkmap    = d_sblkmap_[k];
@@ -869,7 +1132,8 @@ void Engine::launch_probe_t()
     if( any_ddi_ )
     {
         ddi_.run( d_desc_, d_runs_, spins_[0], spins_[1], spins_[2], field_[0], field_[1], field_[2], stream_ );
-        a.h = soa<R>( field_ );
+        w1_valid_ = false;
+        a.h       = soa<R>( field_ );
     }
     // the probe uses the solver's force definition (direct minimisation / dynamics) only
     llg_stage<R, SOLVER_HEUN, ST_PROBE, 1><<<n_blocks_, 256, 0, stream_>>>( a );
@@ -884,8 +1148,10 @@ void Engine::launch_stages_t( StageArgs<R> & a, bool with_ddi )
     SoA3<R> pA = soa<R>( predA_ ), pB = soa<R>( predB_ );
     auto field = [&]( const SoA3<R> & cfg ) {
         if( with_ddi && any_ddi_ )
-            ddi_.run( d_desc_, d_runs_, cfg.x, cfg.y, cfg.z, field_[0], field_[1], field_[2], stream_ );
+            ddi_.run( d_desc_, d_runs_, cfg.x, cfg.y, cfg.z, field_[0], field_[1], field_[2], stream_, rows_ ? 5 : -1 );
     };
+    if( !with_ddi && rows_ )
+        a.h = { nullptr, nullptr, nullptr }; // timing runs of the tuner: plain stage kernels
     switch( solver_ )
     {
     case SOLVER_SIB:
@@ -1026,6 +1292,7 @@ void Engine::profile_steps( int n, void * flush_buf, size_t flush_bytes, void * 
                             double * ms, int * count )
 {
     std::vector<std::pair<int, cudaEvent_t>> tr;
+    ensure_spectrum();
     for( int k = 0; k < n; ++k )
     {
         if( flush_buf && flush_bytes )
@@ -1054,18 +1321,18 @@ void Engine::profile_steps( int n, void * flush_buf, size_t flush_bytes, void * 
 
 int Engine::tuning( int * out, int n ) const
 {
-    const int v[11] = { SPT_OPTIONS[fp64_ ? 0 : spt_idx_], ddi_.tile[0], ddi_.threads[0], ddi_.tile[1],
+    const int v[12] = { SPT_OPTIONS[fp64_ ? 0 : spt_idx_], ddi_.tile[0], ddi_.threads[0], ddi_.tile[1],
                         ddi_.threads[1], ddi_.tile[2], ddi_.threads[2], ddi_.fused ? 1 : 0,
-                        ddi_.cluster_k, ddi_.threads_bc, any_ddi_ ? 1 : 0 };
-    for( int k = 0; k < n && k < 11; ++k )
+                        ddi_.cluster_k, ddi_.threads_bc, any_ddi_ ? 1 : 0, rows_ ? 1 : 0 };
+    for( int k = 0; k < n && k < 12; ++k )
         out[k] = v[k];
-    return 11;
+    return 12;
 }
 
 int Engine::kernels_per_step() const
 {
     int stages = solver_ == SOLVER_RK4 ? 4 : 2;
-    return stages * ( 1 + ( any_ddi_ ? ( ddi_.fused ? 3 : 5 ) : 0 ) );
+    return stages * ( 1 + ( any_ddi_ ? ( rows_ ? 1 : ( ddi_.fused ? 3 : 5 ) ) : 0 ) );
 }
 
 void Engine::llg_start( int solver, const std::vector<int> & n_iterations )
@@ -1101,6 +1368,7 @@ void Engine::llg_launch( int n_steps )
     // steps are replayed from CUDA graphs of G steps and of one step; steps beyond a system's
     // budget or after its convergence are no-ops on the device
     const int G = 8;
+    ensure_spectrum();
     if( !graph_ || graph_solver_ != solver_ )
     {
         if( graph_ )

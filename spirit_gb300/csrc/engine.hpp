@@ -159,6 +159,7 @@ public:
     {
         if( any_ddi_ )
             ddi_.run( d_desc_, runs, cfg[0], cfg[1], cfg[2], field_[0], field_[1], field_[2], stream_ );
+        w1_valid_ = false;
     }
 
 private:
@@ -170,6 +171,10 @@ private:
     void launch_probe_t();
     template<typename R, int SOLVER, int STAGE>
     void launch_stage( StageArgs<R> a, cudaStream_t st );
+    template<typename R, int SOLVER, int STAGE>
+    void launch_stage_rows( StageArgs<R> a, cudaStream_t st );
+    void build_row_map( int n_ddi );
+    void ensure_spectrum();
     template<typename R>
     void launch_stages_t( StageArgs<R> & a, bool with_ddi );
     template<typename R>
@@ -209,6 +214,14 @@ private:
     int tuned_solver_     = -1;
     bool any_ddi_     = false;
     DDIPlan ddi_;
+    // row-fused stages: the stage kernels do the passes along a (llg_stage_rows); the spectrum
+    // then carries the configuration from one stage to the next b/c pass
+    bool rows_          = false;
+    bool w1_valid_      = false; // the spectrum holds the current state's (ready for a step)
+    int4 * d_rowmap_    = nullptr;
+    int * d_rowcount_   = nullptr;
+    int n_rowblocks_    = 0;
+    size_t rows_smem_   = 0;
     int solver_       = SOLVER_HEUN;
     cudaGraphExec_t graph_ = nullptr;
     cudaGraphExec_t graph1_ = nullptr; // single step

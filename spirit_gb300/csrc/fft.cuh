@@ -30,7 +30,13 @@ struct cplx
 template<typename R>
 __device__ __forceinline__ cplx<R> cmul( cplx<R> a, cplx<R> b )
 {
-    return { a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x };
+    // explicit rounding: one product rounded, the other fused, the same in every kernel that
+    // inlines the transform (left to the compiler, the choice of the fused product can differ
+    // between kernels, and so would the transforms of the row-fused stages and of pass A / A')
+    if constexpr( sizeof( R ) == 4 )
+        return { __fmaf_rn( a.x, b.x, -__fmul_rn( a.y, b.y ) ), __fmaf_rn( a.x, b.y, __fmul_rn( a.y, b.x ) ) };
+    else
+        return { __fma_rn( a.x, b.x, -__dmul_rn( a.y, b.y ) ), __fma_rn( a.x, b.y, __dmul_rn( a.y, b.x ) ) };
 }
 template<typename R>
 __device__ __forceinline__ cplx<R> cconj( cplx<R> a )

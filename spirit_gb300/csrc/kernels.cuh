@@ -302,10 +302,12 @@ __device__ __forceinline__ void load_const( SysConst<R> & dst, const SysDesc & d
 // Gradient of the Heisenberg Hamiltonian at spin i of configuration cfg (Gradient_and_Energy,
 // Hamiltonian_Heisenberg.cpp:704-766: anisotropy, exchange + DMI pairs, dipolar field, then
 // Zeeman), and the energy of that spin: 0.5 g_quadratic . s + Zeeman, in the working precision.
+// hval, when given, is the dipolar field of the spin (instead of h[gi]).
 template<typename R>
 __device__ __forceinline__ V3<R> gradient_at( const Geo & d, const SysConst<R> & C, const PairR<R> * pairs,
                                               const SoA3<R> & cfg, const SoA3<R> & h, long long gi, int ib, int a,
-                                              int b, int c, V3<R> si, R mu, R & e, int mode = STENCIL_GENERAL )
+                                              int b, int c, V3<R> si, R mu, R & e, int mode = STENCIL_GENERAL,
+                                              const V3<R> * hval = nullptr )
 {
     V3<R> g = { 0, 0, 0 };
     for( int k = 0; k < C.n_aniso; ++k )
@@ -348,9 +350,10 @@ __device__ __forceinline__ V3<R> gradient_at( const Geo & d, const SysConst<R> &
             g.z -= cr.z;
         }
     }
-    if( h.x )
+    if( hval || h.x )
     {
-        V3<R> hh = h.ld( gi );
+        // dipolar field of the spin: given (computed by the caller) or from the field arrays
+        V3<R> hh = hval ? *hval : h.ld( gi );
         g.x -= mu * hh.x;
         g.y -= mu * hh.y;
         g.z -= mu * hh.z;

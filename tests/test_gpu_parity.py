@@ -127,3 +127,24 @@ def test_thermal_trajectory_vs_oracle_fp32():
         simulation.start(p, simulation.METHOD_LLG, simulation.SOLVER_SIB, 50)
         s = spins_of(p)
     assert np.abs(s - ref).max() < 1e-4
+
+
+@pytest.mark.parametrize("solver", ["Heun", "RK4", "SIB"])
+def test_row_fused_stages_bitwise(solver, monkeypatch):
+    """The row-fused stage kernels (passes along a inside the stage kernel) give the same FP32
+    trajectory, bit for bit, as the separate passes A / A' with the same line pairs (thermal noise
+    on, dipolar field, 40 steps); SPIRIT_GB300_ROWS=0 selects the separate passes."""
+    from oracle.oracle import random_spins
+    from spirit_gb300 import simulation
+
+    spec = dict(GRAD_CASES["sc3d_ddi"], n_cells=[32, 24, 4],
+                llg=dict(dt=5e-4, damping=0.1, temperature=10.0, seed=3))
+    n = 32 * 24 * 4
+    s0 = random_spins(n, 21)
+    out = []
+    for rows in ("1", "0"):
+        monkeypatch.setenv("SPIRIT_GB300_ROWS", rows)
+        with make_state(spec, s0, precision=32, name="rows%s_%s" % (rows, solver)) as p:
+            simulation.start(p, simulation.METHOD_LLG, getattr(simulation, "SOLVER_" + solver.upper()), 40)
+            out.append(spins_of(p))
+    np.testing.assert_array_equal(out[0], out[1])
