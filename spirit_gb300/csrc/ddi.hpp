@@ -80,13 +80,32 @@ private:
                 R * hz, cudaStream_t stream, int only ) const;
 };
 
-// Padded FFT extent per axis (Prepare_DDI, Hamiltonian_Heisenberg.cpp:1510-1518): doubled when the
-// axis has more than one cell and is open or explicitly zero-padded.
+// smallest even number >= m whose prime factors are all <= 7
+inline int ddi_smooth_even( int m )
+{
+    for( int v = m + ( m & 1 );; v += 2 )
+    {
+        int r = v;
+        for( int p : { 2, 3, 5, 7 } )
+            while( r % p == 0 )
+                r /= p;
+        if( r == 1 )
+            return v;
+    }
+}
+
+// Padded FFT extent per axis.  The reference (Prepare_DDI, Hamiltonian_Heisenberg.cpp:1510-1518)
+// doubles an axis with more than one cell that is open or explicitly zero-padded, to 2N.  A
+// zero-padded circular convolution of length M equals the linear one for every M >= 2N - 1 (the
+// offsets between N and M - N are never paired), so here such an axis gets the smallest even
+// 7-smooth M >= 2N: 2N itself when it is 7-smooth (powers of two, most sizes), else slightly more,
+// which keeps every transform on radices <= 7 (2N = 2 * 251 would otherwise be a radix-251
+// stage).  Periodic axes without padding keep M = N.
 inline std::array<int, 3> ddi_padding( const std::array<int, 3> & n, const std::array<int, 3> & bc, bool pb_zero_padding )
 {
     std::array<int, 3> m;
     for( int d = 0; d < 3; ++d )
-        m[d] = ( n[d] > 1 && ( bc[d] == 0 || pb_zero_padding ) ) ? 2 * n[d] : n[d];
+        m[d] = ( n[d] > 1 && ( bc[d] == 0 || pb_zero_padding ) ) ? ddi_smooth_even( 2 * n[d] ) : n[d];
     return m;
 }
 
