@@ -1215,7 +1215,7 @@ void DDIPlan::tune_t( const SysDesc * d_sd, const R * sx, const R * sy, const R 
         // single-block kernel.  The arithmetic of every line is the same for every K.
         float bt = 1e30f;
         int bthr_bc = threads_bc, bk = 1;
-        for( int K : { 1, 2, 4 } )
+        for( int K : { 1, 2, 4, 8 } )
         {
             bool ok = true;
             for( auto & f : fd_host )
@@ -1224,9 +1224,9 @@ void DDIPlan::tune_t( const SysDesc * d_sd, const R * sx, const R * sy, const R 
                 continue;
             cluster_k = K;
             set_tiles( best[0], best[1], best[2] );
-            for( int th : { 256, 512, 1024 } )
+            for( int th : { 128, 256, 512, 1024 } )
             {
-                if( K > 1 && th > 512 )
+                if( ( K > 1 && th > 512 ) || ( K == 1 && th < 256 ) )
                     continue;
                 threads_bc = th;
                 float t    = timed( { 5 } );
