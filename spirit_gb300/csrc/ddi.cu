@@ -13,6 +13,7 @@
 #include <cooperative_groups.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 namespace sg
@@ -43,6 +44,7 @@ struct PassArgs
     FastDiv div_g;
     int ka_major; // W1 layout: 0 [row][b][ka] (split passes B, C, B'), 1 [ka][row][b] (fused pass BC)
     FastDiv div_gq; // (g + 1) / 2: line pairs per block of pass A
+    int lg_a;       // largest register radix (log2) of the line transforms of passes A / A' (0: default)
 };
 
 template<typename R>
@@ -117,7 +119,7 @@ __global__ void pass_a( PassArgs<R> p )
         }
     }
     __syncthreads();
-    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.radix[0], tw, false );
+    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.radix[0], tw, false, p.lg_a );
     if( !p.ka_major )
     {
         cplx<R> * W1 = p.W1 + f.spec_offset + ( (size_t)row * Bin + b0 ) * Mh;
@@ -578,7 +580,7 @@ __global__ void pass_a_inv( PassArgs<R> p )
         a[q * ls + k] = { x.x - y.y, x.y + y.x };
     }
     __syncthreads();
-    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.radix[0], tw, true );
+    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.radix[0], tw, true, p.lg_a );
     const R invT = fft_invT<R>( f );
     const int cb = row / Nc, c = row - cb * Nc;
     const int ib = cb / 3, comp = cb - 3 * ib;
@@ -1089,6 +1091,7 @@ void DDIPlan::launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const
         a.blocks = d_blocks[0];
         a.g      = tile[0];
         a.div_g  = make_fastdiv( tile[0] );
+        a.lg_a   = lg_a;
         launch_pdl( pass_a<R>, dim3( n_blocks[0] ), dim3( threads[0] ), max_smem_a, stream, 1, a );
         break;
     case 1:
@@ -1117,6 +1120,7 @@ void DDIPlan::launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const
         a.g      = tile[0];
         a.div_g  = make_fastdiv( tile[0] );
         a.div_gq = make_fastdiv( ( tile[0] + 1 ) / 2 );
+        a.lg_a   = lg_a;
         launch_pdl( pass_a_inv<R>, dim3( n_blocks[0] ), dim3( threads[0] ), max_smem_a, stream, 1, a );
         break;
     }

@@ -358,29 +358,47 @@ __device__ __forceinline__ cplx<R> * block_fft_const( cplx<R> * a, cplx<R> * b, 
 // starts at k * ls (ls = L, or L + 1 for power-of-two lengths to spread shared-memory banks).
 // rad: 0-terminated radix list; tw: L twiddles exp(-2 pi i t/L) (in shared memory).
 // Returns the buffer that holds the result.  Must be called by all threads of the block.
-template<typename R>
-__device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int ls, int nl, const int * rad,
-                               const cplx<R> * tw, bool inverse )
+// power-of-two lines of 2^LGL with register stages of at most 2^MAXLG
+template<typename R, int MAXLG>
+__device__ __forceinline__ cplx<R> * block_fft_reg( cplx<R> * a, cplx<R> * b, int L, int ls, int nl,
+                                                   const cplx<R> * tw, bool inverse, bool & done )
 {
+    done = true;
+    const FastDiv one{ 1, 0, 0 };
     switch( L )
     {
-    case 1:
-        return a;
     case 16:
-        return stockham_reg<R, 4, 0, MaxRadix<R>::LG, false>( a, b, nl, FastDiv{ 1, 0, 0 }, ls, 1, tw, inverse );
+        return stockham_reg<R, 4, 0, MAXLG, false>( a, b, nl, one, ls, 1, tw, inverse );
     case 32:
-        return stockham_reg<R, 5, 0, MaxRadix<R>::LG, false>( a, b, nl, FastDiv{ 1, 0, 0 }, ls, 1, tw, inverse );
+        return stockham_reg<R, 5, 0, MAXLG, false>( a, b, nl, one, ls, 1, tw, inverse );
     case 64:
-        return stockham_reg<R, 6, 0, MaxRadix<R>::LG, false>( a, b, nl, FastDiv{ 1, 0, 0 }, ls, 1, tw, inverse );
+        return stockham_reg<R, 6, 0, MAXLG, false>( a, b, nl, one, ls, 1, tw, inverse );
     case 128:
-        return stockham_reg<R, 7, 0, MaxRadix<R>::LG, false>( a, b, nl, FastDiv{ 1, 0, 0 }, ls, 1, tw, inverse );
+        return stockham_reg<R, 7, 0, MAXLG, false>( a, b, nl, one, ls, 1, tw, inverse );
     case 256:
-        return stockham_reg<R, 8, 0, MaxRadix<R>::LG, false>( a, b, nl, FastDiv{ 1, 0, 0 }, ls, 1, tw, inverse );
+        return stockham_reg<R, 8, 0, MAXLG, false>( a, b, nl, one, ls, 1, tw, inverse );
     case 512:
-        return stockham_reg<R, 9, 0, MaxRadix<R>::LG, false>( a, b, nl, FastDiv{ 1, 0, 0 }, ls, 1, tw, inverse );
+        return stockham_reg<R, 9, 0, MAXLG, false>( a, b, nl, one, ls, 1, tw, inverse );
     default:
-        break;
+        done = false;
+        return a;
     }
+}
+
+// maxlg: largest register radix 2^maxlg of the power-of-two lengths 16..512 (0: the default,
+// radix 16 in FP32 and 8 in FP64; 2: radix 4, four times the threads per line)
+template<typename R>
+__device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int ls, int nl, const int * rad,
+                               const cplx<R> * tw, bool inverse, int maxlg = 0 )
+{
+    if( L == 1 )
+        return a;
+    bool done   = false;
+    cplx<R> * r = maxlg == 2   ? block_fft_reg<R, 2>( a, b, L, ls, nl, tw, inverse, done )
+                  : maxlg == 3 ? block_fft_reg<R, 3>( a, b, L, ls, nl, tw, inverse, done )
+                               : block_fft_reg<R, MaxRadix<R>::LG>( a, b, L, ls, nl, tw, inverse, done );
+    if( done )
+        return r;
     if( ( L & ( L - 1 ) ) == 0 )
         return block_fft_pow2( a, b, L, ls, nl, tw, inverse );
     int Ns = 1;
