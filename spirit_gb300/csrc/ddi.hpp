@@ -60,11 +60,14 @@ public:
     bool fused         = false; // passes B, C, B' as one kernel per (system, ka) plane
     int threads_bc     = 1024;
     int cluster_k      = 1; // blocks per (system, ka) plane of the fused pass (cluster size)
-    // register radix of passes A / A' (log2): 8, not the radix 16 of the b/c pass -- passes A / A'
-    // have few lines per block, and radix 8 keeps twice as many threads busy per line (128x128x16
-    // Heun: 0.110 ms/step against 0.112-0.113 with radix 16; radix 4 measured the same as 8).
-    // Fixed rather than tuned, so the transforms do not depend on timings.
-    int lg_a           = 3;
+    // largest register radix (log2) of the line transforms of passes A / A' and of the b/c pass:
+    // radix 4.  The lines are short (128 points on the 128x128x16 workload) and few per block, so
+    // threads per line matter more than fewer shared-memory round trips: b/c pass radix 4 gave
+    // 0.105-0.106 ms/step against 0.106-0.109 with radix 8 and 0.112-0.113 with radix 16; passes
+    // A / A' radix 4 or 8 0.110 against 0.112-0.114 with radix 16.  Fixed rather than tuned, so
+    // the transforms never depend on timings.
+    int lg_a           = 2;
+    int lg_bc          = 2;
     int n_fd_slots     = 1;
     size_t smem_bc_max = 0;
     size_t max_smem_a = 0, max_smem_b = 0, max_smem_c = 0;

@@ -667,7 +667,7 @@ __device__ cplx<R> * sfft_generic( cplx<R> * a, cplx<R> * b, int L, int nl, int 
     return a;
 }
 
-template<typename R, bool LINE_FAST>
+template<typename R, bool LINE_FAST, int MAXLG = MaxRadix<R>::LG>
 __device__ cplx<R> * sfft( cplx<R> * a, cplx<R> * b, int L, int nl, const FastDiv & dnl, int ls, int es,
                           const int * rad, const cplx<R> * tw, bool inverse )
 {
@@ -682,22 +682,34 @@ __device__ cplx<R> * sfft( cplx<R> * a, cplx<R> * b, int L, int nl, const FastDi
     case 8:
         return sfft_const<R, 8, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 16:
-        return stockham_reg<R, 4, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 4, 0, MAXLG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 32:
-        return stockham_reg<R, 5, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 5, 0, MAXLG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 64:
-        return stockham_reg<R, 6, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 6, 0, MAXLG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 128:
-        return stockham_reg<R, 7, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 7, 0, MAXLG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 256:
-        return stockham_reg<R, 8, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 8, 0, MAXLG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 512:
-        return stockham_reg<R, 9, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 9, 0, MAXLG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     case 1024:
-        return stockham_reg<R, 10, 0, MaxRadix<R>::LG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
+        return stockham_reg<R, 10, 0, MAXLG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     default:
         return sfft_generic<R>( a, b, L, nl, ls, es, rad, tw, inverse );
     }
+}
+
+// sfft with the largest register radix 2^lg chosen at run time (0: the default)
+template<typename R, bool LINE_FAST>
+__device__ cplx<R> * sfft_lg( int lg, cplx<R> * a, cplx<R> * b, int L, int nl, const FastDiv & dnl, int ls, int es,
+                             const int * rad, const cplx<R> * tw, bool inverse )
+{
+    if( lg == 2 )
+        return sfft<R, LINE_FAST, 2>( a, b, L, nl, dnl, ls, es, rad, tw, inverse );
+    if( lg == 3 )
+        return sfft<R, LINE_FAST, 3>( a, b, L, nl, dnl, ls, es, rad, tw, inverse );
+    return sfft<R, LINE_FAST>( a, b, L, nl, dnl, ls, es, rad, tw, inverse );
 }
 
 // copy a twiddle table into shared memory (all threads)
