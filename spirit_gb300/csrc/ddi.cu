@@ -1184,6 +1184,11 @@ void DDIPlan::tune_t( const SysDesc * d_sd, const R * sx, const R * sy, const R 
         }
         return best_ms;
     };
+    // overrides of the register radices (log2; 0: radix 16 in FP32, 8 in FP64)
+    if( const char * e = std::getenv( "SPIRIT_GB300_LG_A" ) )
+        lg_a = std::atoi( e );
+    if( const char * e = std::getenv( "SPIRIT_GB300_LG_BC" ) )
+        lg_bc = std::atoi( e );
     // warm-up of the whole chain (first launches pay module loading)
     if( fused )
         timed( { 0, 5, 4 } );

@@ -61,13 +61,13 @@ public:
     int threads_bc     = 1024;
     int cluster_k      = 1; // blocks per (system, ka) plane of the fused pass (cluster size)
     // largest register radix (log2) of the line transforms of passes A / A' and of the b/c pass:
-    // radix 4.  The lines are short (128 points on the 128x128x16 workload) and few per block, so
-    // threads per line matter more than fewer shared-memory round trips: b/c pass radix 4 gave
-    // 0.105-0.106 ms/step against 0.106-0.109 with radix 8 and 0.112-0.113 with radix 16; passes
-    // A / A' radix 4 or 8 0.110 against 0.112-0.114 with radix 16.  Fixed rather than tuned, so
-    // the transforms never depend on timings.
-    int lg_a           = 2;
-    int lg_bc          = 2;
+    // radix 8.  The lines are short (128 points on the 128x128x16 workload) and few per block, so
+    // threads per line matter as much as fewer shared-memory round trips.  Interleaved runs in
+    // one session (ms/step, two runs each): radix 8 / 8 0.1035, 0.1037; 8 / 4 0.1051, 0.1061;
+    // 4 / 4 0.119, 0.106; 16 / 16 (the register default) 0.134, 0.111.  Fixed rather than
+    // tuned, so the transforms never depend on timings; SPIRIT_GB300_LG_A / _LG_BC override.
+    int lg_a           = 3;
+    int lg_bc          = 3;
     int n_fd_slots     = 1;
     size_t smem_bc_max = 0;
     size_t max_smem_a = 0, max_smem_b = 0, max_smem_c = 0;
