@@ -1264,6 +1264,11 @@ void Engine::tune_stages_t()
         }
     }
     spt_idx_ = bi;
+    if( const char * e = std::getenv( "SPIRIT_GB300_SPT" ) ) // override (measurements): 1, 2 or 4
+    {
+        const int v = std::atoi( e );
+        spt_idx_    = v == 1 ? 0 : ( v == 2 ? 1 : ( v == 4 ? 2 : spt_idx_ ) );
+    }
     trace_   = saved;
     CUDA_CHECK( cudaEventDestroy( e0 ) );
     CUDA_CHECK( cudaEventDestroy( e1 ) );
