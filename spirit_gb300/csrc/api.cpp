@@ -140,11 +140,9 @@ const char * solver_name( int s )
     }
 }
 
-void finish_llg( Image & img, Engine & E )
+Engine::Status finish_llg( Image & img, Engine & E )
 {
-    auto stv = E.status();
-    E.get_spins( 0, img.spins.data() );
-    auto & s            = stv[0];
+    const Engine::Status s = E.fetch( 0, img.spins.data() );
     if( img.llg.temperature > 0 )
         img.llg_noise_drawn += (unsigned)( s.iteration - img.info.iteration );
     img.E               = s.energy;
@@ -154,6 +152,7 @@ void finish_llg( Image & img, Engine & E )
     auto now            = std::chrono::steady_clock::now();
     img.info.wall_ms    = std::chrono::duration_cast<std::chrono::milliseconds>( now - img.info.t_start ).count();
     img.info.ips        = img.info.wall_ms > 0 ? 1000.0 * s.iteration / img.info.wall_ms : 0.0;
+    return s;
 }
 
 // Method::Iterate (core/src/engine/Method.cpp:57-113): the device stops a system by itself on
@@ -2081,16 +2080,12 @@ void Simulation_N_Shot( State * state, int N, int idx_image, int idx_chain ) noe
             return;
         }
         Engine & E = *img.run;
-        // the host spin buffer is the state: callers may have written into it since the last call
-        E.set_spins( 0, img.spins.data() );
-        auto s = E.status()[0];
-        if( s.active )
-        {
-            E.llg_launch( N );
-            E.sync();
-        }
-        finish_llg( img, E );
-        s = E.status()[0];
+        // the host spin buffer is the state: callers may have written into it since the last call.
+        // Upload, steps and read-back are enqueued together with one synchronisation at the end
+        // (steps of a converged or finished run are no-ops on the device).
+        E.set_spins( 0, img.spins.data(), false );
+        E.llg_launch( N );
+        const Engine::Status s = finish_llg( img, E );
         if( !s.active || stop_file_present() )
         {
             img.iteration_allowed  = false;

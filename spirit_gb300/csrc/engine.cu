@@ -930,7 +930,7 @@ static SoA3<R> soa( void * const * p )
     return { (R *)p[0], (R *)p[1], (R *)p[2] };
 }
 
-void Engine::set_spins( int s, const double * aos )
+void Engine::set_spins( int s, const double * aos, bool sync )
 {
     w1_valid_         = false;
     const SysDesc & d = desc_[s];
@@ -941,7 +941,24 @@ void Engine::set_spins( int s, const double * aos )
     else
         aos_to_soa<float><<<grid, 256, 0, stream_>>>( d_stage_, soa<float>( spins_ ), d.spin_offset, d.nos );
     CUDA_CHECK( cudaGetLastError() );
+    if( sync )
+        CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+}
+
+Engine::Status Engine::fetch( int s, double * aos )
+{
+    const SysDesc & d = desc_[s];
+    int grid          = std::min( 1024, ( d.nos + 255 ) / 256 );
+    if( fp64_ )
+        soa_to_aos<double><<<grid, 256, 0, stream_>>>( soa<double>( spins_ ), d.spin_offset, d.nos, d_stage_ );
+    else
+        soa_to_aos<float><<<grid, 256, 0, stream_>>>( soa<float>( spins_ ), d.spin_offset, d.nos, d_stage_ );
+    CUDA_CHECK( cudaGetLastError() );
+    CUDA_CHECK( cudaMemcpyAsync( aos, d_stage_, sizeof( double ) * 3 * d.nos, cudaMemcpyDeviceToHost, stream_ ) );
+    SysRun r;
+    CUDA_CHECK( cudaMemcpyAsync( &r, d_runs_ + s, sizeof( SysRun ), cudaMemcpyDeviceToHost, stream_ ) );
     CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+    return { r.iteration, r.active, r.max_torque, r.energy };
 }
 
 void Engine::get_spins( int s, double * aos )

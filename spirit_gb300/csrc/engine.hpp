@@ -69,7 +69,9 @@ public:
     }
 
     // host AoS [nos][3] double <-> device SoA in the engine precision
-    void set_spins( int s, const double * aos );
+    // sync = false: the copy and conversion are only enqueued (later launches on the engine's
+    // stream see the new spins)
+    void set_spins( int s, const double * aos, bool sync = true );
     void get_spins( int s, double * aos );
     // batched transfers of every system (one copy each way, converted on the device)
     void set_all_spins( const double * aos_concat );
@@ -94,6 +96,8 @@ public:
         double energy;
     };
     std::vector<Status> status();
+    // the spins of system s (AoS, into aos) and its run status with a single synchronisation
+    Status fetch( int s, double * aos );
     void set_params( int s, const SystemInput & in );
     // time one step of the current method on the stream with CUDA events (ms)
     cudaStream_t stream() const
