@@ -45,8 +45,6 @@ struct PassArgs
     FastDiv div_g;
     int ka_major; // W1 layout: 0 [row][b][ka] (split passes B, C, B'), 1 [ka][row][b] (fused pass BC)
     FastDiv div_gq; // (g + 1) / 2: line pairs per block of pass A
-    int lg_a;       // largest register radix (log2) of the line transforms of passes A / A' (0: default)
-    int lg_bc;      // the same for the b/c pass
 };
 
 template<typename R>
@@ -121,7 +119,7 @@ __global__ void pass_a( PassArgs<R> p )
         }
     }
     __syncthreads();
-    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.radix[0], tw, false, p.lg_a );
+    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.radix[0], tw, false );
     if( !p.ka_major )
     {
         cplx<R> * W1 = p.W1 + f.spec_offset + ( (size_t)row * Bin + b0 ) * Mh;
@@ -347,9 +345,9 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
     }
     __syncthreads();
     const FastDiv none = { 1, 0, 0 };
-    cplx<R> * r = sfft_lg<R, false>( p.lg_bc, A, B, Mb, Nc * ncb, none, Mb, 1, f.radix[1], twb, false );
+    cplx<R> * r = sfft<R, false>( A, B, Mb, Nc * ncb, none, Mb, 1, f.radix[1], twb, false );
     cplx<R> * o = ( r == A ) ? B : A;
-    r           = sfft_lg<R, true>( p.lg_bc, r, o, Mc, plane, f.div_plane, 1, plane, f.radix[2], twc, false );
+    r           = sfft<R, true>( r, o, Mc, plane, f.div_plane, 1, plane, f.radix[2], twc, false );
     o           = ( r == A ) ? B : A;
     // tensor product H_b1 = sum_b2 D_b1b2 . S_b2 (FFT.hpp:42-49 mult3D rows: xx xy xz | xy yy yz | xz yz zz)
     const int npair    = nb * nb;
@@ -384,9 +382,9 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
             o[kc * plane + ( b1 * 3 + c3 ) * Mb + kb] = acc[c3];
     }
     __syncthreads();
-    r = sfft_lg<R, true>( p.lg_bc, o, ( o == A ) ? B : A, Mc, plane, f.div_plane, 1, plane, f.radix[2], twc, true );
+    r = sfft<R, true>( o, ( o == A ) ? B : A, Mc, plane, f.div_plane, 1, plane, f.radix[2], twc, true );
     o = ( r == A ) ? B : A;
-    r = sfft_lg<R, false>( p.lg_bc, r, o, Mb, Nc * ncb, none, Mb, 1, f.radix[1], twb, true );
+    r = sfft<R, false>( r, o, Mb, Nc * ncb, none, Mb, 1, f.radix[1], twb, true );
     for( int e = threadIdx.x; e < nin; e += blockDim.x )
     {
         const int row = (int)fdiv( (unsigned)e, f.div_Nb ), b = e - row * Nb;
@@ -451,7 +449,7 @@ __global__ void __launch_bounds__( 512 ) pass_bc_cl( PassArgs<R> p, int K )
     // every block's c-phase buffer is zero before any block writes into it
     cluster.sync();
     const FastDiv none = { 1, 0, 0 };
-    cplx<R> * r = sfft_lg<R, false>( p.lg_bc, Bb0, Bb1, Mb, nc * ncb, none, Mb, 1, f.radix[1], twb, false );
+    cplx<R> * r = sfft<R, false>( Bb0, Bb1, Mb, nc * ncb, none, Mb, 1, f.radix[1], twb, false );
     // transpose 1: rows (c0 + cl, cb), all kb -> owner of kb
     for( int e = threadIdx.x; e < nc * ncb * Mb; e += blockDim.x )
     {
@@ -463,7 +461,7 @@ __global__ void __launch_bounds__( 512 ) pass_bc_cl( PassArgs<R> p, int K )
     }
     cluster.sync();
     const FastDiv dcrow = f.div_crow;
-    r           = sfft_lg<R, true>( p.lg_bc, Bc0, Bc1, Mc, crow, dcrow, 1, crow, f.radix[2], twc, false );
+    r           = sfft<R, true>( Bc0, Bc1, Mc, crow, dcrow, 1, crow, f.radix[2], twc, false );
     cplx<R> * o = ( r == Bc0 ) ? Bc1 : Bc0;
     // tensor product at (kc, kb0 + kbl)
     const int npair    = nb * nb;
@@ -498,7 +496,7 @@ __global__ void __launch_bounds__( 512 ) pass_bc_cl( PassArgs<R> p, int K )
             o[kc * crow + ( b1 * 3 + c3 ) * kq + kbl] = acc[c3];
     }
     __syncthreads();
-    r = sfft_lg<R, true>( p.lg_bc, o, ( o == Bc0 ) ? Bc1 : Bc0, Mc, crow, dcrow, 1, crow, f.radix[2], twc, true );
+    r = sfft<R, true>( o, ( o == Bc0 ) ? Bc1 : Bc0, Mc, crow, dcrow, 1, crow, f.radix[2], twc, true );
     // transpose 2: rows c < Nc of the kb range -> owner of row c (its b-phase buffers are free)
     for( int e = threadIdx.x; e < Nc * ncb * kq; e += blockDim.x )
     {
@@ -509,7 +507,7 @@ __global__ void __launch_bounds__( 512 ) pass_bc_cl( PassArgs<R> p, int K )
         dst[( cl * ncb + cb ) * Mb + kb0 + kbl] = r[c * crow + cb * kq + kbl];
     }
     cluster.sync();
-    r = sfft_lg<R, false>( p.lg_bc, Bb0, Bb1, Mb, nc * ncb, none, Mb, 1, f.radix[1], twb, true );
+    r = sfft<R, false>( Bb0, Bb1, Mb, nc * ncb, none, Mb, 1, f.radix[1], twb, true );
     for( int e = threadIdx.x; e < ncb * nc * Nb; e += blockDim.x )
     {
         const int rest = (int)fdiv( (unsigned)e, f.div_Nb ), b = e - rest * Nb;
@@ -582,7 +580,7 @@ __global__ void pass_a_inv( PassArgs<R> p )
         a[q * ls + k] = { x.x - y.y, x.y + y.x };
     }
     __syncthreads();
-    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.radix[0], tw, true, p.lg_a );
+    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.radix[0], tw, true );
     const R invT = fft_invT<R>( f );
     const int cb = row / Nc, c = row - cb * Nc;
     const int ib = cb / 3, comp = cb - 3 * ib;
@@ -1093,7 +1091,6 @@ void DDIPlan::launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const
         a.blocks = d_blocks[0];
         a.g      = tile[0];
         a.div_g  = make_fastdiv( tile[0] );
-        a.lg_a   = lg_a;
         launch_pdl( pass_a<R>, dim3( n_blocks[0] ), dim3( threads[0] ), max_smem_a, stream, 1, a );
         break;
     case 1:
@@ -1111,7 +1108,6 @@ void DDIPlan::launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const
         break;
     case 5:
         a.blocks = d_blocks[3];
-        a.lg_bc  = lg_bc;
         if( cluster_k == 1 )
             launch_pdl( pass_bc<R>, dim3( n_blocks[3] ), dim3( threads_bc ), smem_bc_max, stream, 1, a );
         else
@@ -1123,7 +1119,6 @@ void DDIPlan::launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const
         a.g      = tile[0];
         a.div_g  = make_fastdiv( tile[0] );
         a.div_gq = make_fastdiv( ( tile[0] + 1 ) / 2 );
-        a.lg_a   = lg_a;
         launch_pdl( pass_a_inv<R>, dim3( n_blocks[0] ), dim3( threads[0] ), max_smem_a, stream, 1, a );
         break;
     }
@@ -1185,11 +1180,6 @@ void DDIPlan::tune_t( const SysDesc * d_sd, const R * sx, const R * sy, const R 
         }
         return best_ms;
     };
-    // overrides of the register radices (log2; 0: radix 16 in FP32, 8 in FP64)
-    if( const char * e = std::getenv( "SPIRIT_GB300_LG_A" ) )
-        lg_a = std::atoi( e );
-    if( const char * e = std::getenv( "SPIRIT_GB300_LG_BC" ) )
-        lg_bc = std::atoi( e );
     // warm-up of the whole chain (first launches pay module loading)
     if( fused )
         timed( { 0, 5, 4 } );

@@ -60,14 +60,6 @@ public:
     bool fused         = false; // passes B, C, B' as one kernel per (system, ka) plane
     int threads_bc     = 1024;
     int cluster_k      = 1; // blocks per (system, ka) plane of the fused pass (cluster size)
-    // largest register radix (log2) of the line transforms of passes A / A' and of the b/c pass:
-    // radix 8.  The lines are short (128 points on the 128x128x16 workload) and few per block, so
-    // threads per line matter as much as fewer shared-memory round trips.  Interleaved runs in
-    // one session (ms/step, two runs each): radix 8 / 8 0.1035, 0.1037; 8 / 4 0.1051, 0.1061;
-    // 4 / 4 0.119, 0.106; 16 / 16 (the register default) 0.134, 0.111.  Fixed rather than
-    // tuned, so the transforms never depend on timings; SPIRIT_GB300_LG_A / _LG_BC override.
-    int lg_a           = 3;
-    int lg_bc          = 3;
     int n_fd_slots     = 1;
     size_t smem_bc_max = 0;
     size_t max_smem_a = 0, max_smem_b = 0, max_smem_c = 0;

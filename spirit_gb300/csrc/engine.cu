@@ -320,7 +320,6 @@ struct RowArgs
     const cplx<R> * tw; // twiddle tables
     cplx<R> * W1;       // ka-major spectra [ka][cb][c][b]
     const int4 * map;   // (system, c, first b, rows)
-    int lg;             // register radix of the line transforms (that of passes A / A')
 };
 
 constexpr int ROW_SPT = 4; // spins per thread the row kernel holds (rows * row length <= 1024)
@@ -384,7 +383,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage_rows( StageArgs<R> A, RowArgs
         ba[q * ls + k] = { x.x - y.y, x.y + y.x };
     }
     __syncthreads();
-    const cplx<R> * hr = block_fft( ba, bb, Ma, ls, nq, f.radix[0], tw, true, F.lg );
+    const cplx<R> * hr = block_fft( ba, bb, Ma, ls, nq, f.radix[0], tw, true );
     const R invT       = fft_invT<R>( f );
     // ---- main: the stage on the block's spins
     const int i0        = rowlen * ( b0 + Nb * cc ); // first local spin of the block
@@ -457,7 +456,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage_rows( StageArgs<R> A, RowArgs
             ba[q * ls + t].y = 0;
     }
     __syncthreads();
-    const cplx<R> * r = block_fft( ba, bb, Ma, ls, nq, f.radix[0], tw, false, F.lg );
+    const cplx<R> * r = block_fft( ba, bb, Ma, ls, nq, f.radix[0], tw, false );
     for( int e2 = threadIdx.x; e2 < ncb * nr * Mh; e2 += blockDim.x )
     {
         const int lr = e2 % nr, rest = e2 / nr;
@@ -1112,7 +1111,6 @@ void Engine::launch_stage_rows( StageArgs<R> a, cudaStream_t st )
     F.tw  = (const cplx<R> *)ddi_.d_tw;
     F.W1  = (cplx<R> *)ddi_.d_W1;
     F.map = d_rowmap_;
-    F.lg  = ddi_.lg_a;
     launch_pdl( llg_stage_rows<R, SOLVER, STAGE>, dim3( n_rowblocks_ ), dim3( 256 ), rows_smem_, st, 1, a, F );
 }
 

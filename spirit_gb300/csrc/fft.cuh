@@ -213,11 +213,14 @@ __device__ __forceinline__ cplx<R> * stockham_reg( cplx<R> * a, cplx<R> * b, int
     }
 }
 
-// radix 16 stages in FP32, radix 8 in FP64 (register budget)
+// largest register radix: 8.  Radix 16 needs fewer shared-memory round trips but a quarter of the
+// threads per line; the lines here are short and few per block, and radix 8 measured faster on
+// the 128x128x16 dipolar workload (interleaved runs, ms/step: radix 8 everywhere 0.1035, 0.1037;
+// radix 16 0.134, 0.111; radix 4 0.119, 0.106).
 template<typename R>
 struct MaxRadix
 {
-    static constexpr int LG = sizeof( R ) == 4 ? 4 : 3;
+    static constexpr int LG = 3;
 };
 
 
@@ -385,18 +388,14 @@ __device__ __forceinline__ cplx<R> * block_fft_reg( cplx<R> * a, cplx<R> * b, in
     }
 }
 
-// maxlg: largest register radix 2^maxlg of the power-of-two lengths 16..512 (0: the default,
-// radix 16 in FP32 and 8 in FP64; 2: radix 4, four times the threads per line)
 template<typename R>
 __device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int ls, int nl, const int * rad,
-                               const cplx<R> * tw, bool inverse, int maxlg = 0 )
+                               const cplx<R> * tw, bool inverse )
 {
     if( L == 1 )
         return a;
     bool done   = false;
-    cplx<R> * r = maxlg == 2   ? block_fft_reg<R, 2>( a, b, L, ls, nl, tw, inverse, done )
-                  : maxlg == 3 ? block_fft_reg<R, 3>( a, b, L, ls, nl, tw, inverse, done )
-                               : block_fft_reg<R, MaxRadix<R>::LG>( a, b, L, ls, nl, tw, inverse, done );
+    cplx<R> * r = block_fft_reg<R, MaxRadix<R>::LG>( a, b, L, ls, nl, tw, inverse, done );
     if( done )
         return r;
     if( ( L & ( L - 1 ) ) == 0 )
@@ -698,18 +697,6 @@ __device__ cplx<R> * sfft( cplx<R> * a, cplx<R> * b, int L, int nl, const FastDi
     default:
         return sfft_generic<R>( a, b, L, nl, ls, es, rad, tw, inverse );
     }
-}
-
-// sfft with the largest register radix 2^lg chosen at run time (0: the default)
-template<typename R, bool LINE_FAST>
-__device__ cplx<R> * sfft_lg( int lg, cplx<R> * a, cplx<R> * b, int L, int nl, const FastDiv & dnl, int ls, int es,
-                             const int * rad, const cplx<R> * tw, bool inverse )
-{
-    if( lg == 2 )
-        return sfft<R, LINE_FAST, 2>( a, b, L, nl, dnl, ls, es, rad, tw, inverse );
-    if( lg == 3 )
-        return sfft<R, LINE_FAST, 3>( a, b, L, nl, dnl, ls, es, rad, tw, inverse );
-    return sfft<R, LINE_FAST>( a, b, L, nl, dnl, ls, es, rad, tw, inverse );
 }
 
 // copy a twiddle table into shared memory (all threads)
