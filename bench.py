@@ -632,6 +632,14 @@ def run_gb300(args):
                      [int(tun[k]) for k in range(ntun)]))
     rows = bool(tuned.get("row_fused_stages", 0))
     value = NOS * args.steps * world / (ms / 1000.0)
+    if args.profile_step:
+        # one more step inside a profiler range: `ncu --profile-from-start off` captures exactly
+        # the kernels of one Heun step with the tuned shapes
+        stream.synchronize()
+        torch.cuda.profiler.start()
+        launch(p, 1, -1, -1)
+        stream.synchronize()
+        torch.cuda.profiler.stop()
     # --- per-kernel durations (CUDA events between launches, L2 flushed before every step)
     kms = (ctypes.c_double * 16)()
     kcount = (ctypes.c_int * 16)()
@@ -718,6 +726,8 @@ def main():
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false", help="skip the adjoint measurement")
     ap.add_argument("--no-mc", dest="mc", action="store_false", help="skip the Monte Carlo measurement")
     ap.add_argument("--no-htst", dest="htst", action="store_false", help="skip the HTST measurement")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="run one extra step inside a CUDA profiler range (for ncu --profile-from-start off)")
     ap.add_argument("--no-batched-ddi", dest="batched_ddi", action="store_false",
                     help="skip the dipolar variant of the 256-system batched measurement")
     ap.add_argument("--only-batched-ddi", action="store_true",
