@@ -1254,9 +1254,13 @@ void Engine::tune_stages_t()
     cudaEvent_t e0, e1;
     CUDA_CHECK( cudaEventCreate( &e0 ) );
     CUDA_CHECK( cudaEventCreate( &e1 ) );
-    float best = 1e30f;
+    // 1 and 2 spins per thread only: 4 per thread (a quarter of the blocks) times well here, where
+    // the stage launches run back to back and overlap, but measured 17 % slower inside the step
+    // (128x128x16 Heun, interleaved: 1 -> 0.1033 / 0.1044, 2 -> 0.1030 / 0.1029, 4 -> 0.1207 /
+    // 0.1213 ms/step); 2 is kept unless 1 is more than 5 % faster here.
+    float best = 1e30f, t_two = 1e30f;
     int bi     = 0;
-    for( int k = 0; k < 3; ++k )
+    for( int k = 0; k < 2; ++k )
     {
         spt_idx_ = k;
         launch_stages_t<R>( a, false );
@@ -1272,12 +1276,16 @@ void Engine::tune_stages_t()
             CUDA_CHECK( cudaEventElapsedTime( &t, e0, e1 ) );
             ms = std::min( ms, t );
         }
+        if( k == 1 )
+            t_two = ms;
         if( ms < best )
         {
             best = ms;
             bi   = k;
         }
     }
+    if( t_two <= 1.05f * best )
+        bi = 1;
     spt_idx_ = bi;
     if( const char * e = std::getenv( "SPIRIT_GB300_SPT" ) ) // override (measurements): 1, 2 or 4
     {
