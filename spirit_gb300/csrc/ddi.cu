@@ -1193,8 +1193,11 @@ void DDIPlan::tune_t( const SysDesc * d_sd, const R * sx, const R * sy, const R 
         for( int nl : { 2, 4, 6, 8, 12, 16, 24, 32, 48, 64 } )
         {
             // even counts only: lines are then always paired (even b, odd b) whatever the tile,
-            // so the results do not depend on the tuner's choice
-            if( ( nl > maxN1 && nl > 2 ) || smem_a( elem, maxM0, nl ) > 96 * 1024 )
+            // so the results do not depend on the tuner's choice.  At least 8 lines when the
+            // systems allow: with the ka-major spectrum a block reads / writes runs of its lines
+            // per frequency, and runs of 2-6 complex values (16-48 B) timed well back to back but
+            // left pass A' 60 % stalled on those loads inside the step
+            if( ( nl > maxN1 && nl > 2 ) || smem_a( elem, maxM0, nl ) > 96 * 1024 || ( nl < 8 && maxN1 >= 8 && fused ) )
                 continue;
             set_tiles( nl, best[1], best[2] );
             for( int th : thread_opts )
