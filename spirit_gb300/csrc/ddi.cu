@@ -1213,6 +1213,17 @@ void DDIPlan::tune_t( const SysDesc * d_sd, const R * sx, const R * sy, const R 
             }
         }
         threads[0] = bthr[0];
+        // override "lines,threads" (measurements, profiles)
+        if( const char * e = std::getenv( "SPIRIT_GB300_A" ) )
+        {
+            int nl = 0, th = 0;
+            if( std::sscanf( e, "%d,%d", &nl, &th ) == 2 && nl >= 2 && nl % 2 == 0 && nl <= 64
+                && ( th == 64 || th == 128 || th == 256 ) && smem_a( elem, maxM0, nl ) <= 96 * 1024 )
+            {
+                best[0]    = nl;
+                threads[0] = th;
+            }
+        }
     }
     if( fused )
     {
