@@ -322,13 +322,16 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
     const int plane = ncb * Mb;
     const int vol   = Mc * plane;
     const int ka    = blk.y;
+    // planes of the block: several consecutive ka when the system has one c row (Mc == 1: every
+    // plane is ncb lines along b, and the planes lie one after another in W1 and in shared memory)
+    const int G     = blk.w > 0 ? blk.w : 1;
     cplx<R> * twb   = reinterpret_cast<cplx<R> *>( smem_raw );
     cplx<R> * twc   = twb + Mb;
     cplx<R> * A     = twc + Mc;
-    cplx<R> * B     = A + vol;
+    cplx<R> * B     = A + G * vol;
     load_tw( twb, p.tw + f.tw_offset[1], Mb );
     load_tw( twc, p.tw + f.tw_offset[2], Mc );
-    for( int e = threadIdx.x; e < 2 * vol; e += blockDim.x )
+    for( int e = threadIdx.x; e < 2 * G * vol; e += blockDim.x )
         A[e] = { 0, 0 };
     __syncthreads();
     pdl_wait();
@@ -337,26 +340,28 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
         return;
     const int nin    = ncb * Nc * Nb;
     cplx<R> * W1     = p.W1 + f.spec_offset + (size_t)ka * nin;
-    for( int e = threadIdx.x; e < nin; e += blockDim.x )
+    for( int e = threadIdx.x; e < G * nin; e += blockDim.x )
     {
-        const int row = (int)fdiv( (unsigned)e, f.div_Nb ), b = e - row * Nb;
+        const int g = e / nin, el = e - g * nin;
+        const int row = (int)fdiv( (unsigned)el, f.div_Nb ), b = el - row * Nb;
         const int cb  = (int)fdiv( (unsigned)row, f.div_Nc ), c = row - cb * Nc;
-        A[c * plane + cb * Mb + b] = W1[e];
+        A[g * vol + c * plane + cb * Mb + b] = W1[e];
     }
     __syncthreads();
     const FastDiv none = { 1, 0, 0 };
-    cplx<R> * r = sfft<R, false>( A, B, Mb, Nc * ncb, none, Mb, 1, f.radix[1], twb, false );
+    cplx<R> * r = sfft<R, false>( A, B, Mb, G * Nc * ncb, none, Mb, 1, f.radix[1], twb, false );
     cplx<R> * o = ( r == A ) ? B : A;
     r           = sfft<R, true>( r, o, Mc, plane, f.div_plane, 1, plane, f.radix[2], twc, false );
     o           = ( r == A ) ? B : A;
     // tensor product H_b1 = sum_b2 D_b1b2 . S_b2 (FFT.hpp:42-49 mult3D rows: xx xy xz | xy yy yz | xz yz zz)
     const int npair    = nb * nb;
-    const cplx<R> * Dh = p.Dhat + f.dhat_offset + (size_t)ka * npair * 6 * Mc * Mb;
-    for( int e = threadIdx.x; e < nb * Mc * Mb; e += blockDim.x )
+    for( int e = threadIdx.x; e < G * nb * Mc * Mb; e += blockDim.x )
     {
-        const int rest = (int)fdiv( (unsigned)e, f.div_Mb ), kb = e - rest * Mb;
+        const int g = e / ( nb * Mc * Mb ), eg = e - g * ( nb * Mc * Mb );
+        const cplx<R> * Dh = p.Dhat + f.dhat_offset + (size_t)( ka + g ) * npair * 6 * Mc * Mb;
+        const int rest = (int)fdiv( (unsigned)eg, f.div_Mb ), kb = eg - rest * Mb;
         const int kc   = (int)fdiv( (unsigned)rest, f.div_nb ), b1 = rest - kc * nb;
-        const cplx<R> * S = r + kc * plane + kb;
+        const cplx<R> * S = r + g * vol + kc * plane + kb;
         cplx<R> acc[3]    = { { 0, 0 }, { 0, 0 }, { 0, 0 } };
         for( int b2 = 0; b2 < nb; ++b2 )
         {
@@ -379,17 +384,18 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
         }
 #pragma unroll
         for( int c3 = 0; c3 < 3; ++c3 )
-            o[kc * plane + ( b1 * 3 + c3 ) * Mb + kb] = acc[c3];
+            o[g * vol + kc * plane + ( b1 * 3 + c3 ) * Mb + kb] = acc[c3];
     }
     __syncthreads();
     r = sfft<R, true>( o, ( o == A ) ? B : A, Mc, plane, f.div_plane, 1, plane, f.radix[2], twc, true );
     o = ( r == A ) ? B : A;
-    r = sfft<R, false>( r, o, Mb, Nc * ncb, none, Mb, 1, f.radix[1], twb, true );
-    for( int e = threadIdx.x; e < nin; e += blockDim.x )
+    r = sfft<R, false>( r, o, Mb, G * Nc * ncb, none, Mb, 1, f.radix[1], twb, true );
+    for( int e = threadIdx.x; e < G * nin; e += blockDim.x )
     {
-        const int row = (int)fdiv( (unsigned)e, f.div_Nb ), b = e - row * Nb;
+        const int g = e / nin, el = e - g * nin;
+        const int row = (int)fdiv( (unsigned)el, f.div_Nb ), b = el - row * Nb;
         const int cb  = (int)fdiv( (unsigned)row, f.div_Nc ), c = row - cb * Nc;
-        W1[e]         = r[c * plane + cb * Mb + b];
+        W1[e]         = r[g * vol + c * plane + cb * Mb + b];
     }
 }
 
@@ -619,9 +625,9 @@ __global__ void dhat_relayout( const cplx<R> * W2, cplx<RS> * Dhat, int Mh, int 
 }
 
 // ================================================================== host side
-static size_t smem_bc( size_t elem, const FFTDesc & f )
+static size_t smem_bc( size_t elem, const FFTDesc & f, int G = 1 )
 {
-    return elem * ( f.M[1] + f.M[2] + 2 * (size_t)f.M[2] * 3 * f.nb * f.M[1] );
+    return elem * ( f.M[1] + f.M[2] + 2 * (size_t)G * f.M[2] * 3 * f.nb * f.M[1] );
 }
 
 // fused pass split over a cluster of K blocks (pass_bc_cl)
@@ -836,10 +842,12 @@ void DDIPlan::set_tiles( int nl_a, int g_b, int g_c )
     {
         for( size_t k = 0; k < fd_host.size(); ++k )
         {
-            for( int ka = 0; ka < fd_host[k].Mh; ++ka )
+            // several ka planes per block for one-row systems (single-block kernel only)
+            const int G = ( cluster_k == 1 && fd_host[k].M[2] == 1 ) ? planes_bc : 1;
+            for( int ka = 0; ka < fd_host[k].Mh; ka += G )
                 for( int r = 0; r < cluster_k; ++r )
-                    tbc.push_back( make_int4( sys_index[k], ka, r, 0 ) );
-            smem_bc_max = std::max( smem_bc_max, cluster_k == 1 ? smem_bc( elem, fd_host[k] )
+                    tbc.push_back( make_int4( sys_index[k], ka, r, std::min( G, fd_host[k].Mh - ka ) ) );
+            smem_bc_max = std::max( smem_bc_max, cluster_k == 1 ? smem_bc( elem, fd_host[k], G )
                                                                 : smem_bcl( elem, fd_host[k], cluster_k ) );
             fd_host[k].div_crow = make_fastdiv( 3 * fd_host[k].nb * fd_host[k].M[1] / cluster_k );
         }
@@ -1271,6 +1279,33 @@ void DDIPlan::tune_t( const SysDesc * d_sd, const R * sx, const R * sy, const R 
         }
         threads_bc = bthr_bc;
         cluster_k  = bk;
+        // planes per block on one-row (2D) systems: their planes are only 3 nb lines of Mb points,
+        // so one plane per block leaves most threads idle
+        bool one_row = false;
+        for( auto & f : fd_host )
+            one_row = one_row || f.M[2] == 1;
+        if( cluster_k == 1 && one_row )
+        {
+            float bg = 1e30f;
+            int bgv  = 1;
+            for( int G : { 1, 2, 4, 8, 16 } )
+            {
+                bool ok = true;
+                for( auto & f : fd_host )
+                    ok = ok && smem_bc( elem, f, f.M[2] == 1 ? G : 1 ) <= smem_optin();
+                if( !ok )
+                    continue;
+                planes_bc = G;
+                set_tiles( best[0], best[1], best[2] );
+                float t = timed( { 0, 5, 4 } );
+                if( t < bg )
+                {
+                    bg  = t;
+                    bgv = G;
+                }
+            }
+            planes_bc = bgv;
+        }
         // override "K,threads" (measurements)
         if( const char * e = std::getenv( "SPIRIT_GB300_BC" ) )
         {
