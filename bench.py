@@ -459,13 +459,23 @@ def run_adjoint(n_steps=2000, checkpoint=100):
     t0 = time.perf_counter()
     loss_a, g0, gp, _ = adjoint.llg_adjoint(p, tgt, n_steps, checkpoint, prm)
     adj_s = time.perf_counter() - t0 - setup_s
+    # the whole trajectory recorded in HBM (16 stage arrays per step): no recomputation
+    t0 = time.perf_counter()
+    loss_r, g0_r, gp_r, _ = adjoint.llg_adjoint(p, tgt, n_steps, n_steps, prm)
+    rec_s = time.perf_counter() - t0 - setup_s
     state.delete(p)
+    rec_bytes = n_steps * 16 * 3 * nos * 4
     return {
         "workload": "adjoint of RK4 LLG: 128x128 open SC 2D, DDI FFT padded 256x256, J=1, D=0.3, K=0.1 meV, "
                     "B=0.8 T, alpha=0.3, dt=1e-3 ps, %d steps, checkpoint %d; FP32 forward and adjoint, FP64 loss"
                     % (n_steps, checkpoint),
         "n_spins": nos, "steps": n_steps, "forward_s": fwd_s, "adjoint_s": adj_s,
         "adjoint_over_forward": adj_s / fwd_s,
+        "full_record": {"checkpoint": n_steps, "adjoint_s": rec_s, "adjoint_over_forward": rec_s / fwd_s,
+                        "recorded_bytes": rec_bytes,
+                        "max_abs_diff_grad_s0": float(np.max(np.abs(np.asarray(g0_r) - np.asarray(g0)))),
+                        "max_abs_diff_grad_params": float(np.max(np.abs(np.asarray(gp_r) - np.asarray(gp)))),
+                        "loss": loss_r},
         "forward_value": nos * n_steps / fwd_s, "unit": "spin-updates/s", "setup_s": setup_s,
         "loss": loss_a, "loss_forward_only": loss_f,
         "grad_params": {k: float(v) for k, v in zip(adjoint.PARAMS, gp)},

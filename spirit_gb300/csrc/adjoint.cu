@@ -364,7 +364,10 @@ struct AdjPlan
     void * ckpt  = nullptr; // [n_ckpt][3][total]
     double * pgrad = nullptr;
 
-    AdjArgs<R> step_args( const SysDesc * sd, const AdjUnits<R> & u, int slot_base_step, bool recorded ) const
+    // flip: the unrecorded state slots c0 / s_out and the adjoint slots lam_next / lam_s trade
+    // places (ping-pong between steps instead of copying)
+    AdjArgs<R> step_args( const SysDesc * sd, const AdjUnits<R> & u, int slot_base_step, bool recorded,
+                          int flip_state = 0, int flip_lam = 0 ) const
     {
         AdjArgs<R> A{};
         A.sd       = sd;
@@ -389,12 +392,13 @@ struct AdjPlan
         {
             for( int m = 0; m < 4; ++m )
                 A.c[m] = soa_at<R>( work, total, m );
+            A.c[0]   = soa_at<R>( work, total, flip_state ? 5 : 0 );
             A.acc    = soa_at<R>( work, total, 4 );
-            A.s_out  = soa_at<R>( work, total, 5 );
+            A.s_out  = soa_at<R>( work, total, flip_state ? 0 : 5 );
             A.record = 0;
         }
-        A.lam_next = soa_at<R>( work, total, 6 );
-        A.lam_s    = soa_at<R>( work, total, 7 );
+        A.lam_next = soa_at<R>( work, total, flip_lam ? 7 : 6 );
+        A.lam_s    = soa_at<R>( work, total, flip_lam ? 6 : 7 );
         for( int m = 0; m < 4; ++m )
             A.lam_k[m] = soa_at<R>( work, total, 8 + m );
         A.lam_Fo[0] = soa_at<R>( work, total, 12 );
@@ -504,13 +508,15 @@ static double run_t( Engine & E, const AdjointInput & in, AdjointOutput & out )
         for( int i = 0; i < nos; ++i )
             for( int e = 0; e < 3; ++e )
                 soa[e * total + d.spin_offset + i] = (R)in.s0[3 * (size_t)i + e];
-        AdjArgs<R> W = P.step_args( d_sd, u, 0, false );
+        int fs       = 0; // which of the two unrecorded state slots holds the current state
+        AdjArgs<R> W = P.step_args( d_sd, u, 0, false, fs );
         CUDA_CHECK( cudaMemcpyAsync( W.c[0].x, soa.data(), 3 * total * sizeof( R ), cudaMemcpyHostToDevice, st ) );
         // forward with checkpoints; with gradients, the last segment is recorded right away (the
         // backward pass then recomputes every segment but that one)
         const int last0 = in.n_steps > 0 ? ( ( in.n_steps - 1 ) / K ) * K : 0;
         for( int n = 0; n < in.n_steps; ++n )
         {
+            W = P.step_args( d_sd, u, 0, false, fs );
             if( n % K == 0 )
                 copy3( soa_at<R>( P.ckpt, total, n / K ), W.c[0], total, st );
             if( in.gradients && n >= last0 )
@@ -524,9 +530,10 @@ static double run_t( Engine & E, const AdjointInput & in, AdjointOutput & out )
             else
             {
                 forward_step<R>( E, W, nblk, st );
-                copy3( W.c[0], W.s_out, total, st );
+                fs ^= 1; // the new state is in the other slot
             }
         }
+        W = P.step_args( d_sd, u, 0, false, fs );
         std::vector<R> fin( 3 * total );
         CUDA_CHECK( cudaMemcpyAsync( fin.data(), W.c[0].x, 3 * total * sizeof( R ), cudaMemcpyDeviceToHost, st ) );
         CUDA_CHECK( cudaStreamSynchronize( st ) );
@@ -546,7 +553,9 @@ static double run_t( Engine & E, const AdjointInput & in, AdjointOutput & out )
         if( in.gradients )
         {
             CUDA_CHECK( cudaMemsetAsync( P.pgrad, 0, (size_t)5 * nblk * sizeof( double ), st ) );
-            CUDA_CHECK( cudaMemcpyAsync( W.lam_s.x, lam.data(), 3 * total * sizeof( R ), cudaMemcpyHostToDevice, st ) );
+            int fl = 1; // lam_s of flip 0 holds dLoss/ds_T: the first backward step reads it as lam_next
+            CUDA_CHECK( cudaMemcpyAsync( P.step_args( d_sd, u, 0, false, 0, 0 ).lam_s.x, lam.data(),
+                                         3 * total * sizeof( R ), cudaMemcpyHostToDevice, st ) );
             for( int seg = ( in.n_steps - 1 ) / K; seg >= 0; --seg )
             {
                 const int n0 = seg * K, n1 = std::min( in.n_steps, n0 + K );
@@ -565,14 +574,15 @@ static double run_t( Engine & E, const AdjointInput & in, AdjointOutput & out )
                 // adjoint steps of the segment in reverse: lam_s holds dLoss/ds_{n+1} on entry
                 for( int n = n1 - 1; n >= n0; --n )
                 {
-                    AdjArgs<R> A = P.step_args( d_sd, u, n - n0, true );
-                    copy3( A.lam_next, A.lam_s, total, st );
+                    AdjArgs<R> A = P.step_args( d_sd, u, n - n0, true, 0, fl );
                     backward_step<R>( E, A, nblk, st );
+                    fl ^= 1; // lam_s of this step is lam_next of the previous one
                 }
             }
             std::vector<R> g0( 3 * total );
             std::vector<double> pg( (size_t)5 * nblk );
-            CUDA_CHECK( cudaMemcpyAsync( g0.data(), W.lam_s.x, 3 * total * sizeof( R ), cudaMemcpyDeviceToHost, st ) );
+            const SoA3<R> g_last = P.step_args( d_sd, u, 0, false, 0, fl ^ 1 ).lam_s;
+            CUDA_CHECK( cudaMemcpyAsync( g0.data(), g_last.x, 3 * total * sizeof( R ), cudaMemcpyDeviceToHost, st ) );
             CUDA_CHECK( cudaMemcpyAsync( pg.data(), P.pgrad, pg.size() * sizeof( double ), cudaMemcpyDeviceToHost, st ) );
             CUDA_CHECK( cudaStreamSynchronize( st ) );
             if( out.grad_s0 )
