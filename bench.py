@@ -450,6 +450,7 @@ def run_adjoint(n_steps=2000, checkpoint=100):
     tgt = random_spins(nos, 56)
     prm = np.array([1.0, 0.3, 0.1, 0.8, 0.3])
     adjoint.llg_loss(p, tgt, 2, prm)  # warm-up (module loading)
+    adjoint.llg_adjoint(p, tgt, 2, 1, prm)  # builds the second dipolar lane of the pipelined backward pass
     t0 = time.perf_counter()
     adjoint.llg_loss(p, tgt, 0, prm)
     setup_s = time.perf_counter() - t0

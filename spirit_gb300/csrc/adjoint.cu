@@ -416,14 +416,20 @@ static void copy3( SoA3<R> dst, SoA3<R> src, size_t n, cudaStream_t st )
     CUDA_CHECK( cudaMemcpyAsync( dst.z, src.z, n * sizeof( R ), cudaMemcpyDeviceToDevice, st ) );
 }
 
-// one forward RK4 step of A (c[0] -> s_out, or into the recorded slots)
+// one forward RK4 step of A (c[0] -> s_out, or into the recorded slots); with a lane, on the
+// lane's dipolar plan and field arrays (st is then the lane's stream)
 template<typename R>
-static void forward_step( Engine & E, AdjArgs<R> A, int nblk, cudaStream_t st )
+static void forward_step( Engine & E, AdjArgs<R> A, int nblk, cudaStream_t st, Engine::DdiLane * lane = nullptr )
 {
     void * hf[3] = { E.field_ptr( 0 ), E.field_ptr( 1 ), E.field_ptr( 2 ) };
-    A.h          = E.has_ddi() ? SoA3<R>{ (R *)hf[0], (R *)hf[1], (R *)hf[2] } : SoA3<R>{ nullptr, nullptr, nullptr };
-    auto field   = [&]( const SoA3<R> & cfg ) {
-        if( E.has_ddi() )
+    if( lane )
+        for( int c = 0; c < 3; ++c )
+            hf[c] = lane->field[c];
+    A.h        = E.has_ddi() ? SoA3<R>{ (R *)hf[0], (R *)hf[1], (R *)hf[2] } : SoA3<R>{ nullptr, nullptr, nullptr };
+    auto field = [&]( const SoA3<R> & cfg ) {
+        if( lane )
+            lane->plan.run( E.d_desc(), nullptr, cfg.x, cfg.y, cfg.z, hf[0], hf[1], hf[2], st );
+        else if( E.has_ddi() )
         {
             void * cp[3] = { cfg.x, cfg.y, cfg.z };
             E.run_ddi( cp, nullptr );
@@ -494,7 +500,22 @@ static double run_t( Engine & E, const AdjointInput & in, AdjointOutput & out )
     AdjPlan<R> P;
     P.total    = total;
     P.n_blocks = nblk;
-    P.pool     = in.gradients ? dalloc_bytes( (size_t)K * AdjPlan<R>::SLOTS * 3 * total * sizeof( R ) ) : nullptr;
+    // Backward pass as a two-stream pipeline when there are several segments: the recomputation
+    // of segment s - 1 (from its checkpoint, on a second stream with its own dipolar lane) runs
+    // beside the adjoint steps of segment s; the recorded pool then has two halves of K steps.
+    const int n_seg     = in.n_steps > 0 ? ( in.n_steps - 1 ) / K + 1 : 0;
+    const char * penv   = std::getenv( "SPIRIT_GB300_ADJ_PIPE" );
+    const bool pipe     = in.gradients && n_seg >= 2 && !( penv && penv[0] == '0' );
+    Engine::DdiLane * lane = pipe ? E.ddi_lane() : nullptr;
+    cudaStream_t st2       = pipe ? ( lane ? lane->stream : nullptr ) : nullptr;
+    cudaStream_t own_st2   = nullptr;
+    if( pipe && !st2 )
+    {
+        CUDA_CHECK( cudaStreamCreateWithFlags( &own_st2, cudaStreamNonBlocking ) );
+        st2 = own_st2;
+    }
+    P.pool     = in.gradients ? dalloc_bytes( (size_t)( pipe ? 2 : 1 ) * K * AdjPlan<R>::SLOTS * 3 * total * sizeof( R ) )
+                              : nullptr;
     P.work     = dalloc_bytes( (size_t)15 * 3 * total * sizeof( R ) );
     P.ckpt     = dalloc_bytes( (size_t)n_ckpt * 3 * total * sizeof( R ) );
     P.pgrad    = dalloc<double>( (size_t)5 * nblk );
@@ -556,28 +577,76 @@ static double run_t( Engine & E, const AdjointInput & in, AdjointOutput & out )
             int fl = 1; // lam_s of flip 0 holds dLoss/ds_T: the first backward step reads it as lam_next
             CUDA_CHECK( cudaMemcpyAsync( P.step_args( d_sd, u, 0, false, 0, 0 ).lam_s.x, lam.data(),
                                          3 * total * sizeof( R ), cudaMemcpyHostToDevice, st ) );
-            for( int seg = ( in.n_steps - 1 ) / K; seg >= 0; --seg )
-            {
-                const int n0 = seg * K, n1 = std::min( in.n_steps, n0 + K );
-                // recompute the segment, recording every stage of its steps (the last one is recorded)
-                if( n0 != last0 )
-                    copy3( P.step_args( d_sd, u, 0, true ).c[0], soa_at<R>( P.ckpt, total, seg ), total, st );
-                for( int n = n0; n < n1 && n0 != last0; ++n )
+            const int L = n_seg - 1; // the last segment, recorded by the forward pass into half 0
+            auto half   = [&]( int seg ) { return pipe ? ( L - seg ) & 1 : 0; };
+            // recompute segment seg from its checkpoint, recording every stage of its steps
+            auto recompute = [&]( int seg, cudaStream_t s, Engine::DdiLane * ln ) {
+                const int n0 = seg * K, n1 = std::min( in.n_steps, n0 + K ), hb = half( seg ) * K;
+                copy3( P.step_args( d_sd, u, hb, true ).c[0], soa_at<R>( P.ckpt, total, seg ), total, s );
+                for( int n = n0; n < n1; ++n )
                 {
-                    AdjArgs<R> A = P.step_args( d_sd, u, n - n0, true );
+                    AdjArgs<R> A = P.step_args( d_sd, u, hb + n - n0, true );
                     if( n + 1 < n1 )
-                        A.s_out = P.step_args( d_sd, u, n + 1 - n0, true ).c[0];
+                        A.s_out = P.step_args( d_sd, u, hb + n + 1 - n0, true ).c[0];
                     else
-                        A.s_out = W.s_out; // not needed further
-                    forward_step<R>( E, A, nblk, st );
+                        A.s_out = P.step_args( d_sd, u, 0, false, fs ).s_out; // not needed further
+                    forward_step<R>( E, A, nblk, s, ln );
                 }
-                // adjoint steps of the segment in reverse: lam_s holds dLoss/ds_{n+1} on entry
-                for( int n = n1 - 1; n >= n0; --n )
+            };
+            cudaEvent_t ev_rec = nullptr, ev_bwd = nullptr;
+            if( pipe )
+            {
+                CUDA_CHECK( cudaEventCreateWithFlags( &ev_rec, cudaEventDisableTiming ) );
+                CUDA_CHECK( cudaEventCreateWithFlags( &ev_bwd, cudaEventDisableTiming ) );
+                // the checkpoints are written on the main stream
+                CUDA_CHECK( cudaEventRecord( ev_bwd, st ) );
+            }
+            try
+            {
+                for( int seg = L; seg >= 0; --seg )
                 {
-                    AdjArgs<R> A = P.step_args( d_sd, u, n - n0, true, 0, fl );
-                    backward_step<R>( E, A, nblk, st );
-                    fl ^= 1; // lam_s of this step is lam_next of the previous one
+                    const int n0 = seg * K, n1 = std::min( in.n_steps, n0 + K ), hb = half( seg ) * K;
+                    if( pipe )
+                    {
+                        // segment seg was recomputed on the second stream (the last one: recorded)
+                        if( seg != L )
+                            CUDA_CHECK( cudaStreamWaitEvent( st, ev_rec, 0 ) );
+                        // segment seg - 1 into the other half, once the adjoint of seg + 1 is done with it
+                        if( seg >= 1 )
+                        {
+                            CUDA_CHECK( cudaStreamWaitEvent( st2, ev_bwd, 0 ) );
+                            recompute( seg - 1, st2, lane );
+                            CUDA_CHECK( cudaGetLastError() );
+                            CUDA_CHECK( cudaEventRecord( ev_rec, st2 ) );
+                        }
+                    }
+                    else if( n0 != last0 )
+                        recompute( seg, st, nullptr );
+                    // adjoint steps of the segment in reverse: lam_next holds dLoss/ds_{n+1} on entry
+                    for( int n = n1 - 1; n >= n0; --n )
+                    {
+                        AdjArgs<R> A = P.step_args( d_sd, u, hb + n - n0, true, 0, fl );
+                        backward_step<R>( E, A, nblk, st );
+                        fl ^= 1; // lam_s of this step is lam_next of the previous one
+                    }
+                    if( pipe )
+                        CUDA_CHECK( cudaEventRecord( ev_bwd, st ) );
                 }
+            }
+            catch( ... )
+            {
+                if( pipe )
+                {
+                    cudaStreamSynchronize( st2 );
+                    cudaEventDestroy( ev_rec );
+                    cudaEventDestroy( ev_bwd );
+                }
+                throw;
+            }
+            if( pipe )
+            {
+                CUDA_CHECK( cudaEventDestroy( ev_rec ) );
+                CUDA_CHECK( cudaEventDestroy( ev_bwd ) );
             }
             std::vector<R> g0( 3 * total );
             std::vector<double> pg( (size_t)5 * nblk );
@@ -600,12 +669,19 @@ static double run_t( Engine & E, const AdjointInput & in, AdjointOutput & out )
     }
     catch( ... )
     {
+        if( st2 )
+            cudaStreamSynchronize( st2 );
+        cudaStreamSynchronize( st );
+        if( own_st2 )
+            cudaStreamDestroy( own_st2 );
         dfree( P.pool );
         dfree( P.work );
         dfree( P.ckpt );
         dfree( P.pgrad );
         throw;
     }
+    if( own_st2 )
+        CUDA_CHECK( cudaStreamDestroy( own_st2 ) );
     dfree( P.pool );
     dfree( P.work );
     dfree( P.ckpt );

@@ -863,6 +863,18 @@ void DDIPlan::set_tiles( int nl_a, int g_b, int g_c )
     tile[2] = g_c;
 }
 
+void DDIPlan::copy_shape_from( const DDIPlan & o )
+{
+    if( o.fp64 != fp64 || o.fused != fused || o.fd_host.size() != fd_host.size() )
+        throw std::runtime_error( "DDI plans of different systems" );
+    for( int k = 0; k < 3; ++k )
+        threads[k] = o.threads[k];
+    threads_bc = o.threads_bc;
+    cluster_k  = o.cluster_k;
+    planes_bc  = o.planes_bc;
+    set_tiles( o.tile[0], o.tile[1], o.tile[2] );
+}
+
 void DDIPlan::build_block_tables( const std::vector<DDISystem> & )
 {
     // defaults until tune() measures better ones; shrink the groups until they fit (nl even)

@@ -42,6 +42,8 @@ public:
     void tune( const SysDesc * d_sd, const void * sx, const void * sy, const void * sz, void * hx, void * hy,
                void * hz, cudaStream_t stream );
     void set_tiles( int nl_a, int g_b, int g_c );
+    // the tuned launch shapes of another plan built on the same systems (no timing runs)
+    void copy_shape_from( const DDIPlan & o );
     // optional per-launch event trace (kernel id, event recorded before the launch)
     std::vector<std::pair<int, cudaEvent_t>> * trace = nullptr;
     int n_sys = 0;

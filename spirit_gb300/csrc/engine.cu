@@ -748,8 +748,46 @@ Engine::~Engine()
     }
     dfree( d_rowmap_ );
     dfree( d_rowcount_ );
+    if( lane_ )
+    {
+        for( int c = 0; c < 3; ++c )
+            dfree( lane_->field[c] );
+        if( lane_->stream )
+            cudaStreamDestroy( lane_->stream );
+    }
     if( own_stream_ )
         cudaStreamDestroy( own_stream_ );
+}
+
+Engine::DdiLane * Engine::ddi_lane()
+{
+    if( !any_ddi_ )
+        return nullptr;
+    if( !lane_ )
+    {
+        auto L = std::make_unique<DdiLane>();
+        CUDA_CHECK( cudaStreamCreateWithFlags( &L->stream, cudaStreamNonBlocking ) );
+        try
+        {
+            for( int c = 0; c < 3; ++c )
+            {
+                L->field[c] = dalloc_bytes( total_ * elem_ );
+                CUDA_CHECK( cudaMemsetAsync( L->field[c], 0, total_ * elem_, stream_ ) );
+            }
+            L->plan.build( ddi_systems_, fp64_, d_desc_, stream_ );
+            L->plan.copy_shape_from( ddi_ );
+            CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+        }
+        catch( ... )
+        {
+            for( int c = 0; c < 3; ++c )
+                dfree( L->field[c] );
+            cudaStreamDestroy( L->stream );
+            throw;
+        }
+        lane_ = std::move( L );
+    }
+    return lane_.get();
 }
 
 void Engine::set_stream( cudaStream_t s )
@@ -845,6 +883,7 @@ void Engine::build_systems( const std::vector<SystemInput> & systems )
             field_[c] = dalloc_bytes( total_ * elem_ );
         ddi_.build( ddis, fp64_, d_desc_, stream_ );
         ddi_.tune( d_desc_, spins_[0], spins_[1], spins_[2], field_[0], field_[1], field_[2], stream_ );
+        ddi_systems_ = ddis;
         build_row_map( (int)ddis.size() );
     }
 }

@@ -166,6 +166,17 @@ public:
         w1_valid_ = false;
     }
 
+    // A second dipolar lane: its own plan (work spectra), field arrays and stream, with the main
+    // plan's tuned shapes, for dipolar fields computed beside the main stream (the adjoint's
+    // recomputation of the previous segment).  Built on first use; null without dipolar systems.
+    struct DdiLane
+    {
+        DDIPlan plan;
+        void * field[3]     = { nullptr, nullptr, nullptr };
+        cudaStream_t stream = nullptr;
+    };
+    DdiLane * ddi_lane();
+
 private:
     void build_systems( const std::vector<SystemInput> & systems );
     void launch_step_kernels();
@@ -218,6 +229,8 @@ private:
     int tuned_solver_     = -1;
     bool any_ddi_     = false;
     DDIPlan ddi_;
+    std::vector<DDISystem> ddi_systems_;
+    std::unique_ptr<DdiLane> lane_;
     // row-fused stages: the stage kernels do the passes along a (llg_stage_rows); the spectrum
     // then carries the configuration from one stage to the next b/c pass
     bool rows_          = false;

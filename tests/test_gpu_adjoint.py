@@ -112,6 +112,24 @@ def test_adjoint_checkpoint_interval_invariant():
         np.testing.assert_array_equal(o[2], out[0][2])
 
 
+@pytest.mark.parametrize("precision", [64, 32])
+def test_adjoint_pipelined_equals_serial(precision, monkeypatch):
+    """Several segments run as a two-stream pipeline (recomputation of segment s - 1 on a second
+    stream and dipolar lane beside the adjoint of segment s); SPIRIT_GB300_ADJ_PIPE=0 runs them one
+    after another.  Odd K with a ragged last segment (40 = 5 * 7 + 5) flips the ping-pong parity."""
+    from spirit_gb300 import adjoint
+
+    s0, tgt = _setup(ADJ, seed=5)
+    res = {}
+    with make_state(ADJ, s0, precision=precision) as p:
+        for pipe in ("1", "0"):
+            monkeypatch.setenv("SPIRIT_GB300_ADJ_PIPE", pipe)
+            res[pipe] = adjoint.llg_adjoint(p, tgt, N_STEPS, checkpoint=7, params=ADJ_PARAMS)
+    assert res["1"][0] == res["0"][0]
+    np.testing.assert_array_equal(res["1"][1], res["0"][1])
+    np.testing.assert_array_equal(res["1"][2], res["0"][2])
+
+
 def test_adjoint_fp32_vs_fp64():
     from spirit_gb300 import adjoint
 
