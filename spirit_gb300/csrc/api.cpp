@@ -231,6 +231,7 @@ void geometry_changed( State * st )
     for( auto & img : st->chain->images )
     {
         update_interactions( *img->geom, img->ham );
+        img->spin_pin.release(); // the buffer may move
         img->spins.assign( 3 * (size_t)img->nos(), 0.0 );
         for( int i = 0; i < img->nos(); ++i )
             img->spins[3 * i + 2] = 1.0;
@@ -2082,7 +2083,9 @@ void Simulation_N_Shot( State * state, int N, int idx_image, int idx_chain ) noe
         Engine & E = *img.run;
         // the host spin buffer is the state: callers may have written into it since the last call.
         // Upload, steps and read-back are enqueued together with one synchronisation at the end
-        // (steps of a converged or finished run are no-ops on the device).
+        // (steps of a converged or finished run are no-ops on the device).  The buffer is
+        // page-locked on first use (direct DMA both ways).
+        img.spin_pin.ensure( img.spins.data(), img.spins.size() * sizeof( double ) );
         E.set_spins( 0, img.spins.data(), false );
         E.llg_launch( N );
         const Engine::Status s = finish_llg( img, E );

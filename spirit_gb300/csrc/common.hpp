@@ -172,6 +172,15 @@ struct SysRun
     double reserved;
 };
 
+// Radix sequence of one axis (0-terminated) with the divisors of each Stockham stage s of a
+// length-L transform: L / radix[s] (butterflies per line) and the product of the earlier radices.
+struct RadixPlan
+{
+    int radix[12];
+    FastDiv div_lr[12];
+    FastDiv div_ns[12];
+};
+
 // FFT plan of one system's dipolar convolution.  Padded extents M[d] = N[d] or 2 N[d]
 // (Hamiltonian_Heisenberg.cpp:1510-1518); the real-to-complex axis is a (half length Ma/2+1).
 struct FFTDesc
@@ -183,7 +192,7 @@ struct FFTDesc
     long long spec_offset;   // complex element offset of this system's spectrum work arrays
     long long dhat_offset;   // complex element offset of its dipole spectrum
     long long tw_offset[3];  // twiddle table offsets (one table of M[d] entries per axis)
-    int radix[3][12];        // radix sequence per axis (0-terminated)
+    RadixPlan plan[3];       // radix sequence per axis
     float mu_f[MAX_BASIS];   // mu_s per basis atom
     double mu_d[MAX_BASIS];
     float invT_f;            // 1 / (Ma Mb Mc)

@@ -119,7 +119,7 @@ __global__ void pass_a( PassArgs<R> p )
         }
     }
     __syncthreads();
-    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.radix[0], tw, false );
+    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.plan[0], tw, false );
     if( !p.ka_major )
     {
         cplx<R> * W1 = p.W1 + f.spec_offset + ( (size_t)row * Bin + b0 ) * Mh;
@@ -192,7 +192,7 @@ __global__ void pass_b( PassArgs<R> p, int inverse )
         a[li * ls + t] = v;
     }
     __syncthreads();
-    const cplx<R> * r = block_fft( a, b, Mb, ls, nl, f.radix[1], tw, inverse != 0 );
+    const cplx<R> * r = block_fft( a, b, Mb, ls, nl, f.plan[1], tw, inverse != 0 );
     const int Bout    = inverse ? f.N[1] : Mb;
     cplx<R> * dst     = inverse ? p.W1 + f.spec_offset : p.W2 + f.spec_offset;
     for( int e = threadIdx.x; e < Bout * G; e += blockDim.x )
@@ -243,7 +243,7 @@ __global__ void pass_c( PassArgs<R> p )
         a[( cb * G + g ) * ls + c] = v;
     }
     __syncthreads();
-    cplx<R> * r = Mc > 1 ? block_fft( a, b, Mc, ls, nl, f.radix[2], tw, false ) : a;
+    cplx<R> * r = Mc > 1 ? block_fft( a, b, Mc, ls, nl, f.plan[2], tw, false ) : a;
     if( p.mode == 1 )
     {
         // dense forward transform: write every kc
@@ -292,7 +292,7 @@ __global__ void pass_c( PassArgs<R> p )
     }
     __syncthreads();
     cplx<R> * other = ( h == a ) ? b : a;
-    const cplx<R> * o = Mc > 1 ? block_fft( h, other, Mc, ls, nl, f.radix[2], tw, true ) : h;
+    const cplx<R> * o = Mc > 1 ? block_fft( h, other, Mc, ls, nl, f.plan[2], tw, true ) : h;
     const int Cout    = f.N[2];
     for( int e = threadIdx.x; e < total; e += blockDim.x )
     {
@@ -349,9 +349,9 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
     }
     __syncthreads();
     const FastDiv none = { 1, 0, 0 };
-    cplx<R> * r = sfft<R, false>( A, B, Mb, G * Nc * ncb, none, Mb, 1, f.radix[1], twb, false );
+    cplx<R> * r = sfft<R, false>( A, B, Mb, G * Nc * ncb, none, Mb, 1, f.plan[1], twb, false );
     cplx<R> * o = ( r == A ) ? B : A;
-    r           = sfft<R, true>( r, o, Mc, plane, f.div_plane, 1, plane, f.radix[2], twc, false );
+    r           = sfft<R, true>( r, o, Mc, plane, f.div_plane, 1, plane, f.plan[2], twc, false );
     o           = ( r == A ) ? B : A;
     // tensor product H_b1 = sum_b2 D_b1b2 . S_b2 (FFT.hpp:42-49 mult3D rows: xx xy xz | xy yy yz | xz yz zz)
     const int npair    = nb * nb;
@@ -387,9 +387,9 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
             o[g * vol + kc * plane + ( b1 * 3 + c3 ) * Mb + kb] = acc[c3];
     }
     __syncthreads();
-    r = sfft<R, true>( o, ( o == A ) ? B : A, Mc, plane, f.div_plane, 1, plane, f.radix[2], twc, true );
+    r = sfft<R, true>( o, ( o == A ) ? B : A, Mc, plane, f.div_plane, 1, plane, f.plan[2], twc, true );
     o = ( r == A ) ? B : A;
-    r = sfft<R, false>( r, o, Mb, G * Nc * ncb, none, Mb, 1, f.radix[1], twb, true );
+    r = sfft<R, false>( r, o, Mb, G * Nc * ncb, none, Mb, 1, f.plan[1], twb, true );
     for( int e = threadIdx.x; e < G * nin; e += blockDim.x )
     {
         const int g = e / nin, el = e - g * nin;
@@ -406,7 +406,7 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
 // [c][cb][kb_local].  The two transposes between the phases go through distributed shared memory.
 // Block table: (system, ka, rank, 0), the K blocks of a plane consecutive.
 template<typename R>
-__global__ void __launch_bounds__( 512 ) pass_bc_cl( PassArgs<R> p, int K )
+__global__ void __launch_bounds__( 512, 2 ) pass_bc_cl( PassArgs<R> p, int K )
 {
     namespace cg = cooperative_groups;
     extern __shared__ unsigned char smem_raw[];
@@ -455,7 +455,7 @@ __global__ void __launch_bounds__( 512 ) pass_bc_cl( PassArgs<R> p, int K )
     // every block's c-phase buffer is zero before any block writes into it
     cluster.sync();
     const FastDiv none = { 1, 0, 0 };
-    cplx<R> * r = sfft<R, false>( Bb0, Bb1, Mb, nc * ncb, none, Mb, 1, f.radix[1], twb, false );
+    cplx<R> * r = sfft<R, false>( Bb0, Bb1, Mb, nc * ncb, none, Mb, 1, f.plan[1], twb, false );
     // transpose 1: rows (c0 + cl, cb), all kb -> owner of kb
     for( int e = threadIdx.x; e < nc * ncb * Mb; e += blockDim.x )
     {
@@ -467,7 +467,7 @@ __global__ void __launch_bounds__( 512 ) pass_bc_cl( PassArgs<R> p, int K )
     }
     cluster.sync();
     const FastDiv dcrow = f.div_crow;
-    r           = sfft<R, true>( Bc0, Bc1, Mc, crow, dcrow, 1, crow, f.radix[2], twc, false );
+    r           = sfft<R, true>( Bc0, Bc1, Mc, crow, dcrow, 1, crow, f.plan[2], twc, false );
     cplx<R> * o = ( r == Bc0 ) ? Bc1 : Bc0;
     // tensor product at (kc, kb0 + kbl)
     const int npair    = nb * nb;
@@ -502,7 +502,7 @@ __global__ void __launch_bounds__( 512 ) pass_bc_cl( PassArgs<R> p, int K )
             o[kc * crow + ( b1 * 3 + c3 ) * kq + kbl] = acc[c3];
     }
     __syncthreads();
-    r = sfft<R, true>( o, ( o == Bc0 ) ? Bc1 : Bc0, Mc, crow, dcrow, 1, crow, f.radix[2], twc, true );
+    r = sfft<R, true>( o, ( o == Bc0 ) ? Bc1 : Bc0, Mc, crow, dcrow, 1, crow, f.plan[2], twc, true );
     // transpose 2: rows c < Nc of the kb range -> owner of row c (its b-phase buffers are free)
     for( int e = threadIdx.x; e < Nc * ncb * kq; e += blockDim.x )
     {
@@ -513,7 +513,7 @@ __global__ void __launch_bounds__( 512 ) pass_bc_cl( PassArgs<R> p, int K )
         dst[( cl * ncb + cb ) * Mb + kb0 + kbl] = r[c * crow + cb * kq + kbl];
     }
     cluster.sync();
-    r = sfft<R, false>( Bb0, Bb1, Mb, nc * ncb, none, Mb, 1, f.radix[1], twb, true );
+    r = sfft<R, false>( Bb0, Bb1, Mb, nc * ncb, none, Mb, 1, f.plan[1], twb, true );
     for( int e = threadIdx.x; e < ncb * nc * Nb; e += blockDim.x )
     {
         const int rest = (int)fdiv( (unsigned)e, f.div_Nb ), b = e - rest * Nb;
@@ -586,7 +586,7 @@ __global__ void pass_a_inv( PassArgs<R> p )
         a[q * ls + k] = { x.x - y.y, x.y + y.x };
     }
     __syncthreads();
-    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.radix[0], tw, true );
+    const cplx<R> * r = block_fft( a, b, Ma, ls, nq, f.plan[0], tw, true );
     const R invT = fft_invT<R>( f );
     const int cb = row / Nc, c = row - cb * Nc;
     const int ib = cb / 3, comp = cb - 3 * ib;
@@ -646,9 +646,11 @@ static size_t smem_optin()
     return (size_t)v;
 }
 
-static void factorize( int L, int * rad )
+static void factorize( int L, RadixPlan & P )
 {
-    int n = 0;
+    const int L0 = L;
+    int * rad    = P.radix;
+    int n        = 0;
     while( L % 4 == 0 && L > 4 )
     {
         rad[n++] = 4;
@@ -667,6 +669,13 @@ static void factorize( int L, int * rad )
             L /= p;
         }
     rad[n] = 0;
+    int ns = 1;
+    for( int s = 0; s < n; ++s )
+    {
+        P.div_lr[s] = make_fastdiv( (unsigned)( L0 / rad[s] ) );
+        P.div_ns[s] = make_fastdiv( (unsigned)ns );
+        ns *= rad[s];
+    }
 }
 
 DDIPlan::~DDIPlan()
@@ -732,7 +741,7 @@ void DDIPlan::build( const std::vector<DDISystem> & systems, bool fp64, const Sy
                 tw_host.push_back( std::cos( ang ) );
                 tw_host.push_back( std::sin( ang ) );
             }
-            factorize( f.M[d], f.radix[d] );
+            factorize( f.M[d], f.plan[d] );
         }
         f.spec_offset = spec;
         long long w2  = 3LL * f.nb * f.N[2] * f.M[1] * f.Mh;

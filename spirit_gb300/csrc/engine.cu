@@ -383,7 +383,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage_rows( StageArgs<R> A, RowArgs
         ba[q * ls + k] = { x.x - y.y, x.y + y.x };
     }
     __syncthreads();
-    const cplx<R> * hr = block_fft( ba, bb, Ma, ls, nq, f.radix[0], tw, true );
+    const cplx<R> * hr = block_fft( ba, bb, Ma, ls, nq, f.plan[0], tw, true );
     const R invT       = fft_invT<R>( f );
     // ---- main: the stage on the block's spins
     const int i0        = rowlen * ( b0 + Nb * cc ); // first local spin of the block
@@ -456,7 +456,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage_rows( StageArgs<R> A, RowArgs
             ba[q * ls + t].y = 0;
     }
     __syncthreads();
-    const cplx<R> * r = block_fft( ba, bb, Ma, ls, nq, f.radix[0], tw, false );
+    const cplx<R> * r = block_fft( ba, bb, Ma, ls, nq, f.plan[0], tw, false );
     for( int e2 = threadIdx.x; e2 < ncb * nr * Mh; e2 += blockDim.x )
     {
         const int lr = e2 % nr, rest = e2 / nr;

@@ -388,8 +388,12 @@ __device__ __forceinline__ cplx<R> * block_fft_reg( cplx<R> * a, cplx<R> * b, in
     }
 }
 
+template<typename R, bool CLOSED>
+__device__ __noinline__ cplx<R> * mixed_fft( cplx<R> * a, cplx<R> * b, int L, int nl, int ls, int es,
+                                             const RadixPlan & P, const cplx<R> * tw, bool inverse );
+
 template<typename R>
-__device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int ls, int nl, const int * rad,
+__device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int ls, int nl, const RadixPlan & P,
                                const cplx<R> * tw, bool inverse )
 {
     if( L == 1 )
@@ -400,105 +404,7 @@ __device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int ls, int nl,
         return r;
     if( ( L & ( L - 1 ) ) == 0 )
         return block_fft_pow2( a, b, L, ls, nl, tw, inverse );
-    int Ns = 1;
-    for( int s = 0; s < 12 && rad[s] > 0; ++s )
-    {
-        const int Rr   = rad[s];
-        const int LR   = L / Rr;
-        const int span = L / ( Ns * Rr );
-        if( Rr <= 8 )
-        {
-            for( int idx = threadIdx.x; idx < nl * LR; idx += blockDim.x )
-            {
-                int line           = idx / LR;
-                int j              = idx - line * LR;
-                const cplx<R> * src = a + line * L;
-                cplx<R> * dst       = b + line * L;
-                int k              = j % Ns;
-                cplx<R> v[8];
-#pragma unroll
-                for( int r = 0; r < 8; ++r )
-                {
-                    if( r < Rr )
-                    {
-                        cplx<R> w = tw[r * k * span];
-                        if( inverse )
-                            w = cconj( w );
-                        v[r] = r == 0 ? src[j] : cmul( src[j + r * LR], w );
-                    }
-                }
-                int d0 = ( j / Ns ) * Ns * Rr + k;
-                if( Rr == 2 )
-                {
-                    dst[d0]      = { v[0].x + v[1].x, v[0].y + v[1].y };
-                    dst[d0 + Ns] = { v[0].x - v[1].x, v[0].y - v[1].y };
-                }
-                else if( Rr == 4 )
-                {
-                    // W4 = -i (forward) / +i (inverse)
-                    cplx<R> s02 = { v[0].x + v[2].x, v[0].y + v[2].y };
-                    cplx<R> d02 = { v[0].x - v[2].x, v[0].y - v[2].y };
-                    cplx<R> s13 = { v[1].x + v[3].x, v[1].y + v[3].y };
-                    cplx<R> d13 = { v[1].x - v[3].x, v[1].y - v[3].y };
-                    // forward: out1 = d02 - i d13, out3 = d02 + i d13
-                    cplx<R> id13 = inverse ? cplx<R>{ -d13.y, d13.x } : cplx<R>{ d13.y, -d13.x };
-                    dst[d0]          = { s02.x + s13.x, s02.y + s13.y };
-                    dst[d0 + Ns]     = { d02.x + id13.x, d02.y + id13.y };
-                    dst[d0 + 2 * Ns] = { s02.x - s13.x, s02.y - s13.y };
-                    dst[d0 + 3 * Ns] = { d02.x - id13.x, d02.y - id13.y };
-                }
-                else
-                {
-                    for( int m = 0; m < Rr; ++m )
-                    {
-                        cplx<R> acc = v[0];
-                        for( int r = 1; r < Rr; ++r )
-                        {
-                            cplx<R> w = tw[( ( r * m ) % Rr ) * LR];
-                            if( inverse )
-                                w = cconj( w );
-                            cplx<R> t = cmul( v[r], w );
-                            acc.x += t.x;
-                            acc.y += t.y;
-                        }
-                        dst[d0 + m * Ns] = acc;
-                    }
-                }
-            }
-        }
-        else
-        {
-            // large prime radix: one output per thread, O(R) work each
-            for( int o = threadIdx.x; o < nl * L; o += blockDim.x )
-            {
-                int line           = o / L;
-                int q              = o - line * L;
-                const cplx<R> * src = a + line * L;
-                int k              = q % Ns;
-                int m              = ( q / Ns ) % Rr;
-                int jhi            = q / ( Ns * Rr );
-                int j              = jhi * Ns + k;
-                cplx<R> acc        = { 0, 0 };
-                for( int r = 0; r < Rr; ++r )
-                {
-                    int t     = ( r * k * span + ( ( r * m ) % Rr ) * LR ) % L;
-                    cplx<R> w = tw[t];
-                    if( inverse )
-                        w = cconj( w );
-                    cplx<R> p = cmul( src[j + r * LR], w );
-                    acc.x += p.x;
-                    acc.y += p.y;
-                }
-                b[line * L + q] = acc;
-            }
-        }
-        __syncthreads();
-        cplx<R> * t = a;
-        a           = b;
-        b           = t;
-        Ns *= Rr;
-    }
-    return a;
+    return mixed_fft<R, true>( a, b, L, nl, L, 1, P, tw, inverse );
 }
 
 // ------------------------------------------------------------------ strided line transforms
@@ -582,80 +488,178 @@ __device__ __forceinline__ cplx<R> * sfft_const( cplx<R> * a, cplx<R> * b, int n
     return a;
 }
 
-// Mixed-radix (any L) strided Stockham: radix <= 8 butterflies, larger prime factors one output
-// per thread.  Consecutive threads take consecutive butterflies of a line.
-template<typename R>
-__device__ cplx<R> * sfft_generic( cplx<R> * a, cplx<R> * b, int L, int nl, int ls, int es, const int * rad,
-                                  const cplx<R> * tw, bool inverse )
+// One Stockham stage of compile-time radix RR over nl lines (element t of line l at l*ls + t*es):
+// butterfly j = 0 .. L/RR - 1 of every line, k = j mod Ns, twiddles W_L^(r k span) on the inputs and
+// the RR-point DFT W_RR^(r m) = tw[((r m) mod RR) L/RR] on the outputs.  CLOSED: radix 2 and 4 by
+// their closed butterflies (block_fft), else the direct RR-point sums accumulated in r order
+// (sfft) -- each keeps the operation order of its path.
+template<typename R, int RR, bool CLOSED>
+__device__ __forceinline__ void mixed_stage( const cplx<R> * a, cplx<R> * b, int nl, int ls, int es, int LR, int Ns,
+                                             int span, const FastDiv & dlr, const FastDiv & dns, const cplx<R> * tw,
+                                             bool inverse )
 {
-    int Ns = 1;
-    for( int s = 0; s < 12 && rad[s] > 0; ++s )
-    {
-        const int Rr   = rad[s];
-        const int LR   = L / Rr;
-        const int span = L / ( Ns * Rr );
-        if( Rr <= 8 )
-        {
-            for( int idx = threadIdx.x; idx < nl * LR; idx += blockDim.x )
-            {
-                const int line      = idx / LR;
-                const int j         = idx - line * LR;
-                const cplx<R> * src = a + line * ls;
-                cplx<R> * dst       = b + line * ls;
-                const int k         = j % Ns;
-                cplx<R> v[8];
+    cplx<R> wq[RR];
 #pragma unroll
-                for( int r = 0; r < 8; ++r )
-                {
-                    if( r < Rr )
-                    {
-                        cplx<R> w = tw[r * k * span];
-                        if( inverse )
-                            w = cconj( w );
-                        v[r] = r == 0 ? src[j * es] : cmul( src[( j + r * LR ) * es], w );
-                    }
-                }
-                const int d0 = ( j / Ns ) * Ns * Rr + k;
-                for( int m = 0; m < Rr; ++m )
-                {
-                    cplx<R> acc = v[0];
-                    for( int r = 1; r < Rr; ++r )
-                    {
-                        cplx<R> w = tw[( ( r * m ) % Rr ) * LR];
-                        if( inverse )
-                            w = cconj( w );
-                        cplx<R> t = cmul( v[r], w );
-                        acc.x += t.x;
-                        acc.y += t.y;
-                    }
-                    dst[( d0 + m * Ns ) * es] = acc;
-                }
-            }
+    for( int q = 0; q < RR; ++q )
+    {
+        wq[q] = tw[q * LR];
+        if( inverse )
+            wq[q] = cconj( wq[q] );
+    }
+    for( int idx = threadIdx.x; idx < nl * LR; idx += blockDim.x )
+    {
+        const int line      = (int)fdiv( (unsigned)idx, dlr );
+        const int j         = idx - line * LR;
+        const int jq        = (int)fdiv( (unsigned)j, dns );
+        const int k         = j - jq * Ns;
+        const cplx<R> * src = a + line * ls;
+        cplx<R> * dst       = b + line * ls;
+        cplx<R> v[RR];
+        v[0] = src[j * es];
+#pragma unroll
+        for( int r = 1; r < RR; ++r )
+        {
+            cplx<R> w = tw[r * k * span];
+            if( inverse )
+                w = cconj( w );
+            v[r] = cmul( src[( j + r * LR ) * es], w );
+        }
+        const int d0 = jq * Ns * RR + k;
+        if( CLOSED && RR == 2 )
+        {
+            dst[d0 * es]          = { v[0].x + v[1].x, v[0].y + v[1].y };
+            dst[( d0 + Ns ) * es] = { v[0].x - v[1].x, v[0].y - v[1].y };
+        }
+        else if( CLOSED && RR == 4 )
+        {
+            // W4 = -i (forward) / +i (inverse): out1 = d02 - i d13, out3 = d02 + i d13 (forward)
+            const cplx<R> s02  = { v[0].x + v[2 % RR].x, v[0].y + v[2 % RR].y };
+            const cplx<R> d02  = { v[0].x - v[2 % RR].x, v[0].y - v[2 % RR].y };
+            const cplx<R> s13  = { v[1].x + v[3 % RR].x, v[1].y + v[3 % RR].y };
+            const cplx<R> d13  = { v[1].x - v[3 % RR].x, v[1].y - v[3 % RR].y };
+            const cplx<R> id13 = inverse ? cplx<R>{ -d13.y, d13.x } : cplx<R>{ d13.y, -d13.x };
+            dst[d0 * es]              = { s02.x + s13.x, s02.y + s13.y };
+            dst[( d0 + Ns ) * es]     = { d02.x + id13.x, d02.y + id13.y };
+            dst[( d0 + 2 * Ns ) * es] = { s02.x - s13.x, s02.y - s13.y };
+            dst[( d0 + 3 * Ns ) * es] = { d02.x - id13.x, d02.y - id13.y };
         }
         else
         {
-            for( int o = threadIdx.x; o < nl * L; o += blockDim.x )
+#pragma unroll
+            for( int m = 0; m < RR; ++m )
             {
-                const int line      = o / L;
-                const int q         = o - line * L;
-                const cplx<R> * src = a + line * ls;
-                const int k         = q % Ns;
-                const int m         = ( q / Ns ) % Rr;
-                const int jhi       = q / ( Ns * Rr );
-                const int j         = jhi * Ns + k;
-                cplx<R> acc         = { 0, 0 };
-                for( int r = 0; r < Rr; ++r )
+                cplx<R> acc = v[0];
+#pragma unroll
+                for( int r = 1; r < RR; ++r )
                 {
-                    const int t = ( r * k * span + ( ( r * m ) % Rr ) * LR ) % L;
-                    cplx<R> w   = tw[t];
-                    if( inverse )
-                        w = cconj( w );
-                    const cplx<R> p = cmul( src[( j + r * LR ) * es], w );
-                    acc.x += p.x;
-                    acc.y += p.y;
+                    const cplx<R> t = cmul( v[r], wq[( r * m ) % RR] );
+                    acc.x += t.x;
+                    acc.y += t.y;
                 }
-                b[line * ls + q * es] = acc;
+                dst[( d0 + m * Ns ) * es] = acc;
             }
+        }
+    }
+}
+
+// Mixed-radix (any L) strided Stockham over the radix plan P: radices 2, 3, 4, 5, 7 (all that the
+// padded extents produce) with compile-time butterflies and the stage divisors precomputed on the
+// host; other radices <= 8 by a runtime-radix loop; larger prime factors one output per thread.
+// Consecutive threads take consecutive butterflies of a line.  Not inlined: one copy serves every
+// call site of a kernel.
+template<typename R, bool CLOSED>
+__device__ __noinline__ cplx<R> * mixed_fft( cplx<R> * a, cplx<R> * b, int L, int nl, int ls, int es,
+                                             const RadixPlan & P, const cplx<R> * tw, bool inverse )
+{
+    int Ns = 1;
+    for( int s = 0; s < 12 && P.radix[s] > 0; ++s )
+    {
+        const int Rr   = P.radix[s];
+        const int LR   = L / Rr;
+        const int span = L / ( Ns * Rr );
+        const FastDiv dlr = P.div_lr[s], dns = P.div_ns[s];
+        switch( Rr )
+        {
+        case 2:
+            mixed_stage<R, 2, CLOSED>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
+            break;
+        case 3:
+            mixed_stage<R, 3, CLOSED>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
+            break;
+        case 4:
+            mixed_stage<R, 4, CLOSED>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
+            break;
+        case 5:
+            mixed_stage<R, 5, CLOSED>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
+            break;
+        case 7:
+            mixed_stage<R, 7, CLOSED>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
+            break;
+        default:
+            if( Rr <= 8 )
+            {
+                for( int idx = threadIdx.x; idx < nl * LR; idx += blockDim.x )
+                {
+                    const int line      = idx / LR;
+                    const int j         = idx - line * LR;
+                    const cplx<R> * src = a + line * ls;
+                    cplx<R> * dst       = b + line * ls;
+                    const int k         = j % Ns;
+                    cplx<R> v[8];
+#pragma unroll
+                    for( int r = 0; r < 8; ++r )
+                    {
+                        if( r < Rr )
+                        {
+                            cplx<R> w = tw[r * k * span];
+                            if( inverse )
+                                w = cconj( w );
+                            v[r] = r == 0 ? src[j * es] : cmul( src[( j + r * LR ) * es], w );
+                        }
+                    }
+                    const int d0 = ( j / Ns ) * Ns * Rr + k;
+                    for( int m = 0; m < Rr; ++m )
+                    {
+                        cplx<R> acc = v[0];
+                        for( int r = 1; r < Rr; ++r )
+                        {
+                            cplx<R> w = tw[( ( r * m ) % Rr ) * LR];
+                            if( inverse )
+                                w = cconj( w );
+                            cplx<R> t = cmul( v[r], w );
+                            acc.x += t.x;
+                            acc.y += t.y;
+                        }
+                        dst[( d0 + m * Ns ) * es] = acc;
+                    }
+                }
+            }
+            else
+            {
+                for( int o = threadIdx.x; o < nl * L; o += blockDim.x )
+                {
+                    const int line      = o / L;
+                    const int q         = o - line * L;
+                    const cplx<R> * src = a + line * ls;
+                    const int k         = q % Ns;
+                    const int m         = ( q / Ns ) % Rr;
+                    const int jhi       = q / ( Ns * Rr );
+                    const int j         = jhi * Ns + k;
+                    cplx<R> acc         = { 0, 0 };
+                    for( int r = 0; r < Rr; ++r )
+                    {
+                        const int t = ( r * k * span + ( ( r * m ) % Rr ) * LR ) % L;
+                        cplx<R> w   = tw[t];
+                        if( inverse )
+                            w = cconj( w );
+                        const cplx<R> p = cmul( src[( j + r * LR ) * es], w );
+                        acc.x += p.x;
+                        acc.y += p.y;
+                    }
+                    b[line * ls + q * es] = acc;
+                }
+            }
+            break;
         }
         __syncthreads();
         cplx<R> * t = a;
@@ -668,7 +672,7 @@ __device__ cplx<R> * sfft_generic( cplx<R> * a, cplx<R> * b, int L, int nl, int 
 
 template<typename R, bool LINE_FAST, int MAXLG = MaxRadix<R>::LG>
 __device__ cplx<R> * sfft( cplx<R> * a, cplx<R> * b, int L, int nl, const FastDiv & dnl, int ls, int es,
-                          const int * rad, const cplx<R> * tw, bool inverse )
+                          const RadixPlan & P, const cplx<R> * tw, bool inverse )
 {
     switch( L )
     {
@@ -695,7 +699,7 @@ __device__ cplx<R> * sfft( cplx<R> * a, cplx<R> * b, int L, int nl, const FastDi
     case 1024:
         return stockham_reg<R, 10, 0, MAXLG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     default:
-        return sfft_generic<R>( a, b, L, nl, ls, es, rad, tw, inverse );
+        return mixed_fft<R, false>( a, b, L, nl, ls, es, P, tw, inverse );
     }
 }
 

@@ -5,6 +5,7 @@
 #pragma once
 #include "engine.hpp"
 #include "geometry.hpp"
+#include "util.hpp"
 
 #include <atomic>
 #include <chrono>
@@ -113,6 +114,8 @@ struct Image
     std::shared_ptr<void> mc_run; // Monte Carlo run (engine + colouring) of this image
     unsigned int mc_sweeps_drawn = 0; // Monte Carlo sweeps done so far (position in the random stream)
     unsigned int llg_noise_drawn = 0; // LLG iterations whose thermal noise was drawn (noise stream position)
+    // page-locked registration of `spins` for single-shot transfers (declared after it: released first)
+    HostPin spin_pin;
 
     int nos() const
     {

@@ -53,6 +53,50 @@ inline void dfree( T *& p )
     p = nullptr;
 }
 
+// Page-locked registration of a host buffer that outlives many transfers (an image's AoS spin
+// mirror): the copy engines then move it directly, without the driver's staging through a pinned
+// bounce buffer.  ensure() re-registers when the buffer has moved, release() before it is
+// reallocated.  SPIRIT_GB300_PIN=0 leaves buffers pageable; a failed registration leaves the
+// buffer pageable.
+struct HostPin
+{
+    void * ptr   = nullptr;
+    size_t bytes = 0;
+    void ensure( void * p, size_t n )
+    {
+        if( p == ptr && n == bytes )
+            return;
+        release();
+        const char * env = std::getenv( "SPIRIT_GB300_PIN" );
+        if( !p || n == 0 || ( env && env[0] == '0' ) )
+            return;
+        if( cudaHostRegister( p, n, cudaHostRegisterPortable | cudaHostRegisterMapped ) == cudaSuccess )
+        {
+            ptr   = p;
+            bytes = n;
+        }
+        else
+            cudaGetLastError();
+    }
+    void release()
+    {
+        if( ptr )
+        {
+            cudaHostUnregister( ptr );
+            cudaGetLastError();
+        }
+        ptr   = nullptr;
+        bytes = 0;
+    }
+    HostPin() = default;
+    HostPin( const HostPin & ) = delete;
+    HostPin & operator=( const HostPin & ) = delete;
+    ~HostPin()
+    {
+        release();
+    }
+};
+
 template<typename T>
 inline void h2d( T * d, const T * h, size_t n )
 {
