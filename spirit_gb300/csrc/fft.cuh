@@ -388,7 +388,7 @@ __device__ __forceinline__ cplx<R> * block_fft_reg( cplx<R> * a, cplx<R> * b, in
     }
 }
 
-template<typename R, bool CLOSED>
+template<typename R>
 __device__ __noinline__ cplx<R> * mixed_fft( cplx<R> * a, cplx<R> * b, int L, int nl, int ls, int es,
                                              const RadixPlan & P, const cplx<R> * tw, bool inverse );
 
@@ -404,7 +404,7 @@ __device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int ls, int nl,
         return r;
     if( ( L & ( L - 1 ) ) == 0 )
         return block_fft_pow2( a, b, L, ls, nl, tw, inverse );
-    return mixed_fft<R, true>( a, b, L, nl, L, 1, P, tw, inverse );
+    return mixed_fft<R>( a, b, L, nl, L, 1, P, tw, inverse );
 }
 
 // ------------------------------------------------------------------ strided line transforms
@@ -488,23 +488,49 @@ __device__ __forceinline__ cplx<R> * sfft_const( cplx<R> * a, cplx<R> * b, int n
     return a;
 }
 
+// Small-radix DFT helpers (the radix-3/5/7 butterflies): sums, differences, scaling by a real,
+// and the rotation by -i (forward) / +i (inverse).
+template<typename R>
+__device__ __forceinline__ cplx<R> cadd( cplx<R> a, cplx<R> b )
+{
+    return { a.x + b.x, a.y + b.y };
+}
+template<typename R>
+__device__ __forceinline__ cplx<R> csub( cplx<R> a, cplx<R> b )
+{
+    return { a.x - b.x, a.y - b.y };
+}
+template<typename R>
+__device__ __forceinline__ cplx<R> caxpy( R s, cplx<R> a, cplx<R> y ) // y + s a
+{
+    return { y.x + s * a.x, y.y + s * a.y };
+}
+template<typename R>
+__device__ __forceinline__ cplx<R> crot( cplx<R> u, bool inverse )
+{
+    return inverse ? cplx<R>{ -u.y, u.x } : cplx<R>{ u.y, -u.x };
+}
+
 // One Stockham stage of compile-time radix RR over nl lines (element t of line l at l*ls + t*es):
-// butterfly j = 0 .. L/RR - 1 of every line, k = j mod Ns, twiddles W_L^(r k span) on the inputs and
-// the RR-point DFT W_RR^(r m) = tw[((r m) mod RR) L/RR] on the outputs.  CLOSED: radix 2 and 4 by
-// their closed butterflies (block_fft), else the direct RR-point sums accumulated in r order
-// (sfft) -- each keeps the operation order of its path.
-template<typename R, int RR, bool CLOSED>
+// butterfly j = 0 .. L/RR - 1 of every line, k = j mod Ns, twiddles W_L^(r k span) on the inputs,
+// then the RR-point DFT in closed form: radix 2 and 4 by sums and +-i swaps; radix 3, 5, 7 by the
+// symmetric pairs a_k = v_k + v_(RR-k), b_k = v_k - v_(RR-k):
+//   y_m = v_0 + sum_k cos(2 pi k m / RR) a_k  -/+  i sum_k sin(2 pi k m / RR) b_k,
+//   y_(RR-m) with the opposite sign of the i term,
+// the cosines and sines read from the twiddle table (W_RR^q = tw[q L/RR]).
+template<typename R, int RR>
 __device__ __forceinline__ void mixed_stage( const cplx<R> * a, cplx<R> * b, int nl, int ls, int es, int LR, int Ns,
                                              int span, const FastDiv & dlr, const FastDiv & dns, const cplx<R> * tw,
                                              bool inverse )
 {
-    cplx<R> wq[RR];
+    constexpr int NH = ( RR - 1 ) / 2;
+    R cs[NH + 1], sn[NH + 1]; // cos(2 pi q / RR), sin(2 pi q / RR)
 #pragma unroll
-    for( int q = 0; q < RR; ++q )
+    for( int q = 1; q <= NH; ++q )
     {
-        wq[q] = tw[q * LR];
-        if( inverse )
-            wq[q] = cconj( wq[q] );
+        const cplx<R> w = tw[q * LR];
+        cs[q]           = w.x;
+        sn[q]           = -w.y;
     }
     for( int idx = threadIdx.x; idx < nl * LR; idx += blockDim.x )
     {
@@ -525,49 +551,63 @@ __device__ __forceinline__ void mixed_stage( const cplx<R> * a, cplx<R> * b, int
             v[r] = cmul( src[( j + r * LR ) * es], w );
         }
         const int d0 = jq * Ns * RR + k;
-        if( CLOSED && RR == 2 )
+        cplx<R> y[RR];
+        if( RR == 2 )
         {
-            dst[d0 * es]          = { v[0].x + v[1].x, v[0].y + v[1].y };
-            dst[( d0 + Ns ) * es] = { v[0].x - v[1].x, v[0].y - v[1].y };
+            y[0]      = cadd( v[0], v[1 % RR] );
+            y[1 % RR] = csub( v[0], v[1 % RR] );
         }
-        else if( CLOSED && RR == 4 )
+        else if( RR == 4 )
         {
-            // W4 = -i (forward) / +i (inverse): out1 = d02 - i d13, out3 = d02 + i d13 (forward)
-            const cplx<R> s02  = { v[0].x + v[2 % RR].x, v[0].y + v[2 % RR].y };
-            const cplx<R> d02  = { v[0].x - v[2 % RR].x, v[0].y - v[2 % RR].y };
-            const cplx<R> s13  = { v[1].x + v[3 % RR].x, v[1].y + v[3 % RR].y };
-            const cplx<R> d13  = { v[1].x - v[3 % RR].x, v[1].y - v[3 % RR].y };
-            const cplx<R> id13 = inverse ? cplx<R>{ -d13.y, d13.x } : cplx<R>{ d13.y, -d13.x };
-            dst[d0 * es]              = { s02.x + s13.x, s02.y + s13.y };
-            dst[( d0 + Ns ) * es]     = { d02.x + id13.x, d02.y + id13.y };
-            dst[( d0 + 2 * Ns ) * es] = { s02.x - s13.x, s02.y - s13.y };
-            dst[( d0 + 3 * Ns ) * es] = { d02.x - id13.x, d02.y - id13.y };
+            const cplx<R> s02 = cadd( v[0], v[2 % RR] ), d02 = csub( v[0], v[2 % RR] );
+            const cplx<R> s13 = cadd( v[1 % RR], v[3 % RR] ), d13 = crot( csub( v[1 % RR], v[3 % RR] ), inverse );
+            y[0]      = cadd( s02, s13 );
+            y[1 % RR] = cadd( d02, d13 );
+            y[2 % RR] = csub( s02, s13 );
+            y[3 % RR] = csub( d02, d13 );
         }
         else
         {
+            cplx<R> ap[NH + 1], bm[NH + 1];
+            y[0] = v[0];
 #pragma unroll
-            for( int m = 0; m < RR; ++m )
+            for( int q = 1; q <= NH; ++q )
             {
-                cplx<R> acc = v[0];
+                ap[q] = cadd( v[q], v[RR - q] );
+                bm[q] = csub( v[q], v[RR - q] );
+                y[0]  = cadd( y[0], ap[q] );
+            }
 #pragma unroll
-                for( int r = 1; r < RR; ++r )
+            for( int m = 1; m <= NH; ++m )
+            {
+                cplx<R> t = v[0], u = { 0, 0 };
+#pragma unroll
+                for( int q = 1; q <= NH; ++q )
                 {
-                    const cplx<R> t = cmul( v[r], wq[( r * m ) % RR] );
-                    acc.x += t.x;
-                    acc.y += t.y;
+                    const int e  = ( q * m ) % RR; // angle index of cos/sin(2 pi q m / RR)
+                    const int ef = e <= NH ? e : RR - e;
+                    const R sg   = e <= NH ? R( 1 ) : R( -1 );
+                    t            = caxpy( cs[ef], ap[q], t );
+                    u            = caxpy( sg * sn[ef], bm[q], u );
                 }
-                dst[( d0 + m * Ns ) * es] = acc;
+                const cplx<R> iu = crot( u, inverse );
+                y[m]             = cadd( t, iu );
+                y[RR - m]        = csub( t, iu );
             }
         }
+#pragma unroll
+        for( int m = 0; m < RR; ++m )
+            dst[( d0 + m * Ns ) * es] = y[m];
     }
 }
 
 // Mixed-radix (any L) strided Stockham over the radix plan P: radices 2, 3, 4, 5, 7 (all that the
-// padded extents produce) with compile-time butterflies and the stage divisors precomputed on the
-// host; other radices <= 8 by a runtime-radix loop; larger prime factors one output per thread.
+// padded extents produce) with closed-form compile-time butterflies and the stage divisors
+// precomputed on the host; other radices <= 8 by a runtime-radix loop; larger prime factors one
+// output per thread.
 // Consecutive threads take consecutive butterflies of a line.  Not inlined: one copy serves every
 // call site of a kernel.
-template<typename R, bool CLOSED>
+template<typename R>
 __device__ __noinline__ cplx<R> * mixed_fft( cplx<R> * a, cplx<R> * b, int L, int nl, int ls, int es,
                                              const RadixPlan & P, const cplx<R> * tw, bool inverse )
 {
@@ -581,19 +621,19 @@ __device__ __noinline__ cplx<R> * mixed_fft( cplx<R> * a, cplx<R> * b, int L, in
         switch( Rr )
         {
         case 2:
-            mixed_stage<R, 2, CLOSED>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
+            mixed_stage<R, 2>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
             break;
         case 3:
-            mixed_stage<R, 3, CLOSED>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
+            mixed_stage<R, 3>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
             break;
         case 4:
-            mixed_stage<R, 4, CLOSED>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
+            mixed_stage<R, 4>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
             break;
         case 5:
-            mixed_stage<R, 5, CLOSED>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
+            mixed_stage<R, 5>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
             break;
         case 7:
-            mixed_stage<R, 7, CLOSED>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
+            mixed_stage<R, 7>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
             break;
         default:
             if( Rr <= 8 )
@@ -699,7 +739,7 @@ __device__ cplx<R> * sfft( cplx<R> * a, cplx<R> * b, int L, int nl, const FastDi
     case 1024:
         return stockham_reg<R, 10, 0, MAXLG, LINE_FAST>( a, b, nl, dnl, ls, es, tw, inverse );
     default:
-        return mixed_fft<R, false>( a, b, L, nl, ls, es, P, tw, inverse );
+        return mixed_fft<R>( a, b, L, nl, ls, es, P, tw, inverse );
     }
 }
 
