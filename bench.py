@@ -236,13 +236,14 @@ def c4_specs(n=256, seed=4, ddi=False):
     return specs
 
 
-def run_batched_vs_plain(steps, warmup, plain=True, check=True, ddi=False):
+def run_batched_vs_plain(steps, warmup, plain=True, check=True, ddi=False, profile_step=False):
     """256 uneven systems: spin-updates/s of the batched path (all systems in one launch per SIB
     stage, CUDA graphs) against the plain path (every system its own engine and launches, on the
     same stream), both FP32 and device-timed with CUDA events; the ensemble's arrays (~290 MB)
     exceed L2.  Accuracy: the 8 smallest systems run 1000 batched FP32 steps against the FP64
     oracle consuming the same Philox streams.  ddi=True: the dipolar variant of the ensemble
-    (c4_specs), one batched FFT plan over all 256 systems."""
+    (c4_specs), one batched FFT plan over all 256 systems.  profile_step: one more batched step
+    inside a profiler range (for `ncu --profile-from-start off`)."""
     import torch
 
     from oracle.oracle import OracleSystem, random_spins
@@ -294,6 +295,11 @@ def run_batched_vs_plain(steps, warmup, plain=True, check=True, ddi=False):
     b.record(stream)
     stream.synchronize()
     batched_ms = a.elapsed_time(b)
+    if profile_step:
+        torch.cuda.profiler.start()
+        simulation.batched_launch_steps(states, simulation.SOLVER_SIB, 1)
+        stream.synchronize()
+        torch.cuda.profiler.stop()
     simulation.batched_finish(states)
     for p in states:
         state.delete(p)
@@ -765,7 +771,9 @@ def main():
         import torch
 
         torch.cuda.set_device(0)
-        print(json.dumps(run_batched_vs_plain(max(20, args.steps), max(3, args.warmup), ddi=True)))
+        prof = args.profile_step  # profiling: the batched path alone
+        print(json.dumps(run_batched_vs_plain(max(20, args.steps), max(3, args.warmup), plain=not prof,
+                                              check=not prof, ddi=True, profile_step=prof)))
         return
     if args.only_htst:
         import torch
