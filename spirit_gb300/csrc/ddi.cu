@@ -63,9 +63,9 @@ __device__ __forceinline__ bool sys_inactive( const PassArgs<R> & p, int s )
 // Two real lines x, y go through one complex transform of z = x + i y:
 //   X[k] = (Z[k] + conj Z[-k]) / 2,   Y[k] = (Z[k] - conj Z[-k]) / 2i
 template<typename R>
-__global__ void pass_a( PassArgs<R> p )
+__global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 4 : 2 ) pass_a( PassArgs<R> p )
 {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__( 16 ) unsigned char smem_raw[];
     const int4 blk = p.blocks[blockIdx.x];
     const int s    = blk.x;
     const FFTDesc & f = p.fd[s];
@@ -155,9 +155,9 @@ __global__ void pass_a( PassArgs<R> p )
 // block: p.g consecutive lines (row, ka) of the flattened line index row*Mh + ka.
 // forward: W1 -> W2 (rows b >= Bin are zero), inverse: W2 -> W1 (only b < Nb kept).
 template<typename R>
-__global__ void pass_b( PassArgs<R> p, int inverse )
+__global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 4 : 2 ) pass_b( PassArgs<R> p, int inverse )
 {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__( 16 ) unsigned char smem_raw[];
     const int4 blk = p.blocks[blockIdx.x];
     const int s    = blk.x;
     if( sys_inactive( p, s ) )
@@ -210,9 +210,9 @@ __global__ void pass_b( PassArgs<R> p, int inverse )
 // block: p.g consecutive columns col = kb*Mh + ka (contiguous in W2 and in Dhat), all 3*nb
 // components (smem line cb*G + g).
 template<typename R>
-__global__ void pass_c( PassArgs<R> p )
+__global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 4 : 2 ) pass_c( PassArgs<R> p )
 {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__( 16 ) unsigned char smem_raw[];
     const int4 blk = p.blocks[blockIdx.x];
     const int s    = blk.x;
     if( sys_inactive( p, s ) )
@@ -312,7 +312,7 @@ __global__ void pass_c( PassArgs<R> p )
 template<typename R>
 __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
 {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__( 16 ) unsigned char smem_raw[];
     const int4 blk = p.blocks[blockIdx.x];
     const int s    = blk.x;
     const FFTDesc & f = p.fd[s];
@@ -409,7 +409,7 @@ template<typename R>
 __global__ void __launch_bounds__( 512, 2 ) pass_bc_cl( PassArgs<R> p, int K )
 {
     namespace cg = cooperative_groups;
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__( 16 ) unsigned char smem_raw[];
     cg::cluster_group cluster = cg::this_cluster();
     const int rank            = (int)cluster.block_rank();
     const int4 blk            = p.blocks[blockIdx.x];
@@ -527,9 +527,9 @@ __global__ void __launch_bounds__( 512, 2 ) pass_bc_cl( PassArgs<R> p, int K )
 // real part is x, the imaginary part y.  The imaginary parts of X and Y at k = 0 and k = Ma/2
 // are dropped, as a real inverse transform does.
 template<typename R>
-__global__ void pass_a_inv( PassArgs<R> p )
+__global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 4 : 2 ) pass_a_inv( PassArgs<R> p )
 {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__( 16 ) unsigned char smem_raw[];
     const int4 blk = p.blocks[blockIdx.x];
     const int s    = blk.x;
     const FFTDesc & f = p.fd[s];

@@ -327,7 +327,7 @@ constexpr int ROW_SPT = 4; // spins per thread the row kernel holds (rows * row 
 template<typename R, int SOLVER, int STAGE>
 __global__ void __launch_bounds__( 256 ) llg_stage_rows( StageArgs<R> A, RowArgs<R> F )
 {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__( 16 ) unsigned char smem_raw[];
     __shared__ PairR<R> pairs[MAX_PAIRS];
     __shared__ SysConst<R> C;
     __shared__ Geo GS;

@@ -488,6 +488,60 @@ __device__ __forceinline__ cplx<R> * sfft_const( cplx<R> * a, cplx<R> * b, int n
     return a;
 }
 
+// Element access of a complex line buffer.  GenBuf: through a generic pointer.  SmemBuf: by the
+// buffer's 32-bit shared-window address with ld/st.shared of two components, for code that is
+// handed generic pointers (a non-inlined function) which it has checked to point into shared
+// memory, element-aligned -- it saves the generic-to-shared conversion and the 64-bit address
+// arithmetic of every access.
+template<typename R>
+struct GenBuf
+{
+    cplx<R> * p;
+    __device__ __forceinline__ cplx<R> ld( int i ) const
+    {
+        return p[i];
+    }
+    __device__ __forceinline__ void st( int i, cplx<R> v ) const
+    {
+        p[i] = v;
+    }
+};
+
+template<typename R>
+struct SmemBuf;
+
+template<>
+struct SmemBuf<float>
+{
+    unsigned int base;
+    __device__ __forceinline__ cplx<float> ld( int i ) const
+    {
+        cplx<float> v;
+        asm volatile( "ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"( v.x ), "=f"( v.y ) : "r"( base + 8u * (unsigned)i ) : "memory" );
+        return v;
+    }
+    __device__ __forceinline__ void st( int i, cplx<float> v ) const
+    {
+        asm volatile( "st.shared.v2.f32 [%0], {%1, %2};" ::"r"( base + 8u * (unsigned)i ), "f"( v.x ), "f"( v.y ) : "memory" );
+    }
+};
+
+template<>
+struct SmemBuf<double>
+{
+    unsigned int base;
+    __device__ __forceinline__ cplx<double> ld( int i ) const
+    {
+        cplx<double> v;
+        asm volatile( "ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"( v.x ), "=d"( v.y ) : "r"( base + 16u * (unsigned)i ) : "memory" );
+        return v;
+    }
+    __device__ __forceinline__ void st( int i, cplx<double> v ) const
+    {
+        asm volatile( "st.shared.v2.f64 [%0], {%1, %2};" ::"r"( base + 16u * (unsigned)i ), "d"( v.x ), "d"( v.y ) : "memory" );
+    }
+};
+
 // Small-radix DFT helpers (the radix-3/5/7 butterflies): sums, differences, scaling by a real,
 // and the rotation by -i (forward) / +i (inverse).
 template<typename R>
@@ -518,9 +572,9 @@ __device__ __forceinline__ cplx<R> crot( cplx<R> u, bool inverse )
 //   y_m = v_0 + sum_k cos(2 pi k m / RR) a_k  -/+  i sum_k sin(2 pi k m / RR) b_k,
 //   y_(RR-m) with the opposite sign of the i term,
 // the cosines and sines read from the twiddle table (W_RR^q = tw[q L/RR]).
-template<typename R, int RR>
-__device__ __forceinline__ void mixed_stage( const cplx<R> * a, cplx<R> * b, int nl, int ls, int es, int LR, int Ns,
-                                             int span, const FastDiv & dlr, const FastDiv & dns, const cplx<R> * tw,
+template<typename R, int RR, typename BUF>
+__device__ __forceinline__ void mixed_stage( const BUF & a, const BUF & b, int nl, int ls, int es, int LR, int Ns,
+                                             int span, const FastDiv & dlr, const FastDiv & dns, const BUF & tw,
                                              bool inverse )
 {
     constexpr int NH = ( RR - 1 ) / 2;
@@ -528,29 +582,30 @@ __device__ __forceinline__ void mixed_stage( const cplx<R> * a, cplx<R> * b, int
 #pragma unroll
     for( int q = 1; q <= NH; ++q )
     {
-        const cplx<R> w = tw[q * LR];
+        const cplx<R> w = tw.ld( q * LR );
         cs[q]           = w.x;
         sn[q]           = -w.y;
     }
+    const int lres = LR * es, nses = Ns * es;
     for( int idx = threadIdx.x; idx < nl * LR; idx += blockDim.x )
     {
-        const int line      = (int)fdiv( (unsigned)idx, dlr );
-        const int j         = idx - line * LR;
-        const int jq        = (int)fdiv( (unsigned)j, dns );
-        const int k         = j - jq * Ns;
-        const cplx<R> * src = a + line * ls;
-        cplx<R> * dst       = b + line * ls;
+        const int line = (int)fdiv( (unsigned)idx, dlr );
+        const int j    = idx - line * LR;
+        const int jq   = (int)fdiv( (unsigned)j, dns );
+        const int k    = j - jq * Ns;
+        const int s0   = line * ls + j * es;                   // input r at s0 + r L/RR
+        const int d0   = line * ls + ( jq * Ns * RR + k ) * es; // output m at d0 + m Ns
+        const int ks   = k * span;
         cplx<R> v[RR];
-        v[0] = src[j * es];
+        v[0] = a.ld( s0 );
 #pragma unroll
         for( int r = 1; r < RR; ++r )
         {
-            cplx<R> w = tw[r * k * span];
+            cplx<R> w = tw.ld( r * ks );
             if( inverse )
                 w = cconj( w );
-            v[r] = cmul( src[( j + r * LR ) * es], w );
+            v[r] = cmul( a.ld( s0 + r * lres ), w );
         }
-        const int d0 = jq * Ns * RR + k;
         cplx<R> y[RR];
         if( RR == 2 )
         {
@@ -597,26 +652,24 @@ __device__ __forceinline__ void mixed_stage( const cplx<R> * a, cplx<R> * b, int
         }
 #pragma unroll
         for( int m = 0; m < RR; ++m )
-            dst[( d0 + m * Ns ) * es] = y[m];
+            b.st( d0 + m * nses, y[m] );
     }
 }
 
-// Mixed-radix (any L) strided Stockham over the radix plan P: radices 2, 3, 4, 5, 7 (all that the
-// padded extents produce) with closed-form compile-time butterflies and the stage divisors
-// precomputed on the host; other radices <= 8 by a runtime-radix loop; larger prime factors one
-// output per thread.
-// Consecutive threads take consecutive butterflies of a line.  Not inlined: one copy serves every
-// call site of a kernel.
-template<typename R>
-__device__ __noinline__ cplx<R> * mixed_fft( cplx<R> * a, cplx<R> * b, int L, int nl, int ls, int es,
-                                             const RadixPlan & P, const cplx<R> * tw, bool inverse )
+// The stages of mixed_fft from buffer a into b (ping-pong); returns true when the result is in a.
+template<typename R, typename BUF>
+__device__ __forceinline__ bool mixed_stages( const BUF & A0, const BUF & B0, int L, int nl, int ls, int es,
+                                              const RadixPlan & P, const BUF & tw, bool inverse )
 {
-    int Ns = 1;
+    int Ns    = 1;
+    bool in_a = true;
     for( int s = 0; s < 12 && P.radix[s] > 0; ++s )
     {
-        const int Rr   = P.radix[s];
-        const int LR   = L / Rr;
-        const int span = L / ( Ns * Rr );
+        const BUF & a     = in_a ? A0 : B0;
+        const BUF & b     = in_a ? B0 : A0;
+        const int Rr      = P.radix[s];
+        const int LR      = L / Rr;
+        const int span    = L / ( Ns * Rr );
         const FastDiv dlr = P.div_lr[s], dns = P.div_ns[s];
         switch( Rr )
         {
@@ -636,78 +689,64 @@ __device__ __noinline__ cplx<R> * mixed_fft( cplx<R> * a, cplx<R> * b, int L, in
             mixed_stage<R, 7>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
             break;
         default:
-            if( Rr <= 8 )
+            // other radices (not produced by the padded extents): runtime-radix direct sums
+            for( int o = threadIdx.x; o < nl * L; o += blockDim.x )
             {
-                for( int idx = threadIdx.x; idx < nl * LR; idx += blockDim.x )
+                const int line = o / L;
+                const int q    = o - line * L;
+                const int k    = q % Ns;
+                const int m    = ( q / Ns ) % Rr;
+                const int jhi  = q / ( Ns * Rr );
+                const int j    = jhi * Ns + k;
+                cplx<R> acc    = { 0, 0 };
+                for( int r = 0; r < Rr; ++r )
                 {
-                    const int line      = idx / LR;
-                    const int j         = idx - line * LR;
-                    const cplx<R> * src = a + line * ls;
-                    cplx<R> * dst       = b + line * ls;
-                    const int k         = j % Ns;
-                    cplx<R> v[8];
-#pragma unroll
-                    for( int r = 0; r < 8; ++r )
-                    {
-                        if( r < Rr )
-                        {
-                            cplx<R> w = tw[r * k * span];
-                            if( inverse )
-                                w = cconj( w );
-                            v[r] = r == 0 ? src[j * es] : cmul( src[( j + r * LR ) * es], w );
-                        }
-                    }
-                    const int d0 = ( j / Ns ) * Ns * Rr + k;
-                    for( int m = 0; m < Rr; ++m )
-                    {
-                        cplx<R> acc = v[0];
-                        for( int r = 1; r < Rr; ++r )
-                        {
-                            cplx<R> w = tw[( ( r * m ) % Rr ) * LR];
-                            if( inverse )
-                                w = cconj( w );
-                            cplx<R> t = cmul( v[r], w );
-                            acc.x += t.x;
-                            acc.y += t.y;
-                        }
-                        dst[( d0 + m * Ns ) * es] = acc;
-                    }
+                    const int t = ( r * k * span + ( ( r * m ) % Rr ) * LR ) % L;
+                    cplx<R> w   = tw.ld( t );
+                    if( inverse )
+                        w = cconj( w );
+                    const cplx<R> p = cmul( a.ld( line * ls + ( j + r * LR ) * es ), w );
+                    acc.x += p.x;
+                    acc.y += p.y;
                 }
-            }
-            else
-            {
-                for( int o = threadIdx.x; o < nl * L; o += blockDim.x )
-                {
-                    const int line      = o / L;
-                    const int q         = o - line * L;
-                    const cplx<R> * src = a + line * ls;
-                    const int k         = q % Ns;
-                    const int m         = ( q / Ns ) % Rr;
-                    const int jhi       = q / ( Ns * Rr );
-                    const int j         = jhi * Ns + k;
-                    cplx<R> acc         = { 0, 0 };
-                    for( int r = 0; r < Rr; ++r )
-                    {
-                        const int t = ( r * k * span + ( ( r * m ) % Rr ) * LR ) % L;
-                        cplx<R> w   = tw[t];
-                        if( inverse )
-                            w = cconj( w );
-                        const cplx<R> p = cmul( src[( j + r * LR ) * es], w );
-                        acc.x += p.x;
-                        acc.y += p.y;
-                    }
-                    b[line * ls + q * es] = acc;
-                }
+                b.st( line * ls + q * es, acc );
             }
             break;
         }
         __syncthreads();
-        cplx<R> * t = a;
-        a           = b;
-        b           = t;
+        in_a = !in_a;
         Ns *= Rr;
     }
-    return a;
+    return in_a;
+}
+
+// Mixed-radix (any L) strided Stockham: element t of line l at l*ls + t*es, ping-pong between a
+// and b; returns the buffer that holds the result.  Radices 2, 3, 4, 5, 7 (all that the padded
+// extents produce) with closed-form compile-time butterflies and the stage divisors precomputed
+// on the host (RadixPlan); others by runtime-radix direct sums.  Consecutive threads take
+// consecutive butterflies of a line.  Not inlined (one copy serves every call site of a kernel):
+// the buffers arrive as generic pointers and are accessed through the shared window when all three
+// point into shared memory, element-aligned (every caller's do).
+template<typename R>
+__device__ __noinline__ cplx<R> * mixed_fft( cplx<R> * a, cplx<R> * b, int L, int nl, int ls, int es,
+                                             const RadixPlan & P, const cplx<R> * tw, bool inverse )
+{
+    constexpr unsigned int EL = sizeof( cplx<R> );
+    bool in_a;
+    if( __isShared( a ) && __isShared( b ) && __isShared( tw ) )
+    {
+        const unsigned int sa = (unsigned int)__cvta_generic_to_shared( a );
+        const unsigned int sb = (unsigned int)__cvta_generic_to_shared( b );
+        const unsigned int st = (unsigned int)__cvta_generic_to_shared( tw );
+        if( ( ( sa | sb | st ) & ( EL - 1 ) ) == 0 )
+        {
+            in_a = mixed_stages<R>( SmemBuf<R>{ sa }, SmemBuf<R>{ sb }, L, nl, ls, es, P, SmemBuf<R>{ st }, inverse );
+            return in_a ? a : b;
+        }
+    }
+    in_a = mixed_stages<R>( GenBuf<R>{ a }, GenBuf<R>{ b }, L, nl, ls, es, P, GenBuf<R>{ const_cast<cplx<R> *>( tw ) },
+                            inverse );
+    return in_a ? a : b;
 }
 
 template<typename R, bool LINE_FAST, int MAXLG = MaxRadix<R>::LG>
