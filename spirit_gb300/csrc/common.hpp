@@ -201,6 +201,9 @@ struct FFTDesc
     FastDiv div_Nb, div_Nc, div_nb;
     FastDiv div_plane; // 3 nb Mb: elements of one c-row of the fused b/c pass
     FastDiv div_crow;  // 3 nb Mb / K: one c-row of a block of the clustered b/c pass
+    // index divisors of the single-block fused b/c pass (set with the tiles): 3 nb Nc Nb (one
+    // input plane), nb Mc Mb (tensor points of one plane)
+    FastDiv div_nin, div_tens;
 };
 
 template<>

@@ -342,7 +342,7 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
     cplx<R> * W1     = p.W1 + f.spec_offset + (size_t)ka * nin;
     for( int e = threadIdx.x; e < G * nin; e += blockDim.x )
     {
-        const int g = e / nin, el = e - g * nin;
+        const int g = (int)fdiv( (unsigned)e, f.div_nin ), el = e - g * nin;
         const int row = (int)fdiv( (unsigned)el, f.div_Nb ), b = el - row * Nb;
         const int cb  = (int)fdiv( (unsigned)row, f.div_Nc ), c = row - cb * Nc;
         A[g * vol + c * plane + cb * Mb + b] = W1[e];
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
     const int npair    = nb * nb;
     for( int e = threadIdx.x; e < G * nb * Mc * Mb; e += blockDim.x )
     {
-        const int g = e / ( nb * Mc * Mb ), eg = e - g * ( nb * Mc * Mb );
+        const int g = (int)fdiv( (unsigned)e, f.div_tens ), eg = e - g * ( nb * Mc * Mb );
         const cplx<R> * Dh = p.Dhat + f.dhat_offset + (size_t)( ka + g ) * npair * 6 * Mc * Mb;
         const int rest = (int)fdiv( (unsigned)eg, f.div_Mb ), kb = eg - rest * Mb;
         const int kc   = (int)fdiv( (unsigned)rest, f.div_nb ), b1 = rest - kc * nb;
@@ -392,7 +392,7 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
     r = sfft<R, false>( r, o, Mb, G * Nc * ncb, none, Mb, 1, f.plan[1], twb, true );
     for( int e = threadIdx.x; e < G * nin; e += blockDim.x )
     {
-        const int g = e / nin, el = e - g * nin;
+        const int g = (int)fdiv( (unsigned)e, f.div_nin ), el = e - g * nin;
         const int row = (int)fdiv( (unsigned)el, f.div_Nb ), b = el - row * Nb;
         const int cb  = (int)fdiv( (unsigned)row, f.div_Nc ), c = row - cb * Nc;
         W1[e]         = r[g * vol + c * plane + cb * Mb + b];
@@ -858,7 +858,10 @@ void DDIPlan::set_tiles( int nl_a, int g_b, int g_c )
                     tbc.push_back( make_int4( sys_index[k], ka, r, std::min( G, fd_host[k].Mh - ka ) ) );
             smem_bc_max = std::max( smem_bc_max, cluster_k == 1 ? smem_bc( elem, fd_host[k], G )
                                                                 : smem_bcl( elem, fd_host[k], cluster_k ) );
-            fd_host[k].div_crow = make_fastdiv( 3 * fd_host[k].nb * fd_host[k].M[1] / cluster_k );
+            FFTDesc & g   = fd_host[k];
+            g.div_crow    = make_fastdiv( 3 * g.nb * g.M[1] / cluster_k );
+            g.div_nin     = make_fastdiv( 3 * g.nb * g.N[2] * g.N[1] );
+            g.div_tens    = make_fastdiv( g.nb * g.M[2] * g.M[1] );
         }
         // FFTDesc table indexed by the batch's system index
         std::vector<FFTDesc> by_sys( n_fd_slots );
