@@ -1,0 +1,68 @@
+"""Dipolar field on padded extents with radix 3, 5 and 7 stages (the mixed-radix Stockham path
+of the FFT passes), on one-row (2D: the single-block b/c pass, several ka planes per block) and
+3D layouts, against the FP64 oracle.
+
+Extents (the zero-padded axes are 2N, 7-smooth here, so the oracle's padding is the same):
+  open 7 x 21 x 1    -> 14 x 42      (2*7, 2*3*7)
+  open 15 x 10 x 1   -> 30 x 20      (2*3*5, 4*5)
+  open 5 x 7 x 9     -> 10 x 14 x 18 (2*5, 2*7, 2*3*3)
+  periodic 12 x 9 x 3, no padding -> 12 x 9 x 3 (4*3, 3*3, 3)
+
+Tolerances: FP64 gradient 1e-12 relative to max |g| (as the golden gradient cases); FP32 RK4
+trajectory of 20 steps max |dm| <= 1e-5 against the FP64 oracle (the metric's bar).
+"""
+import numpy as np
+import pytest
+
+from helpers import make_state, spins_of
+
+pytestmark = pytest.mark.gpu
+
+_OPEN = dict(bravais="sc", lattice_constant=1.0, mu_s=[2.0], bc=[0, 0, 0], field=(0.8, (0, 0, 1)),
+             anisotropy=(0.1, (0, 0, 1)), jij=[1.0], dij=[0.3], dm_chirality=2,
+             ddi=dict(method="fft", n_periodic_images=[0, 0, 0], radius=0.0, pb_zero_padding=1),
+             llg=dict(dt=1e-3, damping=0.3, temperature=0.0))
+
+CASES = {
+    "open2d_7x21": dict(_OPEN, n_cells=[7, 21, 1]),
+    "open2d_15x10": dict(_OPEN, n_cells=[15, 10, 1]),
+    "open3d_5x7x9": dict(_OPEN, n_cells=[5, 7, 9], lattice_constant=3.0),
+    "periodic_12x9x3": dict(_OPEN, n_cells=[12, 9, 3], bc=[1, 1, 1], lattice_constant=2.5,
+                            ddi=dict(method="fft", n_periodic_images=[1, 1, 1], radius=0.0, pb_zero_padding=0)),
+}
+
+
+def _spins(spec, seed):
+    from oracle.oracle import random_spins
+
+    n = spec["n_cells"][0] * spec["n_cells"][1] * spec["n_cells"][2]
+    return random_spins(n, seed)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_ddi_gradient_mixed_radix_fp64(name):
+    from oracle.oracle import OracleSystem
+    from spirit_gb300 import hamiltonian
+
+    spec = CASES[name]
+    s = _spins(spec, 31)
+    ref, E_ref = OracleSystem(spec).gradient_and_energy(s)
+    with make_state(spec, s, name="radix_" + name) as p:
+        g, E = hamiltonian.get_gradient(p)
+    scale = np.abs(ref).max()
+    np.testing.assert_allclose(g, ref, rtol=0, atol=1e-12 * scale)
+    assert abs(E - E_ref) <= 1e-10 * abs(E_ref)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_ddi_rk4_mixed_radix_fp32(name):
+    from oracle.oracle import OracleSystem
+    from spirit_gb300 import simulation
+
+    spec = CASES[name]
+    s0 = _spins(spec, 32)
+    ref, _ = OracleSystem(spec).llg(s0, "RK4", 20, dt=1e-3, damping=0.3)
+    with make_state(spec, s0, precision=32, name="radix32_" + name) as p:
+        simulation.start(p, simulation.METHOD_LLG, simulation.SOLVER_RK4, 20)
+        s = spins_of(p)
+    assert np.abs(s - ref).max() <= 1e-5
