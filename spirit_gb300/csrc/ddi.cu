@@ -405,7 +405,37 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
 // range [r kq, (r + 1) kq) (kq = Mb / K) for every c (Mc rows, rows >= Nc zero), layout
 // [c][cb][kb_local].  The two transposes between the phases go through distributed shared memory.
 // Block table: (system, ka, rank, 0), the K blocks of a plane consecutive.
-template<typename R>
+// Index splits of the clustered b/c pass.  POW2: Mb / K and ceil(Nc / K) are powers of two, Nc is
+// a multiple of ceil(Nc / K) (every block of a plane that has c rows has ceil(Nc / K) of them) and
+// the basis has one atom -- shifts and a division by the literal 3; the host checks this for every
+// system of the plan.  Otherwise run-time divisions.
+template<bool POW2>
+struct ClusterSplit
+{
+    int kq, cq, nc, ncb, nb, lkq, lcq;
+    __device__ __forceinline__ int by_kq( int n ) const
+    {
+        return POW2 ? n >> lkq : n / kq;
+    }
+    __device__ __forceinline__ int by_cq( int n ) const
+    {
+        return POW2 ? n >> lcq : n / cq;
+    }
+    __device__ __forceinline__ int by_nc( int n ) const // blocks with c rows only (nc > 0)
+    {
+        return POW2 ? n >> lcq : n / nc;
+    }
+    __device__ __forceinline__ int by_ncb( int n ) const
+    {
+        return POW2 ? n / 3 : n / ncb;
+    }
+    __device__ __forceinline__ int by_nb( int n ) const
+    {
+        return POW2 ? n : n / nb;
+    }
+};
+
+template<typename R, bool POW2>
 __global__ void __launch_bounds__( 512, 2 ) pass_bc_cl( PassArgs<R> p, int K )
 {
     namespace cg = cooperative_groups;
@@ -427,6 +457,7 @@ __global__ void __launch_bounds__( 512, 2 ) pass_bc_cl( PassArgs<R> p, int K )
     const int lb  = cq * ncb * Mb;  // b-phase buffer
     const int lc  = Mc * ncb * kq;  // c-phase buffer
     const int crow = ncb * kq;      // elements of one c-row in the c-phase
+    const ClusterSplit<POW2> sp{ kq, cq, nc, ncb, nb, __ffs( kq ) - 1, __ffs( cq ) - 1 };
     cplx<R> * twb = reinterpret_cast<cplx<R> *>( smem_raw );
     cplx<R> * twc = twb + Mb;
     cplx<R> * Bb0 = twc + Mc;
@@ -449,7 +480,7 @@ __global__ void __launch_bounds__( 512, 2 ) pass_bc_cl( PassArgs<R> p, int K )
     for( int e = threadIdx.x; e < ncb * nc * Nb; e += blockDim.x )
     {
         const int rest = (int)fdiv( (unsigned)e, f.div_Nb ), b = e - rest * Nb;
-        const int cb = rest / nc, cl = rest - cb * nc;
+        const int cb = sp.by_nc( rest ), cl = rest - cb * nc;
         Bb0[( cl * ncb + cb ) * Mb + b] = W1[( (size_t)cb * Nc + c0 + cl ) * Nb + b];
     }
     // every block's c-phase buffer is zero before any block writes into it
@@ -460,8 +491,8 @@ __global__ void __launch_bounds__( 512, 2 ) pass_bc_cl( PassArgs<R> p, int K )
     for( int e = threadIdx.x; e < nc * ncb * Mb; e += blockDim.x )
     {
         const int l = (int)fdiv( (unsigned)e, f.div_Mb ), kb = e - l * Mb;
-        const int cl = l / ncb, cb = l - cl * ncb;
-        const int d = kb / kq, kbl = kb - d * kq;
+        const int cl = sp.by_ncb( l ), cb = l - cl * ncb;
+        const int d = sp.by_kq( kb ), kbl = kb - d * kq;
         cplx<R> * dst = cluster.map_shared_rank( Bc0, d );
         dst[( c0 + cl ) * crow + cb * kq + kbl] = r[l * Mb + kb];
     }
@@ -474,8 +505,8 @@ __global__ void __launch_bounds__( 512, 2 ) pass_bc_cl( PassArgs<R> p, int K )
     const cplx<R> * Dh = p.Dhat + f.dhat_offset + (size_t)ka * npair * 6 * Mc * Mb;
     for( int e = threadIdx.x; e < nb * Mc * kq; e += blockDim.x )
     {
-        const int rest = e / kq, kbl = e - rest * kq;
-        const int kc = rest / nb, b1 = rest - kc * nb;
+        const int rest = sp.by_kq( e ), kbl = e - rest * kq;
+        const int kc = sp.by_nb( rest ), b1 = rest - kc * nb;
         const cplx<R> * S = r + kc * crow + kbl;
         cplx<R> acc[3]    = { { 0, 0 }, { 0, 0 }, { 0, 0 } };
         for( int b2 = 0; b2 < nb; ++b2 )
@@ -506,9 +537,9 @@ __global__ void __launch_bounds__( 512, 2 ) pass_bc_cl( PassArgs<R> p, int K )
     // transpose 2: rows c < Nc of the kb range -> owner of row c (its b-phase buffers are free)
     for( int e = threadIdx.x; e < Nc * ncb * kq; e += blockDim.x )
     {
-        const int l = e / kq, kbl = e - l * kq;
-        const int c = l / ncb, cb = l - c * ncb;
-        const int d = c / cq, cl = c - d * cq;
+        const int l = sp.by_kq( e ), kbl = e - l * kq;
+        const int c = sp.by_ncb( l ), cb = l - c * ncb;
+        const int d = sp.by_cq( c ), cl = c - d * cq;
         cplx<R> * dst = cluster.map_shared_rank( Bb0, d );
         dst[( cl * ncb + cb ) * Mb + kb0 + kbl] = r[c * crow + cb * kq + kbl];
     }
@@ -517,7 +548,7 @@ __global__ void __launch_bounds__( 512, 2 ) pass_bc_cl( PassArgs<R> p, int K )
     for( int e = threadIdx.x; e < ncb * nc * Nb; e += blockDim.x )
     {
         const int rest = (int)fdiv( (unsigned)e, f.div_Nb ), b = e - rest * Nb;
-        const int cb = rest / nc, cl = rest - cb * nc;
+        const int cb = sp.by_nc( rest ), cl = rest - cb * nc;
         W1[( (size_t)cb * Nc + c0 + cl ) * Nb + b] = r[( cl * ncb + cb ) * Mb + b];
     }
 }
@@ -847,6 +878,7 @@ void DDIPlan::set_tiles( int nl_a, int g_b, int g_c )
     upload_table( d_blocks[2], n_blocks[2], tc );
     std::vector<int4> tbc;
     smem_bc_max = 0;
+    bool pow2   = true;
     if( fused )
     {
         for( size_t k = 0; k < fd_host.size(); ++k )
@@ -860,6 +892,9 @@ void DDIPlan::set_tiles( int nl_a, int g_b, int g_c )
                                                                 : smem_bcl( elem, fd_host[k], cluster_k ) );
             FFTDesc & g   = fd_host[k];
             g.div_crow    = make_fastdiv( 3 * g.nb * g.M[1] / cluster_k );
+            const int kq  = g.M[1] / cluster_k, cq = ( g.N[2] + cluster_k - 1 ) / cluster_k;
+            pow2          = pow2 && g.nb == 1 && ( kq & ( kq - 1 ) ) == 0 && ( cq & ( cq - 1 ) ) == 0
+                   && g.N[2] % cq == 0;
             g.div_nin     = make_fastdiv( 3 * g.nb * g.N[2] * g.N[1] );
             g.div_tens    = make_fastdiv( g.nb * g.M[2] * g.M[1] );
         }
@@ -870,6 +905,7 @@ void DDIPlan::set_tiles( int nl_a, int g_b, int g_c )
         h2d( d_fd, by_sys.data(), by_sys.size() );
     }
     upload_table( d_blocks[3], n_blocks[3], tbc );
+    bc_pow2 = fused && cluster_k > 1 && pow2;
     tile[0] = nl_a;
     tile[1] = g_b;
     tile[2] = g_c;
@@ -929,7 +965,8 @@ static void set_smem_limits()
     CUDA_CHECK( cudaFuncSetAttribute( pass_c<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024 ) );
     CUDA_CHECK( cudaFuncSetAttribute( pass_a_inv<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024 ) );
     CUDA_CHECK( cudaFuncSetAttribute( pass_bc<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_optin() ) );
-    CUDA_CHECK( cudaFuncSetAttribute( pass_bc_cl<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_optin() ) );
+    CUDA_CHECK( cudaFuncSetAttribute( pass_bc_cl<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_optin() ) );
+    CUDA_CHECK( cudaFuncSetAttribute( pass_bc_cl<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_optin() ) );
     done = true;
 }
 
@@ -1143,7 +1180,8 @@ void DDIPlan::launch_pass( int k, PassArgs<R> & a, cudaStream_t stream ) const
         if( cluster_k == 1 )
             launch_pdl( pass_bc<R>, dim3( n_blocks[3] ), dim3( threads_bc ), smem_bc_max, stream, 1, a );
         else
-            launch_pdl( pass_bc_cl<R>, dim3( n_blocks[3] ), dim3( std::min( threads_bc, 512 ) ), smem_bc_max, stream,
+            launch_pdl( bc_pow2 ? pass_bc_cl<R, true> : pass_bc_cl<R, false>, dim3( n_blocks[3] ),
+                        dim3( std::min( threads_bc, 512 ) ), smem_bc_max, stream,
                         cluster_k, a, cluster_k );
         break;
     default:

@@ -63,6 +63,7 @@ public:
     int threads_bc     = 1024;
     int cluster_k      = 1; // blocks per (system, ka) plane of the fused pass (cluster size)
     int planes_bc      = 1; // ka planes per block of the single-block fused pass on one-row (2D) systems
+    bool bc_pow2       = false; // every system's cluster index splits are powers of two (pass_bc_cl<R, true>)
     int n_fd_slots     = 1;
     size_t smem_bc_max = 0;
     size_t max_smem_a = 0, max_smem_b = 0, max_smem_c = 0;

@@ -66,3 +66,28 @@ def test_ddi_rk4_mixed_radix_fp32(name):
         simulation.start(p, simulation.METHOD_LLG, simulation.SOLVER_RK4, 20)
         s = spins_of(p)
     assert np.abs(s - ref).max() <= 1e-5
+
+
+@pytest.mark.parametrize("n_cells", [[16, 16, 8], [12, 12, 6]])
+def test_cluster_split_bitwise(n_cells, monkeypatch):
+    """The fused b/c pass on one block per plane (K = 1) and split over clusters of K = 2, 4, 8
+    blocks gives the same FP32 Heun trajectory bit for bit: 16 x 16 x 8 (z-padded to 16) takes the
+    power-of-two index splits, 12 x 12 x 6 (Mb / K = 6, 3) the run-time divisions; shapes the plan
+    cannot take (K > Nc) fall back to the tuned one.  The trajectory matches the FP64 oracle."""
+    from cases import SC3D_DDI
+    from oracle.oracle import OracleSystem, random_spins
+    from spirit_gb300 import simulation
+
+    spec = dict(SC3D_DDI, n_cells=n_cells, llg=dict(dt=5e-4, damping=0.1, temperature=0.0))
+    n = n_cells[0] * n_cells[1] * n_cells[2]
+    s0 = random_spins(n, 41)
+    out = []
+    for K in (1, 2, 4, 8):
+        monkeypatch.setenv("SPIRIT_GB300_BC", "%d,512" % K)
+        with make_state(spec, s0, precision=32, name="bc%d_%d" % (K, n)) as p:
+            simulation.start(p, simulation.METHOD_LLG, simulation.SOLVER_HEUN, 20)
+            out.append(spins_of(p))
+    for o in out[1:]:
+        np.testing.assert_array_equal(o, out[0])
+    ref, _ = OracleSystem(spec).llg(s0, "Heun", 20, dt=5e-4, damping=0.1)
+    assert np.abs(out[0] - ref).max() <= 1e-5
