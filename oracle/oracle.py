@@ -1,6 +1,6 @@
 """ctypes front-end of the oracle (oracle/spirit_oracle.c).
 
-TEST INFRASTRUCTURE ONLY: the oracle is the checker.  tests/, __graft_entry__.smoke() and
+TEST INFRASTRUCTURE ONLY: results are compared against it.  tests/, __graft_entry__.smoke() and
 bench.py's CPU-baseline leg import this module; the product package never does.
 
 The oracle is a CPU FP64 restatement of the reference's hot path (Spirit v2.2.0:

@@ -1,7 +1,7 @@
 /*
  * spirit_oracle.h -- CPU FP64 restatement of the reference's spin-dynamics hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: the parity tests, the smoke
+ * TEST INFRASTRUCTURE ONLY.  Results are compared against this library: the parity tests, the smoke
  * check and the CPU-baseline leg of the benchmark call it.  The product (libspirit_gb300)
  * never links, loads or calls it.
  *

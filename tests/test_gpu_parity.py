@@ -2,7 +2,7 @@
 
 Golden fixtures come from the reference itself (tests/golden/make_golden.py); where a case
 needs inputs the fixtures do not hold (thermal noise, other sizes) the oracle -- the CPU FP64
-restatement pinned by tests/test_oracle_golden.py -- is the checker.
+restatement pinned by tests/test_oracle_golden.py -- is what the device results are compared with.
 
 Tolerances:
   FP64 device path: gradients 1e-12 relative to max |g|, energies 1e-10 relative,
