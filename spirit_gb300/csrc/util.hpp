@@ -54,7 +54,7 @@ inline void dfree( T *& p )
 }
 
 // Page-locked registration of a host buffer that outlives many transfers (an image's AoS spin
-// mirror): the copy engines then move it directly, without the driver's staging through a pinned
+// mirror): the copy engines then move it directly, without the CUDA driver's staging through a pinned
 // bounce buffer.  ensure() re-registers when the buffer has moved, release() before it is
 // reallocated.  SPIRIT_GB300_PIN=0 leaves buffers pageable; a failed registration leaves the
 // buffer pageable.
