@@ -77,10 +77,26 @@ def algorithmic_bytes(kernel, stage, rows=False):
     }[kernel]
 
 
-# DRAM bytes (read + write) per launch of the b/c pass on this workload from one ncu capture
-# (dram__bytes_read.sum 16.09 MB, dram__bytes_write.sum 0; pass_bc_cl inside a warm-up step):
-# below the 19.2 MB of algorithmic bytes because the spectrum written by pass A is still in L2
-DOMINANT_TRAFFIC = {"fft_pass_bc_tensor": 16092928}
+# DRAM bytes (read + write) per launch of the dominant kernels on this workload, from the committed
+# summaries of one ncu capture each (profiles/<file>: a line "dram_bytes_per_launch: N")
+TRAFFIC_PROFILES = {"fft_pass_bc_tensor": "fft_pass_bc_cl_sc128x128x16_dram.md",
+                    "stage": "llg_stage_heun_sc128x128x16_dram.md"}
+
+
+def profiled_traffic(kernel):
+    """dram__bytes_read.sum + dram__bytes_write.sum per launch of `kernel` from its profile summary
+    under profiles/, or None when there is none."""
+    name = TRAFFIC_PROFILES.get(kernel)
+    if not name:
+        return None
+    try:
+        with open(os.path.join(ROOT, "profiles", name)) as f:
+            for line in f:
+                if line.strip().startswith("dram_bytes_per_launch:"):
+                    return int(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
 
 
 def measured_peaks():
@@ -182,6 +198,66 @@ def cpu_baseline(seconds=12.0):
     dt = time.perf_counter() - t0
     return {"value": NOS * n / dt, "unit": "spin-updates/s", "cores": os.cpu_count(), "kind": "port",
             "sample": "%d stochastic Heun steps of the full 128x128x16 DDI system (FP64, OpenMP)" % n}
+
+
+def c2_accuracy(steps=200):
+    """Accuracy of the headline workload: the device FP32 path and the FP64 oracle run `steps`
+    stochastic Heun steps of the full 128x128x16 dipolar system from the same seeded spins,
+    drawing the same Philox stream (seed 2, stream 0); max |dm| over all spins.  Outside the
+    timed region."""
+    from oracle.oracle import OracleSystem, random_spins
+    from spirit_gb300 import simulation, state, system
+    from spirit_gb300.configs import write_config
+
+    s0 = random_spins(NOS, 1)
+    p = state.setup(write_config(SPEC, os.path.join(tempfile.mkdtemp(), "acc.cfg")), True)
+    system.get_spin_directions(p)[:] = s0
+    simulation.set_precision(p, 32)
+    simulation.start(p, simulation.METHOD_LLG, simulation.SOLVER_HEUN, steps)
+    got = np.array(system.get_spin_directions(p))
+    state.delete(p)
+    ref, _ = OracleSystem(SPEC).llg(s0, "Heun", steps, dt=5e-4, damping=0.1, temperature=10.0, seed=2, stream=0)
+    return {"steps": steps, "max_dm_vs_fp64_oracle": float(np.abs(got - ref).max()),
+            "check": "headline workload (T=10 K, same Philox stream), FP32 device vs FP64 oracle"}
+
+
+def cufft_comparison(ddi_ms_per_eval, iters=30):
+    """Timing yardstick for the hand-written dipolar passes (timing only, never a product path):
+    the same field evaluation of the headline system -- R2C of mu*s on the zero-padded 128x128x32
+    volume, the 6-component symmetric tensor product, C2R -- with cuFFT through torch.fft (3 batched
+    transforms each way) and the product as torch elementwise ops, FP32, L2 flushed before every
+    evaluation, CUDA events.  The hand-written path is passes A, b/c (transforms along b and c and
+    the product fused) and A' per evaluation, from the per-kernel profile."""
+    import torch
+
+    Na, Nb, Nc, Mc = 128, 128, 16, 32
+    g = torch.Generator(device="cuda").manual_seed(3)
+    x = torch.randn(3, Nc, Nb, Na, device="cuda", generator=g)
+    Dh = torch.randn(6, Mc, Nb, Na // 2 + 1, 2, device="cuda", generator=g)
+    Dh = torch.view_as_complex(Dh)
+    flush = torch.empty(512 * 2**20, dtype=torch.uint8, device="cuda")
+    t_fft, t_all = [], []
+    for it in range(iters + 3):
+        flush.fill_(it & 0xFF)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        e[0].record()
+        X = torch.fft.rfftn(x, s=(Mc, Nb, Na), dim=(1, 2, 3))
+        e[1].record()
+        H = torch.stack([Dh[0] * X[0] + Dh[1] * X[1] + Dh[2] * X[2],
+                         Dh[1] * X[0] + Dh[3] * X[1] + Dh[4] * X[2],
+                         Dh[2] * X[0] + Dh[4] * X[1] + Dh[5] * X[2]])
+        e[2].record()
+        h = torch.fft.irfftn(H, s=(Mc, Nb, Na), dim=(1, 2, 3))[:, :Nc]
+        e[3].record()
+        torch.cuda.synchronize()
+        if it >= 3:
+            t_fft.append(e[0].elapsed_time(e[1]) + e[2].elapsed_time(e[3]))
+            t_all.append(e[0].elapsed_time(e[3]))
+    del h
+    return {"cufft_transforms_ms": statistics.median(t_fft), "cufft_with_torch_product_ms": statistics.median(t_all),
+            "handwritten_ms": ddi_ms_per_eval,
+            "handwritten_vs_cufft_transforms": statistics.median(t_fft) / ddi_ms_per_eval if ddi_ms_per_eval else None,
+            "what": "one dipolar field evaluation of the 128x128x16 system (padded 128x128x32), FP32"}
 
 
 def run_reference(args):
@@ -346,6 +422,14 @@ def run_batched_vs_plain(steps, warmup, plain=True, check=True, ddi=False, profi
         "max_dm_vs_fp64_oracle": dm,
         "accuracy_check": "8 smallest systems, 1000 batched FP32 steps vs the FP64 oracle on the same Philox streams",
     }
+
+
+def compact_batched(v):
+    """The batched-vs-plain figures the metric names, in a few keys (the end of the JSON line)."""
+    return {"ratio": v["ratio_batched_vs_plain"], "batched_value": v["value"], "plain_value": v["plain_value"],
+            "unit": v["unit"], "ms_per_step": v["ms_per_step"], "plain_ms_per_step": v["plain_ms_per_step"],
+            "n_systems": v["n_systems"], "n_spins": v["n_spins"], "steps": v["steps"],
+            "max_dm_vs_fp64_oracle": v["max_dm_vs_fp64_oracle"], "accuracy_steps": 1000}
 
 
 C3_SPEC = dict(bravais="hex2d60", n_cells=[96, 96, 1], lattice_constant=1.0, mu_s=[2.0], bc=[1, 1, 0],
@@ -693,6 +777,12 @@ def run_gb300(args):
     e2e_s = time.perf_counter() - t0
     simulation.stop(p)
     state.delete(p)
+    ddi_ms = None
+    if all(k in per for k in ("fft_pass_a", "fft_pass_a_inv_c2r")) and per["fft_pass_a"][1] > 0:
+        ddi_ms = sum(per[k][0] for k in ("fft_pass_a", "fft_pass_b", "fft_pass_c_tensor", "fft_pass_b_inv",
+                                          "fft_pass_a_inv_c2r", "fft_pass_bc_tensor") if k in per) / per["fft_pass_a"][1]
+    cufft = cufft_comparison(ddi_ms) if rank == 0 and args.cufft else None
+    accuracy = c2_accuracy() if rank == 0 and args.accuracy else None
     batched = run_batched_vs_plain(max(20, args.steps), max(3, args.warmup)) if args.batched else None
     batched_ddi = (run_batched_vs_plain(max(20, args.steps), max(3, args.warmup), ddi=True)
                    if args.batched and args.batched_ddi else None)
@@ -712,17 +802,19 @@ def run_gb300(args):
         "gpu_launches": n_kernels * args.steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": DOMINANT_TRAFFIC.get(dom) if not rows else None,
+                     "traffic": profiled_traffic(dom) if not rows else None,
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_ms},
         "kernel_share": {k: round(v[0] / total, 4) for k, v in per.items()},
         "autotuned": tuned,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
     }
-    if batched is not None:
-        line["batched"] = batched
-    if batched_ddi is not None:
-        line["batched_ddi"] = batched_ddi
+    if cufft is not None:
+        line["cufft_comparison"] = cufft
+    # verbose sub-measurements first, the metric's own numbers (accuracy, batched vs plain) last
+    if batched is not None or batched_ddi is not None:
+        line["batched_workloads"] = {k: v["workload"] + "; plain: " + v["plain"]
+                                     for k, v in (("batched", batched), ("batched_ddi", batched_ddi)) if v}
     if gneb_line is not None:
         line["gneb"] = gneb_line
     if adj_line is not None:
@@ -731,6 +823,11 @@ def run_gb300(args):
         line["mc"] = mc_line
     if htst_line is not None:
         line["htst"] = htst_line
+    if accuracy is not None:
+        line["accuracy"] = accuracy
+    for key, v in (("batched", batched), ("batched_ddi", batched_ddi)):
+        if v is not None:
+            line[key] = compact_batched(v)
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -750,6 +847,9 @@ def main():
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false", help="skip the adjoint measurement")
     ap.add_argument("--no-mc", dest="mc", action="store_false", help="skip the Monte Carlo measurement")
     ap.add_argument("--no-htst", dest="htst", action="store_false", help="skip the HTST measurement")
+    ap.add_argument("--no-cufft", dest="cufft", action="store_false", help="skip the cuFFT timing comparison")
+    ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
+                    help="skip the FP32-vs-oracle accuracy run of the headline workload")
     ap.add_argument("--profile-step", action="store_true",
                     help="run one extra step inside a CUDA profiler range (for ncu --profile-from-start off)")
     ap.add_argument("--no-batched-ddi", dest="batched_ddi", action="store_false",

@@ -86,6 +86,12 @@ void Hamiltonian_Get_DDI( State * state, int * ddi_method, int n_periodic_images
 /* EXTENSION: FP64 device gradient of the image's spins (AoS [nos][3]); returns the FP64 energy.
  * The reference reaches this only through Hamiltonian::Gradient_and_Energy (C++ internals). */
 double Hamiltonian_Get_Gradient( State * state, double * gradient, int idx_image, int idx_chain );
+/* EXTENSION: FP64 gradients and energies of the active images of n States evaluated as one batch
+ * (one FP64 device engine over all systems; the dipolar term of every system from the batch's shared
+ * FFT plan table, the path batched LLG runs take).  gradients: AoS [sum of nos][3] in the order of
+ * the States (may be NULL); energies[n_states] (may be NULL).  No counterpart in the reference,
+ * which evaluates one image per Hamiltonian call (Hamiltonian_Heisenberg.cpp:704-766). */
+void Hamiltonian_Get_Gradient_Batched( State ** states, int n_states, double * gradients, double * energies );
 /* EXTENSION: FP64 energy per term (Zeeman, Anisotropy, Exchange, DMI, DDI) into terms[5] and,
  * if per_spin != NULL, per spin into per_spin[5][nos]; returns the total (Energy_Contributions_per_Spin). */
 double Hamiltonian_Get_Energy_Contributions( State * state, double * terms, double * per_spin, int idx_image,

@@ -368,6 +368,25 @@ def philox4x32(ctr, key):
     return o
 
 
+def portable_spins(nos, seed):
+    """Uniform directions on S^2 that come out bit-identical on every platform: points drawn
+    uniformly in the cube [-1, 1]^3 by numpy's legacy MT19937 RandomState (a stream numpy keeps
+    frozen), those outside the unit ball or too close to the origin rejected, the rest scaled by
+    1 / |v| -- only additions, multiplications, division and square root (all correctly rounded),
+    no platform libm.  The inputs of the full-size fixtures are regenerated from their seed on any
+    machine."""
+    rs = np.random.RandomState(seed)
+    out = np.empty((0, 3))
+    while len(out) < nos:
+        v = rs.uniform(-1.0, 1.0, (2 * (nos - len(out)) + 16, 3))
+        r2 = (v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1]) + v[:, 2] * v[:, 2]
+        v = v[(r2 <= 1.0) & (r2 >= 0.01)]
+        out = np.concatenate([out, v])
+    out = out[:nos]
+    n = np.sqrt((out[:, 0] * out[:, 0] + out[:, 1] * out[:, 1]) + out[:, 2] * out[:, 2])
+    return np.ascontiguousarray(out / n[:, None])
+
+
 def random_spins(nos, seed):
     """Uniform directions on S^2 (z in U[-1,1], phi in U[-pi,pi], as Vectormath.cpp:41-51)."""
     rng = np.random.default_rng(seed)

@@ -946,6 +946,21 @@ double Hamiltonian_Get_Gradient( State * state, double * gradient, int idx_image
     }
 }
 
+// FP64 gradients (AoS, concatenated in the order of the States) and energies of the active images
+// of n States, evaluated together by one batched FP64 engine (shared dipolar plan table)
+void Hamiltonian_Get_Gradient_Batched( State ** states, int n_states, double * gradients, double * energies ) noexcept
+{
+    State * first = n_states > 0 ? states[0] : nullptr;
+    try
+    {
+        gradient_batched( states, n_states, gradients, energies );
+    }
+    catch( ... )
+    {
+        handle( first, "Hamiltonian_Get_Gradient_Batched" );
+    }
+}
+
 // FP64 energy per term (Zeeman, Anisotropy, Exchange, DMI, DDI); per_spin (optional) gets
 // [5][nos].  Returns the total.
 double Hamiltonian_Get_Energy_Contributions( State * state, double * terms, double * per_spin, int idx_image,
@@ -2025,7 +2040,12 @@ void Simulation_LLG_Start( State * state, int solver_type, int n_iterations, int
         E.set_params( 0, input_of( img, 0 ) );
         E.llg_start( solver_type, { (int)img.llg.n_iterations } );
         if( singleshot )
+        {
+            // the start evaluated the field and energy of the current spins (the method's first
+            // force evaluation): that is the image's energy until the first shot
+            img.E = E.status()[0].energy;
             return;
+        }
         iterate_llg( state, img, E );
         img.iteration_allowed = false;
         fill_run_info( info, img.info );

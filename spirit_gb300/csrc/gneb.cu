@@ -1385,6 +1385,38 @@ void llg_run_batched( State ** states, int n_states, int solver, int n_iteration
     batched_finish( E, ims );
 }
 
+// FP64 gradients and energies of the States' active images evaluated as one batch: one FP64 engine
+// over all systems, so the dipolar term of every system comes from the batch's shared FFT plan
+// table (one launch per pass over all systems, each system on its own padded extents).
+// gradients: AoS [sum nos][3] in the order of the States; energies[n_states].
+void gradient_batched( State ** states, int n_states, double * gradients, double * energies )
+{
+    if( n_states <= 0 )
+        return;
+    std::vector<SystemInput> in;
+    std::vector<double> all;
+    for( int k = 0; k < n_states; ++k )
+    {
+        Image * im = states[k]->chain->images[states[k]->idx_active_image].get();
+        SystemInput s;
+        s.geom = im->geom.get();
+        s.ham  = &im->ham;
+        in.push_back( s );
+        all.insert( all.end(), im->spins.begin(), im->spins.end() );
+    }
+    Engine E( in, true );
+    E.set_all_spins( all.data() );
+    size_t o = 0;
+    for( int k = 0; k < n_states; ++k )
+    {
+        double e = 0;
+        E.gradient( k, gradients ? gradients + o : nullptr, &e, nullptr );
+        if( energies )
+            energies[k] = e;
+        o += 3 * (size_t)E.nos( k );
+    }
+}
+
 // Open-ended batched run driven by the caller: the first call (or a call for another set of
 // States) uploads and starts the batch; every call enqueues n_steps on the batch's stream
 // (states[0]'s stream) without synchronising.  llg_batched_finish ends the run.

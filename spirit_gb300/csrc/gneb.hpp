@@ -22,6 +22,7 @@ void llg_vp_shot( State * st, Image & img, int n );
 void llg_run_batched( State ** states, int n_states, int solver, int n_iterations, void * info, size_t info_size );
 // caller-driven batched run: enqueue n_steps (first call uploads and starts), then finish
 void llg_batched_launch( State ** states, int n_states, int solver, int n_steps );
+void gradient_batched( State ** states, int n_states, double * gradients, double * energies );
 void llg_batched_finish( State ** states, int n_states );
 
 } // namespace sg

@@ -17,14 +17,20 @@
 //     streams, or host threads without ordering) race on it and may return a wrong energy;
 //   * nothing has to start at zero: every scratch entry the energy sum reads is written first by
 //     the same call, in stream order;
-//   * the first call on a device looks up the scratch address (cudaGetSymbolAddress), which can
-//     load the module; make that first call before any stream capture.
+//   * the first call in each CUDA context looks up the scratch address (cudaGetSymbolAddress),
+//     which can load the module; make that first call before any stream capture.  The address is
+//     cached per context (keyed on the driver's unique context id), not per device ordinal: after
+//     cudaDeviceReset, or in a context other than the device's primary one, the module is loaded
+//     anew and the symbol can sit at another address, so the lookup is repeated there;
+//   * the system descriptor (SysDesc, several KB) is passed to the kernel by value: kernel
+//     parameters above 4 KB need CUDA 12.1 or newer on sm_70+ (the limit is 32,764 bytes).
 #include "engine.hpp"
 #include "kernels.cuh"
 #include "state.hpp"
 
 #include <cuda_runtime.h>
 
+#include <map>
 #include <mutex>
 #include <string>
 
@@ -37,6 +43,9 @@ constexpr long long NOALLOC_MAX_SPINS = (long long)NOALLOC_MAX_BLOCKS * NOALLOC_
 
 // per-block partial energies of one call
 static __device__ __align__( 256 ) double g_noalloc_partials[NOALLOC_MAX_BLOCKS];
+
+// the descriptor travels as a kernel parameter (by value): CUDA 12.1+ allows up to 32,764 bytes
+static_assert( sizeof( SysDesc ) <= 32764, "SysDesc exceeds the kernel parameter limit" );
 
 // Variant of the engine's evaluation kernel (engine.cu eval_kernel): SoA FP64 spins of one system
 // at offset 0, gradient to SoA, and the block's energy sum into partials[blockIdx.x].
@@ -85,31 +94,68 @@ __global__ void __launch_bounds__( NOALLOC_THREADS ) noalloc_sum( const double *
         *energy = s;
 }
 
-// Scratch address on the current device, looked up once per device.
+// Unique id of the calling thread's current CUDA context (cuCtxGetId through the runtime's
+// driver entry point, so the library does not link the driver library itself); 0 when unknown.
+static unsigned long long current_context_id()
+{
+    typedef int ( *GetCurrent )( void ** );
+    typedef int ( *GetId )( void *, unsigned long long * );
+    static GetCurrent get_current = nullptr;
+    static GetId get_id           = nullptr;
+    static std::once_flag once;
+    std::call_once( once, [] {
+        void * f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if( cudaGetDriverEntryPointByVersion( "cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q ) == cudaSuccess
+            && q == cudaDriverEntryPointSuccess )
+            get_current = reinterpret_cast<GetCurrent>( f );
+        f = nullptr;
+        if( cudaGetDriverEntryPointByVersion( "cuCtxGetId", &f, 12000, cudaEnableDefault, &q ) == cudaSuccess
+            && q == cudaDriverEntryPointSuccess )
+            get_id = reinterpret_cast<GetId>( f );
+        cudaGetLastError();
+    } );
+    void * ctx             = nullptr;
+    unsigned long long cid = 0;
+    if( get_current && get_id && get_current( &ctx ) == 0 && ctx && get_id( ctx, &cid ) == 0 )
+        return cid;
+    return 0;
+}
+
+// Scratch address in the current context, looked up once per context.  A thread without a current
+// context gets the device's primary one from the lookup itself (the runtime initialises it), and the
+// address is cached under that context's id.
 static double * noalloc_scratch( std::string & err )
 {
     static std::mutex mu;
-    static double * ptr[64] = {};
-    int dev               = -1;
-    cudaError_t e         = cudaGetDevice( &dev );
-    if( e != cudaSuccess || dev < 0 || dev >= 64 )
+    static std::map<unsigned long long, double *> by_context;
+    int dev       = -1;
+    cudaError_t e = cudaGetDevice( &dev );
+    if( e != cudaSuccess || dev < 0 )
     {
         err = "no usable current CUDA device";
         return nullptr;
     }
     std::lock_guard<std::mutex> lk( mu );
-    if( !ptr[dev] )
+    unsigned long long cid = current_context_id();
+    if( cid != 0 )
     {
-        void * p = nullptr;
-        e        = cudaGetSymbolAddress( &p, g_noalloc_partials );
-        if( e != cudaSuccess )
-        {
-            err = std::string( "cudaGetSymbolAddress: " ) + cudaGetErrorString( e );
-            return nullptr;
-        }
-        ptr[dev] = static_cast<double *>( p );
+        auto it = by_context.find( cid );
+        if( it != by_context.end() )
+            return it->second;
     }
-    return ptr[dev];
+    void * p = nullptr;
+    e        = cudaGetSymbolAddress( &p, g_noalloc_partials );
+    if( e != cudaSuccess )
+    {
+        err = std::string( "cudaGetSymbolAddress: " ) + cudaGetErrorString( e );
+        return nullptr;
+    }
+    if( cid == 0 )
+        cid = current_context_id();
+    if( cid != 0 )
+        by_context[cid] = static_cast<double *>( p );
+    return static_cast<double *>( p );
 }
 
 } // namespace sg

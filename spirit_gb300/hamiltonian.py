@@ -36,6 +36,7 @@ _Get_Gradient = fn("Hamiltonian_Get_Gradient", [_vp, _PD, _i, _i], ctypes.c_doub
 _Get_Energy_Contributions = fn("Hamiltonian_Get_Energy_Contributions", [_vp, _PD, _PD, _i, _i], ctypes.c_double)
 _Get_DDI_Field = fn("Hamiltonian_Get_DDI_Field", [_vp, _PD, _i, _i])
 _NOS = fn("System_Get_NOS", [_vp, _i, _i], _i)
+_Get_Gradient_Batched = fn("Hamiltonian_Get_Gradient_Batched", [ctypes.POINTER(_vp), _i, _PD, _PD])
 
 TERMS = ["Zeeman", "Anisotropy", "Exchange", "DMI", "DDI"]
 
@@ -118,6 +119,23 @@ def get_gradient(p_state, idx_image=-1, idx_chain=-1):
     g = np.zeros((nos, 3))
     E = _Get_Gradient(_vp(p_state), g.ctypes.data_as(_PD), _i(idx_image), _i(idx_chain))
     return g, float(E)
+
+
+def get_gradient_batched(p_states):
+    """FP64 gradients and energies of the active images of several States evaluated as one batch on
+    the GPU (the dipolar term of every system from the batch's shared FFT plan table); returns
+    ([gradient [nos_k, 3] per State], energies [n])."""
+    n = len(p_states)
+    nos = [_NOS(_vp(p), _i(-1), _i(-1)) for p in p_states]
+    g = np.zeros((sum(nos), 3))
+    e = np.zeros(n)
+    arr = (_vp * n)(*p_states)
+    _Get_Gradient_Batched(arr, _i(n), g.ctypes.data_as(_PD), e.ctypes.data_as(_PD))
+    out, o = [], 0
+    for k in nos:
+        out.append(g[o:o + k])
+        o += k
+    return out, e
 
 
 def get_energy_contributions(p_state, per_spin=False, idx_image=-1, idx_chain=-1):

@@ -94,6 +94,18 @@ GRAD_CASES = {
     "fd_pairs": FD_PAIRS,
 }
 
+# The benchmark configurations at their full sizes (T = 0): the plain-LLG configuration exactly
+# (SC 64 x 64 periodic, Neel DMI, Depondt, 1000 steps) and the dipolar configuration's system
+# (SC 128 x 128 x 16, bulk DMI, DDI FFT zero-padded along c, Heun) over 100 steps.  Input spins
+# come from oracle.portable_spins(nos, seed), bit-identical on every platform.
+C1_FULL = dict(SQ_C1, n_cells=[64, 64, 1])
+C2_T0 = dict(SC3D_DDI, n_cells=[128, 128, 16])
+# (name, spec, solver name, solver id, iterations, spin seed)
+FULL_CASES = [
+    ("c1_full", C1_FULL, "Depondt", 2, 1000, 101),
+    ("c2_t0", C2_T0, "Heun", 3, 100, 102),
+]
+
 # (case, solver name, solver id, iterations)
 LLG_CASES = [
     ("sq_c1", "Depondt", 2, 200),

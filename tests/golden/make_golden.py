@@ -22,8 +22,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
-from cases import GRAD_CASES, HTST_CASES, LLG_CASES, PAIR_GEOMETRIES, SOLVERS, SPIN_SEED  # noqa: E402
-from oracle.oracle import OracleSystem, image_types_auto, random_spins, transition_homogeneous  # noqa: E402
+from cases import FULL_CASES, GRAD_CASES, HTST_CASES, LLG_CASES, PAIR_GEOMETRIES, SOLVERS, SPIN_SEED  # noqa: E402
+from oracle.oracle import (OracleSystem, image_types_auto, portable_spins, random_spins,  # noqa: E402
+                           transition_homogeneous)
 from spirit_gb300.configs import config_text, write_config  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "golden_harness")
@@ -31,9 +32,9 @@ HTST_KEYS = ["temperature_exponent", "me", "Omega_0", "s", "volume_min", "volume
              "prefactor", "det_min", "det_sp"]
 
 
-def run(args, cwd):
+def run(args, cwd, threads=4):
     r = subprocess.run([HARNESS] + args, cwd=cwd, capture_output=True, text=True,
-                       env=dict(os.environ, OMP_NUM_THREADS="4"))
+                       env=dict(os.environ, OMP_NUM_THREADS=str(threads)))
     if r.returncode != 0:
         raise RuntimeError("harness failed: %s\n%s" % (args, r.stderr[-2000:]))
 
@@ -125,6 +126,31 @@ def main(only=None):
             energy=res["energy_image"], max_torque=res["max_torque"], iterations=int(res["iterations"]),
         )
         out["llg_%s_%s" % (case, sname)] = res
+    # --- the benchmark configurations at full size (T = 0).  The dipolar system runs on one thread:
+    # the reference's kissFFT path slows down with more OpenMP threads.  Outputs of the large
+    # system are kept as FP32 (the device FP32 bar is 1e-5) plus every 16th spin in FP64 (pins the
+    # oracle to rounding) and the FP64 energy; inputs are regenerated from the seed (portable_spins)
+    # and checked against the stored sums.
+    for name, spec, sname, sid, n_iter, seed in FULL_CASES:
+        if not want("full_" + name):
+            continue
+        cfg = write_config(spec, os.path.join(tmp, name + ".cfg"))
+        nos = nos_of(spec)
+        spins = portable_spins(nos, seed)
+        sp = os.path.join(tmp, name + "_spins.bin")
+        spins.tofile(sp)
+        tag = os.path.join(tmp, "full_" + name)
+        run(["llg", cfg, sp, tag, str(sid), str(n_iter)], tmp, threads=1 if spec.get("ddi") else 4)
+        res = load_kv(tag + "_result.txt")
+        so = load_bin(tag + "_spins.bin", (-1, 3))
+        big = nos > 65536
+        np.savez_compressed(
+            os.path.join(HERE, "full_%s.npz" % name), config=config_text(spec), seed=seed, solver=sid,
+            n_iter=n_iter, spins_in_sum=spins.sum(axis=0), spins_in_head=spins[:64],
+            spins_out=so.astype(np.float32) if big else so, spins_out_fp64_every16=so[::16],
+            energy=res["energy_image"], max_torque=res["max_torque"], iterations=int(res["iterations"]),
+        )
+        out["full_" + name] = res
     # --- GNEB (VP) on the reference solver-test system: skyrmion collapse, 9 images
     spec = SOLVERS
     cfg = write_config(spec, os.path.join(tmp, "solvers.cfg"))

@@ -8,9 +8,9 @@ trajectories follow the same operations in the same order.
 import numpy as np
 import pytest
 
-from cases import GRAD_CASES, HTST_CASES, LLG_CASES, PAIR_GEOMETRIES, SOLVERS
+from cases import FULL_CASES, GRAD_CASES, HTST_CASES, LLG_CASES, PAIR_GEOMETRIES, SOLVERS
 from conftest import golden
-from oracle.oracle import OracleSystem, image_types_auto, philox4x32
+from oracle.oracle import OracleSystem, image_types_auto, philox4x32, portable_spins
 
 
 @pytest.mark.parametrize("name", sorted(PAIR_GEOMETRIES))
@@ -65,6 +65,36 @@ def test_ddi_direct_sum(name):
     if _padded_everywhere(GRAD_CASES[name]):
         g = OracleSystem(GRAD_CASES[name]).gradient(s)
         assert np.abs(g - gd).max() <= 1e-9 * np.abs(gd).max()
+
+
+def full_case_input(name):
+    """Fixture, spec and the regenerated input spins of a full-size case; the input is checked
+    against the sums and first spins the fixture stored (the generator is platform-exact)."""
+    (spec, sname, sid, n_iter, seed), = [c[1:] for c in FULL_CASES if c[0] == name]
+    f = golden("full_%s.npz" % name)
+    n = spec["n_cells"]
+    s0 = portable_spins(n[0] * n[1] * n[2], seed)
+    assert np.array_equal(s0[:64], f["spins_in_head"])
+    assert np.array_equal(s0.sum(axis=0), f["spins_in_sum"])
+    return f, spec, s0
+
+
+@pytest.mark.parametrize("name", [c[0] for c in FULL_CASES])
+def test_llg_full_size(name):
+    """The benchmark configurations at full size against the reference: the plain-LLG
+    configuration exactly (64 x 64, Depondt, 1000 steps) and the dipolar system (128 x 128 x 16,
+    DDI zero-padded along c, Heun, 100 steps).  The large system's output is stored as FP32 (plus
+    every 16th spin in FP64), so the full comparison is at FP32 rounding."""
+    f, spec, s0 = full_case_input(name)
+    ll = spec["llg"]
+    s, r = OracleSystem(spec).llg(s0, int(f["solver"]), int(f["n_iter"]), dt=ll["dt"], damping=ll["damping"],
+                                  temperature=0.0)
+    assert r["iterations"] == int(f["iterations"])
+    assert np.abs(s[::16] - f["spins_out_fp64_every16"]).max() <= 1e-11
+    tol = 1e-11 if f["spins_out"].dtype == np.float64 else 1e-7
+    assert np.abs(s - f["spins_out"]).max() <= tol
+    assert abs(r["energy"] - f["energy"]) <= 1e-11 * abs(f["energy"])
+    assert abs(r["max_torque"] - f["max_torque"]) <= 1e-8 * abs(f["max_torque"])
 
 
 @pytest.mark.parametrize("case,solver,sid,n_iter", LLG_CASES)
