@@ -21,12 +21,14 @@
 #include "engine.hpp"
 #include "fft.cuh"
 #include "kernels.cuh"
+#include "tma.cuh"
 #include "util.hpp"
 
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 namespace sg
 {
@@ -216,9 +218,9 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
 // the last block of the system closes the iteration.
 template<typename R, bool PROBE>
 __device__ __forceinline__ void stage_finalize( const StageArgs<R> & A, SysRun * run, int s, const SysDesc & d, R e,
-                                               float t2, double * red_d, float * red_f, int & is_last )
+                                               float t2, double * red_d, float * red_f, int & is_last, R ec = R( 0 ) )
 {
-    double es = block_sum_w( e, red_d );
+    double es = block_sum_comp( e, ec, red_d );
     float tm  = block_max( t2, red_f );
     if( threadIdx.x == 0 )
     {
@@ -276,6 +278,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
     constexpr bool PROBE = STAGE == ST_PROBE;
     const int iteration  = run->iteration;
     R e                  = 0;
+    R ec                 = 0; // compensation of the energy sum
     float t2             = 0;
 #pragma unroll
     for( int k = 0; k < SPT; ++k )
@@ -292,13 +295,238 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
         const V3<R> ci     = A.cfg.ld( gi );
         R ek               = 0;
         V3<R> g            = gradient_at<R>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu, ek, smode );
-        e += ek;
+        comp_add( e, ec, ek );
         stage_update<R, SOLVER, STAGE>( A, C, d, gi, i, ib, ci, g, iteration, t2 );
     }
     }
     if( !( FINAL || PROBE ) )
         return;
-    stage_finalize<R, PROBE>( A, run, s, d, e, t2, red_d, red_f, is_last );
+    stage_finalize<R, PROBE>( A, run, s, d, e, t2, red_d, red_f, is_last, ec );
+}
+
+// ------------------------------------------------------------------ TMA-staged stage kernel (FP32)
+// Persistent variant of llg_stage for FP32 batches whose stencil reaches only a few rows (2D
+// lattices: the batched ensembles).  Each CTA walks a contiguous run of tiles (TT_SPINS
+// consecutive spins of one system).  The stage configuration of a tile and its halo -- the index
+// window [t0 - H, t0 + T + H), H the largest |linear offset| of a pair, which holds every
+// neighbour of a cell that needs no wrap -- is brought into shared memory by bulk tensor copies
+// (TMA: rank-1 boxes of TT_BOX floats of each component array, completed on an mbarrier), double
+// buffered: the next tile's window streams in while the current tile is computed.  Neighbours
+// outside the window (wraps along b or c, the far end of a system) are read from global memory.
+// The arithmetic per spin is llg_stage's (same gradient terms and order, same stage update), so
+// the two kernels give the same results.
+constexpr int TT_SPINS = 1024; // spins per tile (4 per thread)
+constexpr int TT_BOX   = 256;  // floats per tensor copy (largest box extent)
+constexpr int TT_NCOPY = 8;    // tensor copies per component and window at most
+constexpr int TT_WIN   = TT_BOX * TT_NCOPY;
+constexpr size_t TT_SMEM = sizeof( float ) * 2 * 3 * TT_WIN; // two windows of three components
+
+struct TileMaps
+{
+    CUtensorMap m[3]; // components x, y, z of the stage configuration: rank 1, box TT_BOX
+};
+
+// Gradient at spin gi (batch index) from the staged window (same terms and order as gradient_at).
+__device__ __forceinline__ V3<float> gradient_win( const Geo & d, const SysConst<float> & C, const PairR<float> * pairs,
+                                                   const float * wx, const float * wy, const float * wz, int xs,
+                                                   int wlen, const SoA3<float> & cfg, const SoA3<float> & h, int gi,
+                                                   int ib, int a, int b, int c, V3<float> si, float mu, float & e,
+                                                   int mode )
+{
+    V3<float> g = { 0, 0, 0 };
+    for( int k = 0; k < C.n_aniso; ++k )
+        if( C.aniso_idx[k] == ib )
+        {
+            V3<float> n = { C.aniso_n[k][0], C.aniso_n[k][1], C.aniso_n[k][2] };
+            float sc    = 2.f * C.aniso_K[k] * dot( n, si );
+            g.x -= sc * n.x;
+            g.y -= sc * n.y;
+            g.z -= sc * n.z;
+        }
+    const int p0 = d.pair_begin[ib], p1 = d.pair_begin[ib + 1];
+#pragma unroll 6
+    for( int p = p0; p < p1; ++p )
+    {
+        const PairR<float> P = pairs[p];
+        int j;
+        bool have = true, inwin = true;
+        if( mode == STENCIL_INTERIOR )
+            j = gi + P.lin;
+        else
+        {
+            if( mode == STENCIL_ROW )
+            {
+                const int ja = a + P.da;
+                j            = gi + P.lin;
+                if( ja < 0 )
+                {
+                    j += d.row_len;
+                    have = d.bc[0];
+                }
+                else if( ja >= d.n[0] )
+                {
+                    j -= d.row_len;
+                    have = d.bc[0];
+                }
+            }
+            else
+            {
+                const long long jj = pair_index( d, a, b, c, P.j, P.da, P.db, P.dc );
+                have               = jj >= 0;
+                j                  = (int)jj;
+            }
+            inwin = (unsigned)( j - xs ) < (unsigned)wlen;
+        }
+        if( have )
+        {
+            V3<float> sj;
+            if( inwin )
+            {
+                const int w = j - xs;
+                sj          = { wx[w], wy[w], wz[w] };
+            }
+            else
+                sj = cfg.ld( j );
+            g.x -= P.J * sj.x;
+            g.y -= P.J * sj.y;
+            g.z -= P.J * sj.z;
+            V3<float> cr = cross( sj, V3<float>{ P.Dx, P.Dy, P.Dz } );
+            g.x -= cr.x;
+            g.y -= cr.y;
+            g.z -= cr.z;
+        }
+    }
+    if( h.x )
+    {
+        V3<float> hh = h.ld( gi );
+        g.x -= mu * hh.x;
+        g.y -= mu * hh.y;
+        g.z -= mu * hh.z;
+    }
+    e = 0.5f * ( g.x * si.x + g.y * si.y + g.z * si.z );
+    if( C.has_zeeman )
+    {
+        V3<float> B = { C.zeeman[0], C.zeeman[1], C.zeeman[2] };
+        g.x -= mu * B.x;
+        g.y -= mu * B.y;
+        g.z -= mu * B.z;
+        e += -mu * ( B.x * si.x + B.y * si.y + B.z * si.z );
+    }
+    return g;
+}
+
+// tiles[k] = (system, first local spin t0, aligned window start xs in the batch arrays, number
+// of tensor copies per component); err: set to 1 when a copy did not arrive within the wait limit
+template<int SOLVER, int STAGE>
+__global__ void __launch_bounds__( 256, 4 )
+    llg_stage_tma( StageArgs<float> A, const __grid_constant__ TileMaps M, const int4 * tiles, int n_tiles, int * err )
+{
+    extern __shared__ __align__( 128 ) float tt_win[]; // [2][3][TT_WIN]
+    __shared__ __align__( 8 ) uint64_t bar[2];
+    __shared__ PairR<float> pairs[MAX_PAIRS];
+    __shared__ SysConst<float> C;
+    __shared__ Geo GS;
+    __shared__ double red_d[32];
+    __shared__ float red_f[32];
+    __shared__ int is_last;
+    constexpr bool FINAL = ( SOLVER == SOLVER_RK4 ) ? ( STAGE == 4 ) : ( STAGE == 2 );
+    const int k0 = (int)( (long long)blockIdx.x * n_tiles / gridDim.x );
+    const int k1 = (int)( (long long)( blockIdx.x + 1 ) * n_tiles / gridDim.x );
+    if( threadIdx.x == 0 )
+    {
+        mbar_init( &bar[0], 1 );
+        mbar_init( &bar[1], 1 );
+        fence_mbar_init();
+    }
+    __syncthreads();
+    pdl_wait(); // the configuration and run state come from earlier kernels
+    pdl_trigger();
+    auto issue = [&]( int k, int buf ) {
+        const int4 t = tiles[k];
+        mbar_arrive_expect_tx( &bar[buf], 3u * (unsigned)t.w * TT_BOX * (unsigned)sizeof( float ) );
+        for( int comp = 0; comp < 3; ++comp )
+            for( int q = 0; q < t.w; ++q )
+                tma_load_1d( tt_win + ( buf * 3 + comp ) * TT_WIN + q * TT_BOX, &M.m[comp], t.z + q * TT_BOX,
+                             &bar[buf] );
+    };
+    if( threadIdx.x == 0 && k0 < k1 )
+        issue( k0, 0 );
+    unsigned phase = 0; // bit b: parity of the next completion of buffer b
+    int cur        = -1;
+    for( int k = k0; k < k1; ++k )
+    {
+        const int buf = ( k - k0 ) & 1;
+        const int4 t  = tiles[k];
+        if( threadIdx.x == 0 && k + 1 < k1 )
+        {
+            fence_proxy_async_smem(); // the other buffer was last read (generic proxy) by tile k - 1
+            issue( k + 1, buf ^ 1 );
+        }
+        if( t.x != cur )
+        {
+            const SysDesc & d = A.sd[t.x];
+            load_pairs_smem( pairs, d );
+            load_const( C, d );
+            load_geo( GS, d );
+            __syncthreads();
+            cur = t.x;
+        }
+        const bool ok = mbar_wait_bounded( &bar[buf], ( phase >> buf ) & 1u );
+        phase ^= 1u << buf;
+        if( __syncthreads_or( !ok ) )
+        {
+            // a copy did not arrive in time: record it, give the copies in flight a bounded
+            // chance to land in this CTA's shared memory, and stop
+            if( threadIdx.x == 0 )
+            {
+                atomicExch( err, 1 );
+                mbar_wait_bounded( &bar[buf], ( ( phase >> buf ) & 1u ) ^ 1u );
+                if( k + 1 < k1 )
+                    mbar_wait_bounded( &bar[buf ^ 1], ( phase >> ( buf ^ 1 ) ) & 1u );
+            }
+            return;
+        }
+        const int s       = t.x;
+        SysRun * run      = A.runs + s;
+        const SysDesc & d = A.sd[s];
+        if( !A.tune && !run->active )
+        {
+            __syncthreads(); // the window buffer is reused two tiles later
+            continue;
+        }
+        const float * wx   = tt_win + ( buf * 3 + 0 ) * TT_WIN;
+        const float * wy   = tt_win + ( buf * 3 + 1 ) * TT_WIN;
+        const float * wz   = tt_win + ( buf * 3 + 2 ) * TT_WIN;
+        const int xs       = t.z;
+        const int wlen     = t.w * TT_BOX;
+        const int iteration = run->iteration;
+        float e = 0, ec = 0, t2 = 0;
+#pragma unroll
+        for( int q = 0; q < TT_SPINS / 256; ++q )
+        {
+            const int i      = t.y + threadIdx.x + q * 256; // local spin index
+            const bool valid = i < GS.nos && threadIdx.x + q * 256 < TT_SPINS;
+            int ib, a, b, c;
+            cell_of( GS, valid ? i : t.y, ib, a, b, c );
+            const int smode = warp_stencil_mode( GS, a, b, c, valid );
+            if( valid )
+            {
+                const int gi   = (int)GS.off + i;
+                const float mu = C.mu[ib];
+                const int w    = gi - xs;
+                const V3<float> ci = { wx[w], wy[w], wz[w] };
+                float ek           = 0;
+                V3<float> g = gradient_win( GS, C, pairs, wx, wy, wz, xs, wlen, A.cfg, A.h, gi, ib, a, b, c, ci, mu, ek,
+                                            smode );
+                comp_add( e, ec, ek );
+                stage_update<float, SOLVER, STAGE>( A, C, d, gi, i, ib, ci, g, iteration, t2 );
+            }
+        }
+        if( FINAL )
+            stage_finalize<float, false>( A, run, s, d, e, t2, red_d, red_f, is_last, ec ); // ends with a barrier
+        else
+            __syncthreads();
+    }
 }
 
 // ------------------------------------------------------------------ row-fused stage kernel
@@ -748,6 +976,9 @@ Engine::~Engine()
     }
     dfree( d_rowmap_ );
     dfree( d_rowcount_ );
+    dfree( d_tiles_ );
+    dfree( d_tilecount_ );
+    dfree( d_err_ );
     if( lane_ )
     {
         for( int c = 0; c < 3; ++c )
@@ -885,6 +1116,101 @@ void Engine::build_systems( const std::vector<SystemInput> & systems )
         ddi_.tune( d_desc_, spins_[0], spins_[1], spins_[2], field_[0], field_[1], field_[2], stream_ );
         ddi_systems_ = ddis;
         build_row_map( (int)ddis.size() );
+    }
+    d_err_ = dalloc<int>( 1 );
+    build_tiles();
+}
+
+bool encode_tensor_map_1d_f32( CUtensorMap * map, const void * base, unsigned long long n, unsigned box )
+{
+    typedef CUresult ( *Encode )( CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill );
+    static Encode encode = [] {
+        void * f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if( cudaGetDriverEntryPointByVersion( "cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q )
+                != cudaSuccess
+            || q != cudaDriverEntryPointSuccess )
+        {
+            cudaGetLastError();
+            f = nullptr;
+        }
+        return reinterpret_cast<Encode>( f );
+    }();
+    if( !encode || ( reinterpret_cast<uintptr_t>( base ) & 15 ) )
+        return false;
+    const cuuint64_t dim[1]  = { n };
+    const cuuint32_t bx[1]   = { box };
+    const cuuint32_t estr[1] = { 1 };
+    return encode( map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 1, const_cast<void *>( base ), dim, nullptr, bx, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE )
+           == CUDA_SUCCESS;
+}
+
+// The TMA-staged stage kernel serves FP32 batches in which every system's window (a tile of
+// TT_SPINS spins plus the stencil reach H on both sides, aligned to 16 bytes) fits TT_NCOPY
+// copies of TT_BOX floats; SPIRIT_GB300_TMA=0 keeps llg_stage.  Tiles never cross systems.
+void Engine::build_tiles()
+{
+    tma_             = false;
+    const char * env = std::getenv( "SPIRIT_GB300_TMA" );
+    if( fp64_ || rows_ || ( env && env[0] == '0' ) || total_ >= ( 1LL << 30 ) )
+        return;
+    std::vector<int4> tiles;
+    std::vector<int> count( desc_.size(), 0 );
+    for( size_t s = 0; s < desc_.size(); ++s )
+    {
+        const SysDesc & d = desc_[s];
+        long long H       = 0;
+        for( int p = 0; p < d.n_pairs; ++p )
+        {
+            const PairEntry & q = d.pairs[p];
+            const long long lin = q.j - q.i
+                                  + (long long)d.nb
+                                        * ( q.da + (long long)d.n_cells[0] * ( q.db + (long long)d.n_cells[1] * q.dc ) );
+            H = std::max( H, std::abs( lin ) );
+        }
+        for( int t0 = 0; t0 < d.nos; t0 += TT_SPINS )
+        {
+            const int n          = std::min( TT_SPINS, d.nos - t0 );
+            const long long lo   = d.spin_offset + t0 - H;
+            const long long xs   = lo >= 0 ? lo / 4 * 4 : -( ( -lo + 3 ) / 4 * 4 ); // 16-byte aligned start
+            const long long hi   = d.spin_offset + t0 + n + H;
+            const long long ncpy = ( hi - xs + TT_BOX - 1 ) / TT_BOX;
+            if( ncpy > TT_NCOPY )
+                return; // a stencil reaching too far: llg_stage serves this batch
+            tiles.push_back( make_int4( (int)s, t0, (int)xs, (int)ncpy ) );
+            ++count[s];
+        }
+    }
+    void * const * bufs[3] = { spins_, predA_, predB_ };
+    for( int b = 0; b < 3; ++b )
+        for( int c = 0; c < 3; ++c )
+            if( !encode_tensor_map_1d_f32( &tmaps_[b][c], bufs[b][c], (unsigned long long)total_, TT_BOX ) )
+                return;
+    d_tiles_     = dalloc<int4>( std::max<size_t>( tiles.size(), 1 ) );
+    d_tilecount_ = dalloc<int>( std::max<size_t>( count.size(), 1 ) );
+    if( !tiles.empty() )
+        h2d( d_tiles_, tiles.data(), tiles.size() );
+    h2d( d_tilecount_, count.data(), count.size() );
+    n_tiles_ = (int)tiles.size();
+    tma_     = n_tiles_ > 0;
+}
+
+void Engine::check_err()
+{
+    if( !d_err_ )
+        return;
+    int e = 0;
+    CUDA_CHECK( cudaMemcpyAsync( &e, d_err_, sizeof( int ), cudaMemcpyDeviceToHost, stream_ ) );
+    CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+    if( e )
+    {
+        CUDA_CHECK( cudaMemsetAsync( d_err_, 0, sizeof( int ), stream_ ) );
+        CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+        throw CudaError( "stage kernel: a tensor copy did not complete within the wait limit" );
     }
 }
 
@@ -1162,6 +1488,38 @@ void Engine::launch_stage( StageArgs<R> a, cudaStream_t st )
         return;
     }
     trace_mark( trace_, KERNEL_STAGE, st );
+    if constexpr( std::is_same<R, float>::value )
+    {
+        int buf = -1;
+        for( int b = 0; b < 3 && tma_; ++b )
+        {
+            void * const * bb = b == 0 ? spins_ : ( b == 1 ? predA_ : predB_ );
+            if( (void *)a.cfg.x == bb[0] && (void *)a.cfg.y == bb[1] && (void *)a.cfg.z == bb[2] )
+                buf = b;
+        }
+        if( buf >= 0 )
+        {
+            static int grid = 0;
+            if( !grid )
+            {
+                CUDA_CHECK( cudaFuncSetAttribute( llg_stage_tma<SOLVER, STAGE>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TT_SMEM ) );
+                int dev = 0, sms = 0, per = 0;
+                CUDA_CHECK( cudaGetDevice( &dev ) );
+                CUDA_CHECK( cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev ) );
+                CUDA_CHECK( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &per, llg_stage_tma<SOLVER, STAGE>, 256,
+                                                                           TT_SMEM ) );
+                grid = std::max( 1, sms * std::max( per, 1 ) );
+            }
+            TileMaps M;
+            for( int c = 0; c < 3; ++c )
+                M.m[c] = tmaps_[buf][c];
+            a.blkcount = d_tilecount_;
+            launch_pdl( llg_stage_tma<SOLVER, STAGE>, dim3( std::min( grid, n_tiles_ ) ), dim3( 256 ), TT_SMEM, st, 1,
+                        a, M, (const int4 *)d_tiles_, n_tiles_, d_err_ );
+            return;
+        }
+    }
     const int k = sizeof( R ) == 8 ? 0 : spt_idx_;
     a.blkmap    = d_sblkmap_[k];
     a.blkcount  = d_sblkcount_[k];
@@ -1279,6 +1637,8 @@ void Engine::launch_step_t()
 template<typename R>
 void Engine::tune_stages_t()
 {
+    if( tma_ )
+        return; // the TMA-staged kernel has one shape
     StageArgs<R> a{};
     a.sd   = d_desc_;
     a.runs = d_runs_;
@@ -1467,6 +1827,8 @@ void Engine::llg_launch( int n_steps )
 void Engine::sync()
 {
     CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+    if( tma_ )
+        check_err();
 }
 
 std::vector<Engine::Status> Engine::status()
@@ -1474,6 +1836,8 @@ std::vector<Engine::Status> Engine::status()
     std::vector<SysRun> r( desc_.size() );
     CUDA_CHECK( cudaMemcpyAsync( r.data(), d_runs_, sizeof( SysRun ) * r.size(), cudaMemcpyDeviceToHost, stream_ ) );
     CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
+    if( tma_ )
+        check_err();
     std::vector<Status> out( r.size() );
     for( size_t s = 0; s < r.size(); ++s )
         out[s] = { r[s].iteration, r[s].active, r[s].max_torque, r[s].energy };

@@ -4,6 +4,7 @@
 #include "ddi.hpp"
 #include "geometry.hpp"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <memory>
@@ -227,6 +228,18 @@ private:
     int n_sblocks_[3]     = { 0, 0, 0 };
     int spt_idx_          = 0;
     int tuned_solver_     = -1;
+    // TMA-staged persistent stage kernel (FP32 batches with a short stencil reach): tiles
+    // (system, first spin, aligned window start, copies per component), tiles per system, tensor
+    // maps of the three configuration buffers (state, predictor A, predictor B) x 3 components,
+    // and an error flag the kernel sets when a copy does not arrive within its wait limit
+    bool tma_           = false;
+    int4 * d_tiles_     = nullptr;
+    int * d_tilecount_  = nullptr;
+    int n_tiles_        = 0;
+    int * d_err_        = nullptr;
+    CUtensorMap tmaps_[3][3];
+    void build_tiles();
+    void check_err();
     bool any_ddi_     = false;
     DDIPlan ddi_;
     std::vector<DDISystem> ddi_systems_;

@@ -269,6 +269,55 @@ __device__ __forceinline__ double block_sum_w( R v, double * sh )
     return r;
 }
 
+// Compensated accumulation s + c += x: in FP32 the rounding error of every addition is kept in c
+// (TwoSum, Knuth: exact for round-to-nearest, no branch); FP64 accumulates plainly.
+template<typename R>
+__device__ __forceinline__ void comp_add( R & s, R & c, R x )
+{
+    if( sizeof( R ) == 4 )
+    {
+        const R t  = s + x;
+        const R bp = t - s;
+        c += ( s - ( t - bp ) ) + ( x - bp );
+        s = t;
+    }
+    else
+        s += x;
+}
+
+// Block sum of compensated FP32 partials (s, c): the shuffle tree inside each warp combines the
+// pairs with TwoSum (the errors of the tree's additions join c), each warp's s + c is formed in
+// FP64 and the warps are summed in FP64 by warp 0 (result valid in thread 0).  FP64 partials are
+// summed as block_sum_w does.
+template<typename R>
+__device__ __forceinline__ double block_sum_comp( R v, R c, double * sh )
+{
+    if( sizeof( R ) != 4 )
+        return block_sum_w( v, sh );
+    for( int o = 16; o > 0; o >>= 1 )
+    {
+        const R v2 = __shfl_down_sync( 0xffffffffu, v, o );
+        const R c2 = __shfl_down_sync( 0xffffffffu, c, o );
+        const R t  = v + v2;
+        const R bp = t - v;
+        c += c2 + ( ( v - ( t - bp ) ) + ( v2 - bp ) );
+        v = t;
+    }
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if( l == 0 )
+        sh[w] = (double)v + (double)c;
+    __syncthreads();
+    double r = 0;
+    if( threadIdx.x < 32 )
+    {
+        r = threadIdx.x < ( blockDim.x >> 5 ) ? sh[threadIdx.x] : 0.0;
+        for( int o = 16; o > 0; o >>= 1 )
+            r += __shfl_down_sync( 0xffffffffu, r, o );
+    }
+    return r;
+}
+
 __device__ __forceinline__ float block_max( float v, float * sh )
 {
     for( int o = 16; o > 0; o >>= 1 )
