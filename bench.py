@@ -735,7 +735,7 @@ def run_gb300(args):
                                         ctypes.c_int], ctypes.c_int)(p, tun, 16, -1, -1)
     tuned = dict(zip(["stage_spins_per_thread", "fft_a_lines", "fft_a_threads", "fft_b_lines", "fft_b_threads",
                       "fft_c_columns", "fft_c_threads", "fused_bc", "bc_cluster", "bc_threads", "ddi",
-                      "row_fused_stages"],
+                      "row_fused_stages", "tma_stage", "compensated_state"],
                      [int(tun[k]) for k in range(ntun)]))
     rows = bool(tuned.get("row_fused_stages", 0))
     value = NOS * args.steps * world / (ms / 1000.0)

@@ -350,8 +350,10 @@ double Simulation_LLG_Loss( State * state, const double * params, int n_steps, c
  * spins per thread of the stage kernels; lines and threads per block of FFT pass A / A'; lines
  * and threads of pass B / B'; columns and threads of pass C; 1 if the fused b/c pass is used;
  * its cluster size and threads per block; 1 if the run has a dipolar term; 1 if the stage kernels
- * do the passes along a themselves (row-fused stages).  Writes at most n
- * values; returns the number the engine reports (0 without a started run). */
+ * do the passes along a themselves (row-fused stages); 1 if the stage kernels stage each tile's
+ * configuration window in shared memory by tensor copies (TMA); 1 if the FP32 state is kept
+ * compensated (hi + lo float pairs).  Writes at most n values; returns the number the engine
+ * reports (0 without a started run). */
 int Simulation_Get_Tuning( State * state, int * values, int n, int idx_image, int idx_chain );
 /* EXTENSION: device arithmetic of the step loop: 32 (FP32 bulk, default) or 64 */
 void Simulation_Set_Precision( State * state, int bits );

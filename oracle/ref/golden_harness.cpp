@@ -12,6 +12,8 @@
 //   golden_harness grad    <cfg> <spins.bin> <out>         gradient, FP64 energy, per-term energies
 //   golden_harness direct  <cfg> <spins.bin> <out>         same, after switching DDI to the direct sum
 //   golden_harness llg     <cfg> <spins.bin> <out> <solver> <n_iter>
+//   golden_harness llgtime <cfg> <spins.bin> <solver> <n_iter>
+//                                                        wall time of Simulation_LLG_Start only (stdout)
 //   golden_harness gneb    <cfg> <chain.bin> <out> <noi> <solver> <n_iter> [<n_iter_ci>]
 //   golden_harness htst    <cfg> <chain.bin> <out> <noi> <idx_min> <idx_sp> <sparse> <n_keep>
 //                                                        HTST_Calculate on two images of a chain
@@ -30,6 +32,7 @@
 #include <data/State.hpp>
 #include <engine/Hamiltonian_Heisenberg.hpp>
 
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -180,6 +183,16 @@ int main( int argc, char ** argv )
         std::fprintf( f, "iterations %d\n", method->getNIterations() );
         std::fclose( f );
         dump_grad( s, out + "_final" );
+    }
+    else if( op == "llgtime" )
+    {
+        inject( s, read_bin( argv[3] ) );
+        int solver = std::atoi( argv[4] );
+        int n_iter = std::atoi( argv[5] );
+        auto t0    = std::chrono::steady_clock::now();
+        Simulation_LLG_Start( s, solver, n_iter, n_iter + 1 );
+        double dt = std::chrono::duration<double>( std::chrono::steady_clock::now() - t0 ).count();
+        std::printf( "nos %d iterations %d seconds %.6f\n", System_Get_NOS( s ), n_iter, dt );
     }
     else if( op == "gneb" )
     {

@@ -106,6 +106,7 @@ Engine & run_engine( State * st, Image & img )
         img.run         = std::make_unique<Engine>( std::vector<SystemInput>{ input_of( img, 0 ) }, fp64 );
         img.run_version = img.version;
         img.run_fp64    = fp64;
+        img.run->enable_compensation(); // FP32: compensated state of the LLG stage kernels
     }
     img.run->set_stream( (cudaStream_t)st->stream );
     return *img.run;

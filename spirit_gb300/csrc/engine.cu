@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
 #include <type_traits>
 
@@ -48,8 +49,71 @@ struct StageArgs
     SoA3<R> aux2;         // RK4 running sum
     SoA3<R> h;            // dipolar field of cfg (x == nullptr: none)
     SoA3<R> xi;           // thermal field of the iteration: written by stage 1, read by later stages
+    SoA3<R> lo;           // FP32 compensated state: low parts of s (x == nullptr: plain FP32 state)
     int tune;             // 1: timing run of the tuner (ignores and keeps the run state)
 };
+
+// ------------------------------------------------------------------ compensated FP32 state
+// With the compensated state an FP32 system keeps every spin as an unevaluated sum hi + lo of two
+// floats (about 48 significant bits).  Fields and stage arithmetic stay FP32 and read hi only; the
+// last stage of a step forms the solver's update as a small increment D of the state (s_new =
+// normalise(s + D), D of the order dt |field| gamma), and adds it to (hi, lo) with error-free
+// transformations: the rounding of the stored state -- about 3e-8 per step, which random-walks and
+// dominates the FP32 deviation from an FP64 trajectory -- no longer accumulates; what remains is
+// the FP32 error of D itself (1e-7 |D|).
+
+// TwoSum (Knuth): a + b = s + err exactly, round-to-nearest, no branch
+__device__ __forceinline__ float two_sum( float a, float b, float & err )
+{
+    const float s  = a + b;
+    const float bp = s - a;
+    err            = ( a - ( s - bp ) ) + ( b - bp );
+    return s;
+}
+
+// (hi, lo) += x, renormalised so that hi carries the rounded sum
+__device__ __forceinline__ void ff_add( float & hi, float & lo, float x )
+{
+    float e1, e2;
+    const float s = two_sum( hi, x, e1 );
+    const float l = lo + e1;
+    hi            = two_sum( s, l, e2 );
+    lo            = e2;
+}
+
+// Increment of a normalised update: s_new = (s + D) / |s + D| = s + E for s = hi + lo.
+// |s + D|^2 = 1 + u with u = (|s|^2 - 1) + 2 s.D + |D|^2, the first term formed exactly enough from
+// hi and lo (squares split by FMA, their sum by TwoSum; |hi|^2 is near 1, so subtracting 1 is
+// exact); then 1 / |s + D| = 1 + delta, delta = -u / (r (1 + r)), r = sqrt(1 + u) (no cancellation),
+// and E = D + delta (s + D).
+__device__ __forceinline__ V3<float> ff_norm_increment( V3<float> h, V3<float> l, V3<float> D )
+{
+    const float px = h.x * h.x, py = h.y * h.y, pz = h.z * h.z;
+    const float ex = fmaf( h.x, h.x, -px ), ey = fmaf( h.y, h.y, -py ), ez = fmaf( h.z, h.z, -pz );
+    float e1, e2;
+    float S       = two_sum( px, py, e1 );
+    S             = two_sum( S, pz, e2 );
+    const float eps = ( S - 1.f ) + ( ( e1 + e2 ) + ( ex + ey + ez ) ) + 2.f * ( h.x * l.x + h.y * l.y + h.z * l.z );
+    const float u   = eps + 2.f * ( h.x * D.x + h.y * D.y + h.z * D.z ) + ( D.x * D.x + D.y * D.y + D.z * D.z );
+    const float r   = sqrtf( 1.f + u );
+    const float dl  = -u / ( r * ( 1.f + r ) );
+    return { D.x + dl * ( h.x + D.x ), D.y + dl * ( h.y + D.y ), D.z + dl * ( h.z + D.z ) };
+}
+
+// s (= hi + lo at gi) <- normalise(s + D), stored back as hi and lo; returns the new hi
+template<typename R>
+__device__ __forceinline__ V3<float> ff_update( const StageArgs<R> & A, long long gi, V3<float> h, V3<float> D )
+{
+    V3<float> l       = { (float)A.lo.x[gi], (float)A.lo.y[gi], (float)A.lo.z[gi] };
+    const V3<float> E = ff_norm_increment( h, l, D );
+    ff_add( h.x, l.x, E.x );
+    ff_add( h.y, l.y, E.y );
+    ff_add( h.z, l.z, E.z );
+    A.lo.x[gi] = (R)l.x;
+    A.lo.y[gi] = (R)l.y;
+    A.lo.z[gi] = (R)l.z;
+    return h;
+}
 
 enum
 {
@@ -107,10 +171,26 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
         }
         else
         {
-            V3<R> sn = sib( si, fv );
-            // SIB preserves |s| only in exact arithmetic; in FP32 the rounding drift is removed
-            if( sizeof( R ) == 4 )
-                sn = normalized( sn );
+            V3<R> sn;
+            if( sizeof( R ) == 4 && A.lo.x )
+            {
+                // sib(s, fv) - s = 2 (A x s + A x (A x s)) / (1 + |A|^2), A = fv / 2
+                const V3<R> Ah = { R( 0.5 ) * fv.x, R( 0.5 ) * fv.y, R( 0.5 ) * fv.z };
+                const V3<R> c1 = cross( Ah, si );
+                const V3<R> c2 = cross( Ah, c1 );
+                const R w      = R( 2 ) / ( R( 1 ) + dot( Ah, Ah ) );
+                const V3<float> D = { float( w * ( c1.x + c2.x ) ), float( w * ( c1.y + c2.y ) ),
+                                      float( w * ( c1.z + c2.z ) ) };
+                const V3<float> hn = ff_update( A, gi, V3<float>{ (float)si.x, (float)si.y, (float)si.z }, D );
+                sn                 = { (R)hn.x, (R)hn.y, (R)hn.z };
+            }
+            else
+            {
+                sn = sib( si, fv );
+                // SIB preserves |s| only in exact arithmetic; in FP32 the rounding drift is removed
+                if( sizeof( R ) == 4 )
+                    sn = normalized( sn );
+            }
             A.s.st( gi, sn );
             t2 = fmaxf( t2, (float)torque2( A.aux1.ld( gi ), sn ) );
         }
@@ -131,14 +211,25 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
             V3<R> c1        = cross( si, fv1 );
             V3<R> t1        = { R( -1 ) * c1.x, R( -1 ) * c1.y, R( -1 ) * c1.z };
             V3<R> c2        = cross( ci, fv );
-            V3<R> t         = { t1.x * R( 0.5 ), t1.y * R( 0.5 ), t1.z * R( 0.5 ) };
-            t.x += si.x;
-            t.y += si.y;
-            t.z += si.z;
-            t.x += R( 0.5 ) * ( R( -1 ) * c2.x );
-            t.y += R( 0.5 ) * ( R( -1 ) * c2.y );
-            t.z += R( 0.5 ) * ( R( -1 ) * c2.z );
-            V3<R> sn = normalized( t );
+            V3<R> sn;
+            if( sizeof( R ) == 4 && A.lo.x )
+            {
+                const V3<float> D  = { float( R( 0.5 ) * t1.x - R( 0.5 ) * c2.x ), float( R( 0.5 ) * t1.y - R( 0.5 ) * c2.y ),
+                                       float( R( 0.5 ) * t1.z - R( 0.5 ) * c2.z ) };
+                const V3<float> hn = ff_update( A, gi, V3<float>{ (float)si.x, (float)si.y, (float)si.z }, D );
+                sn                 = { (R)hn.x, (R)hn.y, (R)hn.z };
+            }
+            else
+            {
+                V3<R> t = { t1.x * R( 0.5 ), t1.y * R( 0.5 ), t1.z * R( 0.5 ) };
+                t.x += si.x;
+                t.y += si.y;
+                t.z += si.z;
+                t.x += R( 0.5 ) * ( R( -1 ) * c2.x );
+                t.y += R( 0.5 ) * ( R( -1 ) * c2.y );
+                t.z += R( 0.5 ) * ( R( -1 ) * c2.z );
+                sn = normalized( t );
+            }
             A.s.st( gi, sn );
             t2 = fmaxf( t2, (float)torque2( fv1, sn ) );
         }
@@ -160,11 +251,34 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
             ax.x += R( 0.5 ) * fv.x;
             ax.y += R( 0.5 ) * fv.y;
             ax.z += R( 0.5 ) * fv.z;
-            R ang    = sqrt( dot( ax, ax ) );
-            V3<R> sn = rotate( si, normalized( ax ), ang );
-            // a rotation preserves |s| only in exact arithmetic; in FP32 the rounding drift is removed
-            if( sizeof( R ) == 4 )
-                sn = normalized( sn );
+            R ang = sqrt( dot( ax, ax ) );
+            V3<R> sn;
+            if( sizeof( R ) == 4 && A.lo.x )
+            {
+                // rotation by w = ax (angle |w|) as an increment:
+                // D = (sin t / t) w x s + ((1 - cos t) / t^2) w x (w x s), both factors from sin / cos of t/2
+                V3<float> D = { 0.f, 0.f, 0.f };
+                if( ang > R( 0 ) )
+                {
+                    float sh, ch;
+                    sincosf( 0.5f * (float)ang, &sh, &ch );
+                    const float q     = sh / (float)ang;
+                    const float f1    = 2.f * q * ch, f2 = 2.f * q * q;
+                    const V3<R> c1    = cross( ax, si );
+                    const V3<R> c2    = cross( ax, c1 );
+                    D                 = { f1 * (float)c1.x + f2 * (float)c2.x, f1 * (float)c1.y + f2 * (float)c2.y,
+                                          f1 * (float)c1.z + f2 * (float)c2.z };
+                }
+                const V3<float> hn = ff_update( A, gi, V3<float>{ (float)si.x, (float)si.y, (float)si.z }, D );
+                sn                 = { (R)hn.x, (R)hn.y, (R)hn.z };
+            }
+            else
+            {
+                sn = rotate( si, normalized( ax ), ang );
+                // a rotation preserves |s| only in exact arithmetic; in FP32 the rounding drift is removed
+                if( sizeof( R ) == 4 )
+                    sn = normalized( sn );
+            }
             A.s.st( gi, sn );
             t2 = fmaxf( t2, (float)torque2( fv1, sn ) );
         }
@@ -178,7 +292,8 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
         if( STAGE == 1 )
         {
             A.aux1.st( gi, fv );
-            V3<R> acc = si;
+            // compensated state: the running sum holds the increments only (s stays in (hi, lo))
+            V3<R> acc = ( sizeof( R ) == 4 && A.lo.x ) ? V3<R>{ 0, 0, 0 } : si;
             R w6      = R( 1.0 / 6.0 );
             acc.x += w6 * k.x;
             acc.y += w6 * k.y;
@@ -206,7 +321,15 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
             acc.x += w6 * k.x;
             acc.y += w6 * k.y;
             acc.z += w6 * k.z;
-            V3<R> sn = normalized( acc );
+            V3<R> sn;
+            if( sizeof( R ) == 4 && A.lo.x )
+            {
+                const V3<float> hn = ff_update( A, gi, V3<float>{ (float)si.x, (float)si.y, (float)si.z },
+                                                V3<float>{ (float)acc.x, (float)acc.y, (float)acc.z } );
+                sn                 = { (R)hn.x, (R)hn.y, (R)hn.z };
+            }
+            else
+                sn = normalized( acc );
             A.s.st( gi, sn );
             t2 = fmaxf( t2, (float)torque2( A.aux1.ld( gi ), sn ) );
         }
@@ -778,21 +901,36 @@ __global__ void __launch_bounds__( 256 ) eval_kernel( const SysDesc * sd, const 
 }
 
 // ------------------------------------------------------------------ transfers
+// lo (x != nullptr, FP32 compensated state): also the low parts, x - (double)(float)x
 template<typename R>
-__global__ void aos_to_soa( const double * aos, SoA3<R> dst, long long off, int n )
-{
-    for( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
-        dst.st( off + i, V3<R>{ (R)aos[3 * (size_t)i], (R)aos[3 * (size_t)i + 1], (R)aos[3 * (size_t)i + 2] } );
-}
-template<typename R>
-__global__ void soa_to_aos( SoA3<R> src, long long off, int n, double * aos )
+__global__ void aos_to_soa( const double * aos, SoA3<R> dst, long long off, int n, SoA3<R> lo )
 {
     for( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
     {
-        V3<R> v                  = src.ld( off + i );
-        aos[3 * (size_t)i]       = v.x;
-        aos[3 * (size_t)i + 1]   = v.y;
-        aos[3 * (size_t)i + 2]   = v.z;
+        const double v[3] = { aos[3 * (size_t)i], aos[3 * (size_t)i + 1], aos[3 * (size_t)i + 2] };
+        const V3<R> h     = { (R)v[0], (R)v[1], (R)v[2] };
+        dst.st( off + i, h );
+        if( lo.x )
+            lo.st( off + i, V3<R>{ (R)( v[0] - (double)h.x ), (R)( v[1] - (double)h.y ), (R)( v[2] - (double)h.z ) } );
+    }
+}
+template<typename R>
+__global__ void soa_to_aos( SoA3<R> src, long long off, int n, double * aos, SoA3<R> lo )
+{
+    for( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x )
+    {
+        V3<R> v              = src.ld( off + i );
+        double x = v.x, y = v.y, z = v.z;
+        if( lo.x )
+        {
+            const V3<R> l = lo.ld( off + i );
+            x += (double)l.x;
+            y += (double)l.y;
+            z += (double)l.z;
+        }
+        aos[3 * (size_t)i]     = x;
+        aos[3 * (size_t)i + 1] = y;
+        aos[3 * (size_t)i + 2] = z;
     }
 }
 
@@ -961,6 +1099,7 @@ Engine::~Engine()
         dfree( aux2_[c] );
         dfree( noise_[c] );
         dfree( field_[c] );
+        dfree( lo_[c] );
     }
     dfree( d_desc_ );
     dfree( d_runs_ );
@@ -1138,15 +1277,23 @@ bool encode_tensor_map_1d_f32( CUtensorMap * map, const void * base, unsigned lo
         }
         return reinterpret_cast<Encode>( f );
     }();
+    const bool debug = std::getenv( "SPIRIT_GB300_DEBUG" ) != nullptr;
     if( !encode || ( reinterpret_cast<uintptr_t>( base ) & 15 ) )
+    {
+        if( debug )
+            std::fprintf( stderr, "spirit_gb300: no tensor-map encoder (%d) or unaligned base\n", encode != nullptr );
         return false;
+    }
     const cuuint64_t dim[1]  = { n };
+    const cuuint64_t str[1]  = { n * sizeof( float ) }; // rank 1: no stride is read
     const cuuint32_t bx[1]   = { box };
     const cuuint32_t estr[1] = { 1 };
-    return encode( map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 1, const_cast<void *>( base ), dim, nullptr, bx, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE )
-           == CUDA_SUCCESS;
+    const CUresult r = encode( map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 1, const_cast<void *>( base ), dim, str, bx, estr,
+                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE );
+    if( r != CUDA_SUCCESS && debug )
+        std::fprintf( stderr, "spirit_gb300: cuTensorMapEncodeTiled returned %d\n", (int)r );
+    return r == CUDA_SUCCESS;
 }
 
 // The TMA-staged stage kernel serves FP32 batches in which every system's window (a tile of
@@ -1180,7 +1327,11 @@ void Engine::build_tiles()
             const long long hi   = d.spin_offset + t0 + n + H;
             const long long ncpy = ( hi - xs + TT_BOX - 1 ) / TT_BOX;
             if( ncpy > TT_NCOPY )
+            {
+                if( std::getenv( "SPIRIT_GB300_DEBUG" ) )
+                    std::fprintf( stderr, "spirit_gb300: system %zu reaches %lld spins: llg_stage\n", s, H );
                 return; // a stencil reaching too far: llg_stage serves this batch
+            }
             tiles.push_back( make_int4( (int)s, t0, (int)xs, (int)ncpy ) );
             ++count[s];
         }
@@ -1197,6 +1348,9 @@ void Engine::build_tiles()
     h2d( d_tilecount_, count.data(), count.size() );
     n_tiles_ = (int)tiles.size();
     tma_     = n_tiles_ > 0;
+    if( std::getenv( "SPIRIT_GB300_DEBUG" ) )
+        std::fprintf( stderr, "spirit_gb300: TMA-staged stage kernel, %d systems, %d tiles\n", (int)desc_.size(),
+                      n_tiles_ );
 }
 
 void Engine::check_err()
@@ -1294,6 +1448,44 @@ static SoA3<R> soa( void * const * p )
     return { (R *)p[0], (R *)p[1], (R *)p[2] };
 }
 
+// Low parts of the compensated FP32 state as kernel arguments: for writing (set_spins: the low parts
+// of the host values) and for reading (only while they belong to the current high parts)
+SoA3<float> Engine::lo_soa()
+{
+    if( !comp_ )
+        return { nullptr, nullptr, nullptr };
+    if( !lo_valid_ )
+    {
+        // high parts changed behind the state's back (spin_ptr): start the low parts from zero
+        for( int c = 0; c < 3; ++c )
+            CUDA_CHECK( cudaMemsetAsync( lo_[c], 0, total_ * sizeof( float ), stream_ ) );
+        lo_valid_ = true;
+    }
+    return { (float *)lo_[0], (float *)lo_[1], (float *)lo_[2] };
+}
+
+SoA3<float> Engine::lo_valid() const
+{
+    if( comp_ && lo_valid_ )
+        return { (float *)lo_[0], (float *)lo_[1], (float *)lo_[2] };
+    return { nullptr, nullptr, nullptr };
+}
+
+// Keep FP32 spins as hi + lo pairs (the compensated state of the LLG stage kernels);
+// SPIRIT_GB300_COMP=0 keeps the plain FP32 state.  No effect on FP64 engines.
+void Engine::enable_compensation()
+{
+    if( fp64_ || comp_ )
+        return;
+    const char * env = std::getenv( "SPIRIT_GB300_COMP" );
+    if( env && env[0] == '0' )
+        return;
+    for( int c = 0; c < 3; ++c )
+        lo_[c] = dalloc_bytes( total_ * sizeof( float ) ); // zero: the current state is hi exactly
+    comp_     = true;
+    lo_valid_ = true;
+}
+
 void Engine::set_spins( int s, const double * aos, bool sync )
 {
     w1_valid_         = false;
@@ -1301,9 +1493,10 @@ void Engine::set_spins( int s, const double * aos, bool sync )
     CUDA_CHECK( cudaMemcpyAsync( d_stage_, aos, sizeof( double ) * 3 * d.nos, cudaMemcpyHostToDevice, stream_ ) );
     int grid = std::min( 1024, ( d.nos + 255 ) / 256 );
     if( fp64_ )
-        aos_to_soa<double><<<grid, 256, 0, stream_>>>( d_stage_, soa<double>( spins_ ), d.spin_offset, d.nos );
+        aos_to_soa<double><<<grid, 256, 0, stream_>>>( d_stage_, soa<double>( spins_ ), d.spin_offset, d.nos,
+                                                        SoA3<double>{ nullptr, nullptr, nullptr } );
     else
-        aos_to_soa<float><<<grid, 256, 0, stream_>>>( d_stage_, soa<float>( spins_ ), d.spin_offset, d.nos );
+        aos_to_soa<float><<<grid, 256, 0, stream_>>>( d_stage_, soa<float>( spins_ ), d.spin_offset, d.nos, lo_soa() );
     CUDA_CHECK( cudaGetLastError() );
     if( sync )
         CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
@@ -1314,9 +1507,11 @@ Engine::Status Engine::fetch( int s, double * aos )
     const SysDesc & d = desc_[s];
     int grid          = std::min( 1024, ( d.nos + 255 ) / 256 );
     if( fp64_ )
-        soa_to_aos<double><<<grid, 256, 0, stream_>>>( soa<double>( spins_ ), d.spin_offset, d.nos, d_stage_ );
+        soa_to_aos<double><<<grid, 256, 0, stream_>>>( soa<double>( spins_ ), d.spin_offset, d.nos, d_stage_,
+                                                        SoA3<double>{ nullptr, nullptr, nullptr } );
     else
-        soa_to_aos<float><<<grid, 256, 0, stream_>>>( soa<float>( spins_ ), d.spin_offset, d.nos, d_stage_ );
+        soa_to_aos<float><<<grid, 256, 0, stream_>>>( soa<float>( spins_ ), d.spin_offset, d.nos, d_stage_,
+                                                       lo_valid() );
     CUDA_CHECK( cudaGetLastError() );
     CUDA_CHECK( cudaMemcpyAsync( aos, d_stage_, sizeof( double ) * 3 * d.nos, cudaMemcpyDeviceToHost, stream_ ) );
     SysRun r;
@@ -1330,9 +1525,11 @@ void Engine::get_spins( int s, double * aos )
     const SysDesc & d = desc_[s];
     int grid          = std::min( 1024, ( d.nos + 255 ) / 256 );
     if( fp64_ )
-        soa_to_aos<double><<<grid, 256, 0, stream_>>>( soa<double>( spins_ ), d.spin_offset, d.nos, d_stage_ );
+        soa_to_aos<double><<<grid, 256, 0, stream_>>>( soa<double>( spins_ ), d.spin_offset, d.nos, d_stage_,
+                                                        SoA3<double>{ nullptr, nullptr, nullptr } );
     else
-        soa_to_aos<float><<<grid, 256, 0, stream_>>>( soa<float>( spins_ ), d.spin_offset, d.nos, d_stage_ );
+        soa_to_aos<float><<<grid, 256, 0, stream_>>>( soa<float>( spins_ ), d.spin_offset, d.nos, d_stage_,
+                                                       lo_valid() );
     CUDA_CHECK( cudaGetLastError() );
     CUDA_CHECK( cudaMemcpyAsync( aos, d_stage_, sizeof( double ) * 3 * d.nos, cudaMemcpyDeviceToHost, stream_ ) );
     CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
@@ -1351,9 +1548,11 @@ void Engine::set_all_spins( const double * aos )
     {
         int grid = std::min( 1024, ( d.nos + 255 ) / 256 );
         if( fp64_ )
-            aos_to_soa<double><<<grid, 256, 0, stream_>>>( d_stage_ + o, soa<double>( spins_ ), d.spin_offset, d.nos );
+            aos_to_soa<double><<<grid, 256, 0, stream_>>>( d_stage_ + o, soa<double>( spins_ ), d.spin_offset, d.nos,
+                                                            SoA3<double>{ nullptr, nullptr, nullptr } );
         else
-            aos_to_soa<float><<<grid, 256, 0, stream_>>>( d_stage_ + o, soa<float>( spins_ ), d.spin_offset, d.nos );
+            aos_to_soa<float><<<grid, 256, 0, stream_>>>( d_stage_ + o, soa<float>( spins_ ), d.spin_offset, d.nos,
+                                                           lo_soa() );
         o += 3 * (size_t)d.nos;
     }
     CUDA_CHECK( cudaGetLastError() );
@@ -1366,9 +1565,11 @@ void Engine::get_all_spins( double * aos )
     {
         int grid = std::min( 1024, ( d.nos + 255 ) / 256 );
         if( fp64_ )
-            soa_to_aos<double><<<grid, 256, 0, stream_>>>( soa<double>( spins_ ), d.spin_offset, d.nos, d_stage_ + o );
+            soa_to_aos<double><<<grid, 256, 0, stream_>>>( soa<double>( spins_ ), d.spin_offset, d.nos, d_stage_ + o,
+                                                            SoA3<double>{ nullptr, nullptr, nullptr } );
         else
-            soa_to_aos<float><<<grid, 256, 0, stream_>>>( soa<float>( spins_ ), d.spin_offset, d.nos, d_stage_ + o );
+            soa_to_aos<float><<<grid, 256, 0, stream_>>>( soa<float>( spins_ ), d.spin_offset, d.nos, d_stage_ + o,
+                                                           lo_valid() );
         o += 3 * (size_t)d.nos;
     }
     CUDA_CHECK( cudaGetLastError() );
@@ -1441,9 +1642,11 @@ void Engine::ddi_field( int s, double * h_aos )
     w1_valid_ = false;
     int grid = std::min( 1024, ( d.nos + 255 ) / 256 );
     if( fp64_ )
-        soa_to_aos<double><<<grid, 256, 0, stream_>>>( soa<double>( field_ ), d.spin_offset, d.nos, d_stage_ );
+        soa_to_aos<double><<<grid, 256, 0, stream_>>>( soa<double>( field_ ), d.spin_offset, d.nos, d_stage_,
+                                                        SoA3<double>{ nullptr, nullptr, nullptr } );
     else
-        soa_to_aos<float><<<grid, 256, 0, stream_>>>( soa<float>( field_ ), d.spin_offset, d.nos, d_stage_ );
+        soa_to_aos<float><<<grid, 256, 0, stream_>>>( soa<float>( field_ ), d.spin_offset, d.nos, d_stage_,
+                                                       SoA3<float>{ nullptr, nullptr, nullptr } );
     CUDA_CHECK( cudaGetLastError() );
     CUDA_CHECK( cudaMemcpyAsync( h_aos, d_stage_, sizeof( double ) * 3 * d.nos, cudaMemcpyDeviceToHost, stream_ ) );
     CUDA_CHECK( cudaStreamSynchronize( stream_ ) );
@@ -1628,6 +1831,8 @@ void Engine::launch_step_t()
     a.h    = any_ddi_ ? soa<R>( field_ ) : SoA3<R>{ nullptr, nullptr, nullptr };
     a.xi   = soa<R>( noise_ );
     a.tune = 0;
+    if constexpr( std::is_same<R, float>::value )
+        a.lo = lo_soa();
     launch_stages_t<R>( a, true );
 }
 
@@ -1750,12 +1955,13 @@ void Engine::profile_steps( int n, void * flush_buf, size_t flush_bytes, void * 
 
 int Engine::tuning( int * out, int n ) const
 {
-    const int v[12] = { SPT_OPTIONS[fp64_ ? 0 : spt_idx_], ddi_.tile[0], ddi_.threads[0], ddi_.tile[1],
+    const int v[14] = { SPT_OPTIONS[fp64_ ? 0 : spt_idx_], ddi_.tile[0], ddi_.threads[0], ddi_.tile[1],
                         ddi_.threads[1], ddi_.tile[2], ddi_.threads[2], ddi_.fused ? 1 : 0,
-                        ddi_.cluster_k, ddi_.threads_bc, any_ddi_ ? 1 : 0, rows_ ? 1 : 0 };
-    for( int k = 0; k < n && k < 12; ++k )
+                        ddi_.cluster_k, ddi_.threads_bc, any_ddi_ ? 1 : 0, rows_ ? 1 : 0, tma_ ? 1 : 0,
+                        comp_ ? 1 : 0 };
+    for( int k = 0; k < n && k < 14; ++k )
         out[k] = v[k];
-    return 12;
+    return 14;
 }
 
 int Engine::kernels_per_step() const
@@ -1798,6 +2004,16 @@ void Engine::llg_launch( int n_steps )
     // budget or after its convergence are no-ops on the device
     const int G = 8;
     ensure_spectrum();
+    static const bool graphs = [] {
+        const char * e = std::getenv( "SPIRIT_GB300_GRAPHS" ); // 0: direct launches (profilers)
+        return !( e && e[0] == '0' );
+    }();
+    if( !graphs )
+    {
+        for( int k = 0; k < n_steps; ++k )
+            launch_step_kernels();
+        return;
+    }
     if( !graph_ || graph_solver_ != solver_ )
     {
         if( graph_ )

@@ -29,6 +29,8 @@ struct SystemInput
 
 template<typename R>
 struct StageArgs;
+template<typename R>
+struct SoA3;
 
 // Host-side system descriptor of one system (spin_offset 0), as the engine builds it
 void fill_system_desc( SysDesc & d, const SystemInput & in );
@@ -121,10 +123,19 @@ public:
     // DDI field h of the current spins (tests)
     void ddi_field( int s, double * h_aos );
 
-    // raw device pointers (component arrays) for the adjoint / GNEB layers
+    // raw device pointers (component arrays) for the GNEB / Monte Carlo layers; their kernels
+    // write the FP32 spins without the low parts of the compensated state, which therefore restart
+    // from zero at the next LLG use
     void * spin_ptr( int comp ) const
     {
+        lo_valid_ = false;
         return spins_[comp];
+    }
+    // FP32 LLG: keep the state compensated (hi + lo per component, see engine.cu)
+    void enable_compensation();
+    bool compensated() const
+    {
+        return comp_;
     }
     const SysDesc * d_desc() const
     {
@@ -215,6 +226,11 @@ private:
     void * aux2_[3]  = { nullptr, nullptr, nullptr };
     void * noise_[3] = { nullptr, nullptr, nullptr }; // thermal field of the current iteration
     void * field_[3] = { nullptr, nullptr, nullptr };
+    void * lo_[3]    = { nullptr, nullptr, nullptr }; // low parts of the compensated FP32 state
+    bool comp_       = false;
+    mutable bool lo_valid_ = false; // lo_ belongs to the current high parts
+    SoA3<float> lo_soa();
+    SoA3<float> lo_valid() const;
     double * d_stage_ = nullptr; // AoS double staging for transfers
     double * d_red_   = nullptr; // reduction scratch (per-term sums)
     double * d_grad_  = nullptr; // AoS double gradient output

@@ -1287,6 +1287,7 @@ static Engine & batched_prepare( State ** states, int n_states, int solver, int 
             in.push_back( s );
         }
         C.eng  = std::make_unique<Engine>( in, fp64 );
+        C.eng->enable_compensation(); // FP32: compensated state of the LLG stage kernels
         C.key  = key;
         C.fp64 = fp64;
     }

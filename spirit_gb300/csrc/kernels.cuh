@@ -292,7 +292,7 @@ __device__ __forceinline__ void comp_add( R & s, R & c, R x )
 template<typename R>
 __device__ __forceinline__ double block_sum_comp( R v, R c, double * sh )
 {
-    if( sizeof( R ) != 4 )
+    if constexpr( sizeof( R ) != 4 )
         return block_sum_w( v, sh );
     for( int o = 16; o > 0; o >>= 1 )
     {

@@ -116,3 +116,22 @@ def test_c2_fp32_energy_error(which):
     print("FP32 path energy error (%s configuration): %.3e meV per spin, %.3e relative (E = %.6f meV)"
           % (which, err, abs(E - ref) / abs(ref), ref))
     assert err <= 1e-8, (E, ref)
+
+
+@pytest.mark.parametrize("name", ["c1_full", "c2_t0"])
+def test_compensated_state_accuracy(name, monkeypatch):
+    """FP32 with the compensated state (spins kept as hi + lo float pairs, updates added with
+    error-free transformations) against the plain FP32 state, both against the reference run:
+    the compensated state removes the accumulated rounding of the stored spins."""
+    from spirit_gb300 import simulation
+
+    f, spec, s0, sid, n_iter = _case(name)
+    ref = f["spins_out"].astype(np.float64)
+    dm = {}
+    for comp in ("1", "0"):
+        monkeypatch.setenv("SPIRIT_GB300_COMP", comp)
+        with make_state(spec, s0, precision=32, name="comp" + comp) as p:
+            simulation.start(p, simulation.METHOD_LLG, sid, n_iter)
+            dm[comp] = float(np.abs(spins_of(p) - ref).max())
+    print("%s FP32 max|dm| vs reference: compensated %.3e, plain %.3e" % (name, dm["1"], dm["0"]))
+    assert dm["1"] <= dm["0"] and dm["1"] <= 1e-5, dm

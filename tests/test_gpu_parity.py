@@ -150,6 +150,36 @@ def test_row_fused_stages_bitwise(solver, monkeypatch):
     np.testing.assert_array_equal(out[0], out[1])
 
 
+def _tuning(p):
+    import ctypes
+
+    from spirit_gb300.spiritlib import fn
+
+    get = fn("Simulation_Get_Tuning", [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int], ctypes.c_int)
+    v = (ctypes.c_int * 16)()
+    n = get(p, v, 16, -1, -1)
+    return [int(v[k]) for k in range(n)]
+
+
+@pytest.mark.parametrize("tma", ["1", "0"])
+def test_tma_stage_kernel_selected(tma, monkeypatch):
+    """An FP32 2D system runs the TMA-staged stage kernel (tuning value 12) with the compensated
+    state (value 13); SPIRIT_GB300_TMA=0 selects llg_stage; FP64 never uses either."""
+    from oracle.oracle import random_spins
+    from spirit_gb300 import simulation
+
+    monkeypatch.setenv("SPIRIT_GB300_TMA", tma)
+    spec = dict(GRAD_CASES["sq_c1"], n_cells=[48, 40, 1], llg=dict(dt=1e-3, damping=0.2, temperature=5.0, seed=1))
+    for prec in (32, 64):
+        with make_state(spec, random_spins(48 * 40, 5), precision=prec, name="tmasel%s" % tma) as p:
+            simulation.start(p, simulation.METHOD_LLG, simulation.SOLVER_SIB, 4)
+            t = _tuning(p)
+        assert len(t) >= 14
+        assert t[12] == (1 if (tma == "1" and prec == 32) else 0), (prec, t)
+        assert t[13] == (1 if prec == 32 else 0), (prec, t)
+
+
 @pytest.mark.parametrize("solver", ["SIB", "Heun", "RK4", "Depondt"])
 def test_tma_stage_kernel_bitwise(solver, monkeypatch):
     """The TMA-staged persistent stage kernel (tiles of 1024 spins, configuration window in shared
