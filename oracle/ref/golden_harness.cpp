@@ -12,6 +12,8 @@
 //   golden_harness grad    <cfg> <spins.bin> <out>         gradient, FP64 energy, per-term energies
 //   golden_harness direct  <cfg> <spins.bin> <out>         same, after switching DDI to the direct sum
 //   golden_harness llg     <cfg> <spins.bin> <out> <solver> <n_iter>
+//   golden_harness ovfwrite <cfg> <spins.bin> <file> <format>   IO_Image_Write of the injected spins
+//   golden_harness ovfread  <cfg> <file> <out.bin>               IO_Image_Read, then the spins it holds
 //   golden_harness llgtime <cfg> <spins.bin> <solver> <n_iter>
 //                                                        wall time of Simulation_LLG_Start only (stdout)
 //   golden_harness gneb    <cfg> <chain.bin> <out> <noi> <solver> <n_iter> [<n_iter_ci>]
@@ -23,6 +25,7 @@
 #include <Spirit/Configurations.h>
 #include <Spirit/Geometry.h>
 #include <Spirit/HTST.h>
+#include <Spirit/IO.h>
 #include <Spirit/Hamiltonian.h>
 #include <Spirit/Parameters_GNEB.h>
 #include <Spirit/Parameters_LLG.h>
@@ -183,6 +186,16 @@ int main( int argc, char ** argv )
         std::fprintf( f, "iterations %d\n", method->getNIterations() );
         std::fclose( f );
         dump_grad( s, out + "_final" );
+    }
+    else if( op == "ovfwrite" )
+    {
+        inject( s, read_bin( argv[3] ) );
+        IO_Image_Write( s, argv[4], std::atoi( argv[5] ), "written by the reference" );
+    }
+    else if( op == "ovfread" )
+    {
+        IO_Image_Read( s, argv[3] );
+        write_bin( argv[4], System_Get_Spin_Directions( s ), 3 * (size_t)System_Get_NOS( s ) );
     }
     else if( op == "llgtime" )
     {

@@ -146,3 +146,10 @@ HTST_CASES = [
     ("tilted8", dict(_HTST_BASE, n_cells=[8, 1, 1], lattice_constant=3.0, field=(4.0, (0.2, 0.1, -1.0)),
                      anisotropy=(0.5, (0.1, 0.2, 1.0)), dij=[0.0]), 5),
 ]
+
+# OVF interchange with the reference: files written by the reference's IO_Image_Write in each data
+# format (reference format ids: binary 4 = 1, binary 8 = 2, text = 3, csv = 4) are committed under
+# tests/golden/ovf/, and files written by this library are read back by the reference
+OVF_SPEC = dict(bravais="sc", n_cells=[5, 4, 3], lattice_constant=1.0, mu_s=[2.0], bc=[1, 1, 0],
+                field=(0.5, (0, 0, 1)), anisotropy=(0.1, (0, 0, 1)), jij=[1.0], dij=[0.2], dm_chirality=2)
+OVF_FORMATS = {"bin4": 1, "bin8": 2, "text": 3, "csv": 4}

@@ -22,7 +22,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
-from cases import FULL_CASES, GRAD_CASES, HTST_CASES, LLG_CASES, PAIR_GEOMETRIES, SOLVERS, SPIN_SEED  # noqa: E402
+from cases import (FULL_CASES, GRAD_CASES, HTST_CASES, LLG_CASES, OVF_FORMATS, OVF_SPEC, PAIR_GEOMETRIES,  # noqa: E402
+                   SOLVERS, SPIN_SEED)
 from oracle.oracle import (OracleSystem, image_types_auto, portable_spins, random_spins,  # noqa: E402
                            transition_homogeneous)
 from spirit_gb300.configs import config_text, write_config  # noqa: E402
@@ -151,6 +152,33 @@ def main(only=None):
             energy=res["energy_image"], max_torque=res["max_torque"], iterations=int(res["iterations"]),
         )
         out["full_" + name] = res
+    # --- OVF interchange: the reference writes the seeded spins in every format (files committed
+    # under ovf/), and reads back files this library wrote (what it read is stored)
+    if want("ovf"):
+        from spirit_gb300 import io as sio
+        from spirit_gb300 import state as sstate
+        from spirit_gb300 import system as ssystem
+
+        odir = os.path.join(HERE, "ovf")
+        os.makedirs(odir, exist_ok=True)
+        cfg = write_config(OVF_SPEC, os.path.join(tmp, "ovf.cfg"))
+        nos = nos_of(OVF_SPEC)
+        spins = random_spins(nos, 31)
+        sp = os.path.join(tmp, "ovf_spins.bin")
+        spins.tofile(sp)
+        read_back = {}
+        for name, fid in OVF_FORMATS.items():
+            run(["ovfwrite", cfg, sp, os.path.join(odir, "reference_%s.ovf" % name), str(fid)], tmp)
+            ours = os.path.join(odir, "spirit_gb300_%s.ovf" % name)
+            with sstate.State(cfg, True) as p:
+                ssystem.get_spin_directions(p)[:] = spins
+                sio.image_write(p, ours, fid, "written by spirit_gb300")
+            out_bin = os.path.join(tmp, "read_%s.bin" % name)
+            run(["ovfread", cfg, ours, out_bin], tmp)
+            read_back[name] = load_bin(out_bin, (-1, 3))
+        np.savez_compressed(os.path.join(HERE, "ovf_interchange.npz"), config=config_text(OVF_SPEC), spins=spins,
+                            **{"reference_read_" + k: v for k, v in read_back.items()})
+        out["ovf"] = sorted(read_back)
     # --- GNEB (VP) on the reference solver-test system: skyrmion collapse, 9 images
     spec = SOLVERS
     cfg = write_config(spec, os.path.join(tmp, "solvers.cfg"))
