@@ -487,18 +487,35 @@ def run_gneb(iters_cap=60000):
     gneb.set_convergence(p, 1e-6)
     gneb.set_spring_constant(p, 1.0)
     chain0 = np.array([np.array(system.get_spin_directions(p, i)) for i in range(C3_IMAGES)])
+    # FP32 forces until the max torque is below 1e-5 meV (FP32 rounding of the forces leaves a torque
+    # floor of a few 1e-6 meV), then FP64 to the 1e-6 meV criterion from the same chain and image types
     t0 = time.perf_counter()
+    gneb.set_convergence(p, 1e-5)
     info1 = simulation.start(p, simulation.METHOD_GNEB, simulation.SOLVER_VP, 2000)
     gneb.set_image_type_automatically(p)
     info2 = simulation.start(p, simulation.METHOD_GNEB, simulation.SOLVER_VP, iters_cap)
+    t1 = time.perf_counter()
+    it32 = int(info1.total_iterations) + int(info2.total_iterations)
+    mt32 = float(info2.max_torque)
+    E32 = np.array([system.get_energy_fp64(p, i) for i in range(C3_IMAGES)])
+    simulation.set_precision(p, 64)
+    gneb.set_convergence(p, 1e-6)
+    info3 = simulation.start(p, simulation.METHOD_GNEB, simulation.SOLVER_VP, iters_cap)
     t2 = time.perf_counter()
-    mt = float(info2.max_torque)
+    it64 = int(info3.total_iterations)
+    mt = float(info3.max_torque)
     E = np.array([system.get_energy_fp64(p, i) for i in range(C3_IMAGES)])
+    chain1 = np.array([np.array(system.get_spin_directions(p, i)) for i in range(C3_IMAGES)])
+    types = np.array([gneb.get_climbing_falling(p, i) for i in range(C3_IMAGES)])
     state.delete(p)
-    n_it = int(info1.total_iterations) + int(info2.total_iterations)
+    n_it = it32 + it64
     spins = C3_IMAGES * nos
-    # CPU: the oracle's GNEB iteration (FP64, OpenMP) on the same chain, a bounded sample
+    # the oracle (FP64 CPU restatement) continued from the device's converged chain with the same image
+    # types: its barrier and max torque after a bounded number of iterations
     o = OracleSystem(C3_SPEC)
+    _, ro = o.gneb(chain1, 50, image_type=types, spring_constant=1.0, force_convergence=1e-12, dt=1e-3)
+    Eo = np.asarray(ro["energies"])
+    # CPU: the oracle's GNEB iteration (FP64, OpenMP) on the same chain, a bounded sample
     n_cpu = 3
     c0 = time.perf_counter()
     o.gneb(chain0, n_cpu, spring_constant=1.0, force_convergence=1e-6, dt=1e-3)
@@ -506,13 +523,19 @@ def run_gneb(iters_cap=60000):
     return {
         "workload": "GNEB, 32 images of a periodic 96x96 triangular lattice (J=1, Neel D=0.35, K=0.08 meV, "
                     "B=1.5 T), relaxed Neel skyrmion (R=8 sites, tanh profile) to ferromagnet, spring 1, VP, "
-                    "climbing image after 2000 iterations, convergence 1e-6 meV; FP32 forces, FP64 energies",
+                    "climbing image after 2000 iterations, convergence 1e-6 meV; FP32 forces to 1e-5 meV, then "
+                    "FP64 forces to 1e-6 meV; FP64 energies",
         "n_images": C3_IMAGES, "spins_per_image": nos,
-        "iterations": n_it, "converged": bool(mt < 1e-6), "max_torque": mt,
-        "wall_s": t2 - t0, "ms_per_iteration": 1000.0 * (t2 - t0) / n_it,
+        "iterations": n_it, "iterations_fp32": it32, "iterations_fp64": it64, "converged": bool(mt < 1e-6),
+        "max_torque": mt, "max_torque_after_fp32": mt32,
+        "wall_s": t2 - t0, "wall_s_fp32": t1 - t0, "ms_per_iteration": 1000.0 * (t2 - t0) / n_it,
         "value": spins * n_it / (t2 - t0), "unit": "spin-updates/s",
-        "barrier_meV": float(E.max() - E[0]), "saddle_image": int(E.argmax()),
-        "timing": "wall clock of the two Simulation_GNEB_Start calls (host checks between device chunks included)",
+        "barrier_meV": float(E.max() - E[0]), "barrier_meV_after_fp32": float(E32.max() - E32[0]),
+        "saddle_image": int(E.argmax()),
+        "oracle_check": {"iterations": 50, "barrier_meV": float(Eo.max() - Eo[0]),
+                         "max_torque": float(ro["max_torque"]),
+                         "what": "FP64 oracle GNEB continued from the converged device chain (same image types)"},
+        "timing": "wall clock of the three Simulation_GNEB_Start calls (host checks between device chunks included)",
         "cpu_baseline": {"value": spins * n_cpu / cpu_s, "unit": "spin-updates/s", "cores": os.cpu_count(),
                          "kind": "port", "sample": "%d GNEB iterations of the same 32-image chain (FP64, OpenMP)" % n_cpu},
     }

@@ -14,6 +14,9 @@
 //   golden_harness llg     <cfg> <spins.bin> <out> <solver> <n_iter>
 //   golden_harness ovfwrite <cfg> <spins.bin> <file> <format>   IO_Image_Write of the injected spins
 //   golden_harness ovfread  <cfg> <file> <out.bin>               IO_Image_Read, then the spins it holds
+//   golden_harness thermal <cfg> <spins.bin> <out> <llg|mc> <solver> <T> <n_equil> <n_samples> <stride>
+//                                                        time series (E, m_x, m_y, m_z) every stride
+//                                                        iterations after n_equil, at temperature T
 //   golden_harness llgtime <cfg> <spins.bin> <solver> <n_iter>
 //                                                        wall time of Simulation_LLG_Start only (stdout)
 //   golden_harness gneb    <cfg> <chain.bin> <out> <noi> <solver> <n_iter> [<n_iter_ci>]
@@ -29,6 +32,7 @@
 #include <Spirit/Hamiltonian.h>
 #include <Spirit/Parameters_GNEB.h>
 #include <Spirit/Parameters_LLG.h>
+#include <Spirit/Parameters_MC.h>
 #include <Spirit/Simulation.h>
 #include <Spirit/State.h>
 #include <Spirit/System.h>
@@ -196,6 +200,45 @@ int main( int argc, char ** argv )
     {
         IO_Image_Read( s, argv[3] );
         write_bin( argv[4], System_Get_Spin_Directions( s ), 3 * (size_t)System_Get_NOS( s ) );
+    }
+    else if( op == "thermal" )
+    {
+        inject( s, read_bin( argv[3] ) );
+        std::string out = argv[4];
+        bool mc         = std::string( argv[5] ) == "mc";
+        int solver      = std::atoi( argv[6] );
+        float T         = (float)std::atof( argv[7] );
+        int n_equil     = std::atoi( argv[8] );
+        int n_samples   = std::atoi( argv[9] );
+        int stride      = std::atoi( argv[10] );
+        auto advance    = [&]( int n ) {
+            if( n <= 0 )
+                return;
+            if( mc )
+                Simulation_MC_Start( s, n, n + 1 );
+            else
+                Simulation_LLG_Start( s, solver, n, n + 1 );
+        };
+        if( mc )
+            Parameters_MC_Set_Temperature( s, T );
+        else
+            Parameters_LLG_Set_Temperature( s, T );
+        advance( n_equil );
+        int nos = System_Get_NOS( s );
+        std::vector<double> series;
+        for( int k = 0; k < n_samples; ++k )
+        {
+            advance( stride );
+            auto & spins = *s->active_image->spins;
+            double m[3] = { 0, 0, 0 };
+            for( int i = 0; i < nos; ++i )
+                for( int e = 0; e < 3; ++e )
+                    m[e] += spins[i][e];
+            series.push_back( heis( s ).Energy( spins ) );
+            for( int e = 0; e < 3; ++e )
+                series.push_back( m[e] / nos );
+        }
+        write_bin( out + "_series.bin", series.data(), series.size() );
     }
     else if( op == "llgtime" )
     {

@@ -93,6 +93,8 @@ __global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 4 : 2 ) pass_a( PassA
         const R * src        = comp == 0 ? p.sx : ( comp == 1 ? p.sy : p.sz );
         const int rowlen     = nb * d.n_cells[0];
         const long long base = d.spin_offset + ib + (long long)rowlen * ( (long long)b0 + (long long)d.n_cells[1] * c );
+        // unrolled: the loads of several elements are in flight before the first lands in shared memory
+#pragma unroll 4
         for( int e = threadIdx.x; e < nq * Ma; e += blockDim.x )
         {
             const int q = (int)fdiv( (unsigned)e, f.div_Ma ), t = e - q * Ma;
@@ -110,6 +112,7 @@ __global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 4 : 2 ) pass_a( PassA
     else
     {
         const R * src = p.dense + ( (size_t)row * Bin + b0 ) * Ma;
+#pragma unroll 4
         for( int e = threadIdx.x; e < nq * Ma; e += blockDim.x )
         {
             const int q = (int)fdiv( (unsigned)e, f.div_Ma ), t = e - q * Ma;
@@ -585,6 +588,7 @@ __global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 4 : 2 ) pass_a_inv( P
     // [row][b][ka]: consecutive threads take consecutive k of a line pair; [ka][row][b]:
     // consecutive threads take consecutive line pairs of one k (contiguous b)
     const int gq = p.ka_major ? ( p.g + 1 ) >> 1 : nq; // line pairs of a full block
+#pragma unroll 4
     for( int e = threadIdx.x; e < gq * Ma; e += blockDim.x )
     {
         int q, k;

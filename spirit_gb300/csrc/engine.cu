@@ -126,6 +126,17 @@ static const int SPT_OPTIONS[3] = { 1, 2, 4 };
 // Per-spin part of a stage after the field g of configuration ci is known: thermal field, virtual
 // force and the solver's update (Solver_SIB.hpp, Solver_Heun.hpp, Solver_Depondt.hpp,
 // Solver_RK4.hpp); t2 takes the max squared torque.
+// Thermal field of spin i at an iteration: epsilon sqrt(T / mu_s) times three standard normals
+// from the spin's Philox block
+template<typename R>
+__device__ __forceinline__ V3<R> thermal_field( const SysConst<R> & C, const SysDesc & d, int ib, unsigned int counter,
+                                                int i )
+{
+    const R sc    = C.noise[ib];
+    const V3<R> z = gauss3<R>( d.seed, d.stream, counter, (unsigned int)i );
+    return { sc * z.x, sc * z.y, sc * z.z };
+}
+
 template<typename R, int SOLVER, int STAGE>
 __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysConst<R> & C, const SysDesc & d,
                                               long long gi, int i, int ib, V3<R> ci, V3<R> g, int iteration,
@@ -139,10 +150,7 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
         // stage and kept for the later stages of the same iteration
         if( PROBE || STAGE == 1 )
         {
-            const R sc = C.noise[ib];
-            V3<R> z = gauss3<R>( d.seed, d.stream, PROBE ? 0xFFFFFFFFu : (unsigned int)iteration + d.noise_offset,
-                                 (unsigned int)i );
-            xi      = { sc * z.x, sc * z.y, sc * z.z };
+            xi = thermal_field<R>( C, d, ib, PROBE ? 0xFFFFFFFFu : (unsigned int)iteration + d.noise_offset, i );
             if( STAGE == 1 )
                 A.xi.st( gi, xi );
         }
@@ -417,7 +425,8 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
         const R mu         = C.mu[ib];
         const V3<R> ci     = A.cfg.ld( gi );
         R ek               = 0;
-        V3<R> g            = gradient_at<R>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu, ek, smode );
+        V3<R> g = gradient_at<R, false, FINAL || PROBE>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu,
+                                                                    ek, smode );
         comp_add( e, ec, ek );
         stage_update<R, SOLVER, STAGE>( A, C, d, gi, i, ib, ci, g, iteration, t2 );
     }
@@ -450,6 +459,7 @@ struct TileMaps
 };
 
 // Gradient at spin gi (batch index) from the staged window (same terms and order as gradient_at).
+template<bool ENERGY>
 __device__ __forceinline__ V3<float> gradient_win( const Geo & d, const SysConst<float> & C, const PairR<float> * pairs,
                                                    const float * wx, const float * wy, const float * wz, int xs,
                                                    int wlen, const SoA3<float> & cfg, const SoA3<float> & h, int gi,
@@ -510,13 +520,7 @@ __device__ __forceinline__ V3<float> gradient_win( const Geo & d, const SysConst
             }
             else
                 sj = cfg.ld( j );
-            g.x -= P.J * sj.x;
-            g.y -= P.J * sj.y;
-            g.z -= P.J * sj.z;
-            V3<float> cr = cross( sj, V3<float>{ P.Dx, P.Dy, P.Dz } );
-            g.x -= cr.x;
-            g.y -= cr.y;
-            g.z -= cr.z;
+            pair_acc<float, false>( g, P.J, P.Dx, P.Dy, P.Dz, sj );
         }
     }
     if( h.x )
@@ -526,14 +530,16 @@ __device__ __forceinline__ V3<float> gradient_win( const Geo & d, const SysConst
         g.y -= mu * hh.y;
         g.z -= mu * hh.z;
     }
-    e = 0.5f * ( g.x * si.x + g.y * si.y + g.z * si.z );
+    if( ENERGY )
+        e = 0.5f * ( g.x * si.x + g.y * si.y + g.z * si.z );
     if( C.has_zeeman )
     {
         V3<float> B = { C.zeeman[0], C.zeeman[1], C.zeeman[2] };
         g.x -= mu * B.x;
         g.y -= mu * B.y;
         g.z -= mu * B.z;
-        e += -mu * ( B.x * si.x + B.y * si.y + B.z * si.z );
+        if( ENERGY )
+            e += -mu * ( B.x * si.x + B.y * si.y + B.z * si.z );
     }
     return g;
 }
@@ -639,8 +645,8 @@ __global__ void __launch_bounds__( 256, 4 )
                 const int w    = gi - xs;
                 const V3<float> ci = { wx[w], wy[w], wz[w] };
                 float ek           = 0;
-                V3<float> g = gradient_win( GS, C, pairs, wx, wy, wz, xs, wlen, A.cfg, A.h, gi, ib, a, b, c, ci, mu, ek,
-                                            smode );
+                V3<float> g = gradient_win<FINAL>( GS, C, pairs, wx, wy, wz, xs, wlen, A.cfg, A.h, gi, ib, a, b, c, ci,
+                                                   mu, ek, smode );
                 comp_add( e, ec, ek );
                 stage_update<float, SOLVER, STAGE>( A, C, d, gi, i, ib, ci, g, iteration, t2 );
             }
@@ -770,7 +776,8 @@ __global__ void __launch_bounds__( 256 ) llg_stage_rows( StageArgs<R> A, RowArgs
                        ( odd ? vz.y : vz.x ) * invT };
             }
             R ek    = 0;
-            V3<R> g = gradient_at<R>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu, ek, smode, &hv );
+            V3<R> g = gradient_at<R, false, FINAL>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu, ek,
+                                                               smode, &hv );
             e += ek;
             stage_update<R, SOLVER, STAGE>( A, C, d, gi, i, ib, ci, g, iteration, t2 );
             const V3<R> v = FINAL ? A.s.ld( gi ) : A.out.ld( gi ); // this thread's own store
@@ -1296,14 +1303,17 @@ bool encode_tensor_map_1d_f32( CUtensorMap * map, const void * base, unsigned lo
     return r == CUDA_SUCCESS;
 }
 
-// The TMA-staged stage kernel serves FP32 batches in which every system's window (a tile of
+// The TMA-staged stage kernel can serve FP32 batches in which every system's window (a tile of
 // TT_SPINS spins plus the stencil reach H on both sides, aligned to 16 bytes) fits TT_NCOPY
-// copies of TT_BOX floats; SPIRIT_GB300_TMA=0 keeps llg_stage.  Tiles never cross systems.
+// copies of TT_BOX floats; tiles never cross systems.  It is selected by SPIRIT_GB300_TMA=1: measured
+// on the 256-system SIB ensemble it is slower than llg_stage (0.41 against 0.33 ms per step; the
+// stage kernels are bound by instruction issue and the per-spin loads of the state, not by the
+// neighbour reads it stages, and one-tile systems get a single CTA), so llg_stage is the default.
 void Engine::build_tiles()
 {
     tma_             = false;
     const char * env = std::getenv( "SPIRIT_GB300_TMA" );
-    if( fp64_ || rows_ || ( env && env[0] == '0' ) || total_ >= ( 1LL << 30 ) )
+    if( fp64_ || rows_ || !( env && env[0] == '1' ) || total_ >= ( 1LL << 30 ) )
         return;
     std::vector<int4> tiles;
     std::vector<int> count( desc_.size(), 0 );

@@ -41,11 +41,14 @@ __device__ __forceinline__ V3<R> normalized( V3<R> v )
 
 // Pair of the stencil in the kernels' working precision.  lin is the linear index offset of
 // the neighbour, valid for cells whose whole stencil lies inside the system (no wrap, no cut).
+// The couplings first and the record 16-byte aligned, so one pair reads as two or three vector
+// loads from shared memory (J, D) and (lin, da, db, dc).
 template<typename R>
-struct PairR
+struct alignas( 16 ) PairR
 {
-    int j, da, db, dc, lin;
     R J, Dx, Dy, Dz;
+    int lin, da, db, dc;
+    int j;
 };
 
 template<typename R>
@@ -100,6 +103,36 @@ __device__ __forceinline__ V3<R> gauss3( unsigned long long seed, unsigned int s
     sincospi( R( 2 ) * u1, &s1, &c1 );
     sincospi( R( 2 ) * u3, &s3, &c3 );
     return { r0 * c1, r0 * s1, r1 * c3 };
+}
+
+// Accumulation of one exchange + DMI pair, g -= J s_j + s_j x D.  FUSED (FP32 stage kernels):
+// three FMAs per component (the products and the subtraction rounded together); otherwise the
+// reference's order of operations.
+template<typename R, bool FUSED>
+__device__ __forceinline__ void pair_acc( V3<R> & g, R J, R Dx, R Dy, R Dz, V3<R> sj )
+{
+    if constexpr( FUSED )
+    {
+        g.x = fma( -J, sj.x, g.x );
+        g.x = fma( -sj.y, Dz, g.x );
+        g.x = fma( sj.z, Dy, g.x );
+        g.y = fma( -J, sj.y, g.y );
+        g.y = fma( -sj.z, Dx, g.y );
+        g.y = fma( sj.x, Dz, g.y );
+        g.z = fma( -J, sj.z, g.z );
+        g.z = fma( -sj.x, Dy, g.z );
+        g.z = fma( sj.y, Dx, g.z );
+    }
+    else
+    {
+        g.x -= J * sj.x;
+        g.y -= J * sj.y;
+        g.z -= J * sj.z;
+        V3<R> cr = cross( sj, V3<R>{ Dx, Dy, Dz } );
+        g.x -= cr.x;
+        g.y -= cr.y;
+        g.z -= cr.z;
+    }
 }
 
 // Geometry scalars of one system, staged in shared memory by every kernel that walks pairs.
@@ -162,7 +195,7 @@ __device__ __forceinline__ void load_pairs_smem( PairR<R> * pairs, const SysDesc
     {
         const PairEntry & q = d.pairs[p];
         const int lin       = q.j - q.i + nb * ( q.da + Na * ( q.db + Nb * q.dc ) );
-        pairs[p]            = { q.j, q.da, q.db, q.dc, lin, (R)q.J, (R)q.D[0], (R)q.D[1], (R)q.D[2] };
+        pairs[p]            = { (R)q.J, (R)q.D[0], (R)q.D[1], (R)q.D[2], lin, q.da, q.db, q.dc, q.j };
     }
 }
 
@@ -352,7 +385,8 @@ __device__ __forceinline__ void load_const( SysConst<R> & dst, const SysDesc & d
 // Hamiltonian_Heisenberg.cpp:704-766: anisotropy, exchange + DMI pairs, dipolar field, then
 // Zeeman), and the energy of that spin: 0.5 g_quadratic . s + Zeeman, in the working precision.
 // hval, when given, is the dipolar field of the spin (instead of h[gi]).
-template<typename R>
+// FUSED: FMA-fused pair accumulation (pair_acc); ENERGY: form e (false: e is left untouched).
+template<typename R, bool FUSED = false, bool ENERGY = true>
 __device__ __forceinline__ V3<R> gradient_at( const Geo & d, const SysConst<R> & C, const PairR<R> * pairs,
                                               const SoA3<R> & cfg, const SoA3<R> & h, long long gi, int ib, int a,
                                               int b, int c, V3<R> si, R mu, R & e, int mode = STENCIL_GENERAL,
@@ -388,16 +422,7 @@ __device__ __forceinline__ V3<R> gradient_at( const Geo & d, const SysConst<R> &
         else
             j = pair_index( d, a, b, c, P.j, P.da, P.db, P.dc );
         if( j >= 0 )
-        {
-            V3<R> sj = cfg.ld( j );
-            g.x -= P.J * sj.x;
-            g.y -= P.J * sj.y;
-            g.z -= P.J * sj.z;
-            V3<R> cr = cross( sj, V3<R>{ P.Dx, P.Dy, P.Dz } );
-            g.x -= cr.x;
-            g.y -= cr.y;
-            g.z -= cr.z;
-        }
+            pair_acc<R, FUSED>( g, P.J, P.Dx, P.Dy, P.Dz, cfg.ld( j ) );
     }
     if( hval || h.x )
     {
@@ -407,14 +432,16 @@ __device__ __forceinline__ V3<R> gradient_at( const Geo & d, const SysConst<R> &
         g.y -= mu * hh.y;
         g.z -= mu * hh.z;
     }
-    e = R( 0.5 ) * ( g.x * si.x + g.y * si.y + g.z * si.z );
+    if( ENERGY )
+        e = R( 0.5 ) * ( g.x * si.x + g.y * si.y + g.z * si.z );
     if( C.has_zeeman )
     {
         V3<R> B = { C.zeeman[0], C.zeeman[1], C.zeeman[2] };
         g.x -= mu * B.x;
         g.y -= mu * B.y;
         g.z -= mu * B.z;
-        e += -mu * ( B.x * si.x + B.y * si.y + B.z * si.z );
+        if( ENERGY )
+            e += -mu * ( B.x * si.x + B.y * si.y + B.z * si.z );
     }
     return g;
 }

@@ -153,3 +153,27 @@ HTST_CASES = [
 OVF_SPEC = dict(bravais="sc", n_cells=[5, 4, 3], lattice_constant=1.0, mu_s=[2.0], bc=[1, 1, 0],
                 field=(0.5, (0, 0, 1)), anisotropy=(0.1, (0, 0, 1)), jij=[1.0], dij=[0.2], dm_chirality=2)
 OVF_FORMATS = {"bin4": 1, "bin8": 2, "text": 3, "csv": 4}
+
+# Thermal statistics against reference runs at T > 0 (the noise streams differ -- the reference
+# draws from a host mt19937 -- so the comparison is of equilibrium averages within their
+# statistical errors).  (name, spec, method, solver id, T [K], equilibration iterations, samples,
+# iterations between samples, start: "random" (seeded) or "+z")
+_FREE = dict(bravais="sc", n_cells=[32, 32, 1], lattice_constant=1.0, mu_s=[2.0], bc=[1, 1, 0],
+             field=(10.0, (0, 0, 1)), anisotropy=(0.0, (0, 0, 1)), jij=[0.0], dij=[0.0], dm_chirality=2,
+             llg=dict(dt=2e-3, damping=0.5, temperature=10.0, seed=5))
+_FM = dict(bravais="sc", n_cells=[32, 32, 1], lattice_constant=1.0, mu_s=[2.0], bc=[1, 1, 0],
+           field=(2.0, (0, 0, 1)), anisotropy=(0.2, (0, 0, 1)), jij=[1.0], dij=[0.1], dm_chirality=2,
+           llg=dict(dt=1e-3, damping=0.3, temperature=8.0, seed=6))
+THERMAL_CASES = [
+    # free spins in a field: <cos theta> = L(mu_s mu_B B / k_B T), the single-spin Langevin test
+    ("free_spins_llg", _FREE, "llg", 1, 10.0, 3000, 4000, 10, "random"),
+    # ordered 2D ferromagnet with anisotropy, field and weak DMI: <m_z>, <E>, var(E)
+    ("fm_lattice_llg", _FM, "llg", 1, 8.0, 5000, 6000, 10, "+z"),
+    ("fm_lattice_mc", _FM, "mc", 0, 8.0, 3000, 2000, 5, "+z"),
+]
+# The reference's Metropolis step (Method_MC.cpp:155-157) takes the old single-spin energy from the
+# configuration at the start of the sweep and the new one from the configuration updated so far,
+# so its chain does not sample the Boltzmann distribution exactly; this library's Monte Carlo is
+# therefore held to the reference's equilibrium averages from LLG at the same temperature.
+THERMAL_COMPARE = {"free_spins_llg": "free_spins_llg", "fm_lattice_llg": "fm_lattice_llg",
+                   "fm_lattice_mc": "fm_lattice_llg"}

@@ -23,7 +23,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
 from cases import (FULL_CASES, GRAD_CASES, HTST_CASES, LLG_CASES, OVF_FORMATS, OVF_SPEC, PAIR_GEOMETRIES,  # noqa: E402
-                   SOLVERS, SPIN_SEED)
+                   SOLVERS, SPIN_SEED, THERMAL_CASES)
 from oracle.oracle import (OracleSystem, image_types_auto, portable_spins, random_spins,  # noqa: E402
                            transition_homogeneous)
 from spirit_gb300.configs import config_text, write_config  # noqa: E402
@@ -179,6 +179,23 @@ def main(only=None):
         np.savez_compressed(os.path.join(HERE, "ovf_interchange.npz"), config=config_text(OVF_SPEC), spins=spins,
                             **{"reference_read_" + k: v for k, v in read_back.items()})
         out["ovf"] = sorted(read_back)
+    # --- thermal statistics: the reference's own LLG (host mt19937 noise) and Monte Carlo at T > 0;
+    # the time series of (E, m) are stored, the statistics are formed by tests/thermal_stats.py
+    for name, spec, method, sid, T, n_eq, n_s, stride, start in THERMAL_CASES:
+        if not want("thermal_" + name):
+            continue
+        cfg = write_config(spec, os.path.join(tmp, name + ".cfg"))
+        nos = nos_of(spec)
+        spins = random_spins(nos, 41) if start == "random" else np.tile([0.0, 0.0, 1.0], (nos, 1))
+        sp = os.path.join(tmp, name + "_spins.bin")
+        spins.tofile(sp)
+        tag = os.path.join(tmp, "thermal_" + name)
+        run(["thermal", cfg, sp, tag, method, str(sid), repr(T), str(n_eq), str(n_s), str(stride)], tmp, threads=1)
+        ser = load_bin(tag + "_series.bin", (n_s, 4))
+        np.savez_compressed(os.path.join(HERE, "thermal_%s.npz" % name), config=config_text(spec), method=method,
+                            solver=sid, temperature=T, n_equil=n_eq, n_samples=n_s, stride=stride, start=start,
+                            energy=ser[:, 0], m=ser[:, 1:])
+        out["thermal_" + name] = (ser[:, 3].mean(), ser[:, 0].mean() / nos)
     # --- GNEB (VP) on the reference solver-test system: skyrmion collapse, 9 images
     spec = SOLVERS
     cfg = write_config(spec, os.path.join(tmp, "solvers.cfg"))

@@ -164,8 +164,8 @@ def _tuning(p):
 
 @pytest.mark.parametrize("tma", ["1", "0"])
 def test_tma_stage_kernel_selected(tma, monkeypatch):
-    """An FP32 2D system runs the TMA-staged stage kernel (tuning value 12) with the compensated
-    state (value 13); SPIRIT_GB300_TMA=0 selects llg_stage; FP64 never uses either."""
+    """With SPIRIT_GB300_TMA=1 an FP32 2D system runs the TMA-staged stage kernel (tuning value 12);
+    otherwise llg_stage; FP32 keeps the compensated state (value 13); FP64 uses neither."""
     from oracle.oracle import random_spins
     from spirit_gb300 import simulation
 
