@@ -291,6 +291,32 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def partition_by_spins(sizes, world):
+    """Shard independent systems over `world` ranks by spin count (no exchange between systems):
+    largest first, each to the rank with the fewest spins so far (ties: the lowest rank).  Returns
+    one list of system indices per rank, each in ascending order."""
+    load = [0] * world
+    parts = [[] for _ in range(world)]
+    for k in sorted(range(len(sizes)), key=lambda k: (-sizes[k], k)):
+        r = min(range(world), key=lambda r: (load[r], r))
+        parts[r].append(k)
+        load[r] += sizes[k]
+    return [sorted(p) for p in parts]
+
+
+def reduce_sum(v, world):
+    """Sum over the ranks of one number (the spins each rank advanced)."""
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def c4_specs(n=256, seed=4, ddi=False):
     """The batched uneven ensemble: n periodic square lattices with edge lengths log-uniform in
     [32, 256] and per-system J, D (Neel), K, B_z, T drawn from the given seed; SIB, alpha 0.2,
@@ -328,7 +354,12 @@ def run_batched_vs_plain(steps, warmup, plain=True, check=True, ddi=False, profi
     from spirit_gb300.spiritlib import fn
 
     launch = fn("Simulation_Launch_Steps", [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int])
+    rank, world, _ = dist_env()
     specs = c4_specs(ddi=ddi)
+    if world > 1:
+        # the ensemble is sharded over the ranks by spin count; each rank batches its share
+        mine = partition_by_spins([sp["n_cells"][0] * sp["n_cells"][1] for sp in specs], world)[rank]
+        specs = [specs[k] for k in mine]
     tmp = tempfile.mkdtemp()
     states, nos = [], []
     for k, sp in enumerate(specs):
@@ -401,8 +432,14 @@ def run_batched_vs_plain(steps, warmup, plain=True, check=True, ddi=False, profi
         dm = max(dm, float(np.abs(got - ref).max()))
     for p in sub:
         state.delete(p)
-    bv = total * steps / (batched_ms / 1000.0)
-    pv = total * steps / (plain_ms / 1000.0)
+    if dm is not None:
+        dm = reduce_max(dm, world)
+    # whole-job rates: the spins of every rank over the slowest rank's time
+    all_spins = reduce_sum(total, world)
+    batched_ms = reduce_max(batched_ms, world)
+    plain_ms = reduce_max(plain_ms, world) if plain else plain_ms
+    bv = all_spins * steps / (batched_ms / 1000.0)
+    pv = all_spins * steps / (plain_ms / 1000.0)
     if ddi:
         workload = ("256 uneven open SC 2D systems with the dipolar interaction (DDI FFT, zero-padded 2L x 2L, "
                     "a = 4 A), L log-uniform in [32,256] (seed 4), per-system J, D, K, B_z, T in U[0,50] K; "
@@ -414,7 +451,8 @@ def run_batched_vs_plain(steps, warmup, plain=True, check=True, ddi=False, profi
         plain_desc = "one engine per system, 2 launches per system per step (1-step CUDA graph), same stream"
     return {
         "workload": workload,
-        "n_systems": len(specs), "n_spins": total, "steps": steps, "warmup": warmup,
+        "n_systems": int(reduce_sum(len(specs), world)), "n_spins": int(all_spins), "steps": steps, "warmup": warmup,
+        "sharding": "systems split over %d ranks by spin count" % world if world > 1 else "one rank",
         "value": bv, "unit": "spin-updates/s", "ms_per_step": batched_ms / steps,
         "plain_value": pv, "plain_ms_per_step": plain_ms / steps, "ratio_batched_vs_plain": bv / pv,
         "plain": plain_desc,

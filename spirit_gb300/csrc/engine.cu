@@ -102,9 +102,9 @@ __device__ __forceinline__ V3<float> ff_norm_increment( V3<float> h, V3<float> l
 
 // s (= hi + lo at gi) <- normalise(s + D), stored back as hi and lo; returns the new hi
 template<typename R>
-__device__ __forceinline__ V3<float> ff_update( const StageArgs<R> & A, long long gi, V3<float> h, V3<float> D )
+__device__ __forceinline__ V3<float> ff_update( const StageArgs<R> & A, long long gi, V3<float> h, V3<float> l,
+                                                V3<float> D )
 {
-    V3<float> l       = { (float)A.lo.x[gi], (float)A.lo.y[gi], (float)A.lo.z[gi] };
     const V3<float> E = ff_norm_increment( h, l, D );
     ff_add( h.x, l.x, E.x );
     ff_add( h.y, l.y, E.y );
@@ -137,10 +137,41 @@ __device__ __forceinline__ V3<R> thermal_field( const SysConst<R> & C, const Sys
     return { sc * z.x, sc * z.y, sc * z.z };
 }
 
+// The per-spin arrays a stage reads besides the configuration: the state, the stage-1 virtual
+// force, the thermal field, the RK4 sum and the low parts of a compensated state.  The stage
+// kernels load them before the field is evaluated, so these loads are in flight together with the
+// neighbour reads instead of being issued after them.
+template<typename R>
+struct StageIn
+{
+    V3<R> s, fv1, xi, acc;
+    V3<float> lo;
+};
+
+template<typename R, int SOLVER, int STAGE>
+__device__ __forceinline__ StageIn<R> stage_inputs( const StageArgs<R> & A, const SysConst<R> & C, long long gi )
+{
+    constexpr bool LAST = ( SOLVER == SOLVER_RK4 ) ? ( STAGE == 4 ) : ( STAGE == 2 );
+    StageIn<R> in{};
+    if( STAGE >= 2 )
+    {
+        in.s = A.s.ld( gi );
+        if( LAST )
+            in.fv1 = A.aux1.ld( gi );
+        if( C.thermal )
+            in.xi = A.xi.ld( gi );
+        if( SOLVER == SOLVER_RK4 )
+            in.acc = A.aux2.ld( gi );
+        if( LAST && sizeof( R ) == 4 && A.lo.x )
+            in.lo = { (float)A.lo.x[gi], (float)A.lo.y[gi], (float)A.lo.z[gi] };
+    }
+    return in;
+}
+
 template<typename R, int SOLVER, int STAGE>
 __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysConst<R> & C, const SysDesc & d,
                                               long long gi, int i, int ib, V3<R> ci, V3<R> g, int iteration,
-                                              float & t2 )
+                                              float & t2, const StageIn<R> & in )
 {
     constexpr bool PROBE = STAGE == ST_PROBE;
     V3<R> xi             = { 0, 0, 0 };
@@ -155,7 +186,7 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
                 A.xi.st( gi, xi );
         }
         else
-            xi = A.xi.ld( gi );
+            xi = in.xi;
     }
     V3<R> fv = virtual_force<R>( C, ci, g, C.inv_mu[ib], xi );
     if( PROBE )
@@ -164,7 +195,7 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
     }
     else if( SOLVER == SOLVER_SIB )
     {
-        const V3<R> si = ( STAGE == 1 ) ? ci : A.s.ld( gi );
+        const V3<R> si = ( STAGE == 1 ) ? ci : in.s;
         if( STAGE == 1 )
         {
             V3<R> p = sib( si, fv );
@@ -189,7 +220,7 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
                 const R w      = R( 2 ) / ( R( 1 ) + dot( Ah, Ah ) );
                 const V3<float> D = { float( w * ( c1.x + c2.x ) ), float( w * ( c1.y + c2.y ) ),
                                       float( w * ( c1.z + c2.z ) ) };
-                const V3<float> hn = ff_update( A, gi, V3<float>{ (float)si.x, (float)si.y, (float)si.z }, D );
+                const V3<float> hn = ff_update( A, gi, V3<float>{ (float)si.x, (float)si.y, (float)si.z }, in.lo, D );
                 sn                 = { (R)hn.x, (R)hn.y, (R)hn.z };
             }
             else
@@ -200,7 +231,7 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
                     sn = normalized( sn );
             }
             A.s.st( gi, sn );
-            t2 = fmaxf( t2, (float)torque2( A.aux1.ld( gi ), sn ) );
+            t2 = fmaxf( t2, (float)torque2( in.fv1, sn ) );
         }
     }
     else if( SOLVER == SOLVER_HEUN )
@@ -214,8 +245,8 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
         }
         else
         {
-            const V3<R> si  = A.s.ld( gi );
-            const V3<R> fv1 = A.aux1.ld( gi );
+            const V3<R> si  = in.s;
+            const V3<R> fv1 = in.fv1;
             V3<R> c1        = cross( si, fv1 );
             V3<R> t1        = { R( -1 ) * c1.x, R( -1 ) * c1.y, R( -1 ) * c1.z };
             V3<R> c2        = cross( ci, fv );
@@ -224,7 +255,7 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
             {
                 const V3<float> D  = { float( R( 0.5 ) * t1.x - R( 0.5 ) * c2.x ), float( R( 0.5 ) * t1.y - R( 0.5 ) * c2.y ),
                                        float( R( 0.5 ) * t1.z - R( 0.5 ) * c2.z ) };
-                const V3<float> hn = ff_update( A, gi, V3<float>{ (float)si.x, (float)si.y, (float)si.z }, D );
+                const V3<float> hn = ff_update( A, gi, V3<float>{ (float)si.x, (float)si.y, (float)si.z }, in.lo, D );
                 sn                 = { (R)hn.x, (R)hn.y, (R)hn.z };
             }
             else
@@ -253,8 +284,8 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
         }
         else
         {
-            const V3<R> si  = A.s.ld( gi );
-            const V3<R> fv1 = A.aux1.ld( gi );
+            const V3<R> si  = in.s;
+            const V3<R> fv1 = in.fv1;
             V3<R> ax        = { R( 0.5 ) * fv1.x, R( 0.5 ) * fv1.y, R( 0.5 ) * fv1.z };
             ax.x += R( 0.5 ) * fv.x;
             ax.y += R( 0.5 ) * fv.y;
@@ -277,7 +308,7 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
                     D                 = { f1 * (float)c1.x + f2 * (float)c2.x, f1 * (float)c1.y + f2 * (float)c2.y,
                                           f1 * (float)c1.z + f2 * (float)c2.z };
                 }
-                const V3<float> hn = ff_update( A, gi, V3<float>{ (float)si.x, (float)si.y, (float)si.z }, D );
+                const V3<float> hn = ff_update( A, gi, V3<float>{ (float)si.x, (float)si.y, (float)si.z }, in.lo, D );
                 sn                 = { (R)hn.x, (R)hn.y, (R)hn.z };
             }
             else
@@ -296,7 +327,7 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
         // k_m = -(cfg_m x fv_m); cfg_{m+1} = normalize(s + w k_m); running sum acc = s + k1/6 + k2/3 + ...
         V3<R> cr = cross( ci, fv );
         V3<R> k  = { R( -1 ) * cr.x, R( -1 ) * cr.y, R( -1 ) * cr.z };
-        const V3<R> si = ( STAGE == 1 ) ? ci : A.s.ld( gi );
+        const V3<R> si = ( STAGE == 1 ) ? ci : in.s;
         if( STAGE == 1 )
         {
             A.aux1.st( gi, fv );
@@ -312,7 +343,7 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
         }
         else if( STAGE == 2 || STAGE == 3 )
         {
-            V3<R> acc = A.aux2.ld( gi );
+            V3<R> acc = in.acc;
             R w3      = R( 1.0 / 3.0 );
             acc.x += w3 * k.x;
             acc.y += w3 * k.y;
@@ -324,7 +355,7 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
         }
         else
         {
-            V3<R> acc = A.aux2.ld( gi );
+            V3<R> acc = in.acc;
             R w6      = R( 1.0 / 6.0 );
             acc.x += w6 * k.x;
             acc.y += w6 * k.y;
@@ -332,14 +363,14 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
             V3<R> sn;
             if( sizeof( R ) == 4 && A.lo.x )
             {
-                const V3<float> hn = ff_update( A, gi, V3<float>{ (float)si.x, (float)si.y, (float)si.z },
+                const V3<float> hn = ff_update( A, gi, V3<float>{ (float)si.x, (float)si.y, (float)si.z }, in.lo,
                                                 V3<float>{ (float)acc.x, (float)acc.y, (float)acc.z } );
                 sn                 = { (R)hn.x, (R)hn.y, (R)hn.z };
             }
             else
                 sn = normalized( acc );
             A.s.st( gi, sn );
-            t2 = fmaxf( t2, (float)torque2( A.aux1.ld( gi ), sn ) );
+            t2 = fmaxf( t2, (float)torque2( in.fv1, sn ) );
         }
     }
 }
@@ -385,7 +416,7 @@ __device__ __forceinline__ void stage_finalize( const StageArgs<R> & A, SysRun *
 // A block of 256 threads covers SPT * 256 consecutive spins of one system (thread t: spins
 // t, t + 256, ...), so the per-block set-up and reductions are shared by SPT spins per thread.
 template<typename R, int SOLVER, int STAGE, int SPT>
-__global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
+__global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 4 : 1 ) llg_stage( StageArgs<R> A )
 {
     __shared__ PairR<R> pairs[MAX_PAIRS];
     __shared__ SysConst<R> C;
@@ -421,14 +452,15 @@ __global__ void __launch_bounds__( 256 ) llg_stage( StageArgs<R> A )
     const int smode = warp_stencil_mode( GS, a, b, c, valid );
     if( valid )
     {
-        const long long gi = GS.off + i;
-        const R mu         = C.mu[ib];
-        const V3<R> ci     = A.cfg.ld( gi );
-        R ek               = 0;
+        const long long gi   = GS.off + i;
+        const StageIn<R> pin = stage_inputs<R, SOLVER, STAGE>( A, C, gi );
+        const R mu           = C.mu[ib];
+        const V3<R> ci       = A.cfg.ld( gi );
+        R ek                 = 0;
         V3<R> g = gradient_at<R, false, FINAL || PROBE>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu,
                                                                     ek, smode );
         comp_add( e, ec, ek );
-        stage_update<R, SOLVER, STAGE>( A, C, d, gi, i, ib, ci, g, iteration, t2 );
+        stage_update<R, SOLVER, STAGE>( A, C, d, gi, i, ib, ci, g, iteration, t2, pin );
     }
     }
     if( !( FINAL || PROBE ) )
@@ -641,6 +673,7 @@ __global__ void __launch_bounds__( 256, 4 )
             if( valid )
             {
                 const int gi   = (int)GS.off + i;
+                const StageIn<float> pin = stage_inputs<float, SOLVER, STAGE>( A, C, gi );
                 const float mu = C.mu[ib];
                 const int w    = gi - xs;
                 const V3<float> ci = { wx[w], wy[w], wz[w] };
@@ -648,7 +681,7 @@ __global__ void __launch_bounds__( 256, 4 )
                 V3<float> g = gradient_win<FINAL>( GS, C, pairs, wx, wy, wz, xs, wlen, A.cfg, A.h, gi, ib, a, b, c, ci,
                                                    mu, ek, smode );
                 comp_add( e, ec, ek );
-                stage_update<float, SOLVER, STAGE>( A, C, d, gi, i, ib, ci, g, iteration, t2 );
+                stage_update<float, SOLVER, STAGE>( A, C, d, gi, i, ib, ci, g, iteration, t2, pin );
             }
         }
         if( FINAL )
@@ -761,10 +794,11 @@ __global__ void __launch_bounds__( 256 ) llg_stage_rows( StageArgs<R> A, RowArgs
         nx[k]           = { 0, 0, 0 };
         if( valid )
         {
-            const long long gi = GS.off + i;
-            const R mu         = C.mu[ib];
-            const V3<R> ci     = A.cfg.ld( gi );
-            const int lr       = b - b0;
+            const long long gi   = GS.off + i;
+            const StageIn<R> pin = stage_inputs<R, SOLVER, STAGE>( A, C, gi );
+            const R mu           = C.mu[ib];
+            const V3<R> ci       = A.cfg.ld( gi );
+            const int lr         = b - b0;
             V3<R> hv;
             {
                 const int qb      = lr >> 1;
@@ -779,7 +813,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage_rows( StageArgs<R> A, RowArgs
             V3<R> g = gradient_at<R, false, FINAL>( GS, C, pairs, A.cfg, A.h, gi, ib, a, b, c, ci, mu, ek,
                                                                smode, &hv );
             e += ek;
-            stage_update<R, SOLVER, STAGE>( A, C, d, gi, i, ib, ci, g, iteration, t2 );
+            stage_update<R, SOLVER, STAGE>( A, C, d, gi, i, ib, ci, g, iteration, t2, pin );
             const V3<R> v = FINAL ? A.s.ld( gi ) : A.out.ld( gi ); // this thread's own store
             nx[k]         = { mu * v.x, mu * v.y, mu * v.z };
         }

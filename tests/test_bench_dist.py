@@ -1,6 +1,7 @@
 """Multi-process paths of bench.py on CPU (gloo): the path has no exchange between systems, so
-N GPUs run N independent replicas ("replicas only"); the only cross-rank step is the max of the
-timed milliseconds, and only rank 0 prints."""
+N GPUs run N independent replicas of the single-system workload ("replicas only") and split the
+batched ensembles by spin count; the only cross-rank steps are the max of the timed milliseconds
+and the sum of the spins advanced, and only rank 0 prints."""
 import json
 import os
 import socket
@@ -70,3 +71,57 @@ def test_reference_arm_under_torchrun_prints_once():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+
+
+def test_partition_by_spins_balances_and_covers():
+    """Every system lands on exactly one rank; the 256-system ensemble's spin loads differ by less
+    than the largest system."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    sizes = [sp["n_cells"][0] * sp["n_cells"][1] for sp in bench.c4_specs()]
+    for world in (1, 2, 3, 4, 8):
+        parts = bench.partition_by_spins(sizes, world)
+        flat = sorted(k for p in parts for k in p)
+        assert flat == list(range(len(sizes)))
+        loads = [sum(sizes[k] for k in p) for p in parts]
+        assert max(loads) - min(loads) <= max(sizes), (world, loads)
+    assert bench.partition_by_spins([5, 3, 3, 1], 2) == [[0, 3], [1, 2]]
+
+
+def _rank_sum_main(rank, world, port, out):
+    import torch.distributed as dist
+
+    sys.path.insert(0, ROOT)
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+
+    sizes = [sp["n_cells"][0] * sp["n_cells"][1] for sp in bench.c4_specs()]
+    mine = bench.partition_by_spins(sizes, world)[rank]
+    out[rank] = (bench.reduce_sum(sum(sizes[k] for k in mine), world), len(mine))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_sharded_spin_total_gloo_two_ranks():
+    """Two gloo ranks shard the ensemble and sum their spins: both see the whole ensemble's count."""
+    import torch.multiprocessing as mp
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    total = sum(sp["n_cells"][0] * sp["n_cells"][1] for sp in bench.c4_specs())
+    ctx = mp.get_context("spawn")
+    mgr = ctx.Manager()
+    out = mgr.dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_sum_main, args=(r, 2, port, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    assert out[0][0] == out[1][0] == total
+    assert out[0][1] + out[1][1] == 256
