@@ -196,6 +196,47 @@ def main(only=None):
                             solver=sid, temperature=T, n_equil=n_eq, n_samples=n_s, stride=stride, start=start,
                             energy=ser[:, 0], m=ser[:, 1:])
         out["thermal_" + name] = (ser[:, 3].mean(), ser[:, 0].mean() / nos)
+    # --- the GNEB benchmark chain (32 images of the 96x96 triangular lattice): the oracle relaxes the
+    # Neel skyrmion and converges the chain (FP64, climbing image, max torque < 1e-6 meV); the
+    # reference continues from that chain for 50 iterations with its own climbing-image types.
+    # The chain itself is not stored (7 MB); its barrier and energies are.
+    if want("c3_barrier"):
+        import bench
+        from spirit_gb300.configs import write_config as _wc
+
+        spec = bench.C3_SPEC
+        o = OracleSystem(spec)
+        pos = o.positions()
+        center = 0.5 * (pos.min(axis=0) + pos.max(axis=0))
+        sign = min((1.0, -1.0), key=lambda sg: o.energy(bench.neel_skyrmion(pos, center, sign=sg)))
+        # the relaxed skyrmion (a local minimum; the device relaxes it with VP, the oracle with L-BFGS)
+        sk, r0 = o.llg(bench.neel_skyrmion(pos, center, sign=sign), "LBFGS_OSO", 20000, dt=1e-3,
+                       force_convergence=1e-9)
+        noi = bench.C3_IMAGES
+        chain = np.zeros((noi,) + sk.shape)
+        chain[0] = sk
+        chain[-1] = [0.0, 0.0, 1.0]
+        chain = transition_homogeneous(chain, 0, noi - 1)
+        chain, r1 = o.gneb(chain, 2000, spring_constant=1.0, force_convergence=1e-6, dt=1e-3)
+        types = image_types_auto(r1["energies"], np.zeros(noi))
+        chain, r2 = o.gneb(chain, 200000, image_type=types, spring_constant=1.0, force_convergence=1e-6, dt=1e-3)
+        cfg = _wc(spec, os.path.join(tmp, "c3.cfg"))
+        cp = os.path.join(tmp, "c3_chain.bin")
+        chain.tofile(cp)
+        tag = os.path.join(tmp, "c3_ref")
+        run(["gneb", cfg, cp, tag, str(noi), "0", "1", "50"], tmp, threads=8)
+        rows = [l.split() for l in open(tag + "_result.txt")]
+        img = [r_ for r_ in rows if r_[0] == "image"]
+        Eref = np.array([float(r_[3]) for r_ in img])
+        np.savez_compressed(
+            os.path.join(HERE, "gneb_c3_barrier.npz"), config=config_text(spec), skyrmion_sign=sign,
+            oracle_energies=r2["energies"], oracle_barrier=float(r2["energies"].max() - r2["energies"][0]),
+            oracle_iterations=int(r1["iterations"]) + int(r2["iterations"]), oracle_max_torque=r2["max_torque"],
+            reference_energies=Eref, reference_barrier=float(Eref.max() - Eref[0]),
+            reference_max_torque=float([r_ for r_ in rows if r_[0] == "max_torque"][0][1]),
+            reference_image_type=np.array([int(r_[7]) for r_ in img]), image_type=types,
+        )
+        out["c3_barrier"] = (r2["energies"].max() - r2["energies"][0], Eref.max() - Eref[0], r2["max_torque"])
     # --- GNEB (VP) on the reference solver-test system: skyrmion collapse, 9 images
     spec = SOLVERS
     cfg = write_config(spec, os.path.join(tmp, "solvers.cfg"))
