@@ -491,7 +491,8 @@ def run_gneb(iters_cap=60000):
     """Batched GNEB: 32 images of a 96x96 triangular lattice between a relaxed Neel skyrmion
     (radius 8 sites) and the ferromagnet (geodesic interpolation), spring 1, VP; 2000 plain
     iterations, then climbing / falling images set automatically and iterations until the max
-    torque is below 1e-6 meV (or the cap).  FP32 forces, FP64 energies."""
+    torque is below 1e-5 meV with FP32 forces, then FP64 forces to 1e-6 meV (or the cap); FP64
+    energies."""
     from oracle.oracle import OracleSystem
     from spirit_gb300 import chain, geometry, simulation, state, system, transition
     from spirit_gb300.configs import write_config

@@ -57,6 +57,33 @@ def test_noalloc_matches_gradient(name):
             assert abs(float(e.item()) - e_ref) <= 1e-12 * abs(e_ref), (call, float(e.item()), e_ref)
 
 
+@pytest.mark.parametrize("name", ["sq_c1", "hex2d", "fd_pairs"])
+def test_noalloc_matches_reference_fixture(name):
+    """Directly against the reference: the gradient and energy the reference's own
+    Gradient_and_Energy produced for the same spins (tests/golden/grad_<name>.npz), on two calls in
+    a row.  Tolerance: gradients 1e-12 relative to max |g|, energies 1e-10 relative."""
+    torch = pytest.importorskip("torch")
+    from conftest import golden
+    from spirit_gb300 import hamiltonian
+
+    f = golden("grad_%s.npz" % name)
+    spins = f["spins"]
+    with make_state(CASES[name], spins) as p:
+        s = torch.tensor(np.ascontiguousarray(spins.T), dtype=torch.float64, device="cuda")
+        g = torch.full_like(s, float("nan"))
+        e = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+        for call in range(2):
+            rc = hamiltonian.get_gradient_noalloc(p, s[0].data_ptr(), s[1].data_ptr(), s[2].data_ptr(),
+                                                  g[0].data_ptr(), g[1].data_ptr(), g[2].data_ptr(),
+                                                  e.data_ptr(), torch.cuda.current_stream().cuda_stream)
+            torch.cuda.synchronize()
+            assert rc == 0
+            scale = np.abs(f["gradient_ge"]).max()
+            np.testing.assert_allclose(g.T.cpu().numpy(), f["gradient_ge"], rtol=0, atol=1e-12 * scale,
+                                       err_msg="call %d" % call)
+            assert abs(float(e.item()) - float(f["energy_total"])) <= 1e-10 * abs(float(f["energy_total"]))
+
+
 @pytest.mark.parametrize("name", ["sq_c1", "sc3d_open_c"])
 def test_noalloc_side_stream(name):
     """On a non-default stream the call is ordered on that stream alone: the result equals
