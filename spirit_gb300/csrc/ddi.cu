@@ -45,7 +45,17 @@ struct PassArgs
     FastDiv div_g;
     int ka_major; // W1 layout: 0 [row][b][ka] (split passes B, C, B'), 1 [ka][row][b] (fused pass BC)
     FastDiv div_gq; // (g + 1) / 2: line pairs per block of pass A
+    int prefetch;   // fused b/c passes: prefetch the block's dipole-spectrum slice into L2 first
 };
+
+// Prefetch [p, p + bytes) into L2, one 128-byte line per request, spread over the block's threads
+// (no completion: a later load simply finds the lines in L2)
+__device__ __forceinline__ void prefetch_l2_lines( const void * p, size_t bytes, int lane, int nthreads )
+{
+    const char * c = static_cast<const char *>( p );
+    for( size_t o = (size_t)lane * 128; o < bytes; o += (size_t)nthreads * 128 )
+        asm volatile( "prefetch.global.L2 [%0];" ::"l"( c + o ) );
+}
 
 template<typename R>
 __device__ __forceinline__ bool sys_inactive( const PassArgs<R> & p, int s )
@@ -334,6 +344,11 @@ __global__ void __launch_bounds__( 1024 ) pass_bc( PassArgs<R> p )
     cplx<R> * B     = A + G * vol;
     load_tw( twb, p.tw + f.tw_offset[1], Mb );
     load_tw( twc, p.tw + f.tw_offset[2], Mc );
+    // the dipole spectrum is constant: its slice for these planes can stream into L2 while the
+    // predecessor kernel finishes and the forward transforms run
+    if( p.prefetch )
+        prefetch_l2_lines( p.Dhat + f.dhat_offset + (size_t)ka * nb * nb * 6 * Mc * Mb,
+                           sizeof( cplx<R> ) * (size_t)G * nb * nb * 6 * Mc * Mb, threadIdx.x, blockDim.x );
     for( int e = threadIdx.x; e < 2 * G * vol; e += blockDim.x )
         A[e] = { 0, 0 };
     __syncthreads();
@@ -469,6 +484,19 @@ __global__ void __launch_bounds__( 512, 2 ) pass_bc_cl( PassArgs<R> p, int K )
     cplx<R> * Bc1 = Bc0 + lc;
     load_tw( twb, p.tw + f.tw_offset[1], Mb );
     load_tw( twc, p.tw + f.tw_offset[2], Mc );
+    if( p.prefetch )
+    {
+        // this block's kb range of the dipole spectrum: one contiguous run of kq elements per
+        // (pair, component, kc) row; constant, so it is requested before the programmatic wait
+        const cplx<R> * Dp = p.Dhat + f.dhat_offset + (size_t)ka * nb * nb * 6 * Mc * Mb + kb0;
+        const int rows     = nb * nb * 6 * Mc;
+        const int per_row  = ( kq * (int)sizeof( cplx<R> ) + 127 ) / 128;
+        for( int e = threadIdx.x; e < rows * per_row; e += blockDim.x )
+        {
+            const int rw = e / per_row, ln = e - rw * per_row;
+            asm volatile( "prefetch.global.L2 [%0];" ::"l"( reinterpret_cast<const char *>( Dp + (size_t)rw * Mb ) + ln * 128 ) );
+        }
+    }
     for( int e = threadIdx.x; e < lb; e += blockDim.x )
         Bb0[e] = { 0, 0 };
     for( int e = threadIdx.x; e < lc; e += blockDim.x )
@@ -955,6 +983,11 @@ static PassArgs<R> make_args( const DDIPlan & P, const SysDesc * d_sd, const Sys
     a.W1    = (cplx<R> *)P.d_W1;
     a.W2    = (cplx<R> *)P.d_W2;
     a.Dhat  = (const cplx<R> *)P.d_Dhat;
+    static const int pf = [] {
+        const char * e = std::getenv( "SPIRIT_GB300_DHAT_PREFETCH" );
+        return ( e && e[0] == '0' ) ? 0 : 1;
+    }();
+    a.prefetch = pf;
     return a;
 }
 
