@@ -104,6 +104,10 @@ C2_T0 = dict(SC3D_DDI, n_cells=[128, 128, 16])
 FULL_CASES = [
     ("c1_full", C1_FULL, "Depondt", 2, 1000, 101),
     ("c2_t0", C2_T0, "Heun", 3, 100, 102),
+    # the plain-LLG configuration with the other integrators
+    ("c1_full_sib", C1_FULL, "SIB", 1, 1000, 103),
+    ("c1_full_heun", C1_FULL, "Heun", 3, 1000, 104),
+    ("c1_full_rk4", C1_FULL, "RK4", 4, 1000, 105),
 ]
 
 # (case, solver name, solver id, iterations)

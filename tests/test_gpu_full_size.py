@@ -35,11 +35,13 @@ def _case(name):
 
 
 @pytest.mark.parametrize("precision", [64, 32])
-def test_c1_full_1000_steps(precision):
-    """SC 64 x 64, Depondt, 1000 steps against the reference run."""
+@pytest.mark.parametrize("name", ["c1_full", "c1_full_sib", "c1_full_heun", "c1_full_rk4"])
+def test_c1_full_1000_steps(name, precision):
+    """SC 64 x 64, 1000 steps against the reference run: Depondt (the configuration itself), SIB,
+    Heun and RK4."""
     from spirit_gb300 import simulation, system
 
-    f, spec, s0, sid, n_iter = _case("c1_full")
+    f, spec, s0, sid, n_iter = _case(name)
     with make_state(spec, s0, precision=precision) as p:
         simulation.start(p, simulation.METHOD_LLG, sid, n_iter)
         s = spins_of(p)
@@ -47,6 +49,7 @@ def test_c1_full_1000_steps(precision):
         E = system.get_energy_fp64(p)
     assert it == n_iter == int(f["iterations"])
     dm = np.abs(s - f["spins_out"]).max()
+    print("%s FP%d: max|dm| vs reference after %d steps = %.3e" % (name, precision, n_iter, dm))
     if precision == 64:
         assert dm <= 1e-10, dm
         assert abs(E - f["energy"]) <= 1e-10 * abs(f["energy"])
