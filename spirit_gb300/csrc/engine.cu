@@ -415,8 +415,11 @@ __device__ __forceinline__ void stage_finalize( const StageArgs<R> & A, SysRun *
 // SOLVER / STAGE are compile-time; STAGE 0 is the constructor probe (initial torque + energy).
 // A block of 256 threads covers SPT * 256 consecutive spins of one system (thread t: spins
 // t, t + 256, ...), so the per-block set-up and reductions are shared by SPT spins per thread.
+// FP32: at least 5 blocks of 256 threads per SM (48 registers, a few spilled): the 256-system SIB
+// ensemble runs 0.287 ms per step against 0.309 at 4 blocks (64 registers) and 0.284 at 6 (40
+// registers, more spills); the 128x128x16 dipolar step is unchanged (0.099 ms).
 template<typename R, int SOLVER, int STAGE, int SPT>
-__global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 4 : 1 ) llg_stage( StageArgs<R> A )
+__global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 5 : 1 ) llg_stage( StageArgs<R> A )
 {
     __shared__ PairR<R> pairs[MAX_PAIRS];
     __shared__ SysConst<R> C;
