@@ -158,15 +158,16 @@ __host__ __device__ inline const SysConst<double> & sys_const<double>( const Sys
     return d.cd;
 }
 
-// Mutable per-system run state on the device.  Written only by the last block of the last
-// kernel of a step (or of the probe kernel), read by every block of the following kernels.
+// Mutable per-system run state on the device.  The blocks of the last stage kernel of a step (or
+// of the probe kernel) add to the accumulators; the closing kernel launched after it writes the
+// rest, which every block of the following kernels reads.
 struct SysRun
 {
     int iteration;      // completed iterations
     int active;         // 1 while the method keeps iterating this system
     float max_torque;   // last max |P_perp fv| (Hook_Post_Iteration)
     unsigned int torque_bits; // running max of |t|^2 as float bits (non-negative floats order like uints)
-    unsigned int blocks_done; // last-block detection counter
+    unsigned int unused;
     double energy;      // energy of the last force evaluation (Spin_System::E)
     double energy_acc;  // running sum of the current evaluation
     double reserved;

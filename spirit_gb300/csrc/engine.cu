@@ -5,9 +5,10 @@
 // DMI pair stencil, dipolar field from the FFT pipeline, Zeeman), the LLG virtual force with
 // in-kernel Philox thermal noise, and the solver's update -- reading each spin once per stage.
 // The last stage also reduces the FP64 energy of the evaluated configuration and the maximum
-// torque |P_perp(s_new) fv_1| per system; the last block of each system finalises the
-// iteration counter and the convergence flag on the device, so a whole step sequence can be
-// captured in a CUDA graph and replayed without host round trips.
+// torque |P_perp(s_new) fv_1| per system into per-system accumulators; a small kernel launched
+// after it (close_iteration) finalises the iteration counter and the convergence flag on the
+// device, so a whole step sequence can be captured in a CUDA graph and replayed without host
+// round trips.
 //
 // Reference algorithms (file:line in Spirit v2.2.0):
 //   gradient terms        core/src/engine/Hamiltonian_Heisenberg.cpp:704-864
@@ -41,7 +42,6 @@ struct StageArgs
     const SysDesc * sd;
     SysRun * runs;
     const int2 * blkmap;  // (system, first local spin)
-    const int * blkcount; // blocks per system
     SoA3<R> s;            // state
     SoA3<R> cfg;          // stage configuration (neighbour reads)
     SoA3<R> out;          // predictor output
@@ -102,7 +102,7 @@ __device__ __forceinline__ V3<float> ff_norm_increment( V3<float> h, V3<float> l
 
 // s (= hi + lo at gi) <- normalise(s + D), stored back as hi and lo; returns the new hi
 template<typename R>
-__device__ __forceinline__ V3<float> ff_update( const StageArgs<R> & A, long long gi, V3<float> h, V3<float> l,
+__device__ __forceinline__ V3<float> ff_update( const StageArgs<R> & A, int gi, V3<float> h, V3<float> l,
                                                 V3<float> D )
 {
     const V3<float> E = ff_norm_increment( h, l, D );
@@ -149,7 +149,7 @@ struct StageIn
 };
 
 template<typename R, int SOLVER, int STAGE>
-__device__ __forceinline__ StageIn<R> stage_inputs( const StageArgs<R> & A, const SysConst<R> & C, long long gi )
+__device__ __forceinline__ StageIn<R> stage_inputs( const StageArgs<R> & A, const SysConst<R> & C, int gi )
 {
     constexpr bool LAST = ( SOLVER == SOLVER_RK4 ) ? ( STAGE == 4 ) : ( STAGE == 2 );
     StageIn<R> in{};
@@ -170,7 +170,7 @@ __device__ __forceinline__ StageIn<R> stage_inputs( const StageArgs<R> & A, cons
 
 template<typename R, int SOLVER, int STAGE>
 __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysConst<R> & C, const SysDesc & d,
-                                              long long gi, int i, int ib, V3<R> ci, V3<R> g, int iteration,
+                                              int gi, int i, int ib, V3<R> ci, V3<R> g, int iteration,
                                               float & t2, const StageIn<R> & in )
 {
     constexpr bool PROBE = STAGE == ST_PROBE;
@@ -375,40 +375,79 @@ __device__ __forceinline__ void stage_update( const StageArgs<R> & A, const SysC
     }
 }
 
-// End of the final stage (or of the probe): energy of the evaluated configuration and max torque
-// of the step per system (warp sums in the working precision, FP64 across the warps of the block);
-// the last block of the system closes the iteration.
-template<typename R, bool PROBE>
-__device__ __forceinline__ void stage_finalize( const StageArgs<R> & A, SysRun * run, int s, const SysDesc & d, R e,
-                                               float t2, double * red_d, float * red_f, int & is_last, R ec = R( 0 ) )
+// End of the final stage (or of the probe): the block's energy of the evaluated configuration (per
+// warp a compensated FP32 sum -- plain in FP64 -- formed in FP64, the warps summed in FP64) and its
+// max squared torque are added to the system's accumulators.  Nothing waits for the additions: no
+// fence, no returned counter, one barrier; close_iteration, launched next on the same stream,
+// closes the step.  A caller that reduces again reuses red_d / red_f only after another barrier.
+template<typename R>
+__device__ __forceinline__ void stage_reduce( SysRun * run, R e, R ec, float t2, double * red_d, float * red_f )
 {
-    double es = block_sum_comp( e, ec, red_d );
-    float tm  = block_max( t2, red_f );
-    if( threadIdx.x == 0 )
+    for( int o = 16; o > 0; o >>= 1 )
     {
-        atomicAdd( &run->energy_acc, es );
-        atomicMax( &run->torque_bits, __float_as_uint( tm ) );
-        __threadfence();
-        unsigned int prev = atomicAdd( &run->blocks_done, 1u );
-        is_last           = ( prev == (unsigned int)A.blkcount[s] - 1 );
+        const R e2 = __shfl_down_sync( 0xffffffffu, e, o );
+        if constexpr( sizeof( R ) == 4 )
+        {
+            const R c2 = __shfl_down_sync( 0xffffffffu, ec, o );
+            const R t  = e + e2;
+            const R bp = t - e;
+            ec += c2 + ( ( e - ( t - bp ) ) + ( e2 - bp ) );
+            e = t;
+        }
+        else
+            e += e2;
+        t2 = fmaxf( t2, __shfl_down_sync( 0xffffffffu, t2, o ) );
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if( l == 0 )
+    {
+        red_d[w] = sizeof( R ) == 4 ? (double)e + (double)ec : (double)e;
+        red_f[w] = t2;
     }
     __syncthreads();
-    if( is_last && threadIdx.x == 0 )
+    if( threadIdx.x < 32 )
     {
-        __threadfence();
-        volatile SysRun * vr = run;
-        float mt             = sqrtf( __uint_as_float( vr->torque_bits ) );
-        vr->max_torque       = mt;
-        vr->energy           = vr->energy_acc;
-        vr->energy_acc       = 0;
-        vr->torque_bits      = 0;
-        vr->blocks_done      = 0;
-        if( !A.tune )
+        const bool has = threadIdx.x < ( blockDim.x >> 5 );
+        double r       = has ? red_d[threadIdx.x] : 0.0;
+        float tm       = has ? red_f[threadIdx.x] : 0.f;
+        for( int o = 16; o > 0; o >>= 1 )
         {
-            int it        = vr->iteration + ( PROBE ? 0 : 1 );
-            vr->iteration = it;
-            vr->active    = ( it < d.n_iterations ) && !( mt < (float)d.force_convergence );
+            r += __shfl_down_sync( 0xffffffffu, r, o );
+            tm = fmaxf( tm, __shfl_down_sync( 0xffffffffu, tm, o ) );
         }
+        if( threadIdx.x == 0 )
+        {
+            atomicAdd( &run->energy_acc, r );
+            atomicMax( &run->torque_bits, __float_as_uint( tm ) );
+        }
+    }
+}
+
+// Closes the step of every system after the final stage (or the probe): max torque and energy from
+// the accumulators the stage kernel's blocks added to (this launch follows that kernel on the
+// stream, so all of them are complete and visible), accumulators reset, and -- outside tuner runs
+// -- the iteration count and the active flag (budget and force convergence,
+// Method_Solver.hpp:225-230).  Systems the stage kernel skipped as inactive are left as they are.
+__global__ void close_iteration( SysRun * runs, const SysDesc * sd, int n_sys, int tune, int probe )
+{
+    pdl_wait();
+    pdl_trigger();
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if( s >= n_sys )
+        return;
+    SysRun * r = runs + s;
+    if( !tune && !r->active )
+        return;
+    const float mt = sqrtf( __uint_as_float( r->torque_bits ) );
+    r->max_torque  = mt;
+    r->energy      = r->energy_acc;
+    r->energy_acc  = 0;
+    r->torque_bits = 0;
+    if( !tune )
+    {
+        const int it = r->iteration + ( probe ? 0 : 1 );
+        r->iteration = it;
+        r->active    = ( it < sd[s].n_iterations ) && !( mt < (float)sd[s].force_convergence );
     }
 }
 
@@ -426,7 +465,6 @@ __global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 5 : 1 ) llg_stage( St
     __shared__ Geo GS;
     __shared__ double red_d[32];
     __shared__ float red_f[32];
-    __shared__ int is_last;
     const int2 bm = A.blkmap[blockIdx.x];
     const int s   = bm.x;
     SysRun * run  = A.runs + s;
@@ -455,7 +493,7 @@ __global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 5 : 1 ) llg_stage( St
     const int smode = warp_stencil_mode( GS, a, b, c, valid );
     if( valid )
     {
-        const long long gi   = GS.off + i;
+        const int gi         = (int)GS.off + i; // batches hold fewer than 2^31 spins
         const StageIn<R> pin = stage_inputs<R, SOLVER, STAGE>( A, C, gi );
         const R mu           = C.mu[ib];
         const V3<R> ci       = A.cfg.ld( gi );
@@ -468,7 +506,7 @@ __global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 5 : 1 ) llg_stage( St
     }
     if( !( FINAL || PROBE ) )
         return;
-    stage_finalize<R, PROBE>( A, run, s, d, e, t2, red_d, red_f, is_last, ec );
+    stage_reduce<R>( run, e, ec, t2, red_d, red_f );
 }
 
 // ------------------------------------------------------------------ TMA-staged stage kernel (FP32)
@@ -592,7 +630,6 @@ __global__ void __launch_bounds__( 256, 4 )
     __shared__ Geo GS;
     __shared__ double red_d[32];
     __shared__ float red_f[32];
-    __shared__ int is_last;
     constexpr bool FINAL = ( SOLVER == SOLVER_RK4 ) ? ( STAGE == 4 ) : ( STAGE == 2 );
     const int k0 = (int)( (long long)blockIdx.x * n_tiles / gridDim.x );
     const int k1 = (int)( (long long)( blockIdx.x + 1 ) * n_tiles / gridDim.x );
@@ -688,9 +725,8 @@ __global__ void __launch_bounds__( 256, 4 )
             }
         }
         if( FINAL )
-            stage_finalize<float, false>( A, run, s, d, e, t2, red_d, red_f, is_last, ec ); // ends with a barrier
-        else
-            __syncthreads();
+            stage_reduce<float>( run, e, ec, t2, red_d, red_f );
+        __syncthreads(); // the window buffer and red_d / red_f are reused by later tiles
     }
 }
 
@@ -726,7 +762,6 @@ __global__ void __launch_bounds__( 256 ) llg_stage_rows( StageArgs<R> A, RowArgs
     __shared__ Geo GS;
     __shared__ double red_d[32];
     __shared__ float red_f[32];
-    __shared__ int is_last;
     const int4 bm     = F.map[blockIdx.x];
     const int s       = bm.x, cc = bm.y, b0 = bm.z, nr = bm.w;
     SysRun * run      = A.runs + s;
@@ -797,7 +832,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage_rows( StageArgs<R> A, RowArgs
         nx[k]           = { 0, 0, 0 };
         if( valid )
         {
-            const long long gi   = GS.off + i;
+            const int gi         = (int)GS.off + i; // batches hold fewer than 2^31 spins
             const StageIn<R> pin = stage_inputs<R, SOLVER, STAGE>( A, C, gi );
             const R mu           = C.mu[ib];
             const V3<R> ci       = A.cfg.ld( gi );
@@ -864,7 +899,7 @@ __global__ void __launch_bounds__( 256 ) llg_stage_rows( StageArgs<R> A, RowArgs
     }
     if( !FINAL )
         return;
-    stage_finalize<R, false>( A, run, s, d, e, t2, red_d, red_f, is_last );
+    stage_reduce<R>( run, e, R( 0 ), t2, red_d, red_f );
 }
 
 // ------------------------------------------------------------------ evaluation kernel
@@ -1151,16 +1186,12 @@ Engine::~Engine()
     dfree( d_red_ );
     dfree( d_grad_ );
     dfree( d_blkmap_ );
-    dfree( d_blkcount_ );
     for( int k = 0; k < 3; ++k )
     {
         dfree( d_sblkmap_[k] );
-        dfree( d_sblkcount_[k] );
     }
     dfree( d_rowmap_ );
-    dfree( d_rowcount_ );
     dfree( d_tiles_ );
-    dfree( d_tilecount_ );
     dfree( d_err_ );
     if( lane_ )
     {
@@ -1217,7 +1248,6 @@ void Engine::build_systems( const std::vector<SystemInput> & systems )
     long long off = 0;
     int max_nos   = 0;
     std::vector<int2> blkmap;
-    std::vector<int> blkcount;
     std::vector<DDISystem> ddis;
     for( size_t s = 0; s < systems.size(); ++s )
     {
@@ -1229,7 +1259,6 @@ void Engine::build_systems( const std::vector<SystemInput> & systems )
         int nbk = ( desc_[s].nos + threads_ - 1 ) / threads_;
         for( int k = 0; k < nbk; ++k )
             blkmap.push_back( make_int2( (int)s, k * threads_ ) );
-        blkcount.push_back( nbk );
         if( desc_[s].ddi )
         {
             const Geometry & g = *systems[s].geom;
@@ -1250,6 +1279,9 @@ void Engine::build_systems( const std::vector<SystemInput> & systems )
         }
     }
     total_    = std::max<long long>( off, SPIN_ALIGN );
+    // the stage kernels index the batch with 32-bit integers
+    if( total_ >= ( 1LL << 31 ) )
+        throw std::runtime_error( "batch of 2^31 spins or more: not supported by the stage kernels" );
     n_blocks_ = (int)blkmap.size();
     for( int c = 0; c < 3; ++c )
     {
@@ -1266,29 +1298,22 @@ void Engine::build_systems( const std::vector<SystemInput> & systems )
     d_grad_     = dalloc<double>( 3 * (size_t)std::max( max_nos, 1 ) );
     d_red_      = dalloc<double>( N_TERMS * 2 );
     d_blkmap_   = dalloc<int2>( std::max<size_t>( blkmap.size(), 1 ) );
-    d_blkcount_ = dalloc<int>( std::max<size_t>( blkcount.size(), 1 ) );
     h2d( d_desc_, desc_.data(), desc_.size() );
     h2d( d_blkmap_, blkmap.data(), blkmap.size() );
-    h2d( d_blkcount_, blkcount.data(), blkcount.size() );
     for( int k = 0; k < 3; ++k )
     {
         const int span = 256 * SPT_OPTIONS[k];
         std::vector<int2> m;
-        std::vector<int> cnt;
         for( size_t sy = 0; sy < desc_.size(); ++sy )
         {
             int nbk = ( desc_[sy].nos + span - 1 ) / span;
             for( int q = 0; q < nbk; ++q )
                 m.push_back( make_int2( (int)sy, q * span ) );
-            cnt.push_back( nbk );
         }
-        n_sblocks_[k]   = (int)m.size();
-        d_sblkmap_[k]   = dalloc<int2>( std::max<size_t>( m.size(), 1 ) );
-        d_sblkcount_[k] = dalloc<int>( std::max<size_t>( cnt.size(), 1 ) );
+        n_sblocks_[k] = (int)m.size();
+        d_sblkmap_[k] = dalloc<int2>( std::max<size_t>( m.size(), 1 ) );
         if( !m.empty() )
             h2d( d_sblkmap_[k], m.data(), m.size() );
-        if( !cnt.empty() )
-            h2d( d_sblkcount_[k], cnt.data(), cnt.size() );
     }
     any_ddi_ = !ddis.empty();
     if( any_ddi_ )
@@ -1353,7 +1378,6 @@ void Engine::build_tiles()
     if( fp64_ || rows_ || !( env && env[0] == '1' ) || total_ >= ( 1LL << 30 ) )
         return;
     std::vector<int4> tiles;
-    std::vector<int> count( desc_.size(), 0 );
     for( size_t s = 0; s < desc_.size(); ++s )
     {
         const SysDesc & d = desc_[s];
@@ -1380,7 +1404,6 @@ void Engine::build_tiles()
                 return; // a stencil reaching too far: llg_stage serves this batch
             }
             tiles.push_back( make_int4( (int)s, t0, (int)xs, (int)ncpy ) );
-            ++count[s];
         }
     }
     void * const * bufs[3] = { spins_, predA_, predB_ };
@@ -1388,11 +1411,9 @@ void Engine::build_tiles()
         for( int c = 0; c < 3; ++c )
             if( !encode_tensor_map_1d_f32( &tmaps_[b][c], bufs[b][c], (unsigned long long)total_, TT_BOX ) )
                 return;
-    d_tiles_     = dalloc<int4>( std::max<size_t>( tiles.size(), 1 ) );
-    d_tilecount_ = dalloc<int>( std::max<size_t>( count.size(), 1 ) );
+    d_tiles_ = dalloc<int4>( std::max<size_t>( tiles.size(), 1 ) );
     if( !tiles.empty() )
         h2d( d_tiles_, tiles.data(), tiles.size() );
-    h2d( d_tilecount_, count.data(), count.size() );
     n_tiles_ = (int)tiles.size();
     tma_     = n_tiles_ > 0;
     if( std::getenv( "SPIRIT_GB300_DEBUG" ) )
@@ -1451,13 +1472,8 @@ void Engine::build_row_map( int n_ddi )
     }
     if( smem > 96 * 1024 )
         return;
-    std::vector<int> cnt( desc_.size(), 0 );
-    for( auto & x : m )
-        ++cnt[x.x];
-    d_rowmap_   = dalloc<int4>( m.size() );
-    d_rowcount_ = dalloc<int>( cnt.size() );
+    d_rowmap_ = dalloc<int4>( m.size() );
     h2d( d_rowmap_, m.data(), m.size() );
-    h2d( d_rowcount_, cnt.data(), cnt.size() );
     n_rowblocks_ = (int)m.size();
     rows_smem_   = smem;
     rows_        = true;
@@ -1720,7 +1736,6 @@ void Engine::launch_stage_rows( StageArgs<R> a, cudaStream_t st )
                                           96 * 1024 ) );
         attr = true;
     }
-    a.blkcount = d_rowcount_;
     RowArgs<R> F;
     F.fd  = ddi_.d_fd;
     F.tw  = (const cplx<R> *)ddi_.d_tw;
@@ -1764,7 +1779,6 @@ void Engine::launch_stage( StageArgs<R> a, cudaStream_t st )
             TileMaps M;
             for( int c = 0; c < 3; ++c )
                 M.m[c] = tmaps_[buf][c];
-            a.blkcount = d_tilecount_;
             launch_pdl( llg_stage_tma<SOLVER, STAGE>, dim3( std::min( grid, n_tiles_ ) ), dim3( 256 ), TT_SMEM, st, 1,
                         a, M, (const int4 *)d_tiles_, n_tiles_, d_err_ );
             return;
@@ -1772,7 +1786,6 @@ void Engine::launch_stage( StageArgs<R> a, cudaStream_t st )
     }
     const int k = sizeof( R ) == 8 ? 0 : spt_idx_;
     a.blkmap    = d_sblkmap_[k];
-    a.blkcount  = d_sblkcount_[k];
     const int n = n_sblocks_[k];
     if( k == 0 )
         launch_pdl( llg_stage<R, SOLVER, STAGE, 1>, dim3( n ), dim3( 256 ), 0, st, 1, a );
@@ -1789,7 +1802,6 @@ void Engine::launch_probe_t()
     a.sd       = d_desc_;
     a.runs     = d_runs_;
     a.blkmap   = d_blkmap_;
-    a.blkcount = d_blkcount_;
     a.s        = soa<R>( spins_ );
     a.cfg      = a.s;
     a.h        = { nullptr, nullptr, nullptr };
@@ -1802,6 +1814,14 @@ void Engine::launch_probe_t()
     // the probe uses the solver's force definition (direct minimisation / dynamics) only
     llg_stage<R, SOLVER_HEUN, ST_PROBE, 1><<<n_blocks_, 256, 0, stream_>>>( a );
     CUDA_CHECK( cudaGetLastError() );
+    launch_close( 0, 1 );
+}
+
+void Engine::launch_close( int tune, int probe )
+{
+    const int n = (int)desc_.size();
+    launch_pdl( close_iteration, dim3( ( n + 127 ) / 128 ), dim3( 128 ), 0, stream_, 1, d_runs_,
+                (const SysDesc *)d_desc_, n, tune, probe );
 }
 
 // the stage kernels of one step of the current solver; with_ddi: the dipolar field of each
@@ -1839,6 +1859,7 @@ void Engine::launch_stages_t( StageArgs<R> & a, bool with_ddi )
             launch_stage<R, SOLVER_HEUN, 2>( a, stream_ );
         else
             launch_stage<R, SOLVER_DEPONDT, 2>( a, stream_ );
+        launch_close( a.tune, 0 );
         break;
     }
     case SOLVER_RK4:
@@ -1858,6 +1879,7 @@ void Engine::launch_stages_t( StageArgs<R> & a, bool with_ddi )
         a.cfg = pA;
         field( a.cfg );
         launch_stage<R, SOLVER_RK4, 4>( a, stream_ );
+        launch_close( a.tune, 0 );
         break;
     }
     default:
@@ -2014,7 +2036,8 @@ int Engine::tuning( int * out, int n ) const
 int Engine::kernels_per_step() const
 {
     int stages = solver_ == SOLVER_RK4 ? 4 : 2;
-    return stages * ( 1 + ( any_ddi_ ? ( rows_ ? 1 : ( ddi_.fused ? 3 : 5 ) ) : 0 ) );
+    // per stage: the stage kernel and the dipolar passes; per step: close_iteration
+    return stages * ( 1 + ( any_ddi_ ? ( rows_ ? 1 : ( ddi_.fused ? 3 : 5 ) ) : 0 ) ) + 1;
 }
 
 void Engine::llg_start( int solver, const std::vector<int> & n_iterations )

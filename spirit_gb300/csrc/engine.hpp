@@ -149,10 +149,6 @@ public:
     {
         return d_blkmap_;
     }
-    const int * d_blkcount() const
-    {
-        return d_blkcount_;
-    }
     int n_blocks() const
     {
         return n_blocks_;
@@ -196,6 +192,8 @@ private:
     void launch_step_t();
     template<typename R>
     void launch_probe_t();
+    // close_iteration after the final stage of a step (or after the probe)
+    void launch_close( int tune, int probe );
     template<typename R, int SOLVER, int STAGE>
     void launch_stage( StageArgs<R> a, cudaStream_t st );
     template<typename R, int SOLVER, int STAGE>
@@ -235,22 +233,19 @@ private:
     double * d_red_   = nullptr; // reduction scratch (per-term sums)
     double * d_grad_  = nullptr; // AoS double gradient output
     int2 * d_blkmap_  = nullptr;
-    int * d_blkcount_ = nullptr;
     int n_blocks_     = 0;
     int threads_      = 256;
     // block maps of the stage kernels for 1, 2, 4 spins per thread; spt_idx_ picks one (tuned)
     int2 * d_sblkmap_[3]  = { nullptr, nullptr, nullptr };
-    int * d_sblkcount_[3] = { nullptr, nullptr, nullptr };
     int n_sblocks_[3]     = { 0, 0, 0 };
     int spt_idx_          = 0;
     int tuned_solver_     = -1;
     // TMA-staged persistent stage kernel (FP32 batches with a short stencil reach): tiles
-    // (system, first spin, aligned window start, copies per component), tiles per system, tensor
+    // (system, first spin, aligned window start, copies per component), tensor
     // maps of the three configuration buffers (state, predictor A, predictor B) x 3 components,
     // and an error flag the kernel sets when a copy does not arrive within its wait limit
     bool tma_           = false;
     int4 * d_tiles_     = nullptr;
-    int * d_tilecount_  = nullptr;
     int n_tiles_        = 0;
     int * d_err_        = nullptr;
     CUtensorMap tmaps_[3][3];
@@ -265,7 +260,6 @@ private:
     bool rows_          = false;
     bool w1_valid_      = false; // the spectrum holds the current state's (ready for a step)
     int4 * d_rowmap_    = nullptr;
-    int * d_rowcount_   = nullptr;
     int n_rowblocks_    = 0;
     size_t rows_smem_   = 0;
     int solver_       = SOLVER_HEUN;
