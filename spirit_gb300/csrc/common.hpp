@@ -58,28 +58,34 @@ struct PairEntry
 
 struct FFTDesc;
 
-// Exact unsigned division by a runtime constant d: q = floor(n * M / 2^64) with
-// M = ceil(2^64 / d) is exact for every 32-bit n (d = 1 is the identity, M = 0).
+// Exact unsigned division by a runtime constant d >= 1 for dividends n < 2^31 (every index here is
+// a non-negative int): q = (umulhi(n, m) + n) >> l with l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1 (Granlund and Montgomery, PLDI 1994: the round-up method; the sum
+// cannot overflow for n < 2^31) -- a multiply-high, an add and a shift, no branch (d = 1: m = 1, l = 0).
 struct FastDiv
 {
     unsigned int d;
+    unsigned int m;
+    unsigned int l;
     unsigned int pad;
-    unsigned long long m;
 };
 
 __host__ __device__ inline FastDiv make_fastdiv( unsigned int d )
 {
     FastDiv f;
-    f.d   = d;
+    f.d   = d > 0 ? d : 1;
     f.pad = 0;
-    f.m   = d > 1 ? ( ~0ULL ) / d + 1 : 0;
+    f.l   = 0;
+    while( ( 1ull << f.l ) < f.d )
+        ++f.l;
+    f.m = (unsigned int)( ( ( 1ull << 32 ) * ( ( 1ull << f.l ) - f.d ) ) / f.d + 1 );
     return f;
 }
 
 #ifdef __CUDACC__
 __device__ __forceinline__ unsigned int fdiv( unsigned int n, const FastDiv & f )
 {
-    return f.d == 1 ? n : (unsigned int)__umul64hi( (unsigned long long)n, f.m );
+    return ( __umulhi( n, f.m ) + n ) >> f.l;
 }
 #endif
 

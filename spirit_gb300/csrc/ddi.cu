@@ -709,37 +709,6 @@ static size_t smem_optin()
     return (size_t)v;
 }
 
-static void factorize( int L, RadixPlan & P )
-{
-    const int L0 = L;
-    int * rad    = P.radix;
-    int n        = 0;
-    while( L % 4 == 0 && L > 4 )
-    {
-        rad[n++] = 4;
-        L /= 4;
-    }
-    for( int p : { 4, 2, 3, 5, 7 } )
-        while( L % p == 0 && L > 1 )
-        {
-            rad[n++] = p;
-            L /= p;
-        }
-    for( int p = 11; L > 1; p += 2 )
-        while( L % p == 0 )
-        {
-            rad[n++] = p;
-            L /= p;
-        }
-    rad[n] = 0;
-    int ns = 1;
-    for( int s = 0; s < n; ++s )
-    {
-        P.div_lr[s] = make_fastdiv( (unsigned)( L0 / rad[s] ) );
-        P.div_ns[s] = make_fastdiv( (unsigned)ns );
-        ns *= rad[s];
-    }
-}
 
 DDIPlan::~DDIPlan()
 {
@@ -804,7 +773,7 @@ void DDIPlan::build( const std::vector<DDISystem> & systems, bool fp64, const Sy
                 tw_host.push_back( std::cos( ang ) );
                 tw_host.push_back( std::sin( ang ) );
             }
-            factorize( f.M[d], f.plan[d] );
+            radix_plan( f.M[d], f.plan[d] );
         }
         f.spec_offset = spec;
         long long w2  = 3LL * f.nb * f.N[2] * f.M[1] * f.Mh;

@@ -18,6 +18,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 namespace sg
 {
 
@@ -389,8 +391,8 @@ __device__ __forceinline__ cplx<R> * block_fft_reg( cplx<R> * a, cplx<R> * b, in
 }
 
 template<typename R>
-__device__ __noinline__ cplx<R> * mixed_fft( cplx<R> * a, cplx<R> * b, int L, int nl, int ls, int es,
-                                             const RadixPlan & P, const cplx<R> * tw, bool inverse );
+__device__ __forceinline__ cplx<R> * mixed_fft( cplx<R> * a, cplx<R> * b, int L, int nl, int ls, int es,
+                                                const RadixPlan & P, const cplx<R> * tw, bool inverse );
 
 template<typename R>
 __device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int ls, int nl, const RadixPlan & P,
@@ -542,8 +544,8 @@ struct SmemBuf<double>
     }
 };
 
-// Small-radix DFT helpers (the radix-3/5/7 butterflies): sums, differences, scaling by a real,
-// and the rotation by -i (forward) / +i (inverse).
+// Small-DFT helpers: sums, differences, scaling by a real, and the rotation by -i (forward) / +i
+// (inverse).
 template<typename R>
 __device__ __forceinline__ cplx<R> cadd( cplx<R> a, cplx<R> b )
 {
@@ -559,107 +561,280 @@ __device__ __forceinline__ cplx<R> caxpy( R s, cplx<R> a, cplx<R> y ) // y + s a
 {
     return { y.x + s * a.x, y.y + s * a.y };
 }
-template<typename R>
-__device__ __forceinline__ cplx<R> crot( cplx<R> u, bool inverse )
+template<typename R, bool INV>
+__device__ __forceinline__ cplx<R> crot( cplx<R> u )
 {
-    return inverse ? cplx<R>{ -u.y, u.x } : cplx<R>{ u.y, -u.x };
+    return INV ? cplx<R>{ -u.y, u.x } : cplx<R>{ u.y, -u.x };
+}
+
+// cos and sin of 2 pi e / N for the register radices N (0 <= e < N), exact where the angle makes
+// them 0, +-1/2 or +-1.  Called with constant arguments only (the unrolled small DFTs), so every
+// call folds to a literal.
+__host__ __device__ constexpr double root_cos( int N, int e )
+{
+    constexpr double t3[] = { 1.0, -0.5, -0.5 };
+    constexpr double t5[] = { 1.0, 0.309016994374947424102, -0.809016994374947424102, -0.809016994374947424102,
+                              0.309016994374947424102 };
+    constexpr double t6[] = { 1.0, 0.5, -0.5, -1.0, -0.5, 0.5 };
+    constexpr double t7[] = { 1.0, 0.623489801858733530525, -0.222520933956314404289, -0.900968867902419126236,
+                              -0.900968867902419126236, -0.222520933956314404289, 0.623489801858733530525 };
+    constexpr double t8[] = { 1.0, 0.707106781186547524401, 0.0, -0.707106781186547524401, -1.0,
+                              -0.707106781186547524401, 0.0, 0.707106781186547524401 };
+    constexpr double t9[] = { 1.0, 0.766044443118978035202, 0.173648177666930348852, -0.5, -0.939692620785908384054,
+                              -0.939692620785908384054, -0.5, 0.173648177666930348852, 0.766044443118978035202 };
+    constexpr double t10[] = { 1.0, 0.809016994374947424102, 0.309016994374947424102, -0.309016994374947424102,
+                               -0.809016994374947424102, -1.0, -0.809016994374947424102, -0.309016994374947424102,
+                               0.309016994374947424102, 0.809016994374947424102 };
+    constexpr double t12[] = { 1.0, 0.866025403784438646764, 0.5, 0.0, -0.5, -0.866025403784438646764, -1.0,
+                               -0.866025403784438646764, -0.5, 0.0, 0.5, 0.866025403784438646764 };
+    constexpr double t14[] = { 1.0, 0.900968867902419126236, 0.623489801858733530525, 0.222520933956314404289,
+                               -0.222520933956314404289, -0.623489801858733530525, -0.900968867902419126236, -1.0,
+                               -0.900968867902419126236, -0.623489801858733530525, -0.222520933956314404289,
+                               0.222520933956314404289, 0.623489801858733530525, 0.900968867902419126236 };
+    constexpr double t15[] = { 1.0, 0.913545457642600895502, 0.669130606358858213826, 0.309016994374947424102,
+                               -0.1045284632676534714, -0.5, -0.809016994374947424102, -0.978147600733805637929,
+                               -0.978147600733805637929, -0.809016994374947424102, -0.5, -0.1045284632676534714,
+                               0.309016994374947424102, 0.669130606358858213826, 0.913545457642600895502 };
+    constexpr double t16[] = { 1.0, 0.923879532511286756128, 0.707106781186547524401, 0.382683432365089771728, 0.0,
+                               -0.382683432365089771728, -0.707106781186547524401, -0.923879532511286756128, -1.0,
+                               -0.923879532511286756128, -0.707106781186547524401, -0.382683432365089771728, 0.0,
+                               0.382683432365089771728, 0.707106781186547524401, 0.923879532511286756128 };
+    switch( N )
+    {
+    case 3: return t3[e];
+    case 5: return t5[e];
+    case 6: return t6[e];
+    case 7: return t7[e];
+    case 8: return t8[e];
+    case 9: return t9[e];
+    case 10: return t10[e];
+    case 12: return t12[e];
+    case 14: return t14[e];
+    case 15: return t15[e];
+    case 16: return t16[e];
+    default: return 1.0;
+    }
+}
+__host__ __device__ constexpr double root_sin( int N, int e )
+{
+    constexpr double t3[] = { 0.0, 0.866025403784438646764, -0.866025403784438646764 };
+    constexpr double t5[] = { 0.0, 0.951056516295153572116, 0.587785252292473129169, -0.587785252292473129169,
+                              -0.951056516295153572116 };
+    constexpr double t6[] = { 0.0, 0.866025403784438646764, 0.866025403784438646764, 0.0, -0.866025403784438646764,
+                              -0.866025403784438646764 };
+    constexpr double t7[] = { 0.0, 0.781831482468029808708, 0.974927912181823607018, 0.433883739117558120476,
+                              -0.433883739117558120476, -0.974927912181823607018, -0.781831482468029808708 };
+    constexpr double t8[] = { 0.0, 0.707106781186547524401, 1.0, 0.707106781186547524401, 0.0,
+                              -0.707106781186547524401, -1.0, -0.707106781186547524401 };
+    constexpr double t9[] = { 0.0, 0.642787609686539326323, 0.984807753012208059367, 0.866025403784438646764,
+                              0.342020143325668733044, -0.342020143325668733044, -0.866025403784438646764,
+                              -0.984807753012208059367, -0.642787609686539326323 };
+    constexpr double t10[] = { 0.0, 0.587785252292473129169, 0.951056516295153572116, 0.951056516295153572116,
+                               0.587785252292473129169, 0.0, -0.587785252292473129169, -0.951056516295153572116,
+                               -0.951056516295153572116, -0.587785252292473129169 };
+    constexpr double t12[] = { 0.0, 0.5, 0.866025403784438646764, 1.0, 0.866025403784438646764, 0.5, 0.0, -0.5,
+                               -0.866025403784438646764, -1.0, -0.866025403784438646764, -0.5 };
+    constexpr double t14[] = { 0.0, 0.433883739117558120476, 0.781831482468029808708, 0.974927912181823607018,
+                               0.974927912181823607018, 0.781831482468029808708, 0.433883739117558120476, 0.0,
+                               -0.433883739117558120476, -0.781831482468029808708, -0.974927912181823607018,
+                               -0.974927912181823607018, -0.781831482468029808708, -0.433883739117558120476 };
+    constexpr double t15[] = { 0.0, 0.406736643075800207754, 0.743144825477394235015, 0.951056516295153572116,
+                               0.994521895368273336923, 0.866025403784438646764, 0.587785252292473129169,
+                               0.207911690817759337102, -0.207911690817759337102, -0.587785252292473129169,
+                               -0.866025403784438646764, -0.994521895368273336923, -0.951056516295153572116,
+                               -0.743144825477394235015, -0.406736643075800207754 };
+    constexpr double t16[] = { 0.0, 0.382683432365089771728, 0.707106781186547524401, 0.923879532511286756128, 1.0,
+                               0.923879532511286756128, 0.707106781186547524401, 0.382683432365089771728, 0.0,
+                               -0.382683432365089771728, -0.707106781186547524401, -0.923879532511286756128, -1.0,
+                               -0.923879532511286756128, -0.707106781186547524401, -0.382683432365089771728 };
+    switch( N )
+    {
+    case 3: return t3[e];
+    case 5: return t5[e];
+    case 6: return t6[e];
+    case 7: return t7[e];
+    case 8: return t8[e];
+    case 9: return t9[e];
+    case 10: return t10[e];
+    case 12: return t12[e];
+    case 14: return t14[e];
+    case 15: return t15[e];
+    case 16: return t16[e];
+    default: return 0.0;
+    }
+}
+
+// x * W_N^e (forward: W = exp(-2 pi i e / N); inverse: the conjugate) for constant N, e; the
+// multiplications by 1, -1 and -+i are exact swaps and sign changes.
+template<typename R, bool INV>
+__device__ __forceinline__ cplx<R> twiddle_const( cplx<R> x, int N, int e )
+{
+    if( e == 0 )
+        return x;
+    if( 2 * e == N )
+        return { -x.x, -x.y };
+    if( 4 * e == N )
+        return crot<R, INV>( x );
+    if( 4 * e == 3 * N )
+        return crot<R, !INV>( x );
+    const R c = R( root_cos( N, e ) ), sn = R( root_sin( N, e ) );
+    return cmul( x, cplx<R>{ c, INV ? sn : -sn } );
+}
+
+// In-register DFT of N points in natural order, N in {2, 3, 4, 5, 6, 7, 8, 9, 10, 12, 14, 15, 16}:
+//   N = 2, 4, 8, 16: dft_reg;
+//   N = 3, 5, 7: the symmetric pairs a_q = v_q + v_(N-q), b_q = v_q - v_(N-q),
+//     X_m = v_0 + sum_q cos(2 pi q m / N) a_q -/+ i sum_q sin(2 pi q m / N) b_q, X_(N-m) the conjugate pattern;
+//   N = P Q (6 = 2 3, 9 = 3 3, 10 = 2 5, 12 = 4 3, 14 = 2 7, 15 = 3 5): Cooley-Tukey in registers,
+//     Q DFTs of P points over v[Q n1 + n2], twiddles W_N^(n2 k1), P DFTs of Q points, X[k1 + P k2].
+template<int N>
+struct SmallFactor
+{
+    static constexpr int P = ( N == 12 ) ? 4 : ( N % 2 == 0 ) ? 2 : 3;
+};
+
+template<typename R, int N, bool INV>
+__device__ __forceinline__ void dft_small( cplx<R> * v )
+{
+    if constexpr( N == 1 )
+        return;
+    else if constexpr( N == 2 || N == 4 || N == 8 || N == 16 )
+        dft_reg<R, N>( v, INV );
+    else if constexpr( N == 3 || N == 5 || N == 7 )
+    {
+        constexpr int NH = ( N - 1 ) / 2;
+        cplx<R> ap[NH + 1], bm[NH + 1], y[N];
+        y[0] = v[0];
+#pragma unroll
+        for( int q = 1; q <= NH; ++q )
+        {
+            ap[q] = cadd( v[q], v[N - q] );
+            bm[q] = csub( v[q], v[N - q] );
+            y[0]  = cadd( y[0], ap[q] );
+        }
+#pragma unroll
+        for( int m = 1; m <= NH; ++m )
+        {
+            cplx<R> t = v[0], u = { 0, 0 };
+#pragma unroll
+            for( int q = 1; q <= NH; ++q )
+            {
+                t = caxpy( R( root_cos( N, ( q * m ) % N ) ), ap[q], t );
+                u = caxpy( R( root_sin( N, ( q * m ) % N ) ), bm[q], u );
+            }
+            const cplx<R> iu = crot<R, INV>( u );
+            y[m]             = cadd( t, iu );
+            y[N - m]         = csub( t, iu );
+        }
+#pragma unroll
+        for( int m = 0; m < N; ++m )
+            v[m] = y[m];
+    }
+    else
+    {
+        constexpr int P = SmallFactor<N>::P, Q = N / P;
+        static_assert( P * Q == N && ( Q == 2 || Q == 3 || Q == 4 || Q == 5 || Q == 7 ), "register radix" );
+        cplx<R> y[N];
+#pragma unroll
+        for( int n2 = 0; n2 < Q; ++n2 )
+        {
+            cplx<R> t[P];
+#pragma unroll
+            for( int n1 = 0; n1 < P; ++n1 )
+                t[n1] = v[Q * n1 + n2];
+            dft_small<R, P, INV>( t );
+#pragma unroll
+            for( int k1 = 0; k1 < P; ++k1 )
+                y[k1 * Q + n2] = twiddle_const<R, INV>( t[k1], N, ( n2 * k1 ) % N );
+        }
+#pragma unroll
+        for( int k1 = 0; k1 < P; ++k1 )
+        {
+            cplx<R> t[Q];
+#pragma unroll
+            for( int n2 = 0; n2 < Q; ++n2 )
+                t[n2] = y[k1 * Q + n2];
+            dft_small<R, Q, INV>( t );
+#pragma unroll
+            for( int k2 = 0; k2 < Q; ++k2 )
+                v[k1 + P * k2] = t[k2];
+        }
+    }
 }
 
 // One Stockham stage of compile-time radix RR over nl lines (element t of line l at l*ls + t*es):
-// butterfly j = 0 .. L/RR - 1 of every line, k = j mod Ns, twiddles W_L^(r k span) on the inputs,
-// then the RR-point DFT in closed form: radix 2 and 4 by sums and +-i swaps; radix 3, 5, 7 by the
-// symmetric pairs a_k = v_k + v_(RR-k), b_k = v_k - v_(RR-k):
-//   y_m = v_0 + sum_k cos(2 pi k m / RR) a_k  -/+  i sum_k sin(2 pi k m / RR) b_k,
-//   y_(RR-m) with the opposite sign of the i term,
-// the cosines and sines read from the twiddle table (W_RR^q = tw[q L/RR]).
-template<typename R, int RR, typename BUF>
+// butterfly j = 0 .. L/RR - 1 of every line, k = j mod Ns, twiddles W_L^(r k span) on the inputs
+// (none in the first stage, Ns = 1), the RR-point DFT in registers, outputs at (j - k) RR + k + m Ns.
+// Thread t takes butterflies t, t + T, t + 2T, ... (T threads) of the flattened (line, j) range; its
+// position (line, j = jq Ns + k) advances by the precomputed step, so the loop divides nothing.
+template<typename R, int RR, bool INV, bool FIRST, typename BUF>
 __device__ __forceinline__ void mixed_stage( const BUF & a, const BUF & b, int nl, int ls, int es, int LR, int Ns,
-                                             int span, const FastDiv & dlr, const FastDiv & dns, const BUF & tw,
-                                             bool inverse )
+                                             int span, const FastDiv & dlr, const FastDiv & dns, const BUF & tw )
 {
-    constexpr int NH = ( RR - 1 ) / 2;
-    R cs[NH + 1], sn[NH + 1]; // cos(2 pi q / RR), sin(2 pi q / RR)
-#pragma unroll
-    for( int q = 1; q <= NH; ++q )
+    const int T   = blockDim.x;
+    int line      = (int)fdiv( threadIdx.x, dlr );
+    int j         = threadIdx.x - line * LR;
+    int jq        = (int)fdiv( (unsigned)j, dns );
+    int k         = j - jq * Ns;
+    const int dl  = (int)fdiv( (unsigned)T, dlr );
+    const int dj  = T - dl * LR;
+    const int djq = (int)fdiv( (unsigned)dj, dns );
+    const int dk  = dj - djq * Ns;
+    const int lres = LR * es, nses = Ns * es, step = Ns * RR;
+    while( line < nl )
     {
-        const cplx<R> w = tw.ld( q * LR );
-        cs[q]           = w.x;
-        sn[q]           = -w.y;
-    }
-    const int lres = LR * es, nses = Ns * es;
-    for( int idx = threadIdx.x; idx < nl * LR; idx += blockDim.x )
-    {
-        const int line = (int)fdiv( (unsigned)idx, dlr );
-        const int j    = idx - line * LR;
-        const int jq   = (int)fdiv( (unsigned)j, dns );
-        const int k    = j - jq * Ns;
-        const int s0   = line * ls + j * es;                   // input r at s0 + r L/RR
-        const int d0   = line * ls + ( jq * Ns * RR + k ) * es; // output m at d0 + m Ns
-        const int ks   = k * span;
+        const int s0 = line * ls + j * es;
+        const int d0 = line * ls + ( jq * step + k ) * es;
         cplx<R> v[RR];
         v[0] = a.ld( s0 );
 #pragma unroll
         for( int r = 1; r < RR; ++r )
         {
-            cplx<R> w = tw.ld( r * ks );
-            if( inverse )
-                w = cconj( w );
-            v[r] = cmul( a.ld( s0 + r * lres ), w );
-        }
-        cplx<R> y[RR];
-        if( RR == 2 )
-        {
-            y[0]      = cadd( v[0], v[1 % RR] );
-            y[1 % RR] = csub( v[0], v[1 % RR] );
-        }
-        else if( RR == 4 )
-        {
-            const cplx<R> s02 = cadd( v[0], v[2 % RR] ), d02 = csub( v[0], v[2 % RR] );
-            const cplx<R> s13 = cadd( v[1 % RR], v[3 % RR] ), d13 = crot( csub( v[1 % RR], v[3 % RR] ), inverse );
-            y[0]      = cadd( s02, s13 );
-            y[1 % RR] = cadd( d02, d13 );
-            y[2 % RR] = csub( s02, s13 );
-            y[3 % RR] = csub( d02, d13 );
-        }
-        else
-        {
-            cplx<R> ap[NH + 1], bm[NH + 1];
-            y[0] = v[0];
-#pragma unroll
-            for( int q = 1; q <= NH; ++q )
+            v[r] = a.ld( s0 + r * lres );
+            if( !FIRST )
             {
-                ap[q] = cadd( v[q], v[RR - q] );
-                bm[q] = csub( v[q], v[RR - q] );
-                y[0]  = cadd( y[0], ap[q] );
-            }
-#pragma unroll
-            for( int m = 1; m <= NH; ++m )
-            {
-                cplx<R> t = v[0], u = { 0, 0 };
-#pragma unroll
-                for( int q = 1; q <= NH; ++q )
-                {
-                    const int e  = ( q * m ) % RR; // angle index of cos/sin(2 pi q m / RR)
-                    const int ef = e <= NH ? e : RR - e;
-                    const R sg   = e <= NH ? R( 1 ) : R( -1 );
-                    t            = caxpy( cs[ef], ap[q], t );
-                    u            = caxpy( sg * sn[ef], bm[q], u );
-                }
-                const cplx<R> iu = crot( u, inverse );
-                y[m]             = cadd( t, iu );
-                y[RR - m]        = csub( t, iu );
+                cplx<R> w = tw.ld( r * k * span );
+                if( INV )
+                    w.y = -w.y;
+                v[r] = cmul( v[r], w );
             }
         }
+        dft_small<R, RR, INV>( v );
 #pragma unroll
         for( int m = 0; m < RR; ++m )
-            b.st( d0 + m * nses, y[m] );
+            b.st( d0 + m * nses, v[m] );
+        line += dl;
+        j += dj;
+        jq += djq;
+        k += dk;
+        if( k >= Ns )
+        {
+            k -= Ns;
+            ++jq;
+        }
+        if( j >= LR )
+        {
+            j -= LR;
+            ++line;
+            jq -= span;
+        }
     }
 }
 
+template<typename R, int RR, bool INV, typename BUF>
+__device__ __forceinline__ void mixed_stage_any( const BUF & a, const BUF & b, int nl, int ls, int es, int LR, int Ns,
+                                                 int span, const FastDiv & dlr, const FastDiv & dns, const BUF & tw )
+{
+    if( Ns == 1 )
+        mixed_stage<R, RR, INV, true>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw );
+    else
+        mixed_stage<R, RR, INV, false>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw );
+}
+
 // The stages of mixed_fft from buffer a into b (ping-pong); returns true when the result is in a.
-template<typename R, typename BUF>
+template<typename R, bool INV, typename BUF>
 __device__ __forceinline__ bool mixed_stages( const BUF & A0, const BUF & B0, int L, int nl, int ls, int es,
-                                              const RadixPlan & P, const BUF & tw, bool inverse )
+                                              const RadixPlan & P, const BUF & tw )
 {
     int Ns    = 1;
     bool in_a = true;
@@ -673,23 +848,21 @@ __device__ __forceinline__ bool mixed_stages( const BUF & A0, const BUF & B0, in
         const FastDiv dlr = P.div_lr[s], dns = P.div_ns[s];
         switch( Rr )
         {
-        case 2:
-            mixed_stage<R, 2>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
-            break;
-        case 3:
-            mixed_stage<R, 3>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
-            break;
-        case 4:
-            mixed_stage<R, 4>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
-            break;
-        case 5:
-            mixed_stage<R, 5>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
-            break;
-        case 7:
-            mixed_stage<R, 7>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw, inverse );
-            break;
+#define SG_MIXED_CASE( RAD )                                                                                           \
+    case RAD: mixed_stage_any<R, RAD, INV>( a, b, nl, ls, es, LR, Ns, span, dlr, dns, tw ); break;
+            SG_MIXED_CASE( 2 )
+            SG_MIXED_CASE( 3 )
+            SG_MIXED_CASE( 4 )
+            SG_MIXED_CASE( 5 )
+            SG_MIXED_CASE( 6 )
+            SG_MIXED_CASE( 7 )
+            SG_MIXED_CASE( 8 )
+            SG_MIXED_CASE( 9 )
+            SG_MIXED_CASE( 10 )
+            SG_MIXED_CASE( 12 )
+#undef SG_MIXED_CASE
         default:
-            // other radices (not produced by the padded extents): runtime-radix direct sums
+            // other radices (prime factors above 7 of unpadded periodic extents): direct sums
             for( int o = threadIdx.x; o < nl * L; o += blockDim.x )
             {
                 const int line = o / L;
@@ -703,7 +876,7 @@ __device__ __forceinline__ bool mixed_stages( const BUF & A0, const BUF & B0, in
                 {
                     const int t = ( r * k * span + ( ( r * m ) % Rr ) * LR ) % L;
                     cplx<R> w   = tw.ld( t );
-                    if( inverse )
+                    if( INV )
                         w = cconj( w );
                     const cplx<R> p = cmul( a.ld( line * ls + ( j + r * LR ) * es ), w );
                     acc.x += p.x;
@@ -721,15 +894,14 @@ __device__ __forceinline__ bool mixed_stages( const BUF & A0, const BUF & B0, in
 }
 
 // Mixed-radix (any L) strided Stockham: element t of line l at l*ls + t*es, ping-pong between a
-// and b; returns the buffer that holds the result.  Radices 2, 3, 4, 5, 7 (all that the padded
-// extents produce) with closed-form compile-time butterflies and the stage divisors precomputed
-// on the host (RadixPlan); others by runtime-radix direct sums.  Consecutive threads take
-// consecutive butterflies of a line.  Not inlined (one copy serves every call site of a kernel):
-// the buffers arrive as generic pointers and are accessed through the shared window when all three
+// and b; returns the buffer that holds the result.  The radix sequence (RadixPlan, chosen on the
+// host by radix_plan) uses register DFTs of 2 ... 16 points; prime factors above 7 fall back to
+// direct sums.  Not inlined (one copy per direction serves every call site of a kernel): the
+// buffers arrive as generic pointers and are accessed through the shared window when all three
 // point into shared memory, element-aligned (every caller's do).
-template<typename R>
-__device__ __noinline__ cplx<R> * mixed_fft( cplx<R> * a, cplx<R> * b, int L, int nl, int ls, int es,
-                                             const RadixPlan & P, const cplx<R> * tw, bool inverse )
+template<typename R, bool INV>
+__device__ __noinline__ cplx<R> * mixed_fft_dir( cplx<R> * a, cplx<R> * b, int L, int nl, int ls, int es,
+                                                 const RadixPlan & P, const cplx<R> * tw )
 {
     constexpr unsigned int EL = sizeof( cplx<R> );
     bool in_a;
@@ -740,13 +912,77 @@ __device__ __noinline__ cplx<R> * mixed_fft( cplx<R> * a, cplx<R> * b, int L, in
         const unsigned int st = (unsigned int)__cvta_generic_to_shared( tw );
         if( ( ( sa | sb | st ) & ( EL - 1 ) ) == 0 )
         {
-            in_a = mixed_stages<R>( SmemBuf<R>{ sa }, SmemBuf<R>{ sb }, L, nl, ls, es, P, SmemBuf<R>{ st }, inverse );
+            in_a = mixed_stages<R, INV>( SmemBuf<R>{ sa }, SmemBuf<R>{ sb }, L, nl, ls, es, P, SmemBuf<R>{ st } );
             return in_a ? a : b;
         }
     }
-    in_a = mixed_stages<R>( GenBuf<R>{ a }, GenBuf<R>{ b }, L, nl, ls, es, P, GenBuf<R>{ const_cast<cplx<R> *>( tw ) },
-                            inverse );
+    in_a = mixed_stages<R, INV>( GenBuf<R>{ a }, GenBuf<R>{ b }, L, nl, ls, es, P,
+                                 GenBuf<R>{ const_cast<cplx<R> *>( tw ) } );
     return in_a ? a : b;
+}
+
+template<typename R>
+__device__ __forceinline__ cplx<R> * mixed_fft( cplx<R> * a, cplx<R> * b, int L, int nl, int ls, int es,
+                                                const RadixPlan & P, const cplx<R> * tw, bool inverse )
+{
+    return inverse ? mixed_fft_dir<R, true>( a, b, L, nl, ls, es, P, tw )
+                   : mixed_fft_dir<R, false>( a, b, L, nl, ls, es, P, tw );
+}
+
+// Radix sequence of a length-L transform for mixed_fft: the factorisation into register radices
+// {2, ..., 16} of least estimated cost (per point and stage: a fixed part -- the shared-memory
+// round trip, the twiddle and the index work -- plus the butterfly's arithmetic per point), found
+// by dynamic programming over the divisors of L; prime factors above 7 become direct-sum stages.
+// The stage divisors (L / radix and the product of the earlier radices) are filled in for the
+// threads' start positions.
+inline void radix_plan( int L, RadixPlan & P )
+{
+    const int cand[]   = { 12, 10, 9, 8, 7, 6, 5, 4, 3, 2 };
+    const double fp[]  = { 12.3, 12.4, 13.3, 6.5, 12.0, 8.7, 8.0, 4.0, 5.3, 2.0 };
+    const double fixed = 14.0;
+    // L = smooth * rough: smooth has the prime factors 2, 3, 5, 7, rough the others
+    int smooth = 1, rough = L;
+    for( int p : { 2, 3, 5, 7 } )
+        while( rough % p == 0 )
+        {
+            rough /= p;
+            smooth *= p;
+        }
+    std::vector<double> best( smooth + 1, 1e300 );
+    std::vector<int> pick( smooth + 1, 0 );
+    best[1] = 0.0;
+    for( int m = 2; m <= smooth; ++m )
+    {
+        if( smooth % m )
+            continue;
+        for( int c = 0; c < 10; ++c )
+        {
+            const int r = cand[c];
+            if( m % r == 0 && best[m / r] + fixed + fp[c] < best[m] )
+            {
+                best[m] = best[m / r] + fixed + fp[c];
+                pick[m] = r;
+            }
+        }
+    }
+    int ns = 0;
+    for( int m = smooth; m > 1 && ns < 12; m /= pick[m] )
+        P.radix[ns++] = pick[m];
+    for( int p = 11; rough > 1 && ns < 12; p += 2 ) // rough has no factor below 11
+        while( rough % p == 0 && ns < 12 )
+        {
+            P.radix[ns++] = p;
+            rough /= p;
+        }
+    for( int s = ns; s < 12; ++s )
+        P.radix[s] = 0;
+    int prod = 1;
+    for( int s = 0; s < ns; ++s )
+    {
+        P.div_lr[s] = make_fastdiv( (unsigned)( L / P.radix[s] ) );
+        P.div_ns[s] = make_fastdiv( (unsigned)prod );
+        prod *= P.radix[s];
+    }
 }
 
 template<typename R, bool LINE_FAST, int MAXLG = MaxRadix<R>::LG>
