@@ -23,8 +23,11 @@
 namespace sg
 {
 
+// Complex value, aligned to its size so that every load and store of one is a single vector
+// access (every complex array here starts at a shared or global base aligned to 16 bytes and is
+// indexed in whole elements).
 template<typename R>
-struct cplx
+struct alignas( 2 * sizeof( R ) ) cplx
 {
     R x, y;
 };
