@@ -1,12 +1,15 @@
-"""Dipolar field on padded extents with radix 3, 5 and 7 stages (the mixed-radix Stockham path
-of the FFT passes), on one-row (2D: the single-block b/c pass, several ka planes per block) and
-3D layouts, against the FP64 oracle.
+"""Dipolar field on padded extents whose transforms run the mixed-radix Stockham path of the FFT
+passes (register radices 2 ... 12 chosen by the device's cost planner), on one-row (2D: the
+single-block b/c pass, several ka planes per block) and 3D layouts, against the FP64 oracle.
 
-Extents (the zero-padded axes are 2N, 7-smooth here, so the oracle's padding is the same):
-  open 7 x 21 x 1    -> 14 x 42      (2*7, 2*3*7)
-  open 15 x 10 x 1   -> 30 x 20      (2*3*5, 4*5)
-  open 5 x 7 x 9     -> 10 x 14 x 18 (2*5, 2*7, 2*3*3)
-  periodic 12 x 9 x 3, no padding -> 12 x 9 x 3 (4*3, 3*3, 3)
+Extents (the zero-padded axes are 2N, 7-smooth here, so the oracle's padding is the same) and the
+device's radix plans (power-of-two extents take the register power-of-two path):
+  open 7 x 21 x 1    -> 14 x 42      (7*2, 7*6)
+  open 15 x 10 x 1   -> 30 x 20      (6*5, 5*4)
+  open 5 x 7 x 9     -> 10 x 14 x 18 (10, 7*2, 6*3)
+  open 40 x 27 x 1   -> 80 x 54      (10*8, 9*6)
+  open 18 x 6 x 6    -> 36 x 12 x 12 (9*4, 12, 12)
+  periodic 12 x 9 x 3, no padding -> 12 x 9 x 3 (12, 9, 3)
 
 Tolerances: FP64 gradient 1e-12 relative to max |g| (as the golden gradient cases); FP32 RK4
 trajectory of 20 steps max |dm| <= 1e-5 against the FP64 oracle (the metric's bar).
@@ -27,6 +30,8 @@ CASES = {
     "open2d_7x21": dict(_OPEN, n_cells=[7, 21, 1]),
     "open2d_15x10": dict(_OPEN, n_cells=[15, 10, 1]),
     "open3d_5x7x9": dict(_OPEN, n_cells=[5, 7, 9], lattice_constant=3.0),
+    "open2d_40x27": dict(_OPEN, n_cells=[40, 27, 1]),
+    "open3d_18x6x6": dict(_OPEN, n_cells=[18, 6, 6], lattice_constant=3.0),
     "periodic_12x9x3": dict(_OPEN, n_cells=[12, 9, 3], bc=[1, 1, 1], lattice_constant=2.5,
                             ddi=dict(method="fft", n_periodic_images=[1, 1, 1], radius=0.0, pb_zero_padding=0)),
 }
