@@ -338,14 +338,15 @@ def c4_specs(n=256, seed=4, ddi=False):
     return specs
 
 
-def run_batched_vs_plain(steps, warmup, plain=True, check=True, ddi=False, profile_step=False):
+def run_batched_vs_plain(steps, warmup, plain=True, check=True, ddi=False, profile_step=False, n_systems=256):
     """256 uneven systems: spin-updates/s of the batched path (all systems in one launch per SIB
     stage, CUDA graphs) against the plain path (every system its own engine and launches, on the
     same stream), both FP32 and device-timed with CUDA events; the ensemble's arrays (~290 MB)
     exceed L2.  Accuracy: the 8 smallest systems run 1000 batched FP32 steps against the FP64
     oracle consuming the same Philox streams.  ddi=True: the dipolar variant of the ensemble
     (c4_specs), one batched FFT plan over all 256 systems.  profile_step: one more batched step
-    inside a profiler range (for `ncu --profile-from-start off`)."""
+    inside a profiler range (for `ncu --profile-from-start off`).  n_systems: the first n systems of
+    the ensemble (the same seeds), for profiler captures on a small case."""
     import torch
 
     from oracle.oracle import OracleSystem, random_spins
@@ -355,7 +356,7 @@ def run_batched_vs_plain(steps, warmup, plain=True, check=True, ddi=False, profi
 
     launch = fn("Simulation_Launch_Steps", [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int])
     rank, world, _ = dist_env()
-    specs = c4_specs(ddi=ddi)
+    specs = c4_specs(n=n_systems, ddi=ddi)
     if world > 1:
         # the ensemble is sharded over the ranks by spin count; each rank batches its share
         mine = partition_by_spins([sp["n_cells"][0] * sp["n_cells"][1] for sp in specs], world)[rank]
@@ -923,6 +924,8 @@ def main():
                     help="run and print only the dipolar batched-vs-plain measurement")
     ap.add_argument("--only-htst", action="store_true", help="run and print only the HTST measurement")
     ap.add_argument("--only-adjoint", action="store_true", help="run and print only the adjoint measurement")
+    ap.add_argument("--systems", type=int, default=256,
+                    help="--only-batched / --only-batched-ddi: the first N systems of the ensemble (profiling)")
     ap.add_argument("--only-batched", action="store_true",
                     help="run and print only the 256-system batched-vs-plain measurement (profiling)")
     args = ap.parse_args()
@@ -938,7 +941,7 @@ def main():
         torch.cuda.set_device(0)
         prof = args.profile_step  # profiling: the batched path alone
         print(json.dumps(run_batched_vs_plain(max(20, args.steps), max(3, args.warmup), plain=not prof,
-                                              check=not prof, ddi=True, profile_step=prof)))
+                                              check=not prof, ddi=True, profile_step=prof, n_systems=args.systems)))
         return
     if args.only_htst:
         import torch
@@ -956,7 +959,8 @@ def main():
         import torch
 
         torch.cuda.set_device(0)
-        print(json.dumps(run_batched_vs_plain(args.steps, args.warmup, plain=False, check=False)))
+        print(json.dumps(run_batched_vs_plain(args.steps, args.warmup, plain=False, check=False,
+                                              n_systems=args.systems)))
         return
     if args.impl == "reference":
         run_reference(args)
