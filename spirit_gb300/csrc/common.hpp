@@ -173,7 +173,6 @@ struct SysRun
     int active;         // 1 while the method keeps iterating this system
     float max_torque;   // last max |P_perp fv| (Hook_Post_Iteration)
     unsigned int torque_bits; // running max of |t|^2 as float bits (non-negative floats order like uints)
-    unsigned int unused;
     double energy;      // energy of the last force evaluation (Spin_System::E)
     double energy_acc;  // running sum of the current evaluation
     double reserved;

@@ -102,7 +102,8 @@ __global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 4 : 2 ) pass_a( PassA
         const R mu           = fft_mu<R>( f, ib );
         const R * src        = comp == 0 ? p.sx : ( comp == 1 ? p.sy : p.sz );
         const int rowlen     = nb * d.n_cells[0];
-        const long long base = d.spin_offset + ib + (long long)rowlen * ( (long long)b0 + (long long)d.n_cells[1] * c );
+        // spin arrays of a batch hold fewer than 2^31 entries (the engine checks): 32-bit offsets
+        const int base       = (int)d.spin_offset + ib + rowlen * ( b0 + d.n_cells[1] * c );
         // unrolled: the loads of several elements are in flight before the first lands in shared memory
 #pragma unroll 4
         for( int e = threadIdx.x; e < nq * Ma; e += blockDim.x )
@@ -111,8 +112,8 @@ __global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 4 : 2 ) pass_a( PassA
             R x = 0, y = 0;
             if( t < Ain )
             {
-                const long long o = base + (long long)( 2 * q ) * rowlen + (long long)nb * t;
-                x                 = mu * src[o];
+                const int o = base + 2 * q * rowlen + nb * t;
+                x           = mu * src[o];
                 if( 2 * q + 1 < nl )
                     y = mu * src[o + rowlen];
             }
@@ -655,14 +656,14 @@ __global__ void __launch_bounds__( 256, sizeof( R ) == 4 ? 4 : 2 ) pass_a_inv( P
     const int ib = cb / 3, comp = cb - 3 * ib;
     R * dst      = comp == 0 ? p.hx : ( comp == 1 ? p.hy : p.hz );
     const int rowlen     = nb * Na;
-    const long long base = d.spin_offset + ib + (long long)rowlen * ( (long long)b0 + (long long)Nb * c );
+    const int base       = (int)d.spin_offset + ib + rowlen * ( b0 + Nb * c ); // < 2^31 (see pass_a)
     for( int e = threadIdx.x; e < nl * Ma; e += blockDim.x )
     {
         const int li = (int)fdiv( (unsigned)e, f.div_Ma ), t = e - li * Ma;
         if( t < Na )
         {
             const cplx<R> v = r[( li >> 1 ) * ls + t];
-            dst[base + (long long)li * rowlen + (long long)nb * t] = ( ( li & 1 ) ? v.y : v.x ) * invT;
+            dst[base + li * rowlen + nb * t] = ( ( li & 1 ) ? v.y : v.x ) * invT;
         }
     }
 }
