@@ -1820,6 +1820,8 @@ void Engine::launch_probe_t()
 void Engine::launch_close( int tune, int probe )
 {
     const int n = (int)desc_.size();
+    if( n == 0 )
+        return;
     launch_pdl( close_iteration, dim3( ( n + 127 ) / 128 ), dim3( 128 ), 0, stream_, 1, d_runs_,
                 (const SysDesc *)d_desc_, n, tune, probe );
 }

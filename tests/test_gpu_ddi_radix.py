@@ -10,6 +10,7 @@ device's radix plans (power-of-two extents take the register power-of-two path):
   open 40 x 27 x 1   -> 80 x 54      (10*8, 9*6)
   open 18 x 6 x 6    -> 36 x 12 x 12 (9*4, 12, 12)
   periodic 12 x 9 x 3, no padding -> 12 x 9 x 3 (12, 9, 3)
+  periodic 11 x 13 x 2, no padding -> 11 x 13 x 2 (prime lengths 11 and 13: direct-sum stages; 2)
 
 Tolerances: FP64 gradient 1e-12 relative to max |g| (as the golden gradient cases); FP32 RK4
 trajectory of 20 steps max |dm| <= 1e-5 against the FP64 oracle (the metric's bar).
@@ -34,6 +35,8 @@ CASES = {
     "open3d_18x6x6": dict(_OPEN, n_cells=[18, 6, 6], lattice_constant=3.0),
     "periodic_12x9x3": dict(_OPEN, n_cells=[12, 9, 3], bc=[1, 1, 1], lattice_constant=2.5,
                             ddi=dict(method="fft", n_periodic_images=[1, 1, 1], radius=0.0, pb_zero_padding=0)),
+    "periodic_11x13x2": dict(_OPEN, n_cells=[11, 13, 2], bc=[1, 1, 1], lattice_constant=2.5,
+                             ddi=dict(method="fft", n_periodic_images=[1, 1, 1], radius=0.0, pb_zero_padding=0)),
 }
 
 
