@@ -363,7 +363,7 @@ __device__ __forceinline__ cplx<R> * block_fft_const( cplx<R> * a, cplx<R> * b, 
 }
 
 // Stockham stage loop over nl lines of length L in shared memory (a -> b -> a ...); line k
-// starts at k * ls (ls = L, or L + 1 for power-of-two lengths to spread shared-memory banks).
+// starts at k * ls (ls = line_stride(L): L + 1 for even L, to spread shared-memory banks).
 // rad: 0-terminated radix list; tw: L twiddles exp(-2 pi i t/L) (in shared memory).
 // Returns the buffer that holds the result.  Must be called by all threads of the block.
 // power-of-two lines of 2^LGL with register stages of at most 2^MAXLG
@@ -409,7 +409,7 @@ __device__ cplx<R> * block_fft( cplx<R> * a, cplx<R> * b, int L, int ls, int nl,
         return r;
     if( ( L & ( L - 1 ) ) == 0 )
         return block_fft_pow2( a, b, L, ls, nl, tw, inverse );
-    return mixed_fft<R>( a, b, L, nl, L, 1, P, tw, inverse );
+    return mixed_fft<R>( a, b, L, nl, ls, 1, P, tw, inverse );
 }
 
 // ------------------------------------------------------------------ strided line transforms
@@ -1029,10 +1029,13 @@ __device__ __forceinline__ void load_tw( cplx<R> * dst, const cplx<R> * src, int
         dst[t] = src[t];
 }
 
-// shared-memory line stride for lines of length L
+// Shared-memory line stride for lines of length L: odd, so that the transposed accesses of the
+// passes (consecutive threads on consecutive lines at one frequency) spread over the banks -- an
+// even stride puts many lanes of a half-warp on the same banks (16-way for 8-byte elements when L
+// is a multiple of 16).
 __host__ __device__ inline int line_stride( int L )
 {
-    return ( ( L & ( L - 1 ) ) == 0 && L >= 8 && L <= 64 ) ? L + 1 : L;
+    return ( L % 2 == 0 ) ? L + 1 : L;
 }
 
 } // namespace sg
