@@ -192,7 +192,7 @@ def test_positions_write():
     f = _path("pos")
     with make_state(GRAD_CASES["sc3d_ddi"]) as p:
         io.positions_write(p, f, io.FILEFORMAT_OVF_BIN8)
-        pos = geometry.get_positions(p)
+        pos = np.array(geometry.get_positions(p))  # a copy: the getter's array belongs to the State
     raw = open(f, "rb").read()
     assert b"# valuelabels: position_x position_y position_z" in raw
     p0 = raw.index(b"# Begin: Data Binary 8\n") + len(b"# Begin: Data Binary 8\n")
